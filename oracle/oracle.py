@@ -1,0 +1,193 @@
+"""ORACLE (test infrastructure only): ctypes front end of the CPU FP64 restatement in
+dna2_oracle.c.  Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+as the checker; the product package never imports it.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboxgb_oracle.so")
+_lib = None
+
+NTERMS = 8
+TERM_NAMES = ("fene", "bonded_excl", "stacking", "nonbonded_excl", "hb", "cross_stacking", "coaxial_stacking",
+              "debye_huckel")
+
+
+class Settings(C.Structure):
+    _fields_ = [
+        ("T", C.c_double), ("salt", C.c_double), ("average", C.c_int),
+        ("seq_stck", (C.c_double * 4) * 4), ("seq_stck_fact_eps", C.c_double),
+        ("seq_hydr_at", C.c_double), ("seq_hydr_gc", C.c_double), ("hb_multiplier", C.c_double),
+        ("dh_half_charged_ends", C.c_int), ("dh_lambda", C.c_double), ("dh_strength", C.c_double),
+        ("use_mbf", C.c_int), ("mbf_fmax", C.c_double), ("mbf_finf", C.c_double),
+    ]
+
+
+_D2 = C.c_double * 2
+_D255 = ((C.c_double * 5) * 5) * 2
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("T", C.c_double), ("f1_eps", _D255), ("f1_shift", _D255),
+        ("f1_a", _D2), ("f1_rc", _D2), ("f1_r0", _D2), ("f1_blow", _D2), ("f1_bhigh", _D2), ("f1_rlow", _D2),
+        ("f1_rhigh", _D2), ("f1_rclow", _D2), ("f1_rchigh", _D2),
+        ("f2_k", _D2), ("f2_rc", _D2), ("f2_r0", _D2), ("f2_blow", _D2), ("f2_rlow", _D2), ("f2_rclow", _D2),
+        ("f2_bhigh", _D2), ("f2_rhigh", _D2), ("f2_rchigh", _D2),
+        ("f4_a", C.c_double * 13), ("f4_b", C.c_double * 13), ("f4_t0", C.c_double * 13),
+        ("f4_ts", C.c_double * 13), ("f4_tc", C.c_double * 13), ("f4_sa", C.c_double), ("f4_sb", C.c_double),
+        ("f5_a", C.c_double * 4), ("f5_b", C.c_double * 4), ("f5_xc", C.c_double * 4), ("f5_xs", C.c_double * 4),
+        ("hb_multiplier", C.c_double), ("dh_half_charged_ends", C.c_int),
+        ("dh_prefactor", C.c_double), ("dh_rhigh", C.c_double), ("dh_rc", C.c_double), ("dh_b", C.c_double),
+        ("dh_minus_kappa", C.c_double), ("dh_lambda", C.c_double),
+        ("use_mbf", C.c_int), ("mbf_fmax", C.c_double), ("mbf_finf", C.c_double), ("mbf_xmax", C.c_double),
+        ("fene_r0", C.c_double), ("rcut", C.c_double),
+    ]
+
+
+class MD(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double), ("thermostat", C.c_int), ("newtonian_steps", C.c_int), ("pt", C.c_double),
+        ("pr", C.c_double), ("bussi_tau", C.c_double), ("bussi_K_t", C.c_double), ("bussi_K_r", C.c_double),
+        ("seed", C.c_ulonglong), ("verlet_skin", C.c_double),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle library (gcc, a few seconds)."""
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        fp = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        L.oxo_params_init.argtypes = [C.POINTER(Settings), C.POINTER(Params)]
+        L.oxo_params_init.restype = C.c_int
+        L.oxo_forces.argtypes = [C.POINTER(Params), C.c_int, dp, dp, dp, dp, ip, ip, ip, ip, C.c_double,
+                                 C.c_void_p, C.c_int, dp, dp, dp, dp, C.c_int]
+        L.oxo_forces.restype = C.c_int
+        L.oxo_pairs_within.argtypes = [C.c_int, dp, C.c_double, C.c_double, ip, C.c_long]
+        L.oxo_pairs_within.restype = C.c_long
+        L.oxo_verlet_f32.argtypes = [C.c_int, fp, C.c_float, C.c_float, ip, ip, C.c_int, C.POINTER(C.c_int), ip, ip,
+                                     ip, C.c_int]
+        L.oxo_verlet_f32.restype = C.c_int
+        L.oxo_philox.argtypes = [C.c_uint] * 6 + [np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")]
+        L.oxo_md_run.argtypes = [C.POINTER(Params), C.POINTER(MD), C.c_int, dp, dp, dp, dp, ip, ip, ip, ip, C.c_double,
+                                 dp, dp, C.c_longlong, C.c_int, dp, C.c_int]
+        L.oxo_md_run.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def make_settings(T: float, salt: float = 0.5, average: bool = True, seq: Optional[dict] = None,
+                  hb_multiplier: float = 1.0, half_charged_ends: bool = True, dh_lambda: float = 0.3616455,
+                  dh_strength: float = 0.0543, mbf_fmax: Optional[float] = None, mbf_finf: float = 0.04) -> Settings:
+    s = Settings()
+    s.T = T
+    s.salt = salt
+    s.average = 1 if average else 0
+    if seq is not None:
+        order = "AGCT"
+        for i in range(4):
+            for j in range(4):
+                s.seq_stck[i][j] = seq[f"STCK_{order[i]}_{order[j]}"]
+        s.seq_stck_fact_eps = seq["STCK_FACT_EPS"]
+        s.seq_hydr_at = seq.get("HYDR_A_T", seq.get("HYDR_T_A"))
+        s.seq_hydr_gc = seq.get("HYDR_G_C", seq.get("HYDR_C_G"))
+    s.hb_multiplier = hb_multiplier
+    s.dh_half_charged_ends = 1 if half_charged_ends else 0
+    s.dh_lambda = dh_lambda
+    s.dh_strength = dh_strength
+    if mbf_fmax is not None:
+        s.use_mbf = 1
+        s.mbf_fmax = mbf_fmax
+        s.mbf_finf = mbf_finf
+    return s
+
+
+def make_params(settings: Settings) -> Params:
+    p = Params()
+    rc = lib().oxo_params_init(C.byref(settings), C.byref(p))
+    if rc != 0:
+        raise ValueError(f"oracle parameter error {rc}")
+    return p
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def forces(params: Params, pos, a1, a2, a3, n3, n5, typ, btype, L: float, pairs=None, nthreads: int = 1):
+    """Forces (lab), torques (body), energy split [8] and per-particle energies."""
+    N = int(np.asarray(pos).shape[0])
+    F = np.zeros(3 * N)
+    T = np.zeros(3 * N)
+    Es = np.zeros(NTERMS)
+    Ep = np.zeros(max(N, 1))
+    if pairs is None:
+        pp, npairs = None, -1
+    else:
+        parr = _c(pairs, np.int32).reshape(-1)
+        pp, npairs = parr.ctypes.data_as(C.c_void_p), parr.size // 2
+    rc = lib().oxo_forces(C.byref(params), N, _c(pos, np.float64).reshape(-1), _c(a1, np.float64).reshape(-1),
+                          _c(a2, np.float64).reshape(-1), _c(a3, np.float64).reshape(-1), _c(n3, np.int32),
+                          _c(n5, np.int32), _c(typ, np.int32), _c(btype, np.int32), float(L), pp, npairs, F, T, Es,
+                          Ep, nthreads)
+    return rc, F.reshape(N, 3), T.reshape(N, 3), Es, Ep[:N]
+
+
+def pairs_within(pos, L: float, rc: float) -> np.ndarray:
+    pos = _c(pos, np.float64).reshape(-1)
+    N = pos.size // 3
+    cap = 64 * N + 1024
+    while True:
+        buf = np.zeros(2 * cap, np.int32)
+        n = lib().oxo_pairs_within(N, pos, float(L), float(rc), buf, cap)
+        if n <= cap:
+            return buf[:2 * n].reshape(-1, 2)
+        cap = n
+
+
+def verlet_f32(pos4: np.ndarray, L: float, rverlet: float, n3, n5, auto_opt: bool = True, max_nb: int = 256):
+    pos4 = _c(pos4, np.float32).reshape(-1)
+    N = pos4.size // 4
+    ncs = C.c_int(0)
+    cell = np.zeros(N, np.int32)
+    nnb = np.zeros(N, np.int32)
+    nb = np.zeros(N * max_nb, np.int32)
+    rc = lib().oxo_verlet_f32(N, pos4, float(L), float(rverlet), _c(n3, np.int32), _c(n5, np.int32),
+                              1 if auto_opt else 0, C.byref(ncs), cell, nnb, nb, max_nb)
+    return rc, ncs.value, cell, nnb, nb.reshape(N, max_nb)
+
+
+def philox(key0, key1, c0, c1, c2, c3) -> np.ndarray:
+    out = np.zeros(4, np.uint32)
+    lib().oxo_philox(key0, key1, c0, c1, c2, c3, out)
+    return out
+
+
+def md_run(params: Params, md: MD, state: dict, n3, n5, typ, btype, L: float, step0: int, nsteps: int,
+           nthreads: int = 1):
+    """Advance `state` (dict of float64 arrays pos[N,3], quat[N,4], vel, Lmom, F, T) in place."""
+    N = state["pos"].shape[0]
+    Es = np.zeros(NTERMS)
+    rc = lib().oxo_md_run(C.byref(params), C.byref(md), N, state["pos"].reshape(-1), state["quat"].reshape(-1),
+                          state["vel"].reshape(-1), state["Lmom"].reshape(-1), _c(n3, np.int32), _c(n5, np.int32),
+                          _c(typ, np.int32), _c(btype, np.int32), float(L), state["F"].reshape(-1),
+                          state["T"].reshape(-1), int(step0), int(nsteps), Es, nthreads)
+    return rc, Es

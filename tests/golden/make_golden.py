@@ -1,0 +1,208 @@
+"""Generate the golden fixtures that pin the oracle (and through it the GPU kernels) to the
+reference implementation.
+
+Each fixture is produced by running the reference oxDNA CPU code, built from its own sources
+by oracle/ref/Makefile into oracle/_ref/ref_dump, on a small input deck: the reference reads the
+topology and configuration, and the harness prints its internal state, full-precision forces,
+torques and energy split (interaction_type = DNA2_nomesh, the exact-f4 oxDNA2 force field).
+Cases that ask for steps also record the state after a short reference MD run.
+
+    make -C oracle/ref -j8 REF=/root/reference      # once
+    python tests/golden/make_golden.py --ref /root/reference
+
+The .npz files are small (tens of KB) and committed; tests never need the reference itself.
+"""
+
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from oxdna_gb300 import generate as G  # noqa: E402
+from oxdna_gb300 import io as oxio  # noqa: E402
+
+DUMP = os.path.join(REPO, "oracle", "_ref", "ref_dump")
+
+
+def parse_dump(path):
+    lines = open(path).read().split("\n")
+    d = {}
+    i = 0
+    while i < len(lines):
+        ln = lines[i].split()
+        if not ln:
+            i += 1
+            continue
+        k = ln[0]
+        if k == "box":
+            d["box"] = np.array(list(map(float, ln[1:4])))
+            i += 1
+        elif k == "rcut":
+            d["rcut"] = float(ln[1])
+            i += 1
+        elif k in ("topology", "state", "forces", "final"):
+            n = int(ln[1])
+            d[k] = np.array([list(map(float, lines[i + 1 + j].split())) for j in range(n)])
+            i += n + 1
+        elif k == "energy":
+            d["energy"] = float(ln[1])
+            i += 1
+        elif k == "split":
+            n = int(ln[1])
+            d["split"] = np.array([float(lines[i + 1 + j].split()[1]) for j in range(n)])
+            i += n + 1
+        else:
+            i += 1
+    return d
+
+
+BASE_INPUT = """backend = CPU
+sim_type = MD
+interaction_type = DNA2_nomesh
+seed = 1
+steps = {steps}
+dt = {dt}
+T = {T}
+salt_concentration = {salt}
+verlet_skin = 0.05
+thermostat = no
+newtonian_steps = 103
+diff_coeff = 2.5
+topology = init.top
+conf_file = init.dat
+trajectory_file = trajectory.dat
+lastconf_file = last_conf.dat
+energy_file = energy.dat
+refresh_vel = 0
+restart_step_counter = 1
+no_stdout_energy = 1
+time_scale = linear
+print_conf_interval = 100000
+print_energy_every = 100000
+external_forces = 0
+"""
+
+
+def run_case(name, top_path, conf_path, settings, extra="", steps=0, dt=0.003):
+    with tempfile.TemporaryDirectory() as tmp:
+        open(os.path.join(tmp, "init.top"), "w").write(open(top_path).read())
+        open(os.path.join(tmp, "init.dat"), "w").write(open(conf_path).read())
+        text = BASE_INPUT.format(steps=steps, dt=dt, T=settings["T_str"], salt=settings["salt"]) + extra
+        open(os.path.join(tmp, "input"), "w").write(text)
+        out = os.path.join(tmp, "dump.txt")
+        subprocess.run([DUMP, "input", out], cwd=tmp, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        d = parse_dump(out)
+    top = d["topology"].astype(np.int64)
+    st = d["state"]
+    rec = dict(
+        box=d["box"][0], rcut=d["rcut"], T=oxio.get_temperature(settings["T_str"]), salt=float(settings["salt"]),
+        n3=top[:, 0].astype(np.int32), n5=top[:, 1].astype(np.int32), type=top[:, 2].astype(np.int32),
+        btype=top[:, 3].astype(np.int32), pos=st[:, 0:3], a1=st[:, 3:6], a2=st[:, 6:9], a3=st[:, 9:12],
+        vel=st[:, 12:15], Lmom=st[:, 15:18], F=d["forces"][:, 0:3], Tq=d["forces"][:, 3:6], split=d["split"],
+        energy=d["energy"], average=int(settings.get("average", 1)),
+        hb_multiplier=float(settings.get("hb_multiplier", 1.0)),
+        half_charged_ends=int(settings.get("half_charged_ends", 1)),
+        dh_lambda=float(settings.get("dh_lambda", 0.3616455)), dh_strength=float(settings.get("dh_strength", 0.0543)),
+        mbf_fmax=float(settings.get("mbf_fmax", -1.0)), mbf_finf=float(settings.get("mbf_finf", 0.04)),
+        steps=steps, dt=dt)
+    if "seq" in settings:
+        order = "AGCT"
+        rec["seq_stck"] = np.array([[settings["seq"][f"STCK_{order[i]}_{order[j]}"] for j in range(4)] for i in range(4)])
+        rec["seq_fact"] = settings["seq"]["STCK_FACT_EPS"]
+        rec["seq_hydr_at"] = settings["seq"].get("HYDR_A_T", settings["seq"].get("HYDR_T_A"))
+        rec["seq_hydr_gc"] = settings["seq"].get("HYDR_G_C", settings["seq"].get("HYDR_C_G"))
+    if "final" in d:
+        fs = d["final"]
+        rec.update(final_pos=fs[:, 0:3], final_a1=fs[:, 3:6], final_a2=fs[:, 6:9], final_a3=fs[:, 9:12],
+                   final_vel=fs[:, 12:15], final_Lmom=fs[:, 15:18])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **rec)
+    print(f"{name}: N={top.shape[0]} E={d['energy']:.6f} max|F|={np.abs(rec['F']).max():.3f}")
+
+
+def write_system(tmp, s):
+    tp, cp = os.path.join(tmp, "s.top"), os.path.join(tmp, "s.dat")
+    s.write(tp, cp)
+    return tp, cp
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    if not os.path.exists(DUMP):
+        subprocess.run(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8", f"REF={args.ref}"], check=True)
+    ff = os.path.join(args.ref, "test", "DNA", "FORCE_FIELD")
+
+    # 1-2: the reference's own DNA2 force-field test system (16 nt, 3 strands)
+    base = dict(T_str="20C", salt="1.0")
+    run_case("ff16_avg", os.path.join(ff, "init.top"), os.path.join(ff, "init.dat"), base)
+    seq = oxio.read_seq_dep_file(os.path.join(args.ref, "oxDNA2_sequence_dependent_parameters.txt"))
+    seq_file = os.path.join(args.ref, "oxDNA2_sequence_dependent_parameters.txt")
+    run_case("ff16_seqdep", os.path.join(ff, "init.top"), os.path.join(ff, "init.dat"), dict(base, average=0, seq=seq),
+             extra=f"use_average_seq = false\nseq_dep_file = {seq_file}\n")
+    # golden split energies the reference's regression test checks (mesh DNA2, 6 decimals)
+    gold = {k: np.loadtxt(os.path.join(ff, k, "reference.dat")) for k in ("AVG_SEQ", "SEQ_DEP")}
+    np.savez_compressed(os.path.join(HERE, "ff16_reference_dat.npz"), avg_seq=gold["AVG_SEQ"], seq_dep=gold["SEQ_DEP"])
+
+    rng = np.random.default_rng(20240601)
+    with tempfile.TemporaryDirectory() as tmp:
+        T300 = dict(T_str="300K", salt="0.5")
+        # 3: workload-0 system, a 12-bp duplex in a cube of side 20
+        s = G.system_for_config(0, seed=1)
+        run_case("duplex24", *write_system(tmp, s), T300)
+
+        # 4: a dense mixture exercising every non-bonded term (duplexes, hairpins, coils)
+        mols = [G.duplex(G.random_sequence(rng, int(rng.integers(8, 16)))) for _ in range(5)]
+        mols += [G.hairpin(G.random_sequence(rng, 7), int(rng.integers(4, 9)), rng) for _ in range(3)]
+        mols += [G.random_walk_strand(24, rng) for _ in range(3)]
+        s = G.assemble(G.place(mols, 16.0, rng, min_dist=1.3), 16.0, G.kelvin(300), rng)
+        # thermal jiggle so that angular terms sample away from their ideal values
+        s.pos = s.pos + rng.normal(scale=0.01, size=s.pos.shape)
+        s.a1 = s.a1 + rng.normal(scale=0.02, size=s.a1.shape)
+        s.a3 = s.a3 + rng.normal(scale=0.02, size=s.a3.shape)
+        run_case("mixed", *write_system(tmp, s), T300)
+        # the same molecules packed with close contacts: excluded-volume forces up to ~1e5
+        s2 = G.assemble(G.place(mols, 16.0, rng, min_dist=0.95), 16.0, G.kelvin(300), rng)
+        run_case("contact", *write_system(tmp, s2), T300)
+
+        # 5: different salt, temperature and Debye-Hueckel settings, full charges at the ends
+        run_case("dh_variants", *write_system(tmp, s), dict(T_str="330K", salt="0.2", half_charged_ends=0,
+                                                            dh_lambda=0.35, dh_strength=0.06),
+                 extra="dh_half_charged_ends = false\ndh_lambda = 0.35\ndh_strength = 0.06\n")
+
+        # 6: max_backbone_force with stretched and compressed bonds
+        m = G.random_walk_strand(40, rng)
+        s = G.assemble(G.place([m], 30.0, rng), 30.0, G.kelvin(300), rng)
+        s.pos = s.pos * 1.0 + rng.normal(scale=0.15, size=s.pos.shape)
+        run_case("mbf", *write_system(tmp, s), dict(T300, mbf_fmax=5.0, mbf_finf=0.04),
+                 extra="max_backbone_force = 5.0\nmax_backbone_force_far = 0.04\n")
+
+        # 7: custom pairing codes >= 300 with an hb_multiplier
+        s = G.system_for_config(0, seed=2)
+        bt = s.top.btype.copy()
+        n = bt.size // 2
+        for i in range(n):
+            j = bt.size - 1 - i
+            if i % 2 == 0:
+                bt[i] = 300 + bt[i]
+                bt[j] = 3 - bt[i]
+        s.top = oxio.Topology(s.top.n3, s.top.n5, bt, np.array([oxio.type_from_btype(int(b)) for b in bt], np.int32),
+                              s.top.strand, s.top.n_strands)
+        run_case("hbmult", *write_system(tmp, s), dict(T300, hb_multiplier=3.5), extra="hb_multiplier = 3.5\n")
+
+        # 8: integrator pin, 200 NVE steps of a thermal 12-bp duplex
+        s = G.system_for_config(0, seed=3)
+        run_case("md_nve", *write_system(tmp, s), T300, steps=200, dt=0.003)
+
+
+if __name__ == "__main__":
+    main()
