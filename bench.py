@@ -1,0 +1,353 @@
+"""oxDNA2 MD throughput on one GB300: particle-steps/s of the GPU hot path.
+
+Workload (default): the 40,000-nucleotide plain system -- 1,000 random-sequence 20-bp duplexes
+as ideal B helices at 0.01 nucleotides/unit^3 (cube side 158.74), T = 300 K, 0.5 M salt,
+dt = 0.003, Bussi thermostat (tau = 1000 steps, applied every step), Verlet skin 0.05, FP32
+forces with FP64 integration.  Inputs are generated from a seed (no dataset is involved).
+
+One bench "step" is one timed iteration of M MD steps (default 100) on state resident in HBM;
+L2 is flushed (a 256 MiB write) before every timed iteration, outside the timed interval.
+`value` = nucleotides x MD steps / device time of the K timed iterations.  `e2e` is the same
+metric through the C ABI with host buffers: every iteration uploads the state from host memory,
+runs M steps and downloads the state.  The roofline is that of the force kernel (FP32 CUDA-core
+bound): algorithmic FLOPs per launch (the kernel's own pair physics counted with a counting
+scalar type) / its CUDA-event time, against an FP32 FMA throughput measured on the same GPU.
+
+--impl reference times the CPU implementation of the same path on the host cores: the
+reference's C++ CPU backend is not available on the GPU machine, so this is the FP64 oracle
+restatement (oracle/), all host threads, on a bounded sample of the same workload.
+
+Multi-GPU (torchrun): the plain path does not shard; every rank runs an independent replica
+(weak scaling) and rank 0 reports the summed throughput over the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+WORKLOADS = {
+    "plain40k": dict(cfg=1, scale=1.0, thermostat="bussi", newtonian_steps=1, bussi_tau=1000.0, dt=0.003,
+                     desc="1000 x 20-bp duplexes (40,000 nt), cube 158.74, Bussi tau 1000"),
+    "large250k": dict(cfg=2, scale=1.0, thermostat="john", newtonian_steps=103, diff_coeff=2.5, dt=0.003,
+                      desc="250 x 1000-nt random-walk strands (250,000 nt), cube 232.08, Brownian n=103"),
+    "duplex24": dict(cfg=0, scale=1.0, thermostat="no", newtonian_steps=1, dt=0.005,
+                     desc="one 12-bp duplex (24 nt), cube 20, NVE"),
+}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_system(wl, seed):
+    from oxdna_gb300 import generate as G
+    cache = os.path.join(tempfile.gettempdir(), f"oxgb_{wl['cfg']}_{wl['scale']}_{seed}.npz")
+    if os.path.exists(cache):
+        d = np.load(cache)
+        from oxdna_gb300 import io as oxio
+        top = oxio.Topology(d["n3"], d["n5"], d["btype"], d["type"], d["strand"], int(d["nstr"]))
+        return G.System(float(d["box"]), d["pos"], d["a1"], d["a3"], d["vel"], d["L"], top, float(d["T"]))
+    s = G.system_for_config(wl["cfg"], seed=seed, scale=wl["scale"])
+    np.savez(cache, box=s.box, pos=s.pos, a1=s.a1, a3=s.a3, vel=s.vel, L=s.L, n3=s.top.n3, n5=s.top.n5,
+             btype=s.top.btype, type=s.top.type, strand=s.top.strand, nstr=s.top.n_strands, T=s.T)
+    return s
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(tempfile.gettempdir(), f"oxgb_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = [ln.split(",") for ln in open(self.path).read().strip().split("\n") if ln.strip()]
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def oracle_baseline(sysm_data, wl, nsteps, nthreads):
+    """CPU FP64 oracle: nsteps full MD steps (pair search, forces, integration)."""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+    from oxdna_gb300 import io as oxio
+    s = sysm_data
+    p = oracle.make_params(oracle.make_settings(s.T, 0.5))
+    a1, a2, a3 = s.frames()
+    N = s.N
+    st = dict(pos=s.pos.copy(), quat=oxio.frame_to_quat(a1, a2, a3), vel=s.vel.copy(), Lmom=s.L.copy(),
+              F=np.zeros((N, 3)), T=np.zeros((N, 3)))
+    rc, F, T, Es, Ep = oracle.forces(p, s.pos, a1, a2, a3, s.top.n3, s.top.n5, s.top.type, s.top.btype, s.box,
+                                     nthreads=nthreads)
+    st["F"][:], st["T"][:] = F, T
+    md = oracle.MD()
+    md.dt = wl["dt"]
+    md.thermostat = {"no": 0, "john": 1, "bussi": 2}[wl["thermostat"]]
+    md.newtonian_steps = wl["newtonian_steps"]
+    md.bussi_tau = wl.get("bussi_tau", 1000.0)
+    md.bussi_K_t = 0.5 * 3 * (N - 1) * s.T
+    md.bussi_K_r = 0.5 * 3 * N * s.T
+    md.seed = 1
+    md.pt = 0.01228
+    md.pr = 0.0041
+    t0 = time.perf_counter()
+    oracle.md_run(p, md, st, s.top.n3, s.top.n5, s.top.type, s.top.btype, s.box, 0, nsteps, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return N * nsteps / dt, dt
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference_arm(args, wl):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    s = make_system(wl, args.seed)
+    cores = cpu_cores()
+    per = []
+    nst = max(1, args.cpu_sample_steps)
+    for _ in range(args.warmup):
+        pass  # the oracle has no device warm-up; each timed step is a fresh bounded sample
+    for _ in range(args.steps):
+        v, _dt = oracle_baseline(s, wl, nst, cores)
+        per.append(v)
+    value = float(np.mean(per))
+    line = {"metric": "oxDNA2 MD particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": s.N * nst / value * 1e3 / nst,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": args.workload, "n_nucleotides": s.N, "description": wl["desc"]},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{nst} full MD steps of the {s.N}-nt system per step, FP64 oracle, {cores} threads"},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plain40k", choices=sorted(WORKLOADS))
+    ap.add_argument("--md-steps", type=int, default=100, help="MD steps per timed iteration")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--cpu-sample-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference_arm(args, wl)
+        return
+
+    import torch
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+
+    import oxdna_gb300 as ox
+    from oxdna_gb300 import _abi
+    from oxdna_gb300 import io as oxio
+
+    s = make_system(wl, args.seed + rank)
+    a1, a2, a3 = s.frames()
+    quat = oxio.frame_to_quat(a1, a2, a3)
+    dna = ox.dna2_settings(s.T, 0.5)
+    md = ox.md_settings(dt=wl["dt"], thermostat=wl["thermostat"], newtonian_steps=wl["newtonian_steps"],
+                        bussi_tau=wl.get("bussi_tau", 1000.0), diff_coeff=wl.get("diff_coeff", 2.5), seed=1 + rank,
+                        precision="mixed", steps_per_graph=25)
+    sysm = ox.MDSystem(s.box, s.top, dna, md)
+    sysm.set_state(s.pos, quat, s.vel, s.L)
+    L = _abi.lib()
+    stream = torch.cuda.ExternalStream(sysm.stream)
+    M = args.md_steps
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+    # warm-up
+    for _ in range(args.warmup):
+        sysm.run(M, sync=False)
+    torch.cuda.synchronize()
+    _abi.check(L.oxgb_md_status(sysm.handle))
+    info0 = sysm.info()
+
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sysm.run(M, sync=False)
+            e1.record(stream)
+            times.append((e0, e1))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    _abi.check(L.oxgb_md_status(sysm.handle))
+    info1 = sysm.info()
+    t_dev = sum(a.elapsed_time(b) for a, b in times) * 1e-3
+    if world > 1:
+        tt = torch.tensor([t_dev], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    steps_total = args.steps * M
+    value = world * s.N * steps_total / t_dev
+    rebuilds = info1["rebuilds"] - info0["rebuilds"]
+
+    # force-kernel time on the engine's stream (device-only launches, current state)
+    R = 50
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            _abi.check(L.oxgb_md_launch_forces(sysm.handle))
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(R):
+            _abi.check(L.oxgb_md_launch_forces(sysm.handle))
+        f1.record(stream)
+    torch.cuda.synchronize()
+    t_force = f0.elapsed_time(f1) * 1e-3 / R
+
+    # algorithmic FLOPs of one force launch, from the kernel's own physics on the host
+    st = sysm.get_state()
+    fa1, fa2, fa3 = oxio.quat_to_frame(st["quat"])
+    nnb, nb, cell, ns = sysm.neighbours()
+    tools = C.CDLL(ox.build.TOOLS)
+    dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    tools.oxgb_count_flops.argtypes = [C.c_int, dp, dp, dp, ip, ip, ip, ip, C.c_double, ip, ip, C.c_int, C.c_double,
+                                       C.c_double, dp]
+    out = np.zeros(4)
+    tools.oxgb_count_flops(s.N, np.ascontiguousarray(st["pos"]), np.ascontiguousarray(fa1), np.ascontiguousarray(fa3),
+                           s.top.n3, s.top.n5, s.top.type, s.top.btype, s.box, np.ascontiguousarray(nb.reshape(-1)),
+                           nnb, nb.shape[1], s.T, 0.5, out)
+    flops_launch, sfu_launch, pairs_listed, pairs_in_range = out
+    peak = C.c_double(0)
+    _abi.check(L.oxgb_probe_fp32_peak(C.byref(peak)))
+    achieved = flops_launch / t_force
+
+    # force error of the mixed path on this state against the FP64 oracle (full system)
+    line_extra = {}
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(HERE, "oracle"))
+        import oracle
+        F, T, E, Es = sysm.compute_forces()
+        p = oracle.make_params(oracle.make_settings(s.T, 0.5))
+        rc, Fo, To, Eso, Epo = oracle.forces(p, st["pos"], fa1, fa2, fa3, s.top.n3, s.top.n5, s.top.type,
+                                             s.top.btype, s.box, nthreads=cpu_cores())
+        n = np.linalg.norm(Fo, axis=1)
+        floor = 0.1 * np.sqrt(np.mean(n ** 2))
+        line_extra["force_error_vs_fp64"] = {
+            "normwise": float(np.linalg.norm(F - Fo) / np.linalg.norm(Fo)),
+            "max_per_particle": float(np.max(np.linalg.norm(F - Fo, axis=1) / np.maximum(n, floor))),
+            "torque_normwise": float(np.linalg.norm(T - To) / np.linalg.norm(To)),
+            "energy_rel": float(abs(Es.sum() - Eso.sum()) / abs(Eso.sum()))}
+        cpu_v, cpu_t = oracle_baseline(s, wl, max(1, args.cpu_sample_steps), cpu_cores())
+        line_extra["cpu_baseline"] = {"value": cpu_v, "unit": "particle-steps/s", "cores": cpu_cores(), "kind": "port",
+                                      "sample": f"{args.cpu_sample_steps} full MD steps of the {s.N}-nt system "
+                                                f"(FP64 oracle, {cpu_t:.1f} s)"}
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = dict(pos=np.ascontiguousarray(st["pos"]), quat=np.ascontiguousarray(st["quat"]),
+                    vel=np.ascontiguousarray(st["vel"]), L=np.ascontiguousarray(st["Lmom"]))
+        ne = max(1, min(args.steps, 5))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            sysm.set_state(host["pos"], host["quat"], host["vel"], host["L"])
+            sysm.run(M, sync=True)
+            got = sysm.get_state()
+        t_e2e = time.perf_counter() - t0
+        h2d = s.N * (3 + 4 + 3 + 3) * 8
+        e2e = {"value": world * s.N * M * ne / t_e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": h2d, "md_steps_per_step": M}
+        assert np.all(np.isfinite(got["pos"]))
+
+    launches_per_step = 1 + 1 + 1 + (3 if wl["thermostat"] == "bussi" else (1 if wl["thermostat"] == "john" else 0)) + 1
+    gpu_launches = steps_total * launches_per_step + rebuilds * 7 + args.steps  # + the L2 flush fills (torch)
+    line = {
+        "metric": "oxDNA2 MD particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "n_nucleotides": s.N, "description": wl["desc"], "md_steps_per_step": M,
+                   "l2": "flushed before every timed iteration (256 MiB write)", "precision": "FP32 forces, FP64 state",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "md_steps_per_s": value / (world * s.N),
+        "list_rebuilds": rebuilds,
+        "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak.value, "traffic": None,
+                     "kernel": "k_forces (FP32 mixed)", "flops_per_launch": flops_launch, "sfu_per_launch": sfu_launch,
+                     "launch_ms": t_force * 1e3, "pairs_listed": pairs_listed, "pairs_in_cutoff": pairs_in_range,
+                     "peak_source": "measured FP32 FMA probe on this GPU"},
+        "clocks": clk,
+        "e2e": e2e,
+        "gpu_launches": int(gpu_launches),
+    }
+    line.update(line_extra)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sysm.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

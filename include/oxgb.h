@@ -1,0 +1,210 @@
+/*
+ * oxgb -- GB300-native oxDNA2 molecular-dynamics hot path, C ABI.
+ *
+ * One shared library (liboxgb.so) exports three layers, each the replacement for one of the
+ * reference's plugin surfaces on the GPU MD path (backend = CUDA, interaction_type = DNA2,
+ * CUDA_list = verlet):
+ *
+ *   oxgb_dna2_*   the interaction: oxDNA2 forces, torques and energies on device buffers in
+ *                 the reference's device layout (CUDABaseInteraction,
+ *                 src/CUDA/Interactions/CUDABaseInteraction.h:20-64);
+ *   oxgb_verlet_* the cell-binned Verlet list (CUDABaseList, src/CUDA/Lists/CUDABaseList.h:25-62);
+ *   oxgb_md_*     the MD backend with its integrator and thermostats on host buffers
+ *                 (MD_CUDABackend / CUDAMixedBackend, src/CUDA/Backends/MD_CUDABackend.h:29-93,
+ *                 and CUDABaseThermostat, src/CUDA/Thermostats/CUDABaseThermostat.h:26-49),
+ *                 including batches of independent systems.
+ *
+ * Conventions: every function returns an oxgb_status (0 = success); oxgb_last_error() gives
+ * the message of the last failure on the calling thread.  Lengths are in oxDNA simulation
+ * units, temperatures in simulation units (1 = 3000 K), quaternions are (x, y, z, w) with the
+ * body axes a1, a2, a3 as the columns of their rotation matrix, forces are in the lab frame and
+ * torques in the body frame (the reference's conventions).  Device pointers are passed as
+ * void * and streams as void * (a cudaStream_t, NULL for the legacy default stream).  A handle
+ * may be used by one host thread at a time.  Nothing in this header depends on PyTorch.
+ */
+#ifndef OXGB_H
+#define OXGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum oxgb_status {
+	OXGB_OK = 0,
+	OXGB_E_INVALID = 1,        /* bad argument or call order */
+	OXGB_E_CUDA = 2,           /* a CUDA runtime call failed */
+	OXGB_E_FENE = 3,           /* a backbone bond left the FENE range */
+	OXGB_E_NEIGH_OVERFLOW = 4, /* a neighbour row exceeded its capacity */
+	OXGB_E_NONFINITE = 5,      /* non-finite or huge coordinates (an exploded simulation) */
+	OXGB_E_NOMEM = 6
+} oxgb_status;
+
+/* model settings: the input keys read by DNAInteraction::get_settings and
+ * DNA2Interaction::get_settings (src/Interactions/DNAInteraction.cpp:216-288,
+ * src/Interactions/DNA2Interaction.cpp:62-99) */
+typedef struct oxgb_dna2_settings {
+	double T;                   /* T, simulation units */
+	double salt;                /* salt_concentration (M) */
+	int average;                /* use_average_seq */
+	double seq_stck[4][4];      /* STCK_X_Y of seq_dep_file, X and Y in A G C T order */
+	double seq_stck_fact_eps;   /* STCK_FACT_EPS */
+	double seq_hydr_at;         /* HYDR_A_T */
+	double seq_hydr_gc;         /* HYDR_G_C */
+	double hb_multiplier;       /* hb_multiplier */
+	int dh_half_charged_ends;   /* dh_half_charged_ends */
+	double dh_lambda;           /* dh_lambda */
+	double dh_strength;         /* dh_strength */
+	int use_mbf;                /* max_backbone_force given */
+	double mbf_fmax;            /* max_backbone_force */
+	double mbf_finf;            /* max_backbone_force_far */
+	int reference_cuda_eps;     /* 1: average-sequence well depths of the reference CUDA
+	                               backend (oxDNA1 values, CUDADNAInteraction.cu:61-64);
+	                               0 (default): the oxDNA2 values of the CPU DNA2 class */
+} oxgb_dna2_settings;
+
+/* fills *s with the reference defaults for the given temperature and salt */
+void oxgb_dna2_default_settings(oxgb_dna2_settings *s, double T, double salt);
+
+/* version string of the library */
+const char *oxgb_version(void);
+/* message of the last failure on this thread */
+const char *oxgb_last_error(void);
+
+/* ------------------------------------------------------------------ interaction layer */
+
+typedef struct oxgb_dna2 oxgb_dna2;
+
+/* CUDADNAInteraction::get_settings + cuda_init (src/CUDA/Interactions/CUDADNAInteraction.cu:28-154):
+ * derives the parameter tables and uploads them to the current device */
+int oxgb_dna2_create(const oxgb_dna2_settings *s, oxgb_dna2 **out);
+/* CUDABaseInteraction::get_cuda_rcut: the interaction cutoff (Debye-Hueckel extended) */
+int oxgb_dna2_get_rcut(const oxgb_dna2 *h, double *rcut);
+/* CUDADNAInteraction::_on_T_update (CUDADNAInteraction.cu:156-158): new temperature */
+int oxgb_dna2_set_temperature(oxgb_dna2 *h, double T);
+/*
+ * CUDADNAInteraction::compute_forces (src/CUDA/Interactions/CUDADNAInteraction.cu:165-203) on
+ * the reference's device layout: d_poss float4 (x, y, z, w = int bits btype << 22 | index),
+ * d_orientations float4 quaternions, d_bonds int2 (n3, n5; -1 for none), the neighbour matrix
+ * with element k of nucleotide i at d_matrix_neighs[i * stride_i + k * stride_k] (the reference's
+ * column-major CUDASimpleVerletList layout is stride_i = 1, stride_k = N) and counts in
+ * d_number_neighs.  d_forces / d_torques (float4) arrive initialised by the caller (zeros or
+ * external forces) and are accumulated into: force in the lab frame with w += energy, torque
+ * in the body frame with w = hydrogen-bonding energy, exactly as the reference kernel leaves
+ * them.  box is the cubic box side.  Asynchronous on `stream`.
+ */
+int oxgb_dna2_compute_forces(oxgb_dna2 *h, int N, double box, const void *d_poss, const void *d_orientations,
+		void *d_forces, void *d_torques, const void *d_bonds, const int *d_matrix_neighs, const int *d_number_neighs,
+		int max_neigh, long long stride_i, long long stride_k, void *stream);
+int oxgb_dna2_destroy(oxgb_dna2 *h);
+
+/* ------------------------------------------------------------------ Verlet list layer */
+
+typedef struct oxgb_verlet oxgb_verlet;
+
+/*
+ * CUDASimpleVerletList::get_settings + init (src/CUDA/Lists/CUDASimpleVerletList.cu:44-52,
+ * 165-202): rcut is the interaction cutoff, skin the verlet_skin, the cells per side follow
+ * _compute_N_cells_side (cells_auto_optimisation), max_neigh bounds each neighbour row.
+ */
+int oxgb_verlet_create(int N, double box, double rcut, double skin, int cells_auto_optimisation, int max_neigh,
+		oxgb_verlet **out);
+/*
+ * CUDASimpleVerletList::update (CUDASimpleVerletList.cu:231-289): rebuilds cells and neighbour
+ * rows from d_poss (float4, reference layout), writes d_list_poss, excludes bonded pairs of
+ * d_bonds.  Rows are written row-major (element k of i at i * max_neigh + k).  Asynchronous;
+ * an overflow is reported by oxgb_verlet_status after the stream is synchronised.
+ */
+int oxgb_verlet_update(oxgb_verlet *h, const void *d_poss, void *d_list_poss, const void *d_bonds, void *stream);
+/* device pointers of the neighbour rows (int[N * max_neigh]) and counts (int[N]) */
+int oxgb_verlet_buffers(oxgb_verlet *h, int **d_matrix_neighs, int **d_number_neighs, int *max_neigh, int *n_cells_side);
+int oxgb_verlet_status(oxgb_verlet *h);
+int oxgb_verlet_destroy(oxgb_verlet *h);
+
+/* ------------------------------------------------------------------ MD backend layer */
+
+typedef struct oxgb_md oxgb_md;
+
+enum { OXGB_THERMOSTAT_NONE = 0, OXGB_THERMOSTAT_BROWNIAN = 1, OXGB_THERMOSTAT_BUSSI = 2 };
+enum { OXGB_PRECISION_MIXED = 0, OXGB_PRECISION_DOUBLE = 1 };
+
+/* MDBackend / thermostat input keys (src/Backends/MDBackend.cpp:25-90,
+ * src/Backends/Thermostats/{Brownian,Bussi}Thermostat.cpp get_settings) */
+typedef struct oxgb_md_settings {
+	double dt;                  /* dt */
+	double verlet_skin;         /* verlet_skin */
+	int thermostat;             /* thermostat: none, john/brownian, bussi */
+	int newtonian_steps;        /* newtonian_steps */
+	double pt;                  /* pt (0: derived from diff_coeff) */
+	double diff_coeff;          /* diff_coeff */
+	double bussi_tau;           /* bussi_tau */
+	uint64_t seed;              /* seed of the counter-based random stream */
+	int precision;              /* backend_precision: mixed (FP32 forces, FP64 state) or double */
+	int cells_auto_optimisation;/* cells_auto_optimisation */
+	int max_neigh;              /* neighbour-row capacity; 0 = sized from the first build */
+	int steps_per_graph;        /* MD steps captured per CUDA graph launch (0 = 16) */
+} oxgb_md_settings;
+
+void oxgb_md_default_settings(oxgb_md_settings *s);
+
+/*
+ * A batch of n_systems independent systems in one engine (n_systems = 1 for a plain run).
+ * offsets[n_systems + 1] partitions the N = offsets[n_systems] nucleotides; system k has its own
+ * cubic box box[k] and model settings dna[k] (temperature, salt, ...).  Allocates device memory
+ * on the current device.  MD_CUDABackend::get_settings + init (MD_CUDABackend.cu:621-755).
+ */
+int oxgb_md_create(int n_systems, const int *offsets, const double *box, const oxgb_dna2_settings *dna,
+		const oxgb_md_settings *md, oxgb_md **out);
+/* topology: n3/n5 neighbour indices (global, -1 for none), pairing code btype, base type 0..4 */
+int oxgb_md_set_topology(oxgb_md *h, const int *n3, const int *n5, const int *btype, const int *type);
+/*
+ * MD_CUDABackend::apply_changes_to_simulation_data (MD_CUDABackend.cu:231-313): uploads
+ * positions pos[3N], quaternions quat[4N], velocities vel[3N] and angular momenta L[3N] (body
+ * frame), rebuilds the Verlet lists and computes the forces of this state.
+ */
+int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *quat, const double *vel, const double *L);
+/* MD_CUDABackend::apply_simulation_data_changes (MD_CUDABackend.cu:315-394): downloads the state */
+int oxgb_md_get_state(oxgb_md *h, double *pos, double *quat, double *vel, double *L);
+/* nsteps calls of sim_step (MD_CUDABackend.cu:567-619), replayed as CUDA graphs; returns when
+ * they are enqueued unless sync is set.  The step counter continues across calls. */
+int oxgb_md_run(oxgb_md *h, int nsteps, int sync);
+/* forces (lab, F[3N]), torques (body, T[3N]) and per-nucleotide energies (E[N], every pair term
+ * counted on both nucleotides) of the current state, plus the per-system split into the 8 terms
+ * of the reference's potential_energy observable (E_split[8 * n_systems]: FENE, bonded excluded
+ * volume, stacking, non-bonded excluded volume, hydrogen bonding, cross stacking, coaxial
+ * stacking, Debye-Hueckel).  Any output pointer may be NULL. */
+int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *E, double *E_split);
+/* per-system potential energy (FP64 sum of the per-nucleotide energies / 2) and the
+ * translational and rotational kinetic energies, each double[n_systems] */
+int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r);
+/* new temperature of system k (parameter tables and thermostat) -- the replica-exchange hook */
+int oxgb_md_set_temperature(oxgb_md *h, int k, double T);
+/* neighbour rows of the last list build: counts nnb[N], rows nb[N * max_neigh] (row-major),
+ * cell index of every nucleotide cell[N]; any pointer may be NULL */
+int oxgb_md_neighbours(oxgb_md *h, int *nnb, int *nb, int max_neigh, int *cell, int *n_cells_side);
+/* number of list rebuilds so far, current step counter, neighbour-row capacity */
+int oxgb_md_info(oxgb_md *h, long long *n_rebuilds, long long *step, int *max_neigh);
+/* status bits raised by the kernels since the last call (and clears them): 0 = healthy */
+int oxgb_md_status(oxgb_md *h);
+/* device pointers (for zero-copy callers): FP64 positions, velocities, angular momenta and
+ * quaternions (double4 each), FP32 forces and torques (float4; double4 in double precision) */
+int oxgb_md_device_buffers(oxgb_md *h, void **pos, void **vel, void **L, void **quat, void **F, void **T);
+/* the CUDA stream all of the engine's work runs on */
+void *oxgb_md_stream(oxgb_md *h);
+/* enqueues one force evaluation on the engine's current buffers and lists, device only (the
+ * engine-side equivalent of CUDABaseInteraction::compute_forces; used to time the kernel) */
+int oxgb_md_launch_forces(oxgb_md *h);
+
+/* ------------------------------------------------------------------ diagnostics */
+
+/* measures the FP32 FMA throughput of the current device (FLOP/s) with a register-resident
+ * multiply-add chain, the denominator of the force kernel's roofline */
+int oxgb_probe_fp32_peak(double *flops_per_s);
+int oxgb_md_destroy(oxgb_md *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,912 @@
+// C-ABI layer: parameter upload, buffer ownership, list control and the graph-captured step
+// loop.  The step order is the reference's MD_CUDABackend::sim_step
+// (src/CUDA/Backends/MD_CUDABackend.cu:567-619): first half kick + drift + rotation, list
+// rebuild when any nucleotide moved more than the skin, forces + second half kick, thermostat.
+// Each step is captured once into a CUDA graph (steps_per_graph steps per graph); the list
+// rebuild is a device-side IF conditional node driven by the staleness flag the first-step
+// kernel raises, so a run of many steps needs no host synchronisation at all (the reference
+// synchronises several times per step).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/oxgb.h"
+#include "kernels.h"
+#include "params.h"
+
+using namespace oxgb;
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string &msg) {
+	g_last_error = msg;
+	return code;
+}
+
+#define CK(call)                                                                                                \
+	do {                                                                                                        \
+		cudaError_t _e = (call);                                                                                \
+		if(_e != cudaSuccess) return fail(OXGB_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+	} while(0)
+
+extern "C" const char *oxgb_version(void) { return "oxgb 0.1 (sm_103a)"; }
+extern "C" const char *oxgb_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" void oxgb_dna2_default_settings(oxgb_dna2_settings *s, double T, double salt) { default_settings(s, T, salt); }
+
+extern "C" void oxgb_md_default_settings(oxgb_md_settings *s) {
+	std::memset(s, 0, sizeof(*s));
+	s->dt = 0.003;
+	s->verlet_skin = 0.05;
+	s->thermostat = OXGB_THERMOSTAT_NONE;
+	s->newtonian_steps = 103;
+	s->diff_coeff = 2.5;
+	s->bussi_tau = 1000;
+	s->seed = 1;
+	s->precision = OXGB_PRECISION_MIXED;
+	s->cells_auto_optimisation = 1;
+	s->steps_per_graph = 16;
+}
+
+static int status_to_code(int st) {
+	if(st & OXGB_ERR_NONFINITE) return OXGB_E_NONFINITE;
+	if(st & OXGB_ERR_FENE) return OXGB_E_FENE;
+	if(st & OXGB_ERR_NEIGH_OVERFLOW) return OXGB_E_NEIGH_OVERFLOW;
+	if(st & OXGB_ERR_CELL) return OXGB_E_NONFINITE;
+	return OXGB_OK;
+}
+
+static std::string status_message(int st) {
+	std::string m;
+	if(st & OXGB_ERR_FENE) m += "a backbone bond left the FENE range; ";
+	if(st & OXGB_ERR_NEIGH_OVERFLOW) m += "a neighbour row overflowed its capacity (raise max_neigh); ";
+	if(st & OXGB_ERR_NONFINITE) m += "non-finite or huge coordinates (the simulation exploded); ";
+	if(st & OXGB_ERR_CELL) m += "cell index out of range; ";
+	return m;
+}
+
+// ====================================================================== interaction layer
+
+struct oxgb_dna2 {
+	oxgb_dna2_settings s;
+	DNA2Table<double> tab64;
+	double rcut;
+	double box_uploaded;
+	DNA2Table<float> *d_tab;
+	int *d_status;
+};
+
+static int dna2_upload(oxgb_dna2 *h, double box) {
+	if(build_table(h->s, box, h->tab64, h->rcut)) return fail(OXGB_E_INVALID, "invalid interaction settings");
+	DNA2Table<float> f;
+	to_float(h->tab64, box, f);
+	CK(cudaMemcpy(h->d_tab, &f, sizeof(f), cudaMemcpyHostToDevice));
+	h->box_uploaded = box;
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_dna2_create(const oxgb_dna2_settings *s, oxgb_dna2 **out) {
+	if(!s || !out) return fail(OXGB_E_INVALID, "null argument");
+	oxgb_dna2 *h = new oxgb_dna2();
+	h->s = *s;
+	h->box_uploaded = -1;
+	if(build_table(h->s, 1.0, h->tab64, h->rcut)) {
+		delete h;
+		return fail(OXGB_E_INVALID, "invalid interaction settings");
+	}
+	if(cudaMalloc(&h->d_tab, sizeof(DNA2Table<float>)) != cudaSuccess || cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess) {
+		delete h;
+		return fail(OXGB_E_CUDA, "cudaMalloc failed");
+	}
+	cudaMemset(h->d_status, 0, sizeof(int));
+	*out = h;
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_dna2_get_rcut(const oxgb_dna2 *h, double *rcut) {
+	if(!h || !rcut) return fail(OXGB_E_INVALID, "null argument");
+	*rcut = h->rcut;
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_dna2_set_temperature(oxgb_dna2 *h, double T) {
+	if(!h || !(T > 0)) return fail(OXGB_E_INVALID, "invalid temperature");
+	h->s.T = T;
+	h->box_uploaded = -1;
+	if(build_table(h->s, 1.0, h->tab64, h->rcut)) return fail(OXGB_E_INVALID, "invalid interaction settings");
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_dna2_compute_forces(oxgb_dna2 *h, int N, double box, const void *d_poss, const void *d_orientations,
+		void *d_forces, void *d_torques, const void *d_bonds, const int *d_matrix_neighs, const int *d_number_neighs,
+		int max_neigh, long long stride_i, long long stride_k, void *stream) {
+	if(!h || N < 0 || !(box > 0)) return fail(OXGB_E_INVALID, "invalid argument");
+	if(N == 0) return OXGB_OK;
+	if(!d_poss || !d_orientations || !d_forces || !d_torques || !d_bonds || !d_matrix_neighs || !d_number_neighs)
+		return fail(OXGB_E_INVALID, "null device buffer");
+	if(box != h->box_uploaded) {
+		int rc = dna2_upload(h, box);
+		if(rc) return rc;
+	}
+	ForceArgs a{};
+	a.N = N;
+	a.pos_hi = (const float4 *) d_poss;
+	a.quat = (const float4 *) d_orientations;
+	a.bonds = (const int2 *) d_bonds;
+	a.nb = d_matrix_neighs;
+	a.nnb = d_number_neighs;
+	a.max_nb = max_neigh;
+	a.nb_stride_i = stride_i;
+	a.nb_stride_k = stride_k;
+	a.forces = d_forces;
+	a.torques = d_torques;
+	a.table = h->d_tab;
+	a.status = h->d_status;
+	CK(launch_forces_reference_layout(a, (cudaStream_t) stream));
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_dna2_destroy(oxgb_dna2 *h) {
+	if(!h) return OXGB_OK;
+	cudaFree(h->d_tab);
+	cudaFree(h->d_status);
+	delete h;
+	return OXGB_OK;
+}
+
+// ====================================================================== Verlet list layer
+
+struct ListBuffers {
+	int n_side = 0, n_cells = 0, max_nb = 0, N = 0;
+	int *cell_of = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_cursor = nullptr, *cell_list = nullptr;
+	int *nb = nullptr, *nnb = nullptr;
+
+	int alloc(int N_, int n_side_, int max_nb_) {
+		free_all();
+		N = N_;
+		n_side = n_side_;
+		n_cells = n_side * n_side * n_side;
+		max_nb = max_nb_;
+		CK(cudaMalloc(&cell_of, sizeof(int) * std::max(N, 1)));
+		CK(cudaMalloc(&cell_count, sizeof(int) * n_cells));
+		CK(cudaMalloc(&cell_start, sizeof(int) * (n_cells + 1)));
+		CK(cudaMalloc(&cell_cursor, sizeof(int) * n_cells));
+		CK(cudaMalloc(&cell_list, sizeof(int) * std::max(N, 1)));
+		CK(cudaMalloc(&nb, sizeof(int) * (size_t) std::max(N, 1) * max_nb));
+		CK(cudaMalloc(&nnb, sizeof(int) * std::max(N, 1)));
+		return OXGB_OK;
+	}
+	void free_all() {
+		for(int **p : {&cell_of, &cell_count, &cell_start, &cell_cursor, &cell_list, &nb, &nnb}) {
+			if(*p) cudaFree(*p);
+			*p = nullptr;
+		}
+	}
+};
+
+struct oxgb_verlet {
+	int N;
+	double box, rcut, skin;
+	bool auto_opt;
+	float rverlet;
+	ListBuffers lb;
+	int *d_status, *d_flag;
+};
+
+extern "C" int oxgb_verlet_create(int N, double box, double rcut, double skin, int cells_auto_optimisation, int max_neigh,
+		oxgb_verlet **out) {
+	if(N <= 0 || !(box > 0) || !(rcut > 0) || skin < 0 || !out) return fail(OXGB_E_INVALID, "invalid argument");
+	oxgb_verlet *h = new oxgb_verlet();
+	h->N = N;
+	h->box = box;
+	h->rcut = rcut;
+	h->skin = skin;
+	h->auto_opt = cells_auto_optimisation != 0;
+	h->rverlet = (float) rcut + 2.f * (float) skin;
+	int cap = max_neigh > 0 ? max_neigh : std::min(N, 256);
+	int n_side = cells_per_side(N, (float) box, h->rverlet, h->auto_opt);
+	int rc = h->lb.alloc(N, n_side, cap);
+	if(rc || cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess || cudaMalloc(&h->d_flag, sizeof(int)) != cudaSuccess) {
+		h->lb.free_all();
+		delete h;
+		return rc ? rc : fail(OXGB_E_CUDA, "cudaMalloc failed");
+	}
+	cudaMemset(h->d_status, 0, sizeof(int));
+	cudaMemset(h->d_flag, 0, sizeof(int));
+	*out = h;
+	return OXGB_OK;
+}
+
+static ListArgs list_args(ListBuffers &lb, int N, const float4 *pos, float box, float rverlet, const int2 *bonds,
+		float4 *list_pos, int *status, int *flag, int check_flag) {
+	ListArgs a{};
+	a.N = N;
+	a.pos = pos;
+	a.box = box;
+	a.rverlet2 = rverlet * rverlet;
+	a.n_side = lb.n_side;
+	a.bonds = bonds;
+	a.cell_of = lb.cell_of;
+	a.cell_count = lb.cell_count;
+	a.cell_start = lb.cell_start;
+	a.cell_cursor = lb.cell_cursor;
+	a.cell_list = lb.cell_list;
+	a.nb = lb.nb;
+	a.nnb = lb.nnb;
+	a.max_nb = lb.max_nb;
+	a.list_pos = list_pos;
+	a.status = status;
+	a.flag = flag;
+	a.check_flag = check_flag;
+	a.rebuilds = nullptr;
+	return a;
+}
+
+extern "C" int oxgb_verlet_update(oxgb_verlet *h, const void *d_poss, void *d_list_poss, const void *d_bonds, void *stream) {
+	if(!h || !d_poss || !d_list_poss || !d_bonds) return fail(OXGB_E_INVALID, "null argument");
+	ListArgs a = list_args(h->lb, h->N, (const float4 *) d_poss, (float) h->box, h->rverlet, (const int2 *) d_bonds,
+			(float4 *) d_list_poss, h->d_status, h->d_flag, 0);
+	CK(launch_list_build(a, (cudaStream_t) stream));
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_verlet_buffers(oxgb_verlet *h, int **d_matrix_neighs, int **d_number_neighs, int *max_neigh, int *n_cells_side) {
+	if(!h) return fail(OXGB_E_INVALID, "null handle");
+	if(d_matrix_neighs) *d_matrix_neighs = h->lb.nb;
+	if(d_number_neighs) *d_number_neighs = h->lb.nnb;
+	if(max_neigh) *max_neigh = h->lb.max_nb;
+	if(n_cells_side) *n_cells_side = h->lb.n_side;
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_verlet_status(oxgb_verlet *h) {
+	if(!h) return fail(OXGB_E_INVALID, "null handle");
+	int st = 0;
+	CK(cudaMemcpy(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+	CK(cudaMemset(h->d_status, 0, sizeof(int)));
+	if(st) return fail(status_to_code(st), status_message(st));
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_verlet_destroy(oxgb_verlet *h) {
+	if(!h) return OXGB_OK;
+	h->lb.free_all();
+	cudaFree(h->d_status);
+	cudaFree(h->d_flag);
+	delete h;
+	return OXGB_OK;
+}
+
+// ====================================================================== MD backend layer
+
+struct oxgb_md {
+	int n_systems = 0, N = 0;
+	std::vector<int> offsets;
+	std::vector<double> box;
+	std::vector<oxgb_dna2_settings> dna;
+	oxgb_md_settings md{};
+	bool dbl = false;
+	double rcut = 0;
+	float rverlet = 0;
+
+	std::vector<int> h_n3, h_n5, h_btype, h_type;
+	bool have_topology = false, have_state = false;
+
+	double4_32a *posd = nullptr, *veld = nullptr, *Ld = nullptr, *quatd = nullptr;
+	float4 *pos_hi = nullptr, *pos_lo = nullptr, *fa1 = nullptr, *fa3 = nullptr, *list_pos = nullptr;
+	int2 *bonds = nullptr;
+	void *F = nullptr, *T = nullptr;
+	void *d_tab = nullptr;
+	ListBuffers lb;
+	int *status = nullptr, *flag = nullptr;
+	long long *step = nullptr;
+	double *esplit = nullptr, *scratch = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
+	int bussi_blocks = 0;
+	double pt = 0, pr = 0;
+
+	cudaStream_t stream = nullptr, side = nullptr;
+	cudaGraphExec_t gexec = nullptr;
+	int graph_steps = 0;
+	bool conditional_ok = true;
+	long long host_step = 0, n_rebuilds = 0;
+	unsigned long long *d_rebuilds = nullptr;
+
+	~oxgb_md() {
+		if(gexec) cudaGraphExecDestroy(gexec);
+		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
+					(void *) list_pos, (void *) bonds, F, T, d_tab, (void *) status, (void *) flag, (void *) step,
+					(void *) esplit, (void *) scratch, (void *) bussi_partials, (void *) bussi_state, (void *) d_rebuilds})
+			if(p) cudaFree(p);
+		lb.free_all();
+		if(stream) cudaStreamDestroy(stream);
+		if(side) cudaStreamDestroy(side);
+	}
+};
+
+static StepArgs step_args(oxgb_md *h) {
+	StepArgs a{};
+	a.N = h->N;
+	a.dt = h->md.dt;
+	a.pos = h->posd;
+	a.vel = h->veld;
+	a.angmom = h->Ld;
+	a.quat = h->quatd;
+	a.pos_hi = h->pos_hi;
+	a.pos_lo = h->pos_lo;
+	a.fa1 = h->fa1;
+	a.fa3 = h->fa3;
+	a.forces = h->F;
+	a.torques = h->T;
+	a.list_pos = h->list_pos;
+	a.skin2 = (float) h->md.verlet_skin * (float) h->md.verlet_skin;
+	a.flag = h->flag;
+	a.status = h->status;
+	a.step = h->step;
+	a.thermostat = h->md.thermostat;
+	a.newtonian_steps = h->md.newtonian_steps > 0 ? h->md.newtonian_steps : 1;
+	a.pt = h->pt;
+	a.pr = h->pr;
+	a.T = h->dna[0].T;
+	a.sqrtT = std::sqrt(h->dna[0].T);
+	a.seed = h->md.seed;
+	a.bussi_c = std::exp(-(double) a.newtonian_steps / h->md.bussi_tau);
+	a.bussi_partials = h->bussi_partials;
+	a.bussi_state = h->bussi_state;
+	a.bussi_blocks = h->bussi_blocks;
+	return a;
+}
+
+static ForceArgs force_args(oxgb_md *h) {
+	ForceArgs a{};
+	a.N = h->N;
+	a.pos_hi = h->pos_hi;
+	a.pos_lo = h->pos_lo;
+	a.fa1 = h->fa1;
+	a.fa3 = h->fa3;
+	a.posd = h->posd;
+	a.quatd = h->quatd;
+	a.bonds = h->bonds;
+	a.nb = h->lb.nb;
+	a.nnb = h->lb.nnb;
+	a.max_nb = h->lb.max_nb;
+	a.nb_stride_i = h->lb.max_nb;
+	a.nb_stride_k = 1;
+	a.forces = h->F;
+	a.torques = h->T;
+	a.table = h->d_tab;
+	a.status = h->status;
+	a.esplit = h->esplit;
+	a.dt = h->md.dt;
+	a.vel = h->veld;
+	a.angmom = h->Ld;
+	return a;
+}
+
+static int upload_tables(oxgb_md *h) {
+	DNA2Table<double> t64;
+	double rc;
+	if(build_table(h->dna[0], h->box[0], t64, rc)) return fail(OXGB_E_INVALID, "invalid interaction settings");
+	h->rcut = rc;
+	if(h->dbl) {
+		CK(cudaMemcpy(h->d_tab, &t64, sizeof(t64), cudaMemcpyHostToDevice));
+	}
+	else {
+		DNA2Table<float> t32;
+		to_float(t64, h->box[0], t32);
+		CK(cudaMemcpy(h->d_tab, &t32, sizeof(t32), cudaMemcpyHostToDevice));
+	}
+	// Brownian probabilities (src/Backends/Thermostats/BrownianThermostat.cpp:43-54); dt and
+	// diff_coeff are read as floats there
+	const double T = h->dna[0].T;
+	const double dtf = (float) h->md.dt;
+	const int n = h->md.newtonian_steps > 0 ? h->md.newtonian_steps : 1;
+	double pt = h->md.pt > 0 ? (double) (float) h->md.pt : (2 * T * n * dtf) / (T * n * dtf + 2 * (double) (float) h->md.diff_coeff);
+	if(pt > 1.0) return fail(OXGB_E_INVALID, "pt must be smaller than 1");
+	const double D = T * n * dtf * (1. / pt - 1. / 2.);
+	h->pt = pt;
+	h->pr = (2 * T * n * dtf) / (T * n * dtf + 2 * 3 * D);
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *box, const oxgb_dna2_settings *dna,
+		const oxgb_md_settings *md, oxgb_md **out) {
+	if(n_systems < 1 || !offsets || !box || !dna || !md || !out) return fail(OXGB_E_INVALID, "null argument");
+	if(n_systems != 1) return fail(OXGB_E_INVALID, "this engine runs one system per handle; use the batched engine");
+	const int N = offsets[n_systems] - offsets[0];
+	if(offsets[0] != 0 || N <= 0 || N >= (1 << 22)) return fail(OXGB_E_INVALID, "invalid offsets (1 <= N < 2^22)");
+	if(!(md->dt > 0) || md->verlet_skin < 0) return fail(OXGB_E_INVALID, "invalid dt or verlet_skin");
+	oxgb_md *h = new oxgb_md();
+	h->n_systems = n_systems;
+	h->N = N;
+	h->offsets.assign(offsets, offsets + n_systems + 1);
+	h->box.assign(box, box + n_systems);
+	h->dna.assign(dna, dna + n_systems);
+	h->md = *md;
+	if(h->md.steps_per_graph <= 0) h->md.steps_per_graph = 16;
+	h->dbl = md->precision == OXGB_PRECISION_DOUBLE;
+	const size_t v4 = h->dbl ? sizeof(double4_32a) : sizeof(float4);
+	auto bail = [&](int rc) {
+		delete h;
+		return rc;
+	};
+	if(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+			cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess)
+		return bail(fail(OXGB_E_CUDA, "stream creation failed"));
+	bool ok = true;
+	ok &= cudaMalloc(&h->posd, sizeof(double4_32a) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->veld, sizeof(double4_32a) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->Ld, sizeof(double4_32a) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->quatd, sizeof(double4_32a) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->pos_hi, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->pos_lo, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->fa1, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->fa3, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->list_pos, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->bonds, sizeof(int2) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->F, v4 * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->T, v4 * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_tab, h->dbl ? sizeof(DNA2Table<double>) : sizeof(DNA2Table<float>)) == cudaSuccess;
+	ok &= cudaMalloc(&h->status, sizeof(int)) == cudaSuccess;
+	ok &= cudaMalloc(&h->flag, sizeof(int)) == cudaSuccess;
+	ok &= cudaMalloc(&h->step, sizeof(long long)) == cudaSuccess;
+	ok &= cudaMalloc(&h->esplit, sizeof(double) * 8 * n_systems) == cudaSuccess;
+	ok &= cudaMalloc(&h->scratch, sizeof(double) * 8 * n_systems) == cudaSuccess;
+	h->bussi_blocks = std::max(1, std::min(1024, (N + 255) / 256));
+	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * h->bussi_blocks) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 8) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
+	if(!ok) return bail(fail(OXGB_E_NOMEM, "device allocation failed"));
+	cudaMemset(h->status, 0, sizeof(int));
+	cudaMemset(h->flag, 0, sizeof(int));
+	cudaMemset(h->step, 0, sizeof(long long));
+	cudaMemset(h->d_rebuilds, 0, sizeof(unsigned long long));
+	int rc = upload_tables(h);
+	if(rc) return bail(rc);
+	h->rverlet = (float) h->rcut + 2.f * (float) h->md.verlet_skin;
+	const int n_side = cells_per_side(N, (float) h->box[0], h->rverlet, h->md.cells_auto_optimisation != 0);
+	const int cap = md->max_neigh > 0 ? md->max_neigh : std::min(std::max(N - 1, 1), 512);
+	rc = h->lb.alloc(N, n_side, cap);
+	if(rc) return bail(rc);
+	// Bussi running kinetic energies start at their targets (BussiThermostat::init)
+	double bs[8] = {0.5 * 3 * (N - 1) * h->dna[0].T, 0.5 * 3 * N * h->dna[0].T, 1, 1, 0, 0, 0, 0};
+	if(cudaMemcpy(h->bussi_state, bs, sizeof(bs), cudaMemcpyHostToDevice) != cudaSuccess) return bail(fail(OXGB_E_CUDA, "upload"));
+	*out = h;
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_set_topology(oxgb_md *h, const int *n3, const int *n5, const int *btype, const int *type) {
+	if(!h || !n3 || !n5 || !btype || !type) return fail(OXGB_E_INVALID, "null argument");
+	const int N = h->N;
+	std::vector<int2> b(N);
+	for(int i = 0; i < N; i++) {
+		if(n3[i] < -1 || n3[i] >= N || n5[i] < -1 || n5[i] >= N || n3[i] == i || n5[i] == i)
+			return fail(OXGB_E_INVALID, "topology: bonded neighbour index out of range");
+		if(btype[i] < -512 || btype[i] > 511) return fail(OXGB_E_INVALID, "topology: btype outside [-512, 511]");
+		if(type[i] < 0 || type[i] > 4) return fail(OXGB_E_INVALID, "topology: base type outside 0..4");
+		b[i] = make_int2(n3[i], n5[i]);
+	}
+	for(int i = 0; i < N; i++) {
+		if(n3[i] >= 0 && n5[n3[i]] != i) return fail(OXGB_E_INVALID, "topology: n3/n5 are not mutual");
+	}
+	h->h_n3.assign(n3, n3 + N);
+	h->h_n5.assign(n5, n5 + N);
+	h->h_btype.assign(btype, btype + N);
+	h->h_type.assign(type, type + N);
+	CK(cudaMemcpy(h->bonds, b.data(), sizeof(int2) * N, cudaMemcpyHostToDevice));
+	h->have_topology = true;
+	return OXGB_OK;
+}
+
+static ListArgs md_list_args(oxgb_md *h, int check_flag) {
+	ListArgs a = list_args(h->lb, h->N, h->pos_hi, (float) h->box[0], h->rverlet, h->bonds, h->list_pos, h->status, h->flag,
+			check_flag);
+	a.rebuilds = h->d_rebuilds;
+	return a;
+}
+
+static int build_list_now(oxgb_md *h) {
+	ListArgs a = md_list_args(h, 0);
+	CK(launch_list_build(a, h->stream));
+	return OXGB_OK;
+}
+
+static int compute_forces_now(oxgb_md *h, bool split) {
+	ForceArgs fa = force_args(h);
+	if(split) CK(cudaMemsetAsync(h->esplit, 0, sizeof(double) * 8, h->stream));
+	if(h->dbl) CK(launch_forces_double(fa, split, false, h->stream));
+	else CK(launch_forces_mixed(fa, split, false, h->stream));
+	return OXGB_OK;
+}
+
+static int read_status(oxgb_md *h) {
+	int st = 0;
+	CK(cudaMemcpyAsync(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+	CK(cudaStreamSynchronize(h->stream));
+	if(st) {
+		CK(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
+		CK(cudaStreamSynchronize(h->stream));
+		return fail(status_to_code(st), status_message(st));
+	}
+	return OXGB_OK;
+}
+
+// first build with a provisional row capacity, then size the rows from the densest one
+static int size_and_build_list(oxgb_md *h) {
+	int rc = build_list_now(h);
+	if(rc) return rc;
+	if(h->md.max_neigh > 0) return read_status(h);
+	std::vector<int> cnt(h->N);
+	CK(cudaMemcpyAsync(cnt.data(), h->lb.nnb, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
+	CK(cudaStreamSynchronize(h->stream));
+	const int mx = *std::max_element(cnt.begin(), cnt.end());
+	int want = ((std::max(64, mx + mx / 2 + 32) + 31) / 32) * 32;
+	if(want != h->lb.max_nb) {
+		if(h->gexec) {
+			cudaGraphExecDestroy(h->gexec);
+			h->gexec = nullptr;
+		}
+		rc = h->lb.alloc(h->N, h->lb.n_side, want);
+		if(rc) return rc;
+		CK(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
+		rc = build_list_now(h);
+		if(rc) return rc;
+	}
+	else {
+		CK(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
+	}
+	return read_status(h);
+}
+
+extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *quat, const double *vel, const double *L) {
+	if(!h || !pos || !quat || !vel || !L) return fail(OXGB_E_INVALID, "null argument");
+	if(!h->have_topology) return fail(OXGB_E_INVALID, "set the topology first");
+	const int N = h->N;
+	std::vector<double4_32a> p(N), q(N), v(N), l(N);
+	std::vector<float4> hi(N), lo(N);
+	for(int i = 0; i < N; i++) {
+		p[i] = make_double4_32a(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
+		double n = std::sqrt(quat[4 * i] * quat[4 * i] + quat[4 * i + 1] * quat[4 * i + 1] + quat[4 * i + 2] * quat[4 * i + 2] +
+				quat[4 * i + 3] * quat[4 * i + 3]);
+		if(!(n > 0.5)) return fail(OXGB_E_INVALID, "quaternion of nucleotide " + std::to_string(i) + " is not normalisable");
+		q[i] = make_double4_32a(quat[4 * i] / n, quat[4 * i + 1] / n, quat[4 * i + 2] / n, quat[4 * i + 3] / n);
+		v[i] = make_double4_32a(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.0);
+		l[i] = make_double4_32a(L[3 * i], L[3 * i + 1], L[3 * i + 2], 0.0);
+		int packed = (h->h_btype[i] << 22) | (i & 0x003FFFFF);
+		float w;
+		std::memcpy(&w, &packed, 4);
+		hi[i] = make_float4(0.f, 0.f, 0.f, w);
+		int t = h->h_type[i];
+		float tw;
+		std::memcpy(&tw, &t, 4);
+		lo[i] = make_float4(0.f, 0.f, 0.f, tw);
+	}
+	CK(cudaMemcpyAsync(h->posd, p.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
+	CK(cudaMemcpyAsync(h->quatd, q.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
+	CK(cudaMemcpyAsync(h->veld, v.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
+	CK(cudaMemcpyAsync(h->Ld, l.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
+	CK(cudaMemcpyAsync(h->pos_hi, hi.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
+	CK(cudaMemcpyAsync(h->pos_lo, lo.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
+	StepArgs sa = step_args(h);
+	CK(launch_make_mirrors(sa, h->stream));
+	int rc = size_and_build_list(h);
+	if(rc) return rc;
+	rc = compute_forces_now(h, false);
+	if(rc) return rc;
+	h->have_state = true;
+	return read_status(h);
+}
+
+extern "C" int oxgb_md_get_state(oxgb_md *h, double *pos, double *quat, double *vel, double *L) {
+	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
+	const int N = h->N;
+	std::vector<double4_32a> buf(N);
+	struct {
+		double *dst;
+		double4_32a *src;
+		int width;
+	} items[4] = {{pos, h->posd, 3}, {quat, h->quatd, 4}, {vel, h->veld, 3}, {L, h->Ld, 3}};
+	for(auto &it : items) {
+		if(!it.dst) continue;
+		CK(cudaMemcpyAsync(buf.data(), it.src, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost, h->stream));
+		CK(cudaStreamSynchronize(h->stream));
+		for(int i = 0; i < N; i++) {
+			const double c[4] = {buf[i].x, buf[i].y, buf[i].z, buf[i].w};
+			for(int k = 0; k < it.width; k++) it.dst[it.width * i + k] = c[k];
+		}
+	}
+	return OXGB_OK;
+}
+
+// one MD step on h->stream (captured into the graph)
+static int enqueue_step(oxgb_md *h, cudaGraph_t capturing) {
+	StepArgs sa = step_args(h);
+	CK(launch_first_step(sa, h->dbl, h->stream));
+	ListArgs la = md_list_args(h, h->conditional_ok ? 0 : 1);
+	if(h->conditional_ok) {
+		cudaGraphConditionalHandle hc;
+		CK(cudaGraphConditionalHandleCreate(&hc, capturing, 0, cudaGraphCondAssignDefault));
+		CK(launch_set_conditional(h->flag, hc, h->stream));
+		cudaStreamCaptureStatus cs;
+		const cudaGraphNode_t *deps = nullptr;
+		size_t ndeps = 0;
+		cudaGraph_t g;
+		CK(cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+		cudaGraphNodeParams cp{};
+		cp.type = cudaGraphNodeTypeConditional;
+		cp.conditional.handle = hc;
+		cp.conditional.type = cudaGraphCondTypeIf;
+		cp.conditional.size = 1;
+		cudaGraphNode_t node;
+		CK(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+		cudaGraph_t body = cp.conditional.phGraph_out[0];
+		CK(cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+		cudaError_t e1 = launch_list_build(la, h->side);
+		cudaGraph_t tmp;
+		cudaError_t e2 = cudaStreamEndCapture(h->side, &tmp);
+		CK(e1);
+		CK(e2);
+		CK(cudaStreamUpdateCaptureDependencies(h->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+	}
+	else {
+		CK(launch_list_build(la, h->stream));
+	}
+	ForceArgs fa = force_args(h);
+	if(h->dbl) CK(launch_forces_double(fa, false, true, h->stream));
+	else CK(launch_forces_mixed(fa, false, true, h->stream));
+	CK(launch_thermostat(sa, h->stream));
+	CK(launch_step_advance(sa, h->stream));
+	return OXGB_OK;
+}
+
+static int build_graph(oxgb_md *h) {
+	if(h->gexec) {
+		cudaGraphExecDestroy(h->gexec);
+		h->gexec = nullptr;
+	}
+	const int K = h->md.steps_per_graph;
+	for(int attempt = 0; attempt < 2; attempt++) {
+		cudaGraph_t g;
+		CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
+		cudaStreamCaptureStatus cs;
+		cudaGraph_t cap;
+		CK(cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &cap, nullptr, nullptr, nullptr));
+		int rc = OXGB_OK;
+		for(int k = 0; k < K && rc == OXGB_OK; k++) rc = enqueue_step(h, cap);
+		cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+		if(rc == OXGB_OK && ee == cudaSuccess) {
+			cudaError_t ie = cudaGraphInstantiate(&h->gexec, g, 0);
+			cudaGraphDestroy(g);
+			if(ie == cudaSuccess) {
+				h->graph_steps = K;
+				return OXGB_OK;
+			}
+			rc = fail(OXGB_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+		}
+		else if(ee == cudaSuccess) {
+			cudaGraphDestroy(g);
+		}
+		cudaGetLastError();
+		if(!h->conditional_ok) return rc ? rc : fail(OXGB_E_CUDA, "graph capture failed");
+		// fall back to always-launched rebuild kernels that exit early on a fresh list
+		h->conditional_ok = false;
+	}
+	return fail(OXGB_E_CUDA, "graph capture failed");
+}
+
+extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
+	if(!h || !h->have_state || nsteps < 0) return fail(OXGB_E_INVALID, "invalid call");
+	if(!h->gexec) {
+		int rc = build_graph(h);
+		if(rc) return rc;
+	}
+	int done = 0;
+	while(done + h->graph_steps <= nsteps) {
+		CK(cudaGraphLaunch(h->gexec, h->stream));
+		done += h->graph_steps;
+	}
+	// remainder, eagerly
+	for(; done < nsteps; done++) {
+		StepArgs sa = step_args(h);
+		CK(launch_first_step(sa, h->dbl, h->stream));
+		ListArgs la = md_list_args(h, 1);
+		CK(launch_list_build(la, h->stream));
+		ForceArgs fa = force_args(h);
+		if(h->dbl) CK(launch_forces_double(fa, false, true, h->stream));
+		else CK(launch_forces_mixed(fa, false, true, h->stream));
+		CK(launch_thermostat(sa, h->stream));
+		CK(launch_step_advance(sa, h->stream));
+	}
+	h->host_step += nsteps;
+	if(sync) return read_status(h);
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *E, double *E_split) {
+	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
+	int rc = build_list_now(h);
+	if(rc) return rc;
+	rc = compute_forces_now(h, true);
+	if(rc) return rc;
+	rc = read_status(h);
+	if(rc) return rc;
+	const int N = h->N;
+	if(h->dbl) {
+		std::vector<double4_32a> f(N), t(N);
+		CK(cudaMemcpy(f.data(), h->F, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(t.data(), h->T, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
+		for(int i = 0; i < N; i++) {
+			if(F) F[3 * i] = f[i].x, F[3 * i + 1] = f[i].y, F[3 * i + 2] = f[i].z;
+			if(T) T[3 * i] = t[i].x, T[3 * i + 1] = t[i].y, T[3 * i + 2] = t[i].z;
+			if(E) E[i] = f[i].w;
+		}
+	}
+	else {
+		std::vector<float4> f(N), t(N);
+		CK(cudaMemcpy(f.data(), h->F, sizeof(float4) * N, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(t.data(), h->T, sizeof(float4) * N, cudaMemcpyDeviceToHost));
+		for(int i = 0; i < N; i++) {
+			if(F) F[3 * i] = f[i].x, F[3 * i + 1] = f[i].y, F[3 * i + 2] = f[i].z;
+			if(T) T[3 * i] = t[i].x, T[3 * i + 1] = t[i].y, T[3 * i + 2] = t[i].z;
+			if(E) E[i] = f[i].w;
+		}
+	}
+	if(E_split) CK(cudaMemcpy(E_split, h->esplit, sizeof(double) * 8, cudaMemcpyDeviceToHost));
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r) {
+	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
+	CK(cudaStreamSynchronize(h->stream));
+	const int N = h->N;
+	if(U) {
+		double u = 0;
+		if(h->dbl) {
+			std::vector<double4_32a> f(N);
+			CK(cudaMemcpy(f.data(), h->F, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
+			for(int i = 0; i < N; i++) u += f[i].w;
+		}
+		else {
+			std::vector<float4> f(N);
+			CK(cudaMemcpy(f.data(), h->F, sizeof(float4) * N, cudaMemcpyDeviceToHost));
+			for(int i = 0; i < N; i++) u += f[i].w;
+		}
+		*U = 0.5 * u;
+	}
+	if(K_t || K_r) {
+		StepArgs sa = step_args(h);
+		CK(launch_kinetic(sa, h->scratch, h->stream));
+		double k[2];
+		CK(cudaMemcpyAsync(k, h->scratch, sizeof(k), cudaMemcpyDeviceToHost, h->stream));
+		CK(cudaStreamSynchronize(h->stream));
+		if(K_t) *K_t = k[0];
+		if(K_r) *K_r = k[1];
+	}
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_set_temperature(oxgb_md *h, int k, double T) {
+	if(!h || k < 0 || k >= h->n_systems || !(T > 0)) return fail(OXGB_E_INVALID, "invalid argument");
+	CK(cudaStreamSynchronize(h->stream));
+	h->dna[k].T = T;
+	int rc = upload_tables(h);
+	if(rc) return rc;
+	if(h->gexec) {  // the thermostat parameters are baked into the captured kernels
+		cudaGraphExecDestroy(h->gexec);
+		h->gexec = nullptr;
+	}
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_neighbours(oxgb_md *h, int *nnb, int *nb, int max_neigh, int *cell, int *n_cells_side) {
+	if(!h) return fail(OXGB_E_INVALID, "null handle");
+	CK(cudaStreamSynchronize(h->stream));
+	const int N = h->N;
+	if(nnb) CK(cudaMemcpy(nnb, h->lb.nnb, sizeof(int) * N, cudaMemcpyDeviceToHost));
+	if(cell) CK(cudaMemcpy(cell, h->lb.cell_of, sizeof(int) * N, cudaMemcpyDeviceToHost));
+	if(n_cells_side) *n_cells_side = h->lb.n_side;
+	if(nb) {
+		if(max_neigh < h->lb.max_nb) return fail(OXGB_E_INVALID, "max_neigh smaller than the row capacity");
+		std::vector<int> rows((size_t) N * h->lb.max_nb);
+		CK(cudaMemcpy(rows.data(), h->lb.nb, sizeof(int) * rows.size(), cudaMemcpyDeviceToHost));
+		for(int i = 0; i < N; i++)
+			for(int k = 0; k < h->lb.max_nb; k++) nb[(size_t) i * max_neigh + k] = rows[(size_t) i * h->lb.max_nb + k];
+	}
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_info(oxgb_md *h, long long *n_rebuilds, long long *step, int *max_neigh) {
+	if(!h) return fail(OXGB_E_INVALID, "null handle");
+	if(step) {
+		CK(cudaMemcpyAsync(step, h->step, sizeof(long long), cudaMemcpyDeviceToHost, h->stream));
+		CK(cudaStreamSynchronize(h->stream));
+	}
+	if(n_rebuilds) {
+		unsigned long long r = 0;
+		CK(cudaMemcpyAsync(&r, h->d_rebuilds, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+		CK(cudaStreamSynchronize(h->stream));
+		*n_rebuilds = (long long) r;
+	}
+	if(max_neigh) *max_neigh = h->lb.max_nb;
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_status(oxgb_md *h) {
+	if(!h) return fail(OXGB_E_INVALID, "null handle");
+	return read_status(h);
+}
+
+extern "C" int oxgb_md_device_buffers(oxgb_md *h, void **pos, void **vel, void **L, void **quat, void **F, void **T) {
+	if(!h) return fail(OXGB_E_INVALID, "null handle");
+	if(pos) *pos = h->posd;
+	if(vel) *vel = h->veld;
+	if(L) *L = h->Ld;
+	if(quat) *quat = h->quatd;
+	if(F) *F = h->F;
+	if(T) *T = h->T;
+	return OXGB_OK;
+}
+
+extern "C" void *oxgb_md_stream(oxgb_md *h) { return h ? (void *) h->stream : nullptr; }
+
+extern "C" int oxgb_md_destroy(oxgb_md *h) {
+	if(!h) return OXGB_OK;
+	cudaStreamSynchronize(h->stream);
+	delete h;
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_launch_forces(oxgb_md *h) {
+	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
+	return compute_forces_now(h, false);
+}
+
+// ====================================================================== diagnostics
+
+__global__ void k_fma_probe(float *out, int iters) {
+	float a[8];
+#pragma unroll
+	for(int k = 0; k < 8; k++) a[k] = threadIdx.x * 1e-7f + k;
+	const float b = 0.999999f, c = 1e-7f;
+	for(int it = 0; it < iters; it++) {
+#pragma unroll
+		for(int k = 0; k < 8; k++) a[k] = fmaf(a[k], b, c);
+	}
+	float s = 0;
+#pragma unroll
+	for(int k = 0; k < 8; k++) s += a[k];
+	if(s == 12345.f) out[0] = s;  // keeps the chain alive
+}
+
+extern "C" int oxgb_probe_fp32_peak(double *flops_per_s) {
+	if(!flops_per_s) return fail(OXGB_E_INVALID, "null argument");
+	int dev, sms;
+	CK(cudaGetDevice(&dev));
+	CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	float *out;
+	CK(cudaMalloc(&out, sizeof(float)));
+	const int blocks = sms * 8, threads = 256, iters = 1 << 14;
+	cudaEvent_t e0, e1;
+	CK(cudaEventCreate(&e0));
+	CK(cudaEventCreate(&e1));
+	k_fma_probe<<<blocks, threads>>>(out, 256);  // warm-up
+	float best = 1e30f;
+	for(int rep = 0; rep < 5; rep++) {
+		CK(cudaEventRecord(e0));
+		k_fma_probe<<<blocks, threads>>>(out, iters);
+		CK(cudaEventRecord(e1));
+		CK(cudaEventSynchronize(e1));
+		float ms;
+		CK(cudaEventElapsedTime(&ms, e0, e1));
+		best = std::min(best, ms);
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(out);
+	*flops_per_s = (double) blocks * threads * iters * 8 * 2 / (best * 1e-3);
+	return OXGB_OK;
+}

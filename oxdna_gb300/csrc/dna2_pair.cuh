@@ -1,0 +1,537 @@
+// oxDNA2 pair physics for the GPU kernels, templated on the arithmetic type R (float for the
+// production mixed-precision path, double for the FP64 parity path).
+//
+// The formulation is the reference CPU one (src/Interactions/DNAInteraction.cpp and
+// src/Interactions/DNA2Interaction.cpp, DNA2_nomesh): every angular factor f4 is evaluated
+// from the cosine of its angle, and its derivative enters as f4'(theta)/sin(theta) times
+// un-normalised directions.  That form stays well conditioned in FP32 near aligned vectors,
+// where the reference CUDA kernel's acos + normalised-cross form
+// (src/CUDA/Interactions/CUDA_DNA.cuh:138-174,232-725) loses accuracy.  Only the forces and
+// torques acting on one particle of a pair are formed for non-bonded pairs (the full
+// neighbour list visits every pair from both ends); bonded pairs can return either side.
+#pragma once
+
+#include "dna2_model.h"
+#include "oxgb_vec.cuh"
+
+namespace oxgb {
+
+// per-system parameter tables, filled on the host from the settings
+template <typename R>
+struct DNA2Table {
+	R f1_eps[2][5][5], f1_shift[2][5][5];
+	R f1_a[2], f1_r0[2], f1_blow[2], f1_bhigh[2], f1_rlow[2], f1_rhigh[2], f1_rclow[2], f1_rchigh[2];
+	R f2_k[2], f2_r0[2], f2_rc[2], f2_blow[2], f2_bhigh[2], f2_rlow[2], f2_rhigh[2], f2_rclow[2], f2_rchigh[2];
+	R f4_a[13], f4_b[13], f4_t0[13], f4_ts[13], f4_tc[13];
+	R f4_sa, f4_sb;
+	R f5_a[4], f5_b[4], f5_xc[4], f5_xs[4];
+	R hb_multiplier;
+	R dh_prefactor, dh_rhigh, dh_rc, dh_b, dh_minus_kappa;
+	R mbf_fmax, mbf_finf, mbf_xmax, mbf_fene_xmax, mbf_long_xmax;
+	R fene_r0, rcut2;
+	R box_hi, box_lo;  // box side as an unevaluated sum hi + lo (exact FP64 value)
+	R pos_base_over_stack;
+	int dh_half_charged_ends, use_mbf, pad0, pad1;
+};
+
+// one nucleotide: lab-frame axes and interaction-site offsets from its centre
+template <typename R>
+struct Nuc {
+	v3<R> a1, a2, a3, back, stack, base;
+	int type, btype;
+	bool is_end;
+};
+
+// grooved sites (src/Particles/DNANucleotide.cpp:66-82).  The reference forms the base site as
+// stack * (POS_BASE / POS_STACK); the FP64 path keeps that, the FP32 path uses a1 * POS_BASE
+// (the same value with one rounding instead of two).
+template <typename R>
+OXGB_HD void make_sites(const DNA2Table<R> &P, Nuc<R> &n) {
+	n.back = n.a1 * R(OXM_POS_MM_BACK1) + n.a2 * R(OXM_POS_MM_BACK2);
+	n.stack = n.a1 * R(OXM_POS_STACK);
+	n.base = (sizeof(R) == 4) ? n.a1 * R(OXM_POS_BASE) : n.stack * P.pos_base_over_stack;
+}
+
+// centre-centre separation of a pair as an unevaluated sum hi + lo: the FP32 path carries the
+// low part so that the stiff site-site vectors keep ~ulp accuracy; the other paths have lo = 0
+template <typename R>
+struct Sep {
+	v3<R> hi, lo;
+	OXGB_HD v3<R> plain() const { return hi + lo; }
+};
+
+template <typename R>
+OXGB_HD void two_sum(R a, R b, R &s, R &e) {
+	s = a + b;
+	const R bb = s - a;
+	e = (a - (s - bb)) + (b - bb);
+}
+
+// site-site vector r + qs - ps.  In FP32 the three-term sum is compensated (TwoSum on the site
+// difference and on its sum with the separation), which removes the rounding of the ~1-long
+// separation that otherwise dominates the error of the stiff radial terms (Morse minima of
+// hydrogen bonding and stacking, FENE); in FP64 it is the reference's plain sum.
+template <typename R>
+OXGB_HD v3<R> site_vec(const Sep<R> &s, v3<R> qs, v3<R> ps) {
+	if(sizeof(R) != 4) return (s.hi + qs) - ps;
+	v3<R> d;
+	R oh, ol, t, e;
+	two_sum(qs.x, -ps.x, oh, ol);
+	two_sum(s.hi.x, oh, t, e);
+	d.x = t + ((e + ol) + s.lo.x);
+	two_sum(qs.y, -ps.y, oh, ol);
+	two_sum(s.hi.y, oh, t, e);
+	d.y = t + ((e + ol) + s.lo.y);
+	two_sum(qs.z, -ps.z, oh, ol);
+	two_sum(s.hi.z, oh, t, e);
+	d.z = t + ((e + ol) + s.lo.z);
+	return d;
+}
+
+// energy-term slots, in the reference's split order
+enum { T_FENE = 0, T_BEXC, T_STCK, T_NEXC, T_HB, T_CRST, T_CXST, T_DH, N_TERMS };
+
+template <typename R>
+struct PairOut {
+	v3<R> F, T;  // force and lab-frame torque on the particle
+	R E, Ehb;    // pair energy (all terms) and its hydrogen-bonding part
+	R split[N_TERMS];
+};
+
+template <typename R, bool SPLIT>
+OXGB_HD void add_e(PairOut<R> &o, int term, R e) {
+	o.E += e;
+	if(SPLIT) o.split[term] += e;
+}
+
+// ---------------------------------------------------------------- radial and angular factors
+
+// Morse f1 and its derivative (DNAInteraction.cpp:1239-1276)
+template <typename R>
+OXGB_HD void f1_both(const DNA2Table<R> &P, R r, int t, int i, int j, R &f, R &fd) {
+	f = R(0);
+	fd = R(0);
+	if(r < P.f1_rchigh[t]) {
+		const R eps = P.f1_eps[t][i][j];
+		if(r > P.f1_rhigh[t]) {
+			f = eps * P.f1_bhigh[t] * (r - P.f1_rchigh[t]) * (r - P.f1_rchigh[t]);
+			fd = eps * (R(2) * P.f1_bhigh[t] * (r - P.f1_rchigh[t]));
+		}
+		else if(r > P.f1_rlow[t]) {
+			// FP32: 1 - exp(-y) through expm1, exact near the well bottom where it cancels
+			const R y = -(r - P.f1_r0[t]) * P.f1_a[t];
+			const R x = m_exp(y);
+			const R tmp = (sizeof(R) == 4) ? -m_expm1(y) : R(1) - x;
+			f = eps * tmp * tmp - P.f1_shift[t][i][j];
+			fd = eps * (R(2) * tmp * x * P.f1_a[t]);
+		}
+		else if(r > P.f1_rclow[t]) {
+			f = eps * P.f1_blow[t] * (r - P.f1_rclow[t]) * (r - P.f1_rclow[t]);
+			fd = eps * (R(2) * P.f1_blow[t] * (r - P.f1_rclow[t]));
+		}
+	}
+}
+
+// harmonic f2 and its derivative (DNAInteraction.cpp:1278-1310)
+template <typename R>
+OXGB_HD void f2_both(const DNA2Table<R> &P, R r, int t, R &f, R &fd) {
+	f = R(0);
+	fd = R(0);
+	if(r < P.f2_rchigh[t]) {
+		if(r > P.f2_rhigh[t]) {
+			f = P.f2_k[t] * P.f2_bhigh[t] * (r - P.f2_rchigh[t]) * (r - P.f2_rchigh[t]);
+			fd = R(2) * P.f2_k[t] * P.f2_bhigh[t] * (r - P.f2_rchigh[t]);
+		}
+		else if(r > P.f2_rlow[t]) {
+			f = (P.f2_k[t] / R(2)) * ((r - P.f2_r0[t]) * (r - P.f2_r0[t]) - (P.f2_rc[t] - P.f2_r0[t]) * (P.f2_rc[t] - P.f2_r0[t]));
+			fd = P.f2_k[t] * (r - P.f2_r0[t]);
+		}
+		else if(r > P.f2_rclow[t]) {
+			f = P.f2_k[t] * P.f2_blow[t] * (r - P.f2_rclow[t]) * (r - P.f2_rclow[t]);
+			fd = R(2) * P.f2_k[t] * P.f2_blow[t] * (r - P.f2_rclow[t]);
+		}
+	}
+}
+
+// f4 of the angle whose cosine is c, and "f4D": minus f4'(theta)/sin(theta), the factor that
+// multiplies the cosine's gradient (DNAInteraction.cpp:1312-1416, DNA2Interaction.cpp:308-352).
+// Set OXM_F4_CX_T1 adds the oxDNA2 pure-harmonic coaxial term.
+template <typename R>
+OXGB_HD void f4_both(const DNA2Table<R> &P, R c, int i, R &f, R &fd) {
+	c = m_max(R(-1), m_min(R(1), c));
+	const R t = m_acos(c);
+	const R s2 = m_fma(-c, c, R(1));  // sin^2(theta), with one rounding
+	const R sint = m_sqrt(s2);
+	f = R(0);
+	R dsin = R(0);
+	R tt0 = t - P.f4_t0[i];
+	R m = R(1);
+	if(tt0 < R(0)) {
+		tt0 = -tt0;
+		m = R(-1);
+	}
+	if(tt0 < P.f4_tc[i]) {
+		if(tt0 > P.f4_ts[i]) {
+			f = P.f4_b[i] * (P.f4_tc[i] - tt0) * (P.f4_tc[i] - tt0);
+			dsin = m * R(2) * P.f4_b[i] * (tt0 - P.f4_tc[i]) / sint;
+		}
+		else {
+			f = R(1) - P.f4_a[i] * tt0 * tt0;
+			dsin = (s2 > R(1e-8)) ? -m * R(2) * P.f4_a[i] * tt0 / sint : -m * R(2) * P.f4_a[i];
+		}
+	}
+	if(i == OXM_F4_CX_T1) {
+		const R h = t - P.f4_sb;
+		if(h >= R(0)) {
+			f += P.f4_sa * h * h;
+			dsin += (s2 > R(1e-8)) ? R(2) * P.f4_sa * h / sint : R(2) * P.f4_sa;
+		}
+	}
+	fd = -dsin;
+}
+
+// f5 of cos(phi) and its derivative (DNAInteraction.cpp:1418-1450)
+template <typename R>
+OXGB_HD void f5_both(const DNA2Table<R> &P, R x, int t, R &f, R &fd) {
+	f = R(0);
+	fd = R(0);
+	if(x > P.f5_xc[t]) {
+		if(x < P.f5_xs[t]) {
+			f = P.f5_b[t] * (P.f5_xc[t] - x) * (P.f5_xc[t] - x);
+			fd = R(2) * P.f5_b[t] * (x - P.f5_xc[t]);
+		}
+		else if(x < R(0)) {
+			f = R(1) - P.f5_a[t] * x * x;
+			fd = R(-2) * P.f5_a[t] * x;
+		}
+		else f = R(1);
+	}
+}
+
+// repulsive Lennard-Jones with quadratic smoothing; f = force on the second site
+// (DNAInteraction.cpp:1182-1207)
+template <typename R>
+OXGB_HD R excl_vol(v3<R> r, R sigma, R rstar, R b, R rc, v3<R> &f) {
+	const R rn = dot(r, r);
+	f = v3<R>{R(0), R(0), R(0)};
+	if(rn >= rc * rc) return R(0);
+	if(rn > rstar * rstar) {
+		const R rmod = m_sqrt(rn);
+		const R rrc = rmod - rc;
+		f = r * (-(R(2) * R(OXM_EXCL_EPS) * b * rrc / rmod));
+		return R(OXM_EXCL_EPS) * b * rrc * rrc;
+	}
+	const R tmp = sigma * sigma / rn;
+	const R lj = tmp * tmp * tmp;
+	f = r * (-(R(24) * R(OXM_EXCL_EPS) * (lj - R(2) * lj * lj) / rn));
+	return R(4) * R(OXM_EXCL_EPS) * (lj * lj - lj);
+}
+
+// ---------------------------------------------------------------- non-bonded pair, p side
+
+// r = minimum image of q.centre - p.centre.  Adds to o the force on p and the lab-frame torque
+// on p from the excluded volume, hydrogen bonding, cross stacking, oxDNA2 coaxial stacking and
+// Debye-Hueckel terms (DNA2Interaction.cpp:42-60 and the term functions it calls).
+template <typename R, bool SPLIT>
+OXGB_HD void nonbonded_p(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
+	const v3<R> r = sep.plain();
+	if(dot(r, r) >= P.rcut2) return;
+	v3<R> f;
+
+	// excluded volume: base-base, back(p)-base(q), base(p)-back(q), back-back
+	{
+		R e = excl_vol(r + q.base - p.base, R(OXM_EXCL_S2), R(OXM_EXCL_R2), R(OXM_EXCL_B2), R(OXM_EXCL_RC2), f);
+		o.F -= f;
+		o.T -= cross(p.base, f);
+		e += excl_vol(r + q.base - p.back, R(OXM_EXCL_S4), R(OXM_EXCL_R4), R(OXM_EXCL_B4), R(OXM_EXCL_RC4), f);
+		o.F -= f;
+		o.T -= cross(p.back, f);
+		e += excl_vol(r + q.back - p.base, R(OXM_EXCL_S3), R(OXM_EXCL_R3), R(OXM_EXCL_B3), R(OXM_EXCL_RC3), f);
+		o.F -= f;
+		o.T -= cross(p.base, f);
+		e += excl_vol(r + q.back - p.back, R(OXM_EXCL_S1), R(OXM_EXCL_R1), R(OXM_EXCL_B1), R(OXM_EXCL_RC1), f);
+		o.F -= f;
+		o.T -= cross(p.back, f);
+		add_e<R, SPLIT>(o, T_NEXC, e);
+	}
+
+	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3;
+	const v3<R> rhydro = site_vec(sep, q.base, p.base);
+	const R rh2 = dot(rhydro, rhydro);
+
+	// hydrogen bonding
+	if(p.btype + q.btype == 3 && R(OXM_HYDR_RCLOW) * R(OXM_HYDR_RCLOW) < rh2 && rh2 < R(OXM_HYDR_RCHIGH) * R(OXM_HYDR_RCHIGH)) {
+		const R rmod = m_sqrt(rh2);
+		if(R(OXM_HYDR_RCLOW) < rmod && rmod < R(OXM_HYDR_RCHIGH)) {
+			const v3<R> rd = rhydro * (R(1) / rmod);
+			const R c1 = -dot(a1, b1), c2 = -dot(b1, rd), c3 = dot(a1, rd), c4 = dot(a3, b3), c7 = -dot(b3, rd), c8 = dot(a3, rd);
+			const R hbm = (abs(q.btype) >= 300 && abs(p.btype) >= 300) ? P.hb_multiplier : R(1);
+			R F1, F1D, g1, d1, g2, d2, g3, d3, g4, d4, g7, d7, g8, d8;
+			f1_both(P, rmod, OXM_F1_HB, q.type, p.type, F1, F1D);
+			F1 *= hbm;
+			F1D *= hbm;
+			f4_both(P, c1, OXM_F4_HB_T1, g1, d1);
+			f4_both(P, c2, OXM_F4_HB_T2, g2, d2);
+			f4_both(P, c3, OXM_F4_HB_T2, g3, d3);
+			f4_both(P, c4, OXM_F4_HB_T4, g4, d4);
+			f4_both(P, c7, OXM_F4_HB_T7, g7, d7);
+			f4_both(P, c8, OXM_F4_HB_T7, g8, d8);
+			d3 = -d3;
+			d4 = -d4;
+			d8 = -d8;
+			const R e = F1 * g1 * g2 * g3 * g4 * g7 * g8;
+			if(e != R(0)) {
+				add_e<R, SPLIT>(o, T_HB, e);
+				o.Ehb += e;
+				v3<R> force = rd * (-(F1D * g1 * g2 * g3 * g4 * g7 * g8));
+				v3<R> tp = cross(a3, b3) * (F1 * g1 * g2 * g3 * d4 * g7 * g8);   // theta4: -= dir * (-..)
+				tp += cross(a1, b1) * (F1 * d1 * g2 * g3 * g4 * g7 * g8);         // theta1
+				force += (b1 + rd * c2) * (F1 * g1 * d2 * g3 * g4 * g7 * g8 / rmod);
+				force += (a1 - rd * c3) * (F1 * g1 * g2 * d3 * g4 * g7 * g8 / rmod);
+				tp += cross(rd, a1) * (-(F1 * g1 * g2 * d3 * g4 * g7 * g8));      // theta3
+				force += (b3 + rd * c7) * (F1 * g1 * g2 * g3 * g4 * d7 * g8 / rmod);
+				force += (a3 - rd * c8) * (F1 * g1 * g2 * g3 * g4 * g7 * d8 / rmod);
+				tp += cross(rd, a3) * (-(F1 * g1 * g2 * g3 * g4 * g7 * d8));      // theta8
+				o.F -= force;
+				o.T += tp - cross(p.base, force);
+			}
+		}
+	}
+
+	// cross stacking
+	if(R(OXM_CRST_RCLOW) * R(OXM_CRST_RCLOW) < rh2 && rh2 < R(OXM_CRST_RCHIGH) * R(OXM_CRST_RCHIGH)) {
+		const R rmod = m_sqrt(rh2);
+		if(R(OXM_CRST_RCLOW) < rmod && rmod < R(OXM_CRST_RCHIGH)) {
+			const v3<R> rd = rhydro * (R(1) / rmod);
+			const R c1 = -dot(a1, b1), c2 = -dot(b1, rd), c3 = dot(a1, rd), c4 = dot(a3, b3), c7 = -dot(b3, rd), c8 = dot(a3, rd);
+			R F2, F2D, g1, d1, g2, d2, g3, d3, g4a, d4a, g4b, d4b, g7a, d7a, g7b, d7b, g8a, d8a, g8b, d8b;
+			f2_both(P, rmod, OXM_F2_CRST, F2, F2D);
+			f4_both(P, c1, OXM_F4_CR_T1, g1, d1);
+			f4_both(P, c2, OXM_F4_CR_T2, g2, d2);
+			f4_both(P, c3, OXM_F4_CR_T2, g3, d3);
+			f4_both(P, c4, OXM_F4_CR_T4, g4a, d4a);
+			f4_both(P, -c4, OXM_F4_CR_T4, g4b, d4b);
+			f4_both(P, c7, OXM_F4_CR_T7, g7a, d7a);
+			f4_both(P, -c7, OXM_F4_CR_T7, g7b, d7b);
+			f4_both(P, c8, OXM_F4_CR_T7, g8a, d8a);
+			f4_both(P, -c8, OXM_F4_CR_T7, g8b, d8b);
+			const R g4 = g4a + g4b, g7 = g7a + g7b, g8 = g8a + g8b;
+			d3 = -d3;
+			const R d4 = -d4a + d4b, d7 = d7a - d7b, d8 = -d8a + d8b;
+			const R e = F2 * g1 * g2 * g3 * g4 * g7 * g8;
+			if(e != R(0)) {
+				add_e<R, SPLIT>(o, T_CRST, e);
+				v3<R> force = rd * (-(F2D * g1 * g2 * g3 * g4 * g7 * g8));
+				v3<R> tp = cross(a1, b1) * (F2 * d1 * g2 * g3 * g4 * g7 * g8);
+				force += (b1 + rd * c2) * (F2 * g1 * d2 * g3 * g4 * g7 * g8 / rmod);
+				force += (a1 - rd * c3) * (F2 * g1 * g2 * d3 * g4 * g7 * g8 / rmod);
+				tp += cross(rd, a1) * (-(F2 * g1 * g2 * d3 * g4 * g7 * g8));
+				tp += cross(a3, b3) * (F2 * g1 * g2 * g3 * d4 * g7 * g8);
+				force += (b3 + rd * c7) * (F2 * g1 * g2 * g3 * g4 * d7 * g8 / rmod);
+				force += (a3 - rd * c8) * (F2 * g1 * g2 * g3 * g4 * g7 * d8 / rmod);
+				tp += cross(rd, a3) * (-(F2 * g1 * g2 * g3 * g4 * g7 * d8));
+				o.F -= force;
+				o.T += tp - cross(p.base, force);
+			}
+		}
+	}
+
+	// coaxial stacking (oxDNA2: no phi3 factor, pure-harmonic theta1 term)
+	{
+		const v3<R> rstack = site_vec(sep, q.stack, p.stack);
+		const R rs2 = dot(rstack, rstack);
+		if(R(OXM_CXST_RCLOW) * R(OXM_CXST_RCLOW) < rs2 && rs2 < R(OXM_CXST_RCHIGH) * R(OXM_CXST_RCHIGH)) {
+			const R rmod = m_sqrt(rs2);
+			if(R(OXM_CXST_RCLOW) < rmod && rmod < R(OXM_CXST_RCHIGH)) {
+				const v3<R> rd = rstack * (R(1) / rmod);
+				const R c1 = -dot(a1, b1), c4 = dot(a3, b3), c5 = dot(a3, rd), c6 = -dot(b3, rd);
+				R F2, F2D, g1, d1, g4, d4, g5a, d5a, g5b, d5b, g6a, d6a, g6b, d6b;
+				f2_both(P, rmod, OXM_F2_CXST, F2, F2D);
+				f4_both(P, c1, OXM_F4_CX_T1, g1, d1);
+				f4_both(P, c4, OXM_F4_CX_T4, g4, d4);
+				f4_both(P, c5, OXM_F4_CX_T5, g5a, d5a);
+				f4_both(P, -c5, OXM_F4_CX_T5, g5b, d5b);
+				f4_both(P, c6, OXM_F4_CX_T5, g6a, d6a);
+				f4_both(P, -c6, OXM_F4_CX_T5, g6b, d6b);
+				const R g5 = g5a + g5b, g6 = g6a + g6b;
+				d4 = -d4;
+				const R d5 = -d5a + d5b, d6 = d6a - d6b;
+				const R e = F2 * g1 * g4 * g5 * g6;
+				if(e != R(0)) {
+					add_e<R, SPLIT>(o, T_CXST, e);
+					v3<R> force = rd * (-(F2D * g1 * g4 * g5 * g6));
+					v3<R> tp = cross(a1, b1) * (F2 * d1 * g4 * g5 * g6);
+					tp += cross(a3, b3) * (F2 * g1 * d4 * g5 * g6);
+					const R f5 = F2 * g1 * g4 * d5 * g6;
+					force += (a3 - rd * c5) * (f5 / rmod);
+					tp -= cross(rd, a3) * f5;
+					const R f6 = F2 * g1 * g4 * g5 * d6;
+					force += (b3 + rd * c6) * (f6 / rmod);
+					o.F -= force;
+					o.T += tp - cross(p.stack, force);
+				}
+			}
+		}
+	}
+
+	// Debye-Hueckel (DNA2Interaction.cpp:157-212)
+	{
+		const v3<R> rback = r + q.back - p.back;
+		const R rb2 = dot(rback, rback);
+		if(rb2 < P.dh_rc * P.dh_rc) {
+			const R rmod = m_sqrt(rb2);
+			if(rmod < P.dh_rc) {
+				R cut = R(1);
+				if(P.dh_half_charged_ends && p.is_end) cut *= R(0.5);
+				if(P.dh_half_charged_ends && q.is_end) cut *= R(0.5);
+				const v3<R> rd = rback * (R(1) / rmod);
+				R e, fm;
+				if(rmod < P.dh_rhigh) {
+					const R ex = m_exp(P.dh_minus_kappa * rmod);
+					e = ex * (P.dh_prefactor / rmod);
+					fm = -(P.dh_prefactor * ex) * (P.dh_minus_kappa / rmod - R(1) / (rmod * rmod));
+				}
+				else {
+					e = P.dh_b * (rmod - P.dh_rc) * (rmod - P.dh_rc);
+					fm = -(R(2) * P.dh_b * (rmod - P.dh_rc));
+				}
+				const v3<R> force = rd * (fm * cut);
+				add_e<R, SPLIT>(o, T_DH, e * cut);
+				o.F -= force;
+				o.T -= cross(p.back, force);
+			}
+		}
+	}
+}
+
+// ---------------------------------------------------------------- bonded pair
+
+// p is the nucleotide whose 3' neighbour is q, r = q.centre - p.centre (no periodic image).
+// Backbone FENE (with the optional max_backbone_force log tail), bonded excluded volume and
+// stacking (DNAInteraction.cpp:415-705).  QSIDE selects whose force and lab torque are added.
+// Returns false if the backbone bond left the FENE range.
+template <typename R, bool SPLIT, bool QSIDE>
+OXGB_HD bool bonded(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
+	const v3<R> r = sep.plain();
+	bool ok = true;
+	v3<R> fsum{R(0), R(0), R(0)}, tsum{R(0), R(0), R(0)};  // force on q, torque on the chosen side
+	// FENE
+	{
+		const v3<R> rback = site_vec(sep, q.back, p.back);
+		const R rmod = m_sqrt(dot(rback, rback));
+		const R x = rmod - P.fene_r0;
+		v3<R> force;
+		R e;
+		if(P.use_mbf && m_fabs(x) > P.mbf_xmax) {
+			const R ax = m_fabs(x);
+			e = (P.mbf_fmax - P.mbf_finf) * P.mbf_xmax * m_log(ax) + P.mbf_finf * ax - P.mbf_long_xmax + P.mbf_fene_xmax;
+			force = rback * (-m_copysign(R(1), x) * ((P.mbf_fmax - P.mbf_finf) * P.mbf_xmax / ax + P.mbf_finf) / rmod);
+		}
+		else {
+			if(m_fabs(x) >= R(OXM_FENE_DELTA)) {
+				ok = false;
+				e = R(0);
+				force = v3<R>{R(0), R(0), R(0)};
+			}
+			else {
+				e = -(R(OXM_FENE_EPS) / R(2)) * m_log(R(1) - x * x / R(OXM_FENE_DELTA2));
+				force = rback * (-(R(OXM_FENE_EPS) * x / (R(OXM_FENE_DELTA2) - x * x)) / rmod);
+			}
+		}
+		add_e<R, SPLIT>(o, T_FENE, e);
+		fsum += force;
+		tsum += QSIDE ? cross(q.back, force) : -cross(p.back, force);
+	}
+	// bonded excluded volume: base-base, base(p)-back(q), back(p)-base(q)
+	{
+		v3<R> f;
+		R e = excl_vol(r + q.base - p.base, R(OXM_EXCL_S2), R(OXM_EXCL_R2), R(OXM_EXCL_B2), R(OXM_EXCL_RC2), f);
+		fsum += f;
+		tsum += QSIDE ? cross(q.base, f) : -cross(p.base, f);
+		e += excl_vol(r + q.back - p.base, R(OXM_EXCL_S3), R(OXM_EXCL_R3), R(OXM_EXCL_B3), R(OXM_EXCL_RC3), f);
+		fsum += f;
+		tsum += QSIDE ? cross(q.back, f) : -cross(p.base, f);
+		e += excl_vol(r + q.base - p.back, R(OXM_EXCL_S4), R(OXM_EXCL_R4), R(OXM_EXCL_B4), R(OXM_EXCL_RC4), f);
+		fsum += f;
+		tsum += QSIDE ? cross(q.base, f) : -cross(p.back, f);
+		add_e<R, SPLIT>(o, T_BEXC, e);
+	}
+	// stacking
+	{
+		const v3<R> a1 = p.a1, a2 = p.a2, a3 = p.a3, b1 = q.a1, b2 = q.a2, b3 = q.a3;
+		const v3<R> rbackref = r + b1 * R(OXM_POS_BACK) - a1 * R(OXM_POS_BACK);
+		const R rbr = m_sqrt(dot(rbackref, rbackref));
+		const v3<R> rstack = site_vec(sep, q.stack, p.stack);
+		const R rsm = m_sqrt(dot(rstack, rstack));
+		const v3<R> rd = rstack * (R(1) / rsm);
+		const R c4 = dot(a3, b3), c5 = dot(a3, rd), c6 = -dot(b3, rd);
+		const R cp1 = dot(a2, rbackref) / rbr, cp2 = dot(b2, rbackref) / rbr;
+		R F1, F1D, g4, d4, g5, d5, g6, d6, h1, h1d, h2, h2d;
+		f1_both(P, rsm, OXM_F1_ST, q.type, p.type, F1, F1D);
+		f4_both(P, c4, OXM_F4_ST_T4, g4, d4);
+		f4_both(P, -c5, OXM_F4_ST_T5, g5, d5);
+		f4_both(P, c6, OXM_F4_ST_T5, g6, d6);
+		f5_both(P, cp1, OXM_F5_PHI1, h1, h1d);
+		f5_both(P, cp2, OXM_F5_PHI2, h2, h2d);
+		d4 = -d4;
+		d5 = -d5;
+		d6 = -d6;
+		const R e = F1 * g4 * g5 * g6 * h1 * h2;
+		add_e<R, SPLIT>(o, T_STCK, e);
+		if(e != R(0)) {
+			const R gam = R(OXM_POS_STACK) - R(OXM_POS_BACK);
+			const R rbr3 = rbr * rbr * rbr;
+			v3<R> force = rd * (-(F1D * g4 * g5 * g6 * h1 * h2));
+			force -= (a3 - rd * c5) * (F1 * g4 * d5 * g6 * h1 * h2 / rsm);
+			force -= (b3 + rd * c6) * (F1 * g4 * g5 * d6 * h1 * h2 / rsm);
+
+			const R ra2 = dot(rd, a2), ra1 = dot(rd, a1), rb1 = dot(rd, b1), a2b1 = dot(a2, b1);
+			const R par1 = rsm * ra2 - a2b1 * gam;
+			const R dc1dr = (rsm * rsm * ra2 - ra2 * rbr * rbr - rsm * (a2b1 + ra2 * (-ra1 + rb1)) * gam + a2b1 * (-ra1 + rb1) * gam * gam) / rbr3;
+			const R dc1dra1 = rsm * gam * par1 / rbr3;
+			const R dc1dra2 = -rsm / rbr;
+			const R dc1drb1 = -rsm * gam * par1 / rbr3;
+			const R dc1da1b1 = -gam * gam * par1 / rbr3;
+			const R dc1da2b1 = gam / rbr;
+			const R fp1 = -F1 * g4 * g5 * g6 * h1d * h2;
+			force -= (rd * dc1dr + ((a2 - rd * ra2) * dc1dra2 + (a1 - rd * ra1) * dc1dra1 + (b1 - rd * rb1) * dc1drb1) * (R(1) / rsm)) * fp1;
+
+			const R sb2 = dot(rd, b2), sb1 = dot(rd, b1), sa1 = dot(rd, a1), b2a1 = dot(b2, a1);
+			const R par2 = rsm * sb2 + b2a1 * gam;
+			const R dc2dr = (par2 * (rsm + (sa1 - sb1) * gam) - sb2 * rbr * rbr) / rbr3;
+			const R dc2dra1 = -rsm * gam * (rsm * sb2 + b2a1 * gam) / rbr3;
+			const R dc2dra2 = -rsm / rbr;
+			const R dc2drb1 = rsm * gam * par2 / rbr3;
+			const R dc2da1b1 = -gam * gam * par2 / rbr3;
+			const R dc2da2b1 = -gam / rbr;
+			const R fp2 = -F1 * g4 * g5 * g6 * h1 * h2d;
+			force -= (rd * dc2dr + ((b2 - rd * sb2) * dc2dra2 + (b1 - rd * sb1) * dc2dra1 + (a1 - rd * sa1) * dc2drb1) * (R(1) / rsm)) * fp2;
+
+			fsum += force;
+			const v3<R> t4dir = cross(b3, a3);
+			const R tm4 = F1 * d4 * g5 * g6 * h1 * h2;
+			const v3<R> pure1 = cross(a2, b1) * (fp1 * dc1da2b1) + cross(a1, b1) * (fp1 * dc1da1b1);
+			const v3<R> pure2 = cross(a1, b2) * (fp2 * dc2da2b1) + cross(a1, b1) * (fp2 * dc2da1b1);
+			if(QSIDE) {
+				v3<R> tq = cross(q.stack, force) + t4dir * tm4;
+				tq += cross(rd, b3) * (F1 * g4 * g5 * d6 * h1 * h2);
+				tq += cross(rd, b1) * (fp1 * dc1drb1) + pure1;
+				tq += cross(rd, b2) * (fp2 * dc2dra2) + cross(rd, b1) * (fp2 * dc2dra1) + pure2;
+				tsum += tq;
+			}
+			else {
+				v3<R> tp = -cross(p.stack, force) - t4dir * tm4;
+				tp -= cross(rd, a3) * (-(F1 * g4 * d5 * g6 * h1 * h2));
+				tp += cross(rd, a2) * (fp1 * dc1dra2) + cross(rd, a1) * (fp1 * dc1dra1) - pure1;
+				tp += cross(rd, a1) * (fp2 * dc2drb1) - pure2;
+				tsum += tp;
+			}
+		}
+	}
+	if(QSIDE) o.F += fsum;
+	else o.F -= fsum;
+	o.T += tsum;
+	return ok;
+}
+
+}  // namespace oxgb

@@ -1,0 +1,129 @@
+// Algorithmic work of the force kernel, counted by running the kernel's own pair physics
+// (dna2_pair.cuh, FP32 instantiation) on the host with a counting scalar type.  Every add,
+// subtract, multiply and divide counts one FP32 operation, an FMA two; square root, exp,
+// expm1, log and acos count as one special-function operation each (reported separately).
+// Used by bench.py to turn the measured force-kernel time into achieved FLOP/s.
+//
+// Host-only C++ (g++), built into liboxgb_tools.so.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+static double g_flops = 0, g_sfu = 0;
+
+struct CF {
+	float v;
+	CF() = default;
+	CF(float x) : v(x) {}
+	CF(double x) : v((float) x) {}
+	CF(int x) : v((float) x) {}
+};
+static_assert(sizeof(CF) == 4, "CF must look like a float to the kernels' precision switches");
+
+inline CF operator+(CF a, CF b) { g_flops += 1; return CF(a.v + b.v); }
+inline CF operator-(CF a, CF b) { g_flops += 1; return CF(a.v - b.v); }
+inline CF operator*(CF a, CF b) { g_flops += 1; return CF(a.v * b.v); }
+inline CF operator/(CF a, CF b) { g_flops += 1; return CF(a.v / b.v); }
+inline CF operator-(CF a) { return CF(-a.v); }
+inline CF &operator+=(CF &a, CF b) { g_flops += 1; a.v += b.v; return a; }
+inline CF &operator-=(CF &a, CF b) { g_flops += 1; a.v -= b.v; return a; }
+inline CF &operator*=(CF &a, CF b) { g_flops += 1; a.v *= b.v; return a; }
+inline bool operator<(CF a, CF b) { return a.v < b.v; }
+inline bool operator>(CF a, CF b) { return a.v > b.v; }
+inline bool operator<=(CF a, CF b) { return a.v <= b.v; }
+inline bool operator>=(CF a, CF b) { return a.v >= b.v; }
+inline bool operator!=(CF a, CF b) { return a.v != b.v; }
+inline bool operator==(CF a, CF b) { return a.v == b.v; }
+
+namespace oxgb {
+inline CF m_sqrt(CF x) { g_sfu += 1; return CF(std::sqrt(x.v)); }
+inline CF m_exp(CF x) { g_sfu += 1; return CF(std::exp(x.v)); }
+inline CF m_expm1(CF x) { g_sfu += 1; return CF(std::expm1(x.v)); }
+inline CF m_log(CF x) { g_sfu += 1; return CF(std::log(x.v)); }
+inline CF m_acos(CF x) { g_sfu += 1; return CF(std::acos(x.v)); }
+inline CF m_fabs(CF x) { return CF(std::fabs(x.v)); }
+inline CF m_fma(CF a, CF b, CF c) { g_flops += 2; return CF(std::fma(a.v, b.v, c.v)); }
+inline CF m_rint(CF x) { return CF(std::rint(x.v)); }
+inline CF m_copysign(CF a, CF b) { return CF(std::copysign(a.v, b.v)); }
+inline CF m_min(CF a, CF b) { return CF(std::fmin(a.v, b.v)); }
+inline CF m_max(CF a, CF b) { return CF(std::fmax(a.v, b.v)); }
+}  // namespace oxgb
+
+#include "dna2_pair.cuh"
+#include "params.h"
+
+using namespace oxgb;
+
+static void frame_of(const double *a1, const double *a3, int i, Nuc<CF> &n, const DNA2Table<CF> &P) {
+	n.a1 = v3<CF>{CF(a1[3 * i]), CF(a1[3 * i + 1]), CF(a1[3 * i + 2])};
+	n.a3 = v3<CF>{CF(a3[3 * i]), CF(a3[3 * i + 1]), CF(a3[3 * i + 2])};
+	n.a2 = cross(n.a3, n.a1);
+	make_sites(P, n);
+}
+
+extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, const double *a3, const int *n3, const int *n5,
+		const int *type, const int *btype, double box, const int *nb, const int *nnb, int max_nb, double T, double salt,
+		double *out) {
+	oxgb_dna2_settings s;
+	default_settings(&s, T, salt);
+	DNA2Table<double> P64;
+	double rcut;
+	if(build_table(s, box, P64, rcut)) return 1;
+	DNA2Table<float> P32;
+	to_float(P64, box, P32);
+	DNA2Table<CF> P;
+	std::memcpy(&P, &P32, sizeof(P));
+	g_flops = g_sfu = 0;
+	double pairs = 0, in_range = 0;
+	for(int i = 0; i < N; i++) {
+		Nuc<CF> p;
+		frame_of(a1, a3, i, p, P);
+		p.type = type[i];
+		p.btype = btype[i];
+		p.is_end = n3[i] < 0 || n5[i] < 0;
+		for(int side = 0; side < 2; side++) {
+			const int j = side == 0 ? n3[i] : n5[i];
+			if(j < 0) continue;
+			Nuc<CF> q;
+			frame_of(a1, a3, j, q, P);
+			q.type = type[j];
+			q.btype = btype[j];
+			q.is_end = n3[j] < 0 || n5[j] < 0;
+			PairOut<CF> o{};
+			Sep<CF> sp;
+			const double d[3] = {pos[3 * j] - pos[3 * i], pos[3 * j + 1] - pos[3 * i + 1], pos[3 * j + 2] - pos[3 * i + 2]};
+			const double sg = side == 0 ? 1.0 : -1.0;
+			sp.hi = v3<CF>{CF(sg * d[0]), CF(sg * d[1]), CF(sg * d[2])};
+			sp.lo = v3<CF>{CF(0.f), CF(0.f), CF(0.f)};
+			if(side == 0) bonded<CF, false, false>(P, p, q, sp, o);
+			else bonded<CF, false, true>(P, q, p, sp, o);
+		}
+		const int nn = nnb[i] < max_nb ? nnb[i] : max_nb;
+		for(int k = 0; k < nn; k++) {
+			const int j = nb[(long long) i * max_nb + k];
+			Nuc<CF> q;
+			frame_of(a1, a3, j, q, P);
+			q.type = type[j];
+			q.btype = btype[j];
+			q.is_end = n3[j] < 0 || n5[j] < 0;
+			double d[3];
+			for(int c = 0; c < 3; c++) {
+				d[c] = pos[3 * j + c] - pos[3 * i + c];
+				d[c] -= std::rint(d[c] / box) * box;
+			}
+			g_flops += 3 * 4;  // minimum image of the hi/lo separation
+			Sep<CF> sp;
+			sp.hi = v3<CF>{CF(d[0]), CF(d[1]), CF(d[2])};
+			sp.lo = v3<CF>{CF(0.f), CF(0.f), CF(0.f)};
+			PairOut<CF> o{};
+			nonbonded_p<CF, false>(P, p, q, sp, o);
+			pairs += 1;
+			if(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] < rcut * rcut) in_range += 1;
+		}
+	}
+	out[0] = g_flops;
+	out[1] = g_sfu;
+	out[2] = pairs;
+	out[3] = in_range;
+	return 0;
+}

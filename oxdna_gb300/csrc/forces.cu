@@ -1,0 +1,339 @@
+// oxDNA2 force and torque kernel: one warp per nucleotide.
+//
+// Lanes stride over the nucleotide's neighbour row (full list: every pair is seen from both
+// ends, so no atomics and a fixed summation order); lanes 0 and 1 also take the 3' and 5'
+// bonded pairs.  Each lane accumulates its pair forces, lab-frame torques and energies with
+// compensated (Kahan) sums, the warp combines them with an error-free TwoSum butterfly, and
+// lane 0 rotates the torque into the body frame and writes the result.  Replaces the
+// reference's thread-per-nucleotide dna_forces (src/CUDA/Interactions/CUDA_DNA.cuh:832-904).
+//
+// Three instantiations:
+//  * FP32 "mixed" path: positions as a hi/lo float pair so that pair separations keep ~1e-7
+//    absolute accuracy in boxes of side 200+, quaternions in FP32, FP32 pair math;
+//  * FP64 path: the same physics in double, for parity against the FP64 oracle;
+//  * reference layout: float4 positions with btype/index packed in w, float4 quaternions,
+//    int2 bonds and a neighbour matrix of any stride, accumulating into forces and torques
+//    initialised by the caller, exactly the contract of CUDABaseInteraction::compute_forces.
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+
+namespace oxgb {
+
+template <typename R>
+struct KahanV {
+	v3<R> s, c;
+	OXGB_HD void add(v3<R> x) {
+		kadd(s.x, c.x, x.x);
+		kadd(s.y, c.y, x.y);
+		kadd(s.z, c.z, x.z);
+	}
+	static OXGB_HD void kadd(R &sum, R &comp, R x) {
+		const R y = x - comp;
+		const R t = sum + y;
+		comp = (t - sum) - y;
+		sum = t;
+	}
+};
+
+// sum over the warp of (s - c) pairs with TwoSum at every butterfly level; all lanes get it
+template <typename R>
+__device__ __forceinline__ R warp_sum_comp(R s, R c) {
+	R err = -c;
+#pragma unroll
+	for(int off = 16; off > 0; off >>= 1) {
+		const R so = __shfl_xor_sync(0xffffffffu, s, off);
+		const R eo = __shfl_xor_sync(0xffffffffu, err, off);
+		const R t = s + so;
+		const R bp = t - s;
+		const R e2 = (s - (t - bp)) + (so - bp);
+		s = t;
+		err += eo + e2;
+	}
+	return s + err;
+}
+
+__device__ __forceinline__ int ref_type_of_btype(int bt) {
+	return (bt > 0) ? (bt & 3) : 3 - ((3 - bt) & 3);
+}
+
+template <typename R>
+__device__ __forceinline__ void load_table(const DNA2Table<R> *g, DNA2Table<R> *s) {
+	const int n = sizeof(DNA2Table<R>) / sizeof(int);
+	const int *src = reinterpret_cast<const int *>(g);
+	int *dst = reinterpret_cast<int *>(s);
+	for(int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+	__syncthreads();
+}
+
+// ---------------------------------------------------------------- particle loaders
+
+struct LoadMixed {
+	const float4 *pos_hi, *pos_lo, *fa1, *fa3;
+	__device__ __forceinline__ void load(int i, const DNA2Table<float> &P, const int2 b, Nuc<float> &n, float4 &hi,
+			float4 &lo) const {
+		hi = __ldg(pos_hi + i);
+		lo = __ldg(pos_lo + i);
+		const float4 x1 = __ldg(fa1 + i), x3 = __ldg(fa3 + i);
+		n.a1 = v3<float>{x1.x, x1.y, x1.z};
+		n.a3 = v3<float>{x3.x, x3.y, x3.z};
+		n.a2 = cross(n.a3, n.a1);
+		make_sites(P, n);
+		n.btype = __float_as_int(hi.w) >> 22;
+		n.type = __float_as_int(lo.w) & 7;
+		n.is_end = (b.x < 0 || b.y < 0);
+	}
+	// minimum image of q - p as hi + lo: the hi difference of nearby coordinates and its
+	// shift by a box side are exact (Sterbenz), the low parts and the box remainder go to lo
+	__device__ __forceinline__ Sep<float> sep(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql,
+			const DNA2Table<float> &P) const {
+		float d[3] = {qh.x - ph.x, qh.y - ph.y, qh.z - ph.z};
+		float l[3] = {ql.x - pl.x, ql.y - pl.y, ql.z - pl.z};
+#pragma unroll
+		for(int k = 0; k < 3; k++) {
+			const float m = rintf(d[k] / P.box_hi);
+			d[k] = fmaf(-m, P.box_hi, d[k]);
+			l[k] = fmaf(-m, P.box_lo, l[k]);
+		}
+		return Sep<float>{v3<float>{d[0], d[1], d[2]}, v3<float>{l[0], l[1], l[2]}};
+	}
+	// bonded neighbours: no periodic image
+	__device__ __forceinline__ Sep<float> diff(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql) const {
+		return Sep<float>{v3<float>{qh.x - ph.x, qh.y - ph.y, qh.z - ph.z}, v3<float>{ql.x - pl.x, ql.y - pl.y, ql.z - pl.z}};
+	}
+};
+
+struct LoadDouble {
+	const double4_32a *pos, *quat;
+	const float4 *meta;  // pos_hi of the mixed layout: w carries btype; lo.w carries the type
+	const float4 *meta_lo;
+	__device__ __forceinline__ void load(int i, const DNA2Table<double> &P, const int2 b, Nuc<double> &n, double4_32a &ps,
+			double4_32a &unused) const {
+		ps = pos[i];
+		const double4_32a q = quat[i];
+		quat_frame(q.x, q.y, q.z, q.w, n.a1, n.a2, n.a3);
+		make_sites(P, n);
+		n.btype = __float_as_int(meta[i].w) >> 22;
+		n.type = __float_as_int(meta_lo[i].w) & 7;
+		n.is_end = (b.x < 0 || b.y < 0);
+	}
+	__device__ __forceinline__ Sep<double> sep(const double4_32a &p, const double4_32a &, const double4_32a &q, const double4_32a &,
+			const DNA2Table<double> &P) const {
+		double d[3] = {q.x - p.x, q.y - p.y, q.z - p.z};
+		const double L = P.box_hi + P.box_lo;
+#pragma unroll
+		for(int k = 0; k < 3; k++) d[k] = d[k] - rint(d[k] / L) * L;
+		return Sep<double>{v3<double>{d[0], d[1], d[2]}, v3<double>{0., 0., 0.}};
+	}
+	__device__ __forceinline__ Sep<double> diff(const double4_32a &p, const double4_32a &, const double4_32a &q, const double4_32a &) const {
+		return Sep<double>{v3<double>{q.x - p.x, q.y - p.y, q.z - p.z}, v3<double>{0., 0., 0.}};
+	}
+};
+
+struct LoadRef {
+	const float4 *pos, *quat;
+	__device__ __forceinline__ void load(int i, const DNA2Table<float> &P, const int2 b, Nuc<float> &n, float4 &hi,
+			float4 &lo) const {
+		hi = pos[i];
+		lo = make_float4(0.f, 0.f, 0.f, 0.f);
+		const float4 q = quat[i];
+		quat_frame(q.x, q.y, q.z, q.w, n.a1, n.a2, n.a3);
+		make_sites(P, n);
+		n.btype = __float_as_int(hi.w) >> 22;
+		n.type = ref_type_of_btype(n.btype);
+		n.is_end = (b.x < 0 || b.y < 0);
+	}
+	__device__ __forceinline__ Sep<float> sep(const float4 &ph, const float4 &, const float4 &qh, const float4 &,
+			const DNA2Table<float> &P) const {
+		float d[3] = {qh.x - ph.x, qh.y - ph.y, qh.z - ph.z};
+#pragma unroll
+		for(int k = 0; k < 3; k++) d[k] = fmaf(-rintf(d[k] / P.box_hi), P.box_hi, d[k]);
+		return Sep<float>{v3<float>{d[0], d[1], d[2]}, v3<float>{0.f, 0.f, 0.f}};
+	}
+	__device__ __forceinline__ Sep<float> diff(const float4 &ph, const float4 &, const float4 &qh, const float4 &) const {
+		return Sep<float>{v3<float>{qh.x - ph.x, qh.y - ph.y, qh.z - ph.z}, v3<float>{0.f, 0.f, 0.f}};
+	}
+};
+
+template <typename R>
+struct Vec4Of;
+template <>
+struct Vec4Of<float> {
+	using T = float4;
+};
+template <>
+struct Vec4Of<double> {
+	using T = double4_32a;
+};
+
+// ---------------------------------------------------------------- the kernel
+
+template <typename R, class Loader, bool SPLIT, bool ACCUMULATE, bool FUSE_KICK>
+__global__ void __launch_bounds__(128) k_forces(ForceArgs a, Loader ld) {
+	using V4 = typename Vec4Of<R>::T;
+	__shared__ DNA2Table<R> P;
+	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
+
+	const int lane = threadIdx.x & 31;
+	const int warps_per_block = blockDim.x >> 5;
+	const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+	const int nw = gridDim.x * warps_per_block;
+	V4 *F4 = reinterpret_cast<V4 *>(a.forces);
+	V4 *T4 = reinterpret_cast<V4 *>(a.torques);
+
+	for(int i = gw; i < a.N; i += nw) {
+		const int2 bi = a.bonds[i];
+		Nuc<R> p;
+		V4 ph, pl;
+		ld.load(i, P, bi, p, ph, pl);
+
+		KahanV<R> F{}, T{};
+		R E = R(0), Ec = R(0), Eh = R(0), Ehc = R(0);
+		R split[N_TERMS];
+		if(SPLIT) {
+#pragma unroll
+			for(int k = 0; k < N_TERMS; k++) split[k] = R(0);
+		}
+
+		// bonded pairs: lane 0 the 3' neighbour (p = i), lane 1 the 5' neighbour (q = i)
+		if(lane < 2) {
+			const int j = (lane == 0) ? bi.x : bi.y;
+			if(j >= 0) {
+				const int2 bj = a.bonds[j];
+				Nuc<R> q;
+				V4 qh, ql;
+				ld.load(j, P, bj, q, qh, ql);
+				PairOut<R> o{};
+				bool ok;
+				if(lane == 0) ok = bonded<R, SPLIT, false>(P, p, q, ld.diff(ph, pl, qh, ql), o);
+				else ok = bonded<R, SPLIT, true>(P, q, p, ld.diff(qh, ql, ph, pl), o);
+				if(!ok) atomicOr(a.status, OXGB_ERR_FENE);
+				F.add(o.F);
+				T.add(o.T);
+				KahanV<R>::kadd(E, Ec, o.E);
+				if(SPLIT) {
+#pragma unroll
+					for(int k = 0; k < N_TERMS; k++) split[k] += o.split[k];
+				}
+			}
+		}
+
+		const int nn = a.nnb[i];
+		if(nn > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
+		const int nlim = nn < a.max_nb ? nn : a.max_nb;
+		const long long row = (long long) i * a.nb_stride_i;
+		for(int k = lane; k < nlim; k += 32) {
+			const int j = a.nb[row + (long long) k * a.nb_stride_k];
+			if(j == i || j == bi.x || j == bi.y) continue;
+			const int2 bj = a.bonds[j];
+			Nuc<R> q;
+			V4 qh, ql;
+			ld.load(j, P, bj, q, qh, ql);
+			PairOut<R> o{};
+			nonbonded_p<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
+			F.add(o.F);
+			T.add(o.T);
+			KahanV<R>::kadd(E, Ec, o.E);
+			KahanV<R>::kadd(Eh, Ehc, o.Ehb);
+			if(SPLIT) {
+#pragma unroll
+				for(int k2 = 0; k2 < N_TERMS; k2++) split[k2] += o.split[k2];
+			}
+		}
+
+		const R fx = warp_sum_comp(F.s.x, F.c.x), fy = warp_sum_comp(F.s.y, F.c.y), fz = warp_sum_comp(F.s.z, F.c.z);
+		const R tx = warp_sum_comp(T.s.x, T.c.x), ty = warp_sum_comp(T.s.y, T.c.y), tz = warp_sum_comp(T.s.z, T.c.z);
+		const R e = warp_sum_comp(E, Ec), eh = warp_sum_comp(Eh, Ehc);
+		if(SPLIT) {
+#pragma unroll
+			for(int k = 0; k < N_TERMS; k++) split[k] = warp_sum_comp(split[k], R(0));
+		}
+		if(lane == 0) {
+			const v3<R> tl{tx, ty, tz};
+			// body frame: components along a1, a2, a3
+			const R bx = dot(p.a1, tl), by = dot(p.a2, tl), bz = dot(p.a3, tl);
+			V4 fo, to;
+			if(ACCUMULATE) {
+				fo = F4[i];
+				to = T4[i];
+				fo.x += fx;
+				fo.y += fy;
+				fo.z += fz;
+				fo.w += e;
+				to.x += bx;
+				to.y += by;
+				to.z += bz;
+				to.w = eh;
+			}
+			else {
+				fo.x = fx;
+				fo.y = fy;
+				fo.z = fz;
+				fo.w = e;
+				to.x = bx;
+				to.y = by;
+				to.z = bz;
+				to.w = eh;
+			}
+			F4[i] = fo;
+			T4[i] = to;
+			if(FUSE_KICK) {
+				// second half kick of velocity Verlet, in double (CUDA_mixed.cuh:71-93)
+				const double hdt = 0.5 * a.dt;
+				double4_32a v = a.vel[i], L = a.angmom[i];
+				v.x += (double) fo.x * hdt;
+				v.y += (double) fo.y * hdt;
+				v.z += (double) fo.z * hdt;
+				L.x += (double) to.x * hdt;
+				L.y += (double) to.y * hdt;
+				L.z += (double) to.z * hdt;
+				a.vel[i] = v;
+				a.angmom[i] = L;
+			}
+			if(SPLIT) {
+#pragma unroll
+				for(int k = 0; k < N_TERMS; k++) atomicAdd(a.esplit + k, 0.5 * (double) split[k]);
+			}
+		}
+	}
+}
+
+// ---------------------------------------------------------------- host launchers
+
+static int grid_for(int N, int warps_per_block) {
+	const int blocks = (N + warps_per_block - 1) / warps_per_block;
+	return blocks > 0 ? blocks : 1;
+}
+
+template <bool SPLIT, bool FUSE>
+static cudaError_t launch_mixed(const ForceArgs &a, cudaStream_t s) {
+	LoadMixed ld{a.pos_hi, a.pos_lo, a.fa1, a.fa3};
+	k_forces<float, LoadMixed, SPLIT, false, FUSE><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_forces_mixed(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s) {
+	if(split) return fuse_kick ? launch_mixed<true, true>(a, s) : launch_mixed<true, false>(a, s);
+	return fuse_kick ? launch_mixed<false, true>(a, s) : launch_mixed<false, false>(a, s);
+}
+
+cudaError_t launch_forces_double(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s) {
+	LoadDouble ld{a.posd, a.quatd, a.pos_hi, a.pos_lo};
+	if(split) {
+		if(fuse_kick) k_forces<double, LoadDouble, true, false, true><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
+		else k_forces<double, LoadDouble, true, false, false><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
+	}
+	else {
+		if(fuse_kick) k_forces<double, LoadDouble, false, false, true><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
+		else k_forces<double, LoadDouble, false, false, false><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
+	}
+	return cudaGetLastError();
+}
+
+cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s) {
+	LoadRef ld{a.pos_hi, a.quat};
+	k_forces<float, LoadRef, false, true, false><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
+	return cudaGetLastError();
+}
+
+}  // namespace oxgb

@@ -1,0 +1,94 @@
+// Internal interface between the C-ABI layer (api.cu) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dna2_pair.cuh"
+
+// device status bits (OR-ed by kernels, read by the host between launches)
+#define OXGB_ERR_FENE 1            /* a backbone bond left the FENE range */
+#define OXGB_ERR_NEIGH_OVERFLOW 2  /* a neighbour row exceeded its capacity */
+#define OXGB_ERR_NONFINITE 4       /* a non-finite or huge coordinate */
+#define OXGB_ERR_CELL 8            /* cell index out of range */
+
+namespace oxgb {
+
+struct ForceArgs {
+	int N;
+	const float4 *pos_hi, *pos_lo;         // FP32 mirrors (w of pos_hi: btype<<22 | index, w of pos_lo: type)
+	const float4 *fa1, *fa3;               // FP32 body axes a1, a3 (rounded once from FP64)
+	const float4 *quat;                    // reference layout only: FP32 quaternions
+	const double4_32a *posd, *quatd;          // FP64 state
+	const int2 *bonds;                    // (n3, n5), -1 if none
+	const int *nb, *nnb;                  // neighbour rows and counts
+	int max_nb;
+	long long nb_stride_i, nb_stride_k;   // element (i, k) at nb[i * stride_i + k * stride_k]
+	void *forces, *torques;               // float4 or double4_32a per particle
+	const void *table;                    // DNA2Table<float> or DNA2Table<double>
+	int *status;
+	double *esplit;                       // 8 system energies (split kernels only)
+	double dt;
+	double4_32a *vel, *angmom;                // second half kick (fused kernels only)
+};
+
+cudaError_t launch_forces_mixed(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s);
+cudaError_t launch_forces_double(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s);
+cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
+
+struct ListArgs {
+	int N;
+	const float4 *pos;      // FP32 positions the list is built from (hi part)
+	float box;
+	float rverlet2;
+	int n_side;             // cells per side
+	const int2 *bonds;
+	int *cell_of;           // [N]
+	int *cell_count;        // [n_cells]
+	int *cell_start;        // [n_cells + 1]
+	int *cell_cursor;       // [n_cells]
+	int *cell_list;         // [N]
+	int *nb, *nnb;          // [N * max_nb], [N]
+	int max_nb;
+	float4 *list_pos;       // positions at this build
+	int *status;
+	int *flag;              // rebuild request, cleared by the build
+	int check_flag;         // 1: every kernel exits at once unless *flag is set
+	unsigned long long *rebuilds;  // counts builds (may be null)
+};
+
+// full rebuild: cells (counting sort, deterministic order) then neighbour rows
+cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s);
+
+struct StepArgs {
+	int N;
+	double dt;
+	double4_32a *pos, *vel, *angmom, *quat;   // FP64 state
+	float4 *pos_hi, *pos_lo, *fa1, *fa3;  // FP32 mirrors written by the first step
+	const void *forces, *torques;         // float4 (mixed) or double4_32a (double)
+	const float4 *list_pos;
+	float skin2;
+	int *flag;
+	int *status;
+	long long *step;                       // device step counter
+	// thermostats
+	int thermostat;                        // 0 none, 1 brownian, 2 bussi
+	int newtonian_steps;
+	double pt, pr, sqrtT, T;
+	unsigned long long seed;
+	double bussi_c;                        // exp(-newtonian_steps / tau)
+	double *bussi_partials;                // [blocks * 8]
+	double *bussi_state;                   // K_t, K_r, then scratch: factor_t, factor_r, vcom x y z
+	int bussi_blocks;
+};
+
+cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s);
+cudaError_t launch_thermostat(const StepArgs &a, cudaStream_t s);
+cudaError_t launch_step_advance(const StepArgs &a, cudaStream_t s);
+// sets the graph conditional to (*flag != 0)
+cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h, cudaStream_t s);
+// refresh the FP32 mirrors from the FP64 state (after a host upload)
+cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s);
+// per-particle kinetic energies, translational and rotational (FP64)
+cudaError_t launch_kinetic(const StepArgs &a, double *out2, cudaStream_t s);
+
+}  // namespace oxgb

@@ -181,29 +181,64 @@ def hairpin(stem_seq: str, loop_len: int, rng: np.random.Generator) -> Molecule:
                     [(0, n, False)])
 
 
-def random_walk_strand(n: int, rng: np.random.Generator, step: float = FENE_R0, min_sep: float = 1.0) -> Molecule:
-    """Self-avoiding random walk of the backbone sites with steps of one FENE r0 (so every
-    backbone bond starts unstretched; nucleotide centres end up ~0.7 apart).  a3 points back
-    along the walk (towards the 5' neighbour); a1 is carried along by parallel transport with
-    a small random twist, each centre sits at back - (BACK1 a1 + BACK2 a2), and a step is
-    redrawn if it brings the two bases of a bonded pair within 0.45 of each other."""
-    back = np.zeros((n, 3))
-    a1 = np.zeros((n, 3))
-    a3 = np.zeros((n, 3))
-    cell = {}
+class _Occupancy:
+    """Backbone sites placed so far, hashed on a grid of cells no smaller than the exclusion
+    distance; periodic with minimum-image distances when a box side is given."""
 
-    def key(p):
-        return tuple(np.floor(p / min_sep).astype(int))
+    def __init__(self, cut: float, box: Optional[float] = None):
+        self.cut = cut
+        self.box = box
+        self.n = max(1, int(box // cut)) if box else 0
+        self.cs = box / self.n if box else cut
+        self.cells = {}
 
-    def free(p, upto):
-        k = key(p)
+    def _key(self, p):
+        if self.box:
+            return tuple(int(np.floor((c % self.box) / self.cs)) % self.n for c in p)
+        return tuple(int(np.floor(c / self.cs)) for c in p)
+
+    def free(self, p, skip_tag) -> bool:
+        k = self._key(p)
+        c2 = self.cut * self.cut
         for dx in (-1, 0, 1):
             for dy in (-1, 0, 1):
                 for dz in (-1, 0, 1):
-                    for j in cell.get((k[0] + dx, k[1] + dy, k[2] + dz), ()):
-                        if j < upto - 1 and np.sum((back[j] - p) ** 2) < min_sep * min_sep:
+                    kk = (k[0] + dx, k[1] + dy, k[2] + dz)
+                    if self.box:
+                        kk = (kk[0] % self.n, kk[1] % self.n, kk[2] % self.n)
+                    for (x, y, z, tag) in self.cells.get(kk, ()):
+                        if tag == skip_tag:
+                            continue
+                        d0, d1, d2 = x - p[0], y - p[1], z - p[2]
+                        if self.box:
+                            d0 -= self.box * round(d0 / self.box)
+                            d1 -= self.box * round(d1 / self.box)
+                            d2 -= self.box * round(d2 / self.box)
+                        if d0 * d0 + d1 * d1 + d2 * d2 < c2:
                             return False
         return True
+
+    def add(self, p, tag):
+        self.cells.setdefault(self._key(p), []).append((float(p[0]), float(p[1]), float(p[2]), tag))
+
+
+def random_walk_strand(n: int, rng: np.random.Generator, step: float = FENE_R0, min_sep: float = 0.8,
+                       occ: Optional[_Occupancy] = None, start: Optional[np.ndarray] = None,
+                       strand_tag: int = 0) -> Molecule:
+    """Self-avoiding random walk of the backbone sites with steps of one FENE r0 (so every
+    backbone bond starts unstretched; nucleotide centres end up ~0.7 apart).  a3 points back
+    along the walk (towards the 5' neighbour); a1 is carried along by parallel transport with
+    a small random twist, and each centre sits at back - (BACK1 a1 + BACK2 a2).  A step is
+    redrawn unless its backbone and base sites keep min_sep from every site placed before
+    (bonded predecessor excepted) and clear the bonded excluded-volume ranges of the
+    predecessor.  With a shared occupancy `occ` (periodic for a melt of many strands) the walk
+    avoids every strand grown before; positions are then absolute and not recentred."""
+    own = occ is None
+    if own:
+        occ = _Occupancy(min_sep)
+    back = np.zeros((n, 3))
+    a1 = np.zeros((n, 3))
+    a3 = np.zeros((n, 3))
 
     def frame(t, v_prev):
         v = v_prev - t * np.dot(v_prev, t)
@@ -215,11 +250,14 @@ def random_walk_strand(n: int, rng: np.random.Generator, step: float = FENE_R0, 
     def base_of(i_back, i_a1, i_a3):
         return i_back + (0.4 - BACK1) * i_a1 - BACK2 * np.cross(i_a3, i_a1)
 
+    if start is not None:
+        back[0] = start
     d = rng.normal(size=3)
     d /= np.linalg.norm(d)
     a3[0] = -d
     a1[0] = frame(a3[0], np.cross(a3[0], rng.normal(size=3)))
-    cell.setdefault(key(back[0]), []).append(0)
+    occ.add(back[0], (strand_tag, 0))
+    occ.add(base_of(back[0], a1[0], a3[0]), (strand_tag, 0))
     for i in range(1, n):
         for attempt in range(1000):
             trial = d + (0.25 + 0.002 * attempt) * rng.normal(size=3)
@@ -227,15 +265,34 @@ def random_walk_strand(n: int, rng: np.random.Generator, step: float = FENE_R0, 
             p = back[i - 1] + step * trial
             t3 = -trial
             t1 = frame(t3, a1[i - 1])
-            if np.linalg.norm(base_of(p, t1, t3) - base_of(back[i - 1], a1[i - 1], a3[i - 1])) > 0.45 and free(p, i):
+            bi = base_of(p, t1, t3)
+            bprev = base_of(back[i - 1], a1[i - 1], a3[i - 1])
+            if np.linalg.norm(bi - bprev) > 0.45 and np.linalg.norm(bi - back[i - 1]) > 0.6 and \
+                    np.linalg.norm(p - bprev) > 0.6 and occ.free(p, (strand_tag, i - 1)) and occ.free(bi, (strand_tag, i - 1)):
                 break
         back[i], a3[i], a1[i] = p, t3, t1
         d = trial
-        cell.setdefault(key(p), []).append(i)
+        occ.add(p, (strand_tag, i))
+        occ.add(base_of(p, t1, t3), (strand_tag, i))
     a2 = np.cross(a3, a1)
     pos = back - (BACK1 * a1 + BACK2 * a2)
-    pos -= pos.mean(axis=0)
+    if own:
+        pos -= pos.mean(axis=0)
     return Molecule(pos, a1, a3, random_sequence(rng, n), [(0, n, False)])
+
+
+def random_walk_melt(n_strands: int, n: int, box: float, rng: np.random.Generator, min_sep: float = 0.8) -> List[Molecule]:
+    """n_strands self-avoiding strands of n nucleotides grown one after the other in a periodic
+    cube, each avoiding every backbone site already placed."""
+    occ = _Occupancy(min_sep, box)
+    mols = []
+    for k in range(n_strands):
+        for _ in range(10000):
+            start = rng.uniform(0, box, size=3)
+            if occ.free(start, None):
+                break
+        mols.append(random_walk_strand(n, rng, occ=occ, start=start, strand_tag=k + 1))
+    return mols
 
 
 def _rotate(m: Molecule, R: np.ndarray, shift: np.ndarray) -> Molecule:
@@ -344,8 +401,9 @@ def kelvin(T_K: float) -> float:
 
 def system_for_config(idx: int, seed: int = 1, scale: float = 1.0) -> System:
     """The five workloads: 0 = one 12-bp duplex in a cube of side 20; 1 = 1000 x 20-bp duplexes at
-    0.01 nucleotides/unit^3; 2 = 250 x 1000-nt random-walk strands at 0.02 (scale shrinks the
-    strand count); 3 = the 40,000-nt system of workload 1; 4 is batched (see batched_systems)."""
+    0.01 nucleotides/unit^3; 2 = 250 x 1000-nt self-avoiding random-walk strands grown in the cube
+    at 0.02 (scale shrinks the duplex or strand count); 3 = the 40,000-nt system of workload 1;
+    4 is batched (see batched_systems)."""
     rng = np.random.default_rng(seed)
     T = kelvin(300.0)
     if idx == 0:
@@ -361,8 +419,7 @@ def system_for_config(idx: int, seed: int = 1, scale: float = 1.0) -> System:
         n_str = max(1, int(round(250 * scale)))
         N = 1000 * n_str
         box = (N / 0.02) ** (1.0 / 3.0)
-        mols = [random_walk_strand(1000, rng) for _ in range(n_str)]
-        return assemble(place(mols, box, rng, min_dist=1.0), box, T, rng)
+        return assemble(random_walk_melt(n_str, 1000, box, rng), box, T, rng)
     raise ValueError("workload 4 is batched: use batched_systems()")
 
 

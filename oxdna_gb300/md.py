@@ -1,0 +1,143 @@
+"""Host-side front end of the MD backend (oxgb_md_* in include/oxgb.h).
+
+`MDSystem` mirrors the reference's MD backend life cycle -- get_settings (keyword arguments
+named after the input keys), init (topology + configuration upload), sim_step (run) and
+apply_simulation_data_changes (state download) -- on top of the C ABI.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _abi
+from . import io as oxio
+
+
+def dna2_settings(T: float, salt: float = 0.5, average: bool = True, seq: Optional[dict] = None,
+                  hb_multiplier: float = 1.0, half_charged_ends: bool = True, dh_lambda: float = 0.3616455,
+                  dh_strength: float = 0.0543, mbf_fmax: Optional[float] = None, mbf_finf: float = 0.04,
+                  reference_cuda_eps: bool = False) -> _abi.DNA2Settings:
+    s = _abi.DNA2Settings()
+    _abi.lib().oxgb_dna2_default_settings(C.byref(s), float(T), float(salt))
+    s.average = 1 if average else 0
+    if seq is not None:
+        order = "AGCT"
+        for i in range(4):
+            for j in range(4):
+                s.seq_stck[i][j] = seq[f"STCK_{order[i]}_{order[j]}"]
+        s.seq_stck_fact_eps = seq["STCK_FACT_EPS"]
+        s.seq_hydr_at = seq.get("HYDR_A_T", seq.get("HYDR_T_A"))
+        s.seq_hydr_gc = seq.get("HYDR_G_C", seq.get("HYDR_C_G"))
+    s.hb_multiplier = hb_multiplier
+    s.dh_half_charged_ends = 1 if half_charged_ends else 0
+    s.dh_lambda = dh_lambda
+    s.dh_strength = dh_strength
+    if mbf_fmax is not None:
+        s.use_mbf = 1
+        s.mbf_fmax = mbf_fmax
+        s.mbf_finf = mbf_finf
+    s.reference_cuda_eps = 1 if reference_cuda_eps else 0
+    return s
+
+
+def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = "no", newtonian_steps: int = 103,
+                pt: float = 0.0, diff_coeff: float = 2.5, bussi_tau: float = 1000.0, seed: int = 1,
+                precision: str = "mixed", cells_auto_optimisation: bool = True, max_neigh: int = 0,
+                steps_per_graph: int = 16) -> _abi.MDSettings:
+    m = _abi.MDSettings()
+    _abi.lib().oxgb_md_default_settings(C.byref(m))
+    m.dt = dt
+    m.verlet_skin = verlet_skin
+    m.thermostat = _abi.THERMOSTATS[thermostat]
+    m.newtonian_steps = newtonian_steps
+    m.pt = pt
+    m.diff_coeff = diff_coeff
+    m.bussi_tau = bussi_tau
+    m.seed = seed
+    m.precision = {"mixed": 0, "float": 0, "double": 1}[precision]
+    m.cells_auto_optimisation = 1 if cells_auto_optimisation else 0
+    m.max_neigh = max_neigh
+    m.steps_per_graph = steps_per_graph
+    return m
+
+
+class MDSystem:
+    """One system on the GPU: topology, FP64 state, Verlet lists, integrator and thermostat."""
+
+    def __init__(self, box: float, top: oxio.Topology, dna: _abi.DNA2Settings, md: _abi.MDSettings):
+        L = _abi.lib()
+        self.N = top.N
+        self.box = float(box)
+        h = C.c_void_p()
+        offsets = np.array([0, self.N], np.int32)
+        _abi.check(L.oxgb_md_create(1, offsets, np.array([self.box]), C.byref(dna), C.byref(md), C.byref(h)))
+        self._h = h
+        _abi.check(L.oxgb_md_set_topology(h, np.ascontiguousarray(top.n3, np.int32), np.ascontiguousarray(top.n5, np.int32),
+                                          np.ascontiguousarray(top.btype, np.int32),
+                                          np.ascontiguousarray(top.type, np.int32)))
+
+    def close(self):
+        if self._h:
+            _abi.lib().oxgb_md_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, pos, quat, vel, Lmom):
+        c = lambda a: np.ascontiguousarray(a, np.float64).reshape(-1)
+        _abi.check(_abi.lib().oxgb_md_set_state(self._h, c(pos), c(quat), c(vel), c(Lmom)))
+
+    def get_state(self):
+        N = self.N
+        pos, quat, vel, Lm = np.zeros((N, 3)), np.zeros((N, 4)), np.zeros((N, 3)), np.zeros((N, 3))
+        _abi.check(_abi.lib().oxgb_md_get_state(self._h, _abi.ptr(pos), _abi.ptr(quat), _abi.ptr(vel), _abi.ptr(Lm)))
+        return dict(pos=pos, quat=quat, vel=vel, Lmom=Lm)
+
+    def run(self, nsteps: int, sync: bool = True):
+        _abi.check(_abi.lib().oxgb_md_run(self._h, int(nsteps), 1 if sync else 0))
+
+    def compute_forces(self):
+        N = self.N
+        F, T, E, Es = np.zeros((N, 3)), np.zeros((N, 3)), np.zeros(N), np.zeros(8)
+        _abi.check(_abi.lib().oxgb_md_compute_forces(self._h, _abi.ptr(F), _abi.ptr(T), _abi.ptr(E), _abi.ptr(Es)))
+        return F, T, E, Es
+
+    def energies(self):
+        U, Kt, Kr = np.zeros(1), np.zeros(1), np.zeros(1)
+        _abi.check(_abi.lib().oxgb_md_energies(self._h, _abi.ptr(U), _abi.ptr(Kt), _abi.ptr(Kr)))
+        return float(U[0]), float(Kt[0]), float(Kr[0])
+
+    def set_temperature(self, T: float):
+        _abi.check(_abi.lib().oxgb_md_set_temperature(self._h, 0, float(T)))
+
+    def neighbours(self):
+        N = self.N
+        nnb = np.zeros(N, np.int32)
+        cell = np.zeros(N, np.int32)
+        ns = C.c_int(0)
+        mx = C.c_int(0)
+        _abi.check(_abi.lib().oxgb_md_info(self._h, None, None, C.byref(mx)))
+        nb = np.zeros(N * mx.value, np.int32)
+        _abi.check(_abi.lib().oxgb_md_neighbours(self._h, _abi.ptr(nnb), _abi.ptr(nb), mx.value, _abi.ptr(cell),
+                                                 C.byref(ns)))
+        return nnb, nb.reshape(N, mx.value), cell, ns.value
+
+    def info(self):
+        r, s, m = C.c_longlong(0), C.c_longlong(0), C.c_int(0)
+        _abi.check(_abi.lib().oxgb_md_info(self._h, C.byref(r), C.byref(s), C.byref(m)))
+        return dict(rebuilds=r.value, step=s.value, max_neigh=m.value)
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self):
+        return _abi.lib().oxgb_md_stream(self._h)
