@@ -189,6 +189,54 @@ struct ListBuffers {
 	}
 };
 
+// term lists of the engine's split force path (column-major, element k of i at [k * N + i])
+struct TermLists {
+	int N = 0, ev_cap = 0, base_cap = 0, stk_cap = 0;
+	int *ev_nb = nullptr, *ev_n = nullptr, *base_nb = nullptr, *base_n = nullptr, *stk_nb = nullptr, *stk_n = nullptr;
+
+	int alloc(int N_, int ev, int base, int stk) {
+		free_all();
+		N = std::max(N_, 1);
+		ev_cap = ev;
+		base_cap = base;
+		stk_cap = stk;
+		CK(cudaMalloc(&ev_nb, sizeof(int) * (size_t) N * ev_cap));
+		CK(cudaMalloc(&base_nb, sizeof(int) * (size_t) N * base_cap));
+		CK(cudaMalloc(&stk_nb, sizeof(int) * (size_t) N * stk_cap));
+		CK(cudaMalloc(&ev_n, sizeof(int) * N));
+		CK(cudaMalloc(&base_n, sizeof(int) * N));
+		CK(cudaMalloc(&stk_n, sizeof(int) * N));
+		return OXGB_OK;
+	}
+	void free_all() {
+		for(int **p : {&ev_nb, &ev_n, &base_nb, &base_n, &stk_nb, &stk_n}) {
+			if(*p) cudaFree(*p);
+			*p = nullptr;
+		}
+	}
+};
+
+// pair-distance bounds of the term lists: a term can only act within these distances (model
+// constants), widened by twice the skin so that the lists stay complete until the next build
+struct TermRadii {
+	float ev2, base2, stk2;
+};
+
+static TermRadii term_radii(double skin) {
+	const double back = std::sqrt((double) OXM_POS_MM_BACK1 * OXM_POS_MM_BACK1 + (double) OXM_POS_MM_BACK2 * OXM_POS_MM_BACK2);
+	const double base = OXM_POS_BASE;
+	double ev = OXM_EXCL_RC1 + 2 * back;                // back-back
+	ev = std::max(ev, (double) OXM_EXCL_RC2 + 2 * base);  // base-base
+	ev = std::max(ev, (double) OXM_EXCL_RC3 + base + back);  // base-back
+	const double hb = std::max((double) OXM_HYDR_RCHIGH, (double) OXM_CRST_RCHIGH);
+	const double margin = 1e-3;
+	TermRadii t;
+	t.ev2 = (float) std::pow(ev + 2 * skin + margin, 2);
+	t.base2 = (float) std::pow(hb + 2 * skin + margin, 2);
+	t.stk2 = (float) std::pow((double) OXM_CXST_RCHIGH + 2 * skin + margin, 2);
+	return t;
+}
+
 struct oxgb_verlet {
 	int N;
 	double box, rcut, skin;
@@ -298,11 +346,14 @@ struct oxgb_md {
 	bool have_topology = false, have_state = false;
 
 	double4_32a *posd = nullptr, *veld = nullptr, *Ld = nullptr, *quatd = nullptr;
-	float4 *pos_hi = nullptr, *pos_lo = nullptr, *fa1 = nullptr, *fa3 = nullptr, *list_pos = nullptr;
+	float4 *pos_hi = nullptr, *pos_lo = nullptr, *fa1 = nullptr, *fa3 = nullptr, *fback = nullptr, *list_pos = nullptr;
+	float4 *list_a1 = nullptr, *list_back = nullptr;
 	int2 *bonds = nullptr;
-	void *F = nullptr, *T = nullptr;
+	void *F = nullptr, *T = nullptr, *bond_f = nullptr, *bond_tp = nullptr, *bond_tq = nullptr;
 	void *d_tab = nullptr;
 	ListBuffers lb;
+	TermLists tl;
+	TermRadii radii{};
 	int *status = nullptr, *flag = nullptr;
 	long long *step = nullptr;
 	double *esplit = nullptr, *scratch = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
@@ -319,10 +370,12 @@ struct oxgb_md {
 	~oxgb_md() {
 		if(gexec) cudaGraphExecDestroy(gexec);
 		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
-					(void *) list_pos, (void *) bonds, F, T, d_tab, (void *) status, (void *) flag, (void *) step,
-					(void *) esplit, (void *) scratch, (void *) bussi_partials, (void *) bussi_state, (void *) d_rebuilds})
+					(void *) fback, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, bond_f,
+					bond_tp, bond_tq, d_tab, (void *) status, (void *) flag, (void *) step, (void *) esplit, (void *) scratch,
+					(void *) bussi_partials, (void *) bussi_state, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
+		tl.free_all();
 		if(stream) cudaStreamDestroy(stream);
 		if(side) cudaStreamDestroy(side);
 	}
@@ -343,6 +396,10 @@ static StepArgs step_args(oxgb_md *h) {
 	a.forces = h->F;
 	a.torques = h->T;
 	a.list_pos = h->list_pos;
+	a.fback = h->fback;
+	a.bonds = h->bonds;
+	a.list_a1 = h->list_a1;
+	a.list_back = h->list_back;
 	a.skin2 = (float) h->md.verlet_skin * (float) h->md.verlet_skin;
 	a.flag = h->flag;
 	a.status = h->status;
@@ -374,8 +431,8 @@ static ForceArgs force_args(oxgb_md *h) {
 	a.nb = h->lb.nb;
 	a.nnb = h->lb.nnb;
 	a.max_nb = h->lb.max_nb;
-	a.nb_stride_i = h->lb.max_nb;
-	a.nb_stride_k = 1;
+	a.nb_stride_i = 1;  // the engine's rows are column-major
+	a.nb_stride_k = h->N;
 	a.forces = h->F;
 	a.torques = h->T;
 	a.table = h->d_tab;
@@ -384,6 +441,19 @@ static ForceArgs force_args(oxgb_md *h) {
 	a.dt = h->md.dt;
 	a.vel = h->veld;
 	a.angmom = h->Ld;
+	a.fback = h->fback;
+	a.ev_nb = h->tl.ev_nb;
+	a.ev_n = h->tl.ev_n;
+	a.base_nb = h->tl.base_nb;
+	a.base_n = h->tl.base_n;
+	a.stk_nb = h->tl.stk_nb;
+	a.stk_n = h->tl.stk_n;
+	a.ev_cap = h->tl.ev_cap;
+	a.base_cap = h->tl.base_cap;
+	a.stk_cap = h->tl.stk_cap;
+	a.bond_f = h->bond_f;
+	a.bond_tp = h->bond_tp;
+	a.bond_tq = h->bond_tq;
 	return a;
 }
 
@@ -447,6 +517,12 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->fa1, sizeof(float4) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->fa3, sizeof(float4) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->list_pos, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->fback, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->list_a1, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->list_back, sizeof(float4) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->bond_f, v4 * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->bond_tp, v4 * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->bond_tq, v4 * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->bonds, sizeof(int2) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->F, v4 * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->T, v4 * N) == cudaSuccess;
@@ -471,6 +547,9 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	const int n_side = cells_per_side(N, (float) h->box[0], h->rverlet, h->md.cells_auto_optimisation != 0);
 	const int cap = md->max_neigh > 0 ? md->max_neigh : std::min(std::max(N - 1, 1), 512);
 	rc = h->lb.alloc(N, n_side, cap);
+	if(rc) return bail(rc);
+	h->radii = term_radii(h->md.verlet_skin);
+	rc = h->tl.alloc(N, std::min(std::max(N - 1, 1), 128), std::min(std::max(N - 1, 1), 64), std::min(std::max(N - 1, 1), 64));
 	if(rc) return bail(rc);
 	// Bussi running kinetic energies start at their targets (BussiThermostat::init)
 	double bs[8] = {0.5 * 3 * (N - 1) * h->dna[0].T, 0.5 * 3 * N * h->dna[0].T, 1, 1, 0, 0, 0, 0};
@@ -506,6 +585,23 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	ListArgs a = list_args(h->lb, h->N, h->pos_hi, (float) h->box[0], h->rverlet, h->bonds, h->list_pos, h->status, h->flag,
 			check_flag);
 	a.rebuilds = h->d_rebuilds;
+	a.col_major = 1;
+	a.fa1 = h->fa1;
+	a.fback = h->fback;
+	a.ev_nb = h->tl.ev_nb;
+	a.ev_n = h->tl.ev_n;
+	a.base_nb = h->tl.base_nb;
+	a.base_n = h->tl.base_n;
+	a.stk_nb = h->tl.stk_nb;
+	a.stk_n = h->tl.stk_n;
+	a.ev_cap = h->tl.ev_cap;
+	a.base_cap = h->tl.base_cap;
+	a.stk_cap = h->tl.stk_cap;
+	a.ev_r2 = h->radii.ev2;
+	a.base_r2 = h->radii.base2;
+	a.stk_r2 = h->radii.stk2;
+	a.list_a1 = h->list_a1;
+	a.list_back = h->list_back;
 	return a;
 }
 
@@ -518,8 +614,7 @@ static int build_list_now(oxgb_md *h) {
 static int compute_forces_now(oxgb_md *h, bool split) {
 	ForceArgs fa = force_args(h);
 	if(split) CK(cudaMemsetAsync(h->esplit, 0, sizeof(double) * 8, h->stream));
-	if(h->dbl) CK(launch_forces_double(fa, split, false, h->stream));
-	else CK(launch_forces_mixed(fa, split, false, h->stream));
+	CK(launch_forces_split(fa, h->dbl, split, false, h->stream));
 	return OXGB_OK;
 }
 
@@ -540,12 +635,34 @@ static int size_and_build_list(oxgb_md *h) {
 	int rc = build_list_now(h);
 	if(rc) return rc;
 	if(h->md.max_neigh > 0) return read_status(h);
-	std::vector<int> cnt(h->N);
+	std::vector<int> cnt(h->N), ce(h->N), cb(h->N), cs(h->N);
 	CK(cudaMemcpyAsync(cnt.data(), h->lb.nnb, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
+	CK(cudaMemcpyAsync(ce.data(), h->tl.ev_n, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
+	CK(cudaMemcpyAsync(cb.data(), h->tl.base_n, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
+	CK(cudaMemcpyAsync(cs.data(), h->tl.stk_n, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
 	CK(cudaStreamSynchronize(h->stream));
 	const int mx = *std::max_element(cnt.begin(), cnt.end());
 	int want = ((std::max(64, mx + mx / 2 + 32) + 31) / 32) * 32;
-	if(want != h->lb.max_nb) {
+	auto cap_of = [](const std::vector<int> &v) {
+		const int m = *std::max_element(v.begin(), v.end());
+		return ((std::max(16, m + m / 2 + 8) + 7) / 8) * 8;
+	};
+	const int we = cap_of(ce), wb = cap_of(cb), ws = cap_of(cs);
+	if(we != h->tl.ev_cap || wb != h->tl.base_cap || ws != h->tl.stk_cap) {
+		if(h->gexec) {
+			cudaGraphExecDestroy(h->gexec);
+			h->gexec = nullptr;
+		}
+		rc = h->tl.alloc(h->N, we, wb, ws);
+		if(rc) return rc;
+		want = want > 0 ? want : h->lb.max_nb;
+		rc = h->lb.alloc(h->N, h->lb.n_side, want);
+		if(rc) return rc;
+		CK(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
+		rc = build_list_now(h);
+		if(rc) return rc;
+	}
+	else if(want != h->lb.max_nb) {
 		if(h->gexec) {
 			cudaGraphExecDestroy(h->gexec);
 			h->gexec = nullptr;
@@ -656,8 +773,7 @@ static int enqueue_step(oxgb_md *h, cudaGraph_t capturing) {
 		CK(launch_list_build(la, h->stream));
 	}
 	ForceArgs fa = force_args(h);
-	if(h->dbl) CK(launch_forces_double(fa, false, true, h->stream));
-	else CK(launch_forces_mixed(fa, false, true, h->stream));
+	CK(launch_forces_split(fa, h->dbl, false, true, h->stream));
 	CK(launch_thermostat(sa, h->stream));
 	CK(launch_step_advance(sa, h->stream));
 	return OXGB_OK;
@@ -716,8 +832,7 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 		ListArgs la = md_list_args(h, 1);
 		CK(launch_list_build(la, h->stream));
 		ForceArgs fa = force_args(h);
-		if(h->dbl) CK(launch_forces_double(fa, false, true, h->stream));
-		else CK(launch_forces_mixed(fa, false, true, h->stream));
+		CK(launch_forces_split(fa, h->dbl, false, true, h->stream));
 		CK(launch_thermostat(sa, h->stream));
 		CK(launch_step_advance(sa, h->stream));
 	}
@@ -725,6 +840,8 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 	if(sync) return read_status(h);
 	return OXGB_OK;
 }
+
+static int download_forces(oxgb_md *h, double *F, double *T, double *E);
 
 extern "C" int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *E, double *E_split) {
 	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
@@ -734,6 +851,19 @@ extern "C" int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *
 	if(rc) return rc;
 	rc = read_status(h);
 	if(rc) return rc;
+	rc = download_forces(h, F, T, E);
+	if(rc) return rc;
+	if(E_split) CK(cudaMemcpy(E_split, h->esplit, sizeof(double) * 8, cudaMemcpyDeviceToHost));
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_get_forces(oxgb_md *h, double *F, double *T, double *E) {
+	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
+	CK(cudaStreamSynchronize(h->stream));
+	return download_forces(h, F, T, E);
+}
+
+static int download_forces(oxgb_md *h, double *F, double *T, double *E) {
 	const int N = h->N;
 	if(h->dbl) {
 		std::vector<double4_32a> f(N), t(N);
@@ -755,7 +885,6 @@ extern "C" int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *
 			if(E) E[i] = f[i].w;
 		}
 	}
-	if(E_split) CK(cudaMemcpy(E_split, h->esplit, sizeof(double) * 8, cudaMemcpyDeviceToHost));
 	return OXGB_OK;
 }
 
@@ -814,7 +943,7 @@ extern "C" int oxgb_md_neighbours(oxgb_md *h, int *nnb, int *nb, int max_neigh, 
 		std::vector<int> rows((size_t) N * h->lb.max_nb);
 		CK(cudaMemcpy(rows.data(), h->lb.nb, sizeof(int) * rows.size(), cudaMemcpyDeviceToHost));
 		for(int i = 0; i < N; i++)
-			for(int k = 0; k < h->lb.max_nb; k++) nb[(size_t) i * max_neigh + k] = rows[(size_t) i * h->lb.max_nb + k];
+			for(int k = 0; k < h->lb.max_nb; k++) nb[(size_t) i * max_neigh + k] = rows[(size_t) k * N + i];  // column-major
 	}
 	return OXGB_OK;
 }

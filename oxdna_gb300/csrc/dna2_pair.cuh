@@ -229,15 +229,15 @@ OXGB_HD R excl_vol(v3<R> r, R sigma, R rstar, R b, R rc, v3<R> &f) {
 
 // ---------------------------------------------------------------- non-bonded pair, p side
 
-// r = minimum image of q.centre - p.centre.  Adds to o the force on p and the lab-frame torque
-// on p from the excluded volume, hydrogen bonding, cross stacking, oxDNA2 coaxial stacking and
-// Debye-Hueckel terms (DNA2Interaction.cpp:42-60 and the term functions it calls).
-template <typename R, bool SPLIT>
-OXGB_HD void nonbonded_p(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
-	const v3<R> r = sep.plain();
-	if(dot(r, r) >= P.rcut2) return;
-	v3<R> f;
+// Every term function adds to o the force on p and the lab-frame torque on p for one pair (p, q)
+// with r / sep = minimum image of q.centre - p.centre.  nonbonded_p applies all of them, in the
+// order of DNA2Interaction::pair_interaction_nonbonded (DNA2Interaction.cpp:42-60); the split
+// force kernel runs each over its own candidate list.
 
+// non-bonded excluded volume (DNAInteraction.cpp:707-777)
+template <typename R, bool SPLIT>
+OXGB_HD void pair_ev(const Nuc<R> &p, const Nuc<R> &q, const v3<R> r, PairOut<R> &o) {
+	v3<R> f;
 	// excluded volume: base-base, back(p)-base(q), base(p)-back(q), back-back
 	{
 		R e = excl_vol(r + q.base - p.base, R(OXM_EXCL_S2), R(OXM_EXCL_R2), R(OXM_EXCL_B2), R(OXM_EXCL_RC2), f);
@@ -254,7 +254,11 @@ OXGB_HD void nonbonded_p(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q
 		o.T -= cross(p.back, f);
 		add_e<R, SPLIT>(o, T_NEXC, e);
 	}
+}
 
+// hydrogen bonding and cross stacking, both on the base-base vector (DNAInteraction.cpp:779-1021)
+template <typename R, bool SPLIT>
+OXGB_HD void pair_base(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
 	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3;
 	const v3<R> rhydro = site_vec(sep, q.base, p.base);
 	const R rh2 = dot(rhydro, rhydro);
@@ -335,8 +339,13 @@ OXGB_HD void nonbonded_p(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q
 			}
 		}
 	}
+}
 
-	// coaxial stacking (oxDNA2: no phi3 factor, pure-harmonic theta1 term)
+// coaxial stacking, oxDNA2 form: no phi3 factor, pure-harmonic theta1 term
+// (DNA2Interaction.cpp:214-306)
+template <typename R, bool SPLIT>
+OXGB_HD void pair_stack(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
+	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3;
 	{
 		const v3<R> rstack = site_vec(sep, q.stack, p.stack);
 		const R rs2 = dot(rstack, rstack);
@@ -373,8 +382,12 @@ OXGB_HD void nonbonded_p(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q
 			}
 		}
 	}
+}
 
-	// Debye-Hueckel (DNA2Interaction.cpp:157-212)
+// Debye-Hueckel between backbone sites, halved charges at strand ends (DNA2Interaction.cpp:157-212).
+// Reads only p.back, q.back and the strand-end flags.
+template <typename R, bool SPLIT>
+OXGB_HD void pair_dh(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const v3<R> r, PairOut<R> &o) {
 	{
 		const v3<R> rback = r + q.back - p.back;
 		const R rb2 = dot(rback, rback);
@@ -404,17 +417,36 @@ OXGB_HD void nonbonded_p(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q
 	}
 }
 
+template <typename R, bool SPLIT>
+OXGB_HD void nonbonded_p(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
+	const v3<R> r = sep.plain();
+	if(dot(r, r) >= P.rcut2) return;
+	pair_ev<R, SPLIT>(p, q, r, o);
+	pair_base<R, SPLIT>(P, p, q, sep, o);
+	pair_stack<R, SPLIT>(P, p, q, sep, o);
+	pair_dh<R, SPLIT>(P, p, q, r, o);
+}
+
 // ---------------------------------------------------------------- bonded pair
 
 // p is the nucleotide whose 3' neighbour is q, r = q.centre - p.centre (no periodic image).
 // Backbone FENE (with the optional max_backbone_force log tail), bonded excluded volume and
-// stacking (DNAInteraction.cpp:415-705).  QSIDE selects whose force and lab torque are added.
-// Returns false if the backbone bond left the FENE range.
-template <typename R, bool SPLIT, bool QSIDE>
-OXGB_HD bool bonded(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
+// stacking (DNAInteraction.cpp:415-705), evaluated once for both nucleotides: f is the force on
+// q (-f acts on p), tp / tq the lab-frame torques on p / q.  Returns false if the backbone bond
+// left the FENE range.
+template <typename R>
+struct BondOut {
+	v3<R> f, tp, tq;
+	R E;
+	R split[3];  // FENE, bonded excluded volume, stacking
+};
+
+template <typename R>
+OXGB_HD bool bonded_both(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, BondOut<R> &b) {
 	const v3<R> r = sep.plain();
 	bool ok = true;
-	v3<R> fsum{R(0), R(0), R(0)}, tsum{R(0), R(0), R(0)};  // force on q, torque on the chosen side
+	b.f = b.tp = b.tq = v3<R>{R(0), R(0), R(0)};
+	b.E = R(0);
 	// FENE
 	{
 		const v3<R> rback = site_vec(sep, q.back, p.back);
@@ -427,36 +459,39 @@ OXGB_HD bool bonded(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, con
 			e = (P.mbf_fmax - P.mbf_finf) * P.mbf_xmax * m_log(ax) + P.mbf_finf * ax - P.mbf_long_xmax + P.mbf_fene_xmax;
 			force = rback * (-m_copysign(R(1), x) * ((P.mbf_fmax - P.mbf_finf) * P.mbf_xmax / ax + P.mbf_finf) / rmod);
 		}
-		else {
-			if(m_fabs(x) >= R(OXM_FENE_DELTA)) {
-				ok = false;
-				e = R(0);
-				force = v3<R>{R(0), R(0), R(0)};
-			}
-			else {
-				e = -(R(OXM_FENE_EPS) / R(2)) * m_log(R(1) - x * x / R(OXM_FENE_DELTA2));
-				force = rback * (-(R(OXM_FENE_EPS) * x / (R(OXM_FENE_DELTA2) - x * x)) / rmod);
-			}
+		else if(m_fabs(x) >= R(OXM_FENE_DELTA)) {
+			ok = false;
+			e = R(0);
+			force = v3<R>{R(0), R(0), R(0)};
 		}
-		add_e<R, SPLIT>(o, T_FENE, e);
-		fsum += force;
-		tsum += QSIDE ? cross(q.back, force) : -cross(p.back, force);
+		else {
+			e = -(R(OXM_FENE_EPS) / R(2)) * m_log(R(1) - x * x / R(OXM_FENE_DELTA2));
+			force = rback * (-(R(OXM_FENE_EPS) * x / (R(OXM_FENE_DELTA2) - x * x)) / rmod);
+		}
+		b.split[0] = e;
+		b.f += force;
+		b.tp -= cross(p.back, force);
+		b.tq += cross(q.back, force);
 	}
 	// bonded excluded volume: base-base, base(p)-back(q), back(p)-base(q)
 	{
 		v3<R> f;
 		R e = excl_vol(r + q.base - p.base, R(OXM_EXCL_S2), R(OXM_EXCL_R2), R(OXM_EXCL_B2), R(OXM_EXCL_RC2), f);
-		fsum += f;
-		tsum += QSIDE ? cross(q.base, f) : -cross(p.base, f);
+		b.f += f;
+		b.tp -= cross(p.base, f);
+		b.tq += cross(q.base, f);
 		e += excl_vol(r + q.back - p.base, R(OXM_EXCL_S3), R(OXM_EXCL_R3), R(OXM_EXCL_B3), R(OXM_EXCL_RC3), f);
-		fsum += f;
-		tsum += QSIDE ? cross(q.back, f) : -cross(p.base, f);
+		b.f += f;
+		b.tp -= cross(p.base, f);
+		b.tq += cross(q.back, f);
 		e += excl_vol(r + q.base - p.back, R(OXM_EXCL_S4), R(OXM_EXCL_R4), R(OXM_EXCL_B4), R(OXM_EXCL_RC4), f);
-		fsum += f;
-		tsum += QSIDE ? cross(q.base, f) : -cross(p.back, f);
-		add_e<R, SPLIT>(o, T_BEXC, e);
+		b.f += f;
+		b.tp -= cross(p.back, f);
+		b.tq += cross(q.base, f);
+		b.split[1] = e;
 	}
 	// stacking
+	b.split[2] = R(0);
 	{
 		const v3<R> a1 = p.a1, a2 = p.a2, a3 = p.a3, b1 = q.a1, b2 = q.a2, b3 = q.a3;
 		const v3<R> rbackref = r + b1 * R(OXM_POS_BACK) - a1 * R(OXM_POS_BACK);
@@ -477,7 +512,7 @@ OXGB_HD bool bonded(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, con
 		d5 = -d5;
 		d6 = -d6;
 		const R e = F1 * g4 * g5 * g6 * h1 * h2;
-		add_e<R, SPLIT>(o, T_STCK, e);
+		b.split[2] = e;
 		if(e != R(0)) {
 			const R gam = R(OXM_POS_STACK) - R(OXM_POS_BACK);
 			const R rbr3 = rbr * rbr * rbr;
@@ -507,30 +542,43 @@ OXGB_HD bool bonded(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, con
 			const R fp2 = -F1 * g4 * g5 * g6 * h1 * h2d;
 			force -= (rd * dc2dr + ((b2 - rd * sb2) * dc2dra2 + (b1 - rd * sb1) * dc2dra1 + (a1 - rd * sa1) * dc2drb1) * (R(1) / rsm)) * fp2;
 
-			fsum += force;
+			b.f += force;
 			const v3<R> t4dir = cross(b3, a3);
 			const R tm4 = F1 * d4 * g5 * g6 * h1 * h2;
 			const v3<R> pure1 = cross(a2, b1) * (fp1 * dc1da2b1) + cross(a1, b1) * (fp1 * dc1da1b1);
 			const v3<R> pure2 = cross(a1, b2) * (fp2 * dc2da2b1) + cross(a1, b1) * (fp2 * dc2da1b1);
-			if(QSIDE) {
-				v3<R> tq = cross(q.stack, force) + t4dir * tm4;
-				tq += cross(rd, b3) * (F1 * g4 * g5 * d6 * h1 * h2);
-				tq += cross(rd, b1) * (fp1 * dc1drb1) + pure1;
-				tq += cross(rd, b2) * (fp2 * dc2dra2) + cross(rd, b1) * (fp2 * dc2dra1) + pure2;
-				tsum += tq;
-			}
-			else {
-				v3<R> tp = -cross(p.stack, force) - t4dir * tm4;
-				tp -= cross(rd, a3) * (-(F1 * g4 * d5 * g6 * h1 * h2));
-				tp += cross(rd, a2) * (fp1 * dc1dra2) + cross(rd, a1) * (fp1 * dc1dra1) - pure1;
-				tp += cross(rd, a1) * (fp2 * dc2drb1) - pure2;
-				tsum += tp;
-			}
+			v3<R> tq = cross(q.stack, force) + t4dir * tm4;
+			tq += cross(rd, b3) * (F1 * g4 * g5 * d6 * h1 * h2);
+			tq += cross(rd, b1) * (fp1 * dc1drb1) + pure1;
+			tq += cross(rd, b2) * (fp2 * dc2dra2) + cross(rd, b1) * (fp2 * dc2dra1) + pure2;
+			b.tq += tq;
+			v3<R> tp = -cross(p.stack, force) - t4dir * tm4;
+			tp -= cross(rd, a3) * (-(F1 * g4 * d5 * g6 * h1 * h2));
+			tp += cross(rd, a2) * (fp1 * dc1dra2) + cross(rd, a1) * (fp1 * dc1dra1) - pure1;
+			tp += cross(rd, a1) * (fp2 * dc2drb1) - pure2;
+			b.tp += tp;
 		}
 	}
-	if(QSIDE) o.F += fsum;
-	else o.F -= fsum;
-	o.T += tsum;
+	b.E = b.split[0] + b.split[1] + b.split[2];
+	return ok;
+}
+
+// one side of a bonded pair: QSIDE selects q (force +f, torque tq) or p (force -f, torque tp)
+template <typename R, bool SPLIT, bool QSIDE>
+OXGB_HD bool bonded(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
+	BondOut<R> b;
+	const bool ok = bonded_both(P, p, q, sep, b);
+	if(QSIDE) {
+		o.F += b.f;
+		o.T += b.tq;
+	}
+	else {
+		o.F -= b.f;
+		o.T += b.tp;
+	}
+	add_e<R, SPLIT>(o, T_FENE, b.split[0]);
+	add_e<R, SPLIT>(o, T_BEXC, b.split[1]);
+	add_e<R, SPLIT>(o, T_STCK, b.split[2]);
 	return ok;
 }
 

@@ -337,3 +337,263 @@ cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s) {
 }
 
 }  // namespace oxgb
+
+// ====================================================================== split path
+//
+// The warp-per-nucleotide kernel above leaves most lanes idle: a nucleotide has ~20-30
+// neighbours, only a few of them close enough for hydrogen bonding, cross or coaxial
+// stacking, and the two bonded pairs ran on two lanes.  The split path instead
+//  * evaluates every bonded pair once, one thread per bond, for both nucleotides;
+//  * runs the non-bonded terms one thread per nucleotide, one loop per term over the term
+//    lists of the Verlet build (full rows for Debye-Hueckel, centre-close pairs for the
+//    excluded volume, base-close pairs for hydrogen bonding + cross stacking, stack-close
+//    pairs for coaxial stacking), so all lanes of a warp run the same term code;
+//  * gathers the bonded results in the non-bonded kernel's epilogue (fixed order, no atomics).
+
+namespace oxgb {
+
+struct SplitMixed {
+	const float4 *hi, *lo, *fa1, *fa3, *fback;
+	__device__ __forceinline__ void full(int j, Nuc<float> &n, float4 &h, float4 &l) const {
+		h = __ldg(hi + j);
+		l = __ldg(lo + j);
+		const float4 x1 = __ldg(fa1 + j), x3 = __ldg(fa3 + j), bk = __ldg(fback + j);
+		n.a1 = v3<float>{x1.x, x1.y, x1.z};
+		n.a3 = v3<float>{x3.x, x3.y, x3.z};
+		n.a2 = cross(n.a3, n.a1);
+		n.back = v3<float>{bk.x, bk.y, bk.z};
+		n.stack = n.a1 * float(OXM_POS_STACK);
+		n.base = n.a1 * float(OXM_POS_BASE);
+		n.btype = __float_as_int(h.w) >> 22;
+		n.type = __float_as_int(l.w) & 7;
+		n.is_end = bk.w != 0.f;
+	}
+	__device__ __forceinline__ void dh(int j, Nuc<float> &n, float4 &h, float4 &l) const {
+		h = __ldg(hi + j);
+		l = __ldg(lo + j);
+		const float4 bk = __ldg(fback + j);
+		n.back = v3<float>{bk.x, bk.y, bk.z};
+		n.is_end = bk.w != 0.f;
+	}
+	__device__ __forceinline__ Sep<float> sep(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql,
+			const DNA2Table<float> &P) const {
+		return LoadMixed{}.sep(ph, pl, qh, ql, P);
+	}
+	__device__ __forceinline__ Sep<float> diff(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql) const {
+		return LoadMixed{}.diff(ph, pl, qh, ql);
+	}
+};
+
+struct SplitDouble {
+	const double4_32a *pos, *quat;
+	const float4 *meta, *meta_lo;
+	const int2 *bonds;
+	__device__ __forceinline__ Sep<double> sep(const double4_32a &p, const double4_32a &, const double4_32a &q,
+			const double4_32a &, const DNA2Table<double> &P) const {
+		return LoadDouble{}.sep(p, p, q, q, P);
+	}
+	__device__ __forceinline__ Sep<double> diff(const double4_32a &p, const double4_32a &, const double4_32a &q,
+			const double4_32a &) const {
+		return LoadDouble{}.diff(p, p, q, q);
+	}
+};
+
+// FP64 loads need the table (for the base-site ratio), so the double loader takes it explicitly
+template <class Loader, typename R>
+__device__ __forceinline__ void load_full(const Loader &ld, int j, const DNA2Table<R> &P, Nuc<R> &n,
+		typename Vec4Of<R>::T &h, typename Vec4Of<R>::T &l);
+template <>
+__device__ __forceinline__ void load_full<SplitMixed, float>(const SplitMixed &ld, int j, const DNA2Table<float> &, Nuc<float> &n,
+		float4 &h, float4 &l) {
+	ld.full(j, n, h, l);
+}
+template <>
+__device__ __forceinline__ void load_full<SplitDouble, double>(const SplitDouble &ld, int j, const DNA2Table<double> &P,
+		Nuc<double> &n, double4_32a &h, double4_32a &l) {
+	LoadDouble{ld.pos, ld.quat, ld.meta, ld.meta_lo}.load(j, P, ld.bonds[j], n, h, l);
+}
+template <class Loader, typename R>
+__device__ __forceinline__ void load_dh(const Loader &ld, int j, const DNA2Table<R> &P, Nuc<R> &n, typename Vec4Of<R>::T &h,
+		typename Vec4Of<R>::T &l) {
+	load_full<Loader, R>(ld, j, P, n, h, l);
+}
+template <>
+__device__ __forceinline__ void load_dh<SplitMixed, float>(const SplitMixed &ld, int j, const DNA2Table<float> &, Nuc<float> &n,
+		float4 &h, float4 &l) {
+	ld.dh(j, n, h, l);
+}
+
+template <typename R, class Loader, bool SPLIT>
+__global__ void __launch_bounds__(128) k_bonded_split(ForceArgs a, Loader ld) {
+	using V4 = typename Vec4Of<R>::T;
+	__shared__ DNA2Table<R> P;
+	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
+	for(int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.N; p += gridDim.x * blockDim.x) {
+		const int q = a.bonds[p].x;
+		if(q < 0) continue;
+		Nuc<R> np, nq;
+		V4 ph, pl, qh, ql;
+		load_full<Loader, R>(ld, p, P, np, ph, pl);
+		load_full<Loader, R>(ld, q, P, nq, qh, ql);
+		BondOut<R> b;
+		if(!bonded_both(P, np, nq, ld.diff(ph, pl, qh, ql), b)) atomicOr(a.status, OXGB_ERR_FENE);
+		V4 f, tp, tq;
+		f.x = b.f.x, f.y = b.f.y, f.z = b.f.z, f.w = b.E;
+		tp.x = b.tp.x, tp.y = b.tp.y, tp.z = b.tp.z, tp.w = R(0);
+		tq.x = b.tq.x, tq.y = b.tq.y, tq.z = b.tq.z, tq.w = R(0);
+		reinterpret_cast<V4 *>(a.bond_f)[p] = f;
+		reinterpret_cast<V4 *>(a.bond_tp)[p] = tp;
+		reinterpret_cast<V4 *>(a.bond_tq)[p] = tq;
+		if(SPLIT) {
+			atomicAdd(a.esplit + T_FENE, (double) b.split[0]);
+			atomicAdd(a.esplit + T_BEXC, (double) b.split[1]);
+			atomicAdd(a.esplit + T_STCK, (double) b.split[2]);
+		}
+	}
+}
+
+template <typename R, bool SPLIT>
+struct SplitAcc {
+	KahanV<R> F, T;
+	R E, Ec, Eh, Ehc;
+	R split[N_TERMS];
+	__device__ __forceinline__ void add(const PairOut<R> &o) {
+		F.add(o.F);
+		T.add(o.T);
+		KahanV<R>::kadd(E, Ec, o.E);
+		KahanV<R>::kadd(Eh, Ehc, o.Ehb);
+		if(SPLIT) {
+#pragma unroll
+			for(int k = 0; k < N_TERMS; k++) split[k] += o.split[k];
+		}
+	}
+};
+
+template <typename R, class Loader, bool SPLIT, bool FUSE_KICK>
+__global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld) {
+	using V4 = typename Vec4Of<R>::T;
+	__shared__ DNA2Table<R> P;
+	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
+	const long long N = a.N;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		Nuc<R> p;
+		V4 ph, pl;
+		load_full<Loader, R>(ld, i, P, p, ph, pl);
+		SplitAcc<R, SPLIT> acc{};
+
+		// Debye-Hueckel over the full Verlet row
+		const int ndh = min(a.nnb[i], a.max_nb);
+		for(int k = 0; k < ndh; k++) {
+			const int j = a.nb[(long long) k * N + i];
+			Nuc<R> q;
+			V4 qh, ql;
+			load_dh<Loader, R>(ld, j, P, q, qh, ql);
+			PairOut<R> o{};
+			pair_dh<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P).plain(), o);
+			acc.add(o);
+		}
+		// excluded volume over centre-close pairs
+		const int nev = min(a.ev_n[i], a.ev_cap);
+		for(int k = 0; k < nev; k++) {
+			const int j = a.ev_nb[(long long) k * N + i];
+			Nuc<R> q;
+			V4 qh, ql;
+			load_full<Loader, R>(ld, j, P, q, qh, ql);
+			PairOut<R> o{};
+			pair_ev<R, SPLIT>(p, q, ld.sep(ph, pl, qh, ql, P).plain(), o);
+			acc.add(o);
+		}
+		// hydrogen bonding and cross stacking over base-close pairs
+		const int nb_ = min(a.base_n[i], a.base_cap);
+		for(int k = 0; k < nb_; k++) {
+			const int j = a.base_nb[(long long) k * N + i];
+			Nuc<R> q;
+			V4 qh, ql;
+			load_full<Loader, R>(ld, j, P, q, qh, ql);
+			PairOut<R> o{};
+			pair_base<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
+			acc.add(o);
+		}
+		// coaxial stacking over stack-close pairs
+		const int ns = min(a.stk_n[i], a.stk_cap);
+		for(int k = 0; k < ns; k++) {
+			const int j = a.stk_nb[(long long) k * N + i];
+			Nuc<R> q;
+			V4 qh, ql;
+			load_full<Loader, R>(ld, j, P, q, qh, ql);
+			PairOut<R> o{};
+			pair_stack<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
+			acc.add(o);
+		}
+		if(SPLIT) {
+#pragma unroll
+			for(int k = 0; k < N_TERMS; k++)
+				if(acc.split[k] != R(0)) atomicAdd(a.esplit + k, 0.5 * (double) acc.split[k]);
+		}
+
+		// bonded pairs of this nucleotide, evaluated by k_bonded_split
+		const int2 bi = a.bonds[i];
+		const V4 *bf = reinterpret_cast<const V4 *>(a.bond_f);
+		if(bi.x >= 0) {
+			const V4 f = bf[i], t = reinterpret_cast<const V4 *>(a.bond_tp)[i];
+			acc.F.add(v3<R>{-f.x, -f.y, -f.z});
+			acc.T.add(v3<R>{t.x, t.y, t.z});
+			KahanV<R>::kadd(acc.E, acc.Ec, f.w);
+		}
+		if(bi.y >= 0) {
+			const V4 f = bf[bi.y], t = reinterpret_cast<const V4 *>(a.bond_tq)[bi.y];
+			acc.F.add(v3<R>{f.x, f.y, f.z});
+			acc.T.add(v3<R>{t.x, t.y, t.z});
+			KahanV<R>::kadd(acc.E, acc.Ec, f.w);
+		}
+
+		const v3<R> tl{acc.T.s.x - acc.T.c.x, acc.T.s.y - acc.T.c.y, acc.T.s.z - acc.T.c.z};
+		V4 fo, to;
+		fo.x = acc.F.s.x - acc.F.c.x;
+		fo.y = acc.F.s.y - acc.F.c.y;
+		fo.z = acc.F.s.z - acc.F.c.z;
+		fo.w = acc.E - acc.Ec;
+		to.x = dot(p.a1, tl);
+		to.y = dot(p.a2, tl);
+		to.z = dot(p.a3, tl);
+		to.w = acc.Eh - acc.Ehc;
+		reinterpret_cast<V4 *>(a.forces)[i] = fo;
+		reinterpret_cast<V4 *>(a.torques)[i] = to;
+		if(FUSE_KICK) {
+			const double hdt = 0.5 * a.dt;
+			double4_32a v = a.vel[i], L = a.angmom[i];
+			v.x += (double) fo.x * hdt;
+			v.y += (double) fo.y * hdt;
+			v.z += (double) fo.z * hdt;
+			L.x += (double) to.x * hdt;
+			L.y += (double) to.y * hdt;
+			L.z += (double) to.z * hdt;
+			a.vel[i] = v;
+			a.angmom[i] = L;
+		}
+	}
+}
+
+template <typename R, class Loader, bool SPLIT, bool FUSE>
+static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s) {
+	const int tpb = 128;
+	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
+	k_bonded_split<R, Loader, SPLIT><<<blocks, tpb, 0, s>>>(a, ld);
+	k_nonbonded_split<R, Loader, SPLIT, FUSE><<<blocks, tpb, 0, s>>>(a, ld);
+}
+
+cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s) {
+	if(dbl) {
+		SplitDouble ld{a.posd, a.quatd, a.pos_hi, a.pos_lo, a.bonds};
+		if(split) fuse_kick ? launch_split_t<double, SplitDouble, true, true>(a, ld, s) : launch_split_t<double, SplitDouble, true, false>(a, ld, s);
+		else fuse_kick ? launch_split_t<double, SplitDouble, false, true>(a, ld, s) : launch_split_t<double, SplitDouble, false, false>(a, ld, s);
+	}
+	else {
+		SplitMixed ld{a.pos_hi, a.pos_lo, a.fa1, a.fa3, a.fback};
+		if(split) fuse_kick ? launch_split_t<float, SplitMixed, true, true>(a, ld, s) : launch_split_t<float, SplitMixed, true, false>(a, ld, s);
+		else fuse_kick ? launch_split_t<float, SplitMixed, false, true>(a, ld, s) : launch_split_t<float, SplitMixed, false, false>(a, ld, s);
+	}
+	return cudaGetLastError();
+}
+
+}  // namespace oxgb

@@ -140,6 +140,29 @@ __device__ __forceinline__ void write_mirror(const StepArgs &a, int i, const dou
 	quat_frame(q.x, q.y, q.z, q.w, a1, a2, a3);
 	a.fa1[i] = make_float4((float) a1.x, (float) a1.y, (float) a1.z, 0.f);
 	a.fa3[i] = make_float4((float) a3.x, (float) a3.y, (float) a3.z, 0.f);
+	// grooved backbone offset (src/Particles/DNANucleotide.cpp:79) and the strand-end flag
+	if(a.fback) {
+		const double b1 = (double) OXM_POS_MM_BACK1, b2 = (double) OXM_POS_MM_BACK2;
+		const int2 bd = a.bonds[i];
+		a.fback[i] = make_float4((float) (a1.x * b1 + a2.x * b2), (float) (a1.y * b1 + a2.y * b2), (float) (a1.z * b1 + a2.z * b2),
+				(bd.x < 0 || bd.y < 0) ? 1.f : 0.f);
+	}
+}
+
+// true if the centre or any interaction site moved more than the skin since the last list build
+__device__ __forceinline__ bool list_stale(const StepArgs &a, int i, const double4_32a &r) {
+	const float4 lp = a.list_pos[i];
+	const float dx = (float) r.x - lp.x, dy = (float) r.y - lp.y, dz = (float) r.z - lp.z;
+	if(dx * dx + dy * dy + dz * dz > a.skin2) return true;
+	if(!a.list_a1) return false;
+	const float4 a1 = a.fa1[i], la1 = a.list_a1[i], bk = a.fback[i], lbk = a.list_back[i];
+	const float ex = a1.x - la1.x, ey = a1.y - la1.y, ez = a1.z - la1.z;
+	float sx = dx + 0.4f * ex, sy = dy + 0.4f * ey, sz = dz + 0.4f * ez;  // base site
+	if(sx * sx + sy * sy + sz * sz > a.skin2) return true;
+	sx = dx + 0.34f * ex, sy = dy + 0.34f * ey, sz = dz + 0.34f * ez;  // stacking site
+	if(sx * sx + sy * sy + sz * sz > a.skin2) return true;
+	sx = dx + (bk.x - lbk.x), sy = dy + (bk.y - lbk.y), sz = dz + (bk.z - lbk.z);  // backbone site
+	return sx * sx + sy * sy + sz * sz > a.skin2;
 }
 
 __global__ void k_make_mirrors(StepArgs a) {
@@ -187,10 +210,8 @@ __global__ void k_first_step(StepArgs a) {
 	a.angmom[i] = L;
 	a.quat[i] = q;
 	write_mirror(a, i, r, q);
-	// Verlet list staleness (CUDA_mixed.cuh:68)
-	const float4 lp = a.list_pos[i];
-	const float dx = (float) r.x - lp.x, dy = (float) r.y - lp.y, dz = (float) r.z - lp.z;
-	if(dx * dx + dy * dy + dz * dz > a.skin2) atomicOr(a.flag, 1);
+	// Verlet list staleness (CUDA_mixed.cuh:68, extended to the interaction sites for the term lists)
+	if(list_stale(a, i, r)) atomicOr(a.flag, 1);
 }
 
 // ---------------------------------------------------------------- thermostats

@@ -29,11 +29,20 @@ struct ForceArgs {
 	double *esplit;                       // 8 system energies (split kernels only)
 	double dt;
 	double4_32a *vel, *angmom;                // second half kick (fused kernels only)
+	// split path (engine layout): backbone-site offsets (w = strand-end flag), term lists
+	// (column-major: element k of nucleotide i at [k * N + i]) and the per-bond buffers
+	const float4 *fback;
+	const int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
+	int ev_cap, base_cap, stk_cap;            // capacities (an overflowed list is read up to them)
+	void *bond_f, *bond_tp, *bond_tq;         // per bond owner p (q = n3[p]): f on q with w = energy, torques
 };
 
 cudaError_t launch_forces_mixed(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s);
 cudaError_t launch_forces_double(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s);
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
+// split path: bonded pairs (one thread per bond, both sides), then non-bonded terms (one
+// thread per nucleotide, one loop per term list) with the bonded results gathered in its epilogue
+cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s);
 
 struct ListArgs {
 	int N;
@@ -54,6 +63,15 @@ struct ListArgs {
 	int *flag;              // rebuild request, cleared by the build
 	int check_flag;         // 1: every kernel exits at once unless *flag is set
 	unsigned long long *rebuilds;  // counts builds (may be null)
+	// term lists (null: full rows only).  A pair enters the excluded-volume list when its centres
+	// are closer than ev_r, the base list when its base sites are closer than base_r, the stack
+	// list when its stacking sites are closer than stk_r (all thresholds include twice the skin)
+	const float4 *fa1, *fback;
+	int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
+	int ev_cap, base_cap, stk_cap;
+	float ev_r2, base_r2, stk_r2;
+	float4 *list_a1, *list_back;   // body axis a1 and backbone offset at this build
+	int col_major;          // full rows column-major ([k * N + i]) instead of row-major
 };
 
 // full rebuild: cells (counting sort, deterministic order) then neighbour rows
@@ -66,6 +84,9 @@ struct StepArgs {
 	float4 *pos_hi, *pos_lo, *fa1, *fa3;  // FP32 mirrors written by the first step
 	const void *forces, *torques;         // float4 (mixed) or double4_32a (double)
 	const float4 *list_pos;
+	float4 *fback;                         // backbone offset (w: strand-end flag), written with the mirrors
+	const int2 *bonds;
+	const float4 *list_a1, *list_back;     // site data of the last list build (null: centres only)
 	float skin2;
 	int *flag;
 	int *status;

@@ -111,6 +111,15 @@ __global__ void k_cell_order(ListArgs a, int n_cells) {
 	}
 }
 
+// minimum-image separation vector (the reference's fp32 geometry, explicit fused multiply-adds)
+__device__ __forceinline__ float3 min_image_vec(float4 a, float4 b, float L) {
+	float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+	dx = __fmaf_rn(-rintf(__fdiv_rn(dx, L)), L, dx);
+	dy = __fmaf_rn(-rintf(__fdiv_rn(dy, L)), L, dy);
+	dz = __fmaf_rn(-rintf(__fdiv_rn(dz, L)), L, dz);
+	return make_float3(dx, dy, dz);
+}
+
 __global__ void k_neighbours(ListArgs a) {
 	SKIP_IF_FRESH(a);
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -120,8 +129,14 @@ __global__ void k_neighbours(ListArgs a) {
 	const int n = a.n_side;
 	const int c = a.cell_of[i];
 	const int cx = c % n, cy = (c / n) % n, cz = c / (n * n);
-	int cnt = 0;
-	int *row = a.nb + (long long) i * a.max_nb;
+	const bool terms = a.ev_nb != nullptr;
+	float4 a1i = make_float4(0.f, 0.f, 0.f, 0.f), bki = a1i;
+	if(terms) {
+		a1i = a.fa1[i];
+		bki = a.fback[i];
+	}
+	const long long N = a.N;
+	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
 	for(int dz = -1; dz <= 1; dz++) {
 		const int z = (cz + dz + n) % n;
 		for(int dy = -1; dy <= 1; dy++) {
@@ -133,9 +148,33 @@ __global__ void k_neighbours(ListArgs a) {
 				for(int k = a.cell_start[cc]; k < e; k++) {
 					const int j = a.cell_list[k];
 					if(j == i || j == b.x || j == b.y) continue;
-					if(sqr_min_image(r, a.pos[j], a.box) < a.rverlet2) {
-						if(cnt < a.max_nb) row[cnt] = j;
+					const float4 rj = a.pos[j];
+					const float d2 = sqr_min_image(r, rj, a.box);
+					if(d2 < a.rverlet2) {
+						if(cnt < a.max_nb) {
+							if(a.col_major) a.nb[(long long) cnt * N + i] = j;
+							else a.nb[(long long) i * a.max_nb + cnt] = j;
+						}
 						cnt++;
+						if(terms && d2 < a.ev_r2) {
+							if(nev < a.ev_cap) a.ev_nb[(long long) nev * N + i] = j;
+							nev++;
+							const float3 d = min_image_vec(r, rj, a.box);
+							const float4 a1j = a.fa1[j];
+							// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
+							const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
+									bz = d.z + 0.4f * (a1j.z - a1i.z);
+							if(bx * bx + by * by + bz * bz < a.base_r2) {
+								if(nbase < a.base_cap) a.base_nb[(long long) nbase * N + i] = j;
+								nbase++;
+							}
+							const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy = d.y + 0.34f * (a1j.y - a1i.y),
+									sz = d.z + 0.34f * (a1j.z - a1i.z);
+							if(sx * sx + sy * sy + sz * sz < a.stk_r2) {
+								if(nstk < a.stk_cap) a.stk_nb[(long long) nstk * N + i] = j;
+								nstk++;
+							}
+						}
 					}
 				}
 			}
@@ -144,6 +183,14 @@ __global__ void k_neighbours(ListArgs a) {
 	if(cnt > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
 	a.nnb[i] = cnt;
 	a.list_pos[i] = r;
+	if(terms) {
+		if(nev > a.ev_cap || nbase > a.base_cap || nstk > a.stk_cap) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
+		a.ev_n[i] = nev;
+		a.base_n[i] = nbase;
+		a.stk_n[i] = nstk;
+		a.list_a1[i] = a1i;
+		a.list_back[i] = bki;
+	}
 }
 
 // runs after every other list kernel: counts the build and clears the request

@@ -299,49 +299,32 @@ def _rotate(m: Molecule, R: np.ndarray, shift: np.ndarray) -> Molecule:
     return Molecule(m.pos @ R.T + shift, m.a1 @ R.T, m.a3 @ R.T, m.seq, m.strands)
 
 
-def place(molecules: Sequence[Molecule], box: float, rng: np.random.Generator, min_dist: float = 1.2,
+def _sites(m: Molecule) -> np.ndarray:
+    """backbone and base sites of every nucleotide (grooved backbone), shape [2n, 3]"""
+    a1 = m.a1 / np.linalg.norm(m.a1, axis=1, keepdims=True)
+    a3 = m.a3 / np.linalg.norm(m.a3, axis=1, keepdims=True)
+    a2 = np.cross(a3, a1)
+    back = m.pos + BACK1 * a1 + BACK2 * a2
+    base = m.pos + 0.4 * a1
+    return np.concatenate([back, base])
+
+
+def place(molecules: Sequence[Molecule], box: float, rng: np.random.Generator, min_dist: float = 0.9,
           max_tries: int = 2000) -> List[Molecule]:
-    """Random centres and orientations in a periodic cube; rejects any new nucleotide within
-    min_dist (minimum image) of an already placed one."""
+    """Random centres and orientations in a periodic cube.  A copy is rejected if any of its
+    backbone or base sites comes within min_dist (minimum image) of a site of a molecule placed
+    before, so different molecules start outside every excluded-volume range (at most 0.71)."""
     placed: List[Molecule] = []
-    ncell = max(1, int(box // min_dist))
-    csize = box / ncell
-    grid = {}
-
-    def cells_of(p):
-        c = np.floor((p % box) / csize).astype(int) % ncell
-        return c
-
-    for m in molecules:
+    occ = _Occupancy(min_dist, box)
+    for k, m in enumerate(molecules):
         for _ in range(max_tries):
             R = random_rotation(rng)
             shift = rng.uniform(0, box, size=3)
             cand = _rotate(m, R, shift)
-            cc = cells_of(cand.pos)
-            clash = False
-            for i in range(cand.pos.shape[0]):
-                for dx in (-1, 0, 1):
-                    for dy in (-1, 0, 1):
-                        for dz in (-1, 0, 1):
-                            k = ((cc[i, 0] + dx) % ncell, (cc[i, 1] + dy) % ncell, (cc[i, 2] + dz) % ncell)
-                            for q in grid.get(k, ()):
-                                d = q - cand.pos[i]
-                                d -= box * np.round(d / box)
-                                if d @ d < min_dist * min_dist:
-                                    clash = True
-                                    break
-                            if clash:
-                                break
-                        if clash:
-                            break
-                    if clash:
-                        break
-                if clash:
-                    break
-            if not clash:
-                for i in range(cand.pos.shape[0]):
-                    k = tuple(cc[i])
-                    grid.setdefault(k, []).append(cand.pos[i].copy())
+            sites = _sites(cand)
+            if all(occ.free(p, None) for p in sites):
+                for p in sites:
+                    occ.add(p, k)
                 placed.append(cand)
                 break
         else:

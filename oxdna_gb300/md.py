@@ -109,6 +109,13 @@ class MDSystem:
         _abi.check(_abi.lib().oxgb_md_compute_forces(self._h, _abi.ptr(F), _abi.ptr(T), _abi.ptr(E), _abi.ptr(Es)))
         return F, T, E, Es
 
+    def get_forces(self):
+        """forces, torques and per-nucleotide energies of the last step, not recomputed"""
+        N = self.N
+        F, T, E = np.zeros((N, 3)), np.zeros((N, 3)), np.zeros(N)
+        _abi.check(_abi.lib().oxgb_md_get_forces(self._h, _abi.ptr(F), _abi.ptr(T), _abi.ptr(E)))
+        return F, T, E
+
     def energies(self):
         U, Kt, Kr = np.zeros(1), np.zeros(1), np.zeros(1)
         _abi.check(_abi.lib().oxgb_md_energies(self._h, _abi.ptr(U), _abi.ptr(Kt), _abi.ptr(Kr)))

@@ -164,14 +164,14 @@ def main():
         mols = [G.duplex(G.random_sequence(rng, int(rng.integers(8, 16)))) for _ in range(5)]
         mols += [G.hairpin(G.random_sequence(rng, 7), int(rng.integers(4, 9)), rng) for _ in range(3)]
         mols += [G.random_walk_strand(24, rng) for _ in range(3)]
-        s = G.assemble(G.place(mols, 16.0, rng, min_dist=1.3), 16.0, G.kelvin(300), rng)
+        s = G.assemble(G.place(mols, 16.0, rng), 16.0, G.kelvin(300), rng)
         # thermal jiggle so that angular terms sample away from their ideal values
         s.pos = s.pos + rng.normal(scale=0.01, size=s.pos.shape)
         s.a1 = s.a1 + rng.normal(scale=0.02, size=s.a1.shape)
         s.a3 = s.a3 + rng.normal(scale=0.02, size=s.a3.shape)
         run_case("mixed", *write_system(tmp, s), T300)
         # the same molecules packed with close contacts: excluded-volume forces up to ~1e5
-        s2 = G.assemble(G.place(mols, 16.0, rng, min_dist=0.95), 16.0, G.kelvin(300), rng)
+        s2 = G.assemble(G.place(mols, 16.0, rng, min_dist=0.3), 16.0, G.kelvin(300), rng)
         run_case("contact", *write_system(tmp, s2), T300)
 
         # 5: different salt, temperature and Debye-Hueckel settings, full charges at the ends

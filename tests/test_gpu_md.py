@@ -99,3 +99,20 @@ def test_graph_replay_equals_single_steps():
     assert a.info()["rebuilds"] == b.info()["rebuilds"]
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "double"])
+def test_lists_stay_complete_between_rebuilds(precision):
+    """Forces from term lists carried over many steps equal forces from freshly built lists."""
+    g = load_golden("mixed")
+    sysm, _ = system_from_golden(g, precision=precision, dt=0.003, steps_per_graph=10)
+    for _ in range(6):
+        sysm.run(50)
+        F1, T1, E1 = sysm.get_forces()
+        F2, T2, E2, _ = sysm.compute_forces()  # rebuilds every list first
+        scale = max(1.0, np.abs(F2).max())
+        tol = 1e-12 if precision == "double" else 1e-5
+        assert np.abs(F1 - F2).max() <= tol * scale
+        assert np.abs(T1 - T2).max() <= tol * max(1.0, np.abs(T2).max())
+    assert sysm.info()["rebuilds"] >= 2
+    sysm.close()
