@@ -272,11 +272,11 @@ def main():
     dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
     ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
     tools.oxgb_count_flops.argtypes = [C.c_int, dp, dp, dp, ip, ip, ip, ip, C.c_double, ip, ip, C.c_int, C.c_double,
-                                       C.c_double, dp]
+                                       C.c_double, C.c_double, dp]
     out = np.zeros(4)
     tools.oxgb_count_flops(s.N, np.ascontiguousarray(st["pos"]), np.ascontiguousarray(fa1), np.ascontiguousarray(fa3),
                            s.top.n3, s.top.n5, s.top.type, s.top.btype, s.box, np.ascontiguousarray(nb.reshape(-1)),
-                           nnb, nb.shape[1], s.T, 0.5, out)
+                           nnb, nb.shape[1], s.T, 0.5, 0.05, out)
     flops_launch, sfu_launch, pairs_listed, pairs_in_range = out
     peak = C.c_double(0)
     _abi.check(L.oxgb_probe_fp32_peak(C.byref(peak)))

@@ -216,27 +216,6 @@ struct TermLists {
 	}
 };
 
-// pair-distance bounds of the term lists: a term can only act within these distances (model
-// constants), widened by twice the skin so that the lists stay complete until the next build
-struct TermRadii {
-	float ev2, base2, stk2;
-};
-
-static TermRadii term_radii(double skin) {
-	const double back = std::sqrt((double) OXM_POS_MM_BACK1 * OXM_POS_MM_BACK1 + (double) OXM_POS_MM_BACK2 * OXM_POS_MM_BACK2);
-	const double base = OXM_POS_BASE;
-	double ev = OXM_EXCL_RC1 + 2 * back;                // back-back
-	ev = std::max(ev, (double) OXM_EXCL_RC2 + 2 * base);  // base-base
-	ev = std::max(ev, (double) OXM_EXCL_RC3 + base + back);  // base-back
-	const double hb = std::max((double) OXM_HYDR_RCHIGH, (double) OXM_CRST_RCHIGH);
-	const double margin = 1e-3;
-	TermRadii t;
-	t.ev2 = (float) std::pow(ev + 2 * skin + margin, 2);
-	t.base2 = (float) std::pow(hb + 2 * skin + margin, 2);
-	t.stk2 = (float) std::pow((double) OXM_CXST_RCHIGH + 2 * skin + margin, 2);
-	return t;
-}
-
 struct oxgb_verlet {
 	int N;
 	double box, rcut, skin;

@@ -63,7 +63,7 @@ static void frame_of(const double *a1, const double *a3, int i, Nuc<CF> &n, cons
 
 extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, const double *a3, const int *n3, const int *n5,
 		const int *type, const int *btype, double box, const int *nb, const int *nnb, int max_nb, double T, double salt,
-		double *out) {
+		double skin, double *out) {
 	oxgb_dna2_settings s;
 	default_settings(&s, T, salt);
 	DNA2Table<double> P64;
@@ -73,39 +73,35 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 	to_float(P64, box, P32);
 	DNA2Table<CF> P;
 	std::memcpy(&P, &P32, sizeof(P));
+	// the split force path: every bond once (both nucleotides), Debye-Hueckel over the full rows,
+	// the other terms over the pairs their term lists admit (same bounds as the list build)
+	const TermRadii tr = term_radii(skin);
 	g_flops = g_sfu = 0;
 	double pairs = 0, in_range = 0;
+	auto load = [&](int j, Nuc<CF> &q) {
+		frame_of(a1, a3, j, q, P);
+		q.type = type[j];
+		q.btype = btype[j];
+		q.is_end = n3[j] < 0 || n5[j] < 0;
+	};
 	for(int i = 0; i < N; i++) {
 		Nuc<CF> p;
-		frame_of(a1, a3, i, p, P);
-		p.type = type[i];
-		p.btype = btype[i];
-		p.is_end = n3[i] < 0 || n5[i] < 0;
-		for(int side = 0; side < 2; side++) {
-			const int j = side == 0 ? n3[i] : n5[i];
-			if(j < 0) continue;
+		load(i, p);
+		if(n3[i] >= 0) {
+			const int j = n3[i];
 			Nuc<CF> q;
-			frame_of(a1, a3, j, q, P);
-			q.type = type[j];
-			q.btype = btype[j];
-			q.is_end = n3[j] < 0 || n5[j] < 0;
-			PairOut<CF> o{};
+			load(j, q);
 			Sep<CF> sp;
-			const double d[3] = {pos[3 * j] - pos[3 * i], pos[3 * j + 1] - pos[3 * i + 1], pos[3 * j + 2] - pos[3 * i + 2]};
-			const double sg = side == 0 ? 1.0 : -1.0;
-			sp.hi = v3<CF>{CF(sg * d[0]), CF(sg * d[1]), CF(sg * d[2])};
+			sp.hi = v3<CF>{CF(pos[3 * j] - pos[3 * i]), CF(pos[3 * j + 1] - pos[3 * i + 1]), CF(pos[3 * j + 2] - pos[3 * i + 2])};
 			sp.lo = v3<CF>{CF(0.f), CF(0.f), CF(0.f)};
-			if(side == 0) bonded<CF, false, false>(P, p, q, sp, o);
-			else bonded<CF, false, true>(P, q, p, sp, o);
+			BondOut<CF> b;
+			bonded_both(P, p, q, sp, b);
 		}
 		const int nn = nnb[i] < max_nb ? nnb[i] : max_nb;
 		for(int k = 0; k < nn; k++) {
 			const int j = nb[(long long) i * max_nb + k];
 			Nuc<CF> q;
-			frame_of(a1, a3, j, q, P);
-			q.type = type[j];
-			q.btype = btype[j];
-			q.is_end = n3[j] < 0 || n5[j] < 0;
+			load(j, q);
 			double d[3];
 			for(int c = 0; c < 3; c++) {
 				d[c] = pos[3 * j + c] - pos[3 * i + c];
@@ -115,10 +111,22 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 			Sep<CF> sp;
 			sp.hi = v3<CF>{CF(d[0]), CF(d[1]), CF(d[2])};
 			sp.lo = v3<CF>{CF(0.f), CF(0.f), CF(0.f)};
+			const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
 			PairOut<CF> o{};
-			nonbonded_p<CF, false>(P, p, q, sp, o);
+			pair_dh<CF, false>(P, p, q, sp.plain(), o);
+			if(r2 < tr.ev2) {
+				pair_ev<CF, false>(p, q, sp.plain(), o);
+				double bb = 0, ss = 0;
+				for(int c = 0; c < 3; c++) {
+					const double da = a1[3 * j + c] - a1[3 * i + c];
+					bb += (d[c] + 0.4 * da) * (d[c] + 0.4 * da);
+					ss += (d[c] + 0.34 * da) * (d[c] + 0.34 * da);
+				}
+				if(bb < tr.base2) pair_base<CF, false>(P, p, q, sp, o);
+				if(ss < tr.stk2) pair_stack<CF, false>(P, p, q, sp, o);
+			}
 			pairs += 1;
-			if(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] < rcut * rcut) in_range += 1;
+			if(r2 < rcut * rcut) in_range += 1;
 		}
 	}
 	out[0] = g_flops;

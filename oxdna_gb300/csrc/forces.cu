@@ -469,21 +469,49 @@ struct SplitAcc {
 	}
 };
 
-template <typename R, class Loader, bool SPLIT, bool FUSE_KICK>
+// compensated sum over the K lanes of a group (TwoSum at every level); every lane of the group
+// receives it
+template <typename R, int K>
+__device__ __forceinline__ R group_sum_comp(R s, R c) {
+	R err = -c;
+#pragma unroll
+	for(int off = K / 2; off > 0; off >>= 1) {
+		const R so = __shfl_xor_sync(0xffffffffu, s, off, K);
+		const R eo = __shfl_xor_sync(0xffffffffu, err, off, K);
+		const R t = s + so;
+		const R bp = t - s;
+		const R e2 = (s - (t - bp)) + (so - bp);
+		s = t;
+		err += eo + e2;
+	}
+	return s + err;
+}
+
+// K lanes per nucleotide: lane l of a group takes entries l, l + K, ... of every term list, so a
+// warp holds 32 / K nucleotides and all its lanes run the same term loop
+template <typename R, class Loader, bool SPLIT, bool FUSE_KICK, int K>
 __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	__shared__ DNA2Table<R> P;
 	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
 	const long long N = a.N;
-	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+	const int sub = threadIdx.x % K;
+	const int groups = (gridDim.x * blockDim.x) / K;
+	const int g0 = (blockIdx.x * blockDim.x + threadIdx.x) / K;
+	// every lane iterates the same number of times (all lanes take part in the shuffles)
+	const int rounds = (a.N + groups - 1) / groups;
+	for(int rnd = 0; rnd < rounds; rnd++) {
+		const int i_raw = g0 + rnd * groups;
+		const bool live = i_raw < a.N;
+		const int i = live ? i_raw : a.N - 1;
 		Nuc<R> p;
 		V4 ph, pl;
 		load_full<Loader, R>(ld, i, P, p, ph, pl);
 		SplitAcc<R, SPLIT> acc{};
 
 		// Debye-Hueckel over the full Verlet row
-		const int ndh = min(a.nnb[i], a.max_nb);
-		for(int k = 0; k < ndh; k++) {
+		const int ndh = live ? min(a.nnb[i], a.max_nb) : 0;
+		for(int k = sub; k < ndh; k += K) {
 			const int j = a.nb[(long long) k * N + i];
 			Nuc<R> q;
 			V4 qh, ql;
@@ -493,8 +521,8 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 			acc.add(o);
 		}
 		// excluded volume over centre-close pairs
-		const int nev = min(a.ev_n[i], a.ev_cap);
-		for(int k = 0; k < nev; k++) {
+		const int nev = live ? min(a.ev_n[i], a.ev_cap) : 0;
+		for(int k = sub; k < nev; k += K) {
 			const int j = a.ev_nb[(long long) k * N + i];
 			Nuc<R> q;
 			V4 qh, ql;
@@ -504,8 +532,8 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 			acc.add(o);
 		}
 		// hydrogen bonding and cross stacking over base-close pairs
-		const int nb_ = min(a.base_n[i], a.base_cap);
-		for(int k = 0; k < nb_; k++) {
+		const int nb_ = live ? min(a.base_n[i], a.base_cap) : 0;
+		for(int k = sub; k < nb_; k += K) {
 			const int j = a.base_nb[(long long) k * N + i];
 			Nuc<R> q;
 			V4 qh, ql;
@@ -515,8 +543,8 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 			acc.add(o);
 		}
 		// coaxial stacking over stack-close pairs
-		const int ns = min(a.stk_n[i], a.stk_cap);
-		for(int k = 0; k < ns; k++) {
+		const int ns = live ? min(a.stk_n[i], a.stk_cap) : 0;
+		for(int k = sub; k < ns; k += K) {
 			const int j = a.stk_nb[(long long) k * N + i];
 			Nuc<R> q;
 			V4 qh, ql;
@@ -525,38 +553,45 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 			pair_stack<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
 			acc.add(o);
 		}
-		if(SPLIT) {
+		if(SPLIT && live) {
 #pragma unroll
 			for(int k = 0; k < N_TERMS; k++)
 				if(acc.split[k] != R(0)) atomicAdd(a.esplit + k, 0.5 * (double) acc.split[k]);
 		}
 
-		// bonded pairs of this nucleotide, evaluated by k_bonded_split
-		const int2 bi = a.bonds[i];
-		const V4 *bf = reinterpret_cast<const V4 *>(a.bond_f);
-		if(bi.x >= 0) {
-			const V4 f = bf[i], t = reinterpret_cast<const V4 *>(a.bond_tp)[i];
-			acc.F.add(v3<R>{-f.x, -f.y, -f.z});
-			acc.T.add(v3<R>{t.x, t.y, t.z});
-			KahanV<R>::kadd(acc.E, acc.Ec, f.w);
-		}
-		if(bi.y >= 0) {
-			const V4 f = bf[bi.y], t = reinterpret_cast<const V4 *>(a.bond_tq)[bi.y];
-			acc.F.add(v3<R>{f.x, f.y, f.z});
-			acc.T.add(v3<R>{t.x, t.y, t.z});
-			KahanV<R>::kadd(acc.E, acc.Ec, f.w);
+		// bonded pairs of this nucleotide, evaluated by k_bonded_split (first lane of the group)
+		if(sub == 0 && live) {
+			const int2 bi = a.bonds[i];
+			const V4 *bf = reinterpret_cast<const V4 *>(a.bond_f);
+			if(bi.x >= 0) {
+				const V4 f = bf[i], t = reinterpret_cast<const V4 *>(a.bond_tp)[i];
+				acc.F.add(v3<R>{-f.x, -f.y, -f.z});
+				acc.T.add(v3<R>{t.x, t.y, t.z});
+				KahanV<R>::kadd(acc.E, acc.Ec, f.w);
+			}
+			if(bi.y >= 0) {
+				const V4 f = bf[bi.y], t = reinterpret_cast<const V4 *>(a.bond_tq)[bi.y];
+				acc.F.add(v3<R>{f.x, f.y, f.z});
+				acc.T.add(v3<R>{t.x, t.y, t.z});
+				KahanV<R>::kadd(acc.E, acc.Ec, f.w);
+			}
 		}
 
-		const v3<R> tl{acc.T.s.x - acc.T.c.x, acc.T.s.y - acc.T.c.y, acc.T.s.z - acc.T.c.z};
+		const R fx = group_sum_comp<R, K>(acc.F.s.x, acc.F.c.x), fy = group_sum_comp<R, K>(acc.F.s.y, acc.F.c.y),
+				fz = group_sum_comp<R, K>(acc.F.s.z, acc.F.c.z);
+		const v3<R> tl{group_sum_comp<R, K>(acc.T.s.x, acc.T.c.x), group_sum_comp<R, K>(acc.T.s.y, acc.T.c.y),
+				group_sum_comp<R, K>(acc.T.s.z, acc.T.c.z)};
+		const R e = group_sum_comp<R, K>(acc.E, acc.Ec), eh = group_sum_comp<R, K>(acc.Eh, acc.Ehc);
+		if(sub != 0 || !live) continue;
 		V4 fo, to;
-		fo.x = acc.F.s.x - acc.F.c.x;
-		fo.y = acc.F.s.y - acc.F.c.y;
-		fo.z = acc.F.s.z - acc.F.c.z;
-		fo.w = acc.E - acc.Ec;
+		fo.x = fx;
+		fo.y = fy;
+		fo.z = fz;
+		fo.w = e;
 		to.x = dot(p.a1, tl);
 		to.y = dot(p.a2, tl);
 		to.z = dot(p.a3, tl);
-		to.w = acc.Eh - acc.Ehc;
+		to.w = eh;
 		reinterpret_cast<V4 *>(a.forces)[i] = fo;
 		reinterpret_cast<V4 *>(a.torques)[i] = to;
 		if(FUSE_KICK) {
@@ -574,12 +609,20 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 	}
 }
 
+// lanes per nucleotide in the non-bonded kernel
+#ifndef OXGB_NB_LANES
+#define OXGB_NB_LANES 4
+#endif
+
 template <typename R, class Loader, bool SPLIT, bool FUSE>
 static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s) {
 	const int tpb = 128;
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	k_bonded_split<R, Loader, SPLIT><<<blocks, tpb, 0, s>>>(a, ld);
-	k_nonbonded_split<R, Loader, SPLIT, FUSE><<<blocks, tpb, 0, s>>>(a, ld);
+	constexpr int K = OXGB_NB_LANES;
+	const long long threads = (long long) (a.N > 0 ? a.N : 1) * K;
+	const int nb_blocks = (int) ((threads + tpb - 1) / tpb);
+	k_nonbonded_split<R, Loader, SPLIT, FUSE, K><<<nb_blocks, tpb, 0, s>>>(a, ld);
 }
 
 cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s) {

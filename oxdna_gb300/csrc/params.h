@@ -164,6 +164,29 @@ inline void to_float(const DNA2Table<double> &d, double box, DNA2Table<float> &f
 	f.box_lo = (float) (box - (double) f.box_hi);
 }
 
+// pair-distance bounds of the force kernel's term lists: a term can only act within these
+// distances (model constants), widened by twice the skin so that a list built now stays complete
+// until the next rebuild.  ev: centre-centre (excluded volume), base: base-base (hydrogen bonding,
+// cross stacking), stk: stack-stack (coaxial stacking).  Squared, FP32.
+struct TermRadii {
+	float ev2, base2, stk2;
+};
+
+inline TermRadii term_radii(double skin) {
+	const double back = std::sqrt((double) OXM_POS_MM_BACK1 * OXM_POS_MM_BACK1 + (double) OXM_POS_MM_BACK2 * OXM_POS_MM_BACK2);
+	const double base = OXM_POS_BASE;
+	double ev = OXM_EXCL_RC1 + 2 * back;                     // back-back
+	ev = std::fmax(ev, (double) OXM_EXCL_RC2 + 2 * base);     // base-base
+	ev = std::fmax(ev, (double) OXM_EXCL_RC3 + base + back);  // base-back
+	const double hb = std::fmax((double) OXM_HYDR_RCHIGH, (double) OXM_CRST_RCHIGH);
+	const double margin = 1e-3;
+	TermRadii t;
+	t.ev2 = (float) ((ev + 2 * skin + margin) * (ev + 2 * skin + margin));
+	t.base2 = (float) ((hb + 2 * skin + margin) * (hb + 2 * skin + margin));
+	t.stk2 = (float) (((double) OXM_CXST_RCHIGH + 2 * skin + margin) * ((double) OXM_CXST_RCHIGH + 2 * skin + margin));
+	return t;
+}
+
 // cells per side, CUDASimpleVerletList::_compute_N_cells_side
 // (src/CUDA/Lists/CUDASimpleVerletList.cu:96-110), with the min-3 clamp applied last
 inline int cells_per_side(int N, float L, float rverlet, bool auto_opt) {
