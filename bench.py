@@ -181,6 +181,9 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--list-node", default="conditional", choices=["conditional", "kernel"],
+                    help="list rebuild as a conditional graph node, or as always-launched kernels that "
+                         "return at once on a fresh list (what a kernel-level profiler can see)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -208,7 +211,7 @@ def main():
     dna = ox.dna2_settings(s.T, 0.5)
     md = ox.md_settings(dt=wl["dt"], thermostat=wl["thermostat"], newtonian_steps=wl["newtonian_steps"],
                         bussi_tau=wl.get("bussi_tau", 1000.0), diff_coeff=wl.get("diff_coeff", 2.5), seed=1 + rank,
-                        precision="mixed", steps_per_graph=25)
+                        precision="mixed", steps_per_graph=25, list_rebuild_node=args.list_node)
     sysm = ox.MDSystem(s.box, s.top, dna, md)
     sysm.set_state(s.pos, quat, s.vel, s.L)
     L = _abi.lib()
@@ -334,7 +337,7 @@ def main():
         "list_rebuilds": rebuilds,
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / peak.value, "traffic": None,
-                     "kernel": "k_forces (FP32 mixed)", "flops_per_launch": flops_launch, "sfu_per_launch": sfu_launch,
+                     "kernel": "k_bonded_split + k_nonbonded_split (FP32 pair math)", "flops_per_launch": flops_launch, "sfu_per_launch": sfu_launch,
                      "launch_ms": t_force * 1e3, "pairs_listed": pairs_listed, "pairs_in_cutoff": pairs_in_range,
                      "peak_source": "measured FP32 FMA probe on this GPU"},
         "clocks": clk,

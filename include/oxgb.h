@@ -113,8 +113,9 @@ int oxgb_verlet_create(int N, double box, double rcut, double skin, int cells_au
 /*
  * CUDASimpleVerletList::update (CUDASimpleVerletList.cu:231-289): rebuilds cells and neighbour
  * rows from d_poss (float4, reference layout), writes d_list_poss, excludes bonded pairs of
- * d_bonds.  Rows are written row-major (element k of i at i * max_neigh + k).  Asynchronous;
- * an overflow is reported by oxgb_verlet_status after the stream is synchronised.
+ * d_bonds.  Rows are column-major like the reference's d_matrix_neighs (element k of i at
+ * k * N + i, src/CUDA/Lists/CUDABaseList.h:13).  Asynchronous; an overflow is reported by
+ * oxgb_verlet_status after the stream is synchronised.
  */
 int oxgb_verlet_update(oxgb_verlet *h, const void *d_poss, void *d_list_poss, const void *d_bonds, void *stream);
 /* device pointers of the neighbour rows (int[N * max_neigh]) and counts (int[N]) */
@@ -144,6 +145,9 @@ typedef struct oxgb_md_settings {
 	int cells_auto_optimisation;/* cells_auto_optimisation */
 	int max_neigh;              /* neighbour-row capacity; 0 = sized from the first build */
 	int steps_per_graph;        /* MD steps captured per CUDA graph launch (0 = 16) */
+	int list_rebuild_node;      /* 0: the list rebuild is a device-side IF node of the step graph;
+	                               1: the rebuild kernels are launched every step and return at once
+	                               while the list is fresh (same results; kernel nodes profilable) */
 } oxgb_md_settings;
 
 void oxgb_md_default_settings(oxgb_md_settings *s);

@@ -41,7 +41,7 @@ class MDSettings(C.Structure):
         ("dt", C.c_double), ("verlet_skin", C.c_double), ("thermostat", C.c_int), ("newtonian_steps", C.c_int),
         ("pt", C.c_double), ("diff_coeff", C.c_double), ("bussi_tau", C.c_double), ("seed", C.c_uint64),
         ("precision", C.c_int), ("cells_auto_optimisation", C.c_int), ("max_neigh", C.c_int),
-        ("steps_per_graph", C.c_int),
+        ("steps_per_graph", C.c_int), ("list_rebuild_node", C.c_int),
     ]
 
 

@@ -51,6 +51,7 @@ extern "C" void oxgb_md_default_settings(oxgb_md_settings *s) {
 	s->precision = OXGB_PRECISION_MIXED;
 	s->cells_auto_optimisation = 1;
 	s->steps_per_graph = 16;
+	s->list_rebuild_node = 0;
 }
 
 static int status_to_code(int st) {
@@ -164,6 +165,7 @@ extern "C" int oxgb_dna2_destroy(oxgb_dna2 *h) {
 struct ListBuffers {
 	int n_side = 0, n_cells = 0, max_nb = 0, N = 0;
 	int *cell_of = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_cursor = nullptr, *cell_list = nullptr;
+	int *cell_tmp = nullptr, *scan_part = nullptr;
 	int *nb = nullptr, *nnb = nullptr;
 
 	int alloc(int N_, int n_side_, int max_nb_) {
@@ -177,12 +179,14 @@ struct ListBuffers {
 		CK(cudaMalloc(&cell_start, sizeof(int) * (n_cells + 1)));
 		CK(cudaMalloc(&cell_cursor, sizeof(int) * n_cells));
 		CK(cudaMalloc(&cell_list, sizeof(int) * std::max(N, 1)));
+		CK(cudaMalloc(&cell_tmp, sizeof(int) * std::max(N, 1)));
+		CK(cudaMalloc(&scan_part, sizeof(int) * (scan_tiles(n_cells) + 1)));
 		CK(cudaMalloc(&nb, sizeof(int) * (size_t) std::max(N, 1) * max_nb));
 		CK(cudaMalloc(&nnb, sizeof(int) * std::max(N, 1)));
 		return OXGB_OK;
 	}
 	void free_all() {
-		for(int **p : {&cell_of, &cell_count, &cell_start, &cell_cursor, &cell_list, &nb, &nnb}) {
+		for(int **p : {&cell_of, &cell_count, &cell_start, &cell_cursor, &cell_list, &cell_tmp, &scan_part, &nb, &nnb}) {
 			if(*p) cudaFree(*p);
 			*p = nullptr;
 		}
@@ -263,6 +267,8 @@ static ListArgs list_args(ListBuffers &lb, int N, const float4 *pos, float box, 
 	a.cell_start = lb.cell_start;
 	a.cell_cursor = lb.cell_cursor;
 	a.cell_list = lb.cell_list;
+	a.cell_tmp = lb.cell_tmp;
+	a.scan_part = lb.scan_part;
 	a.nb = lb.nb;
 	a.nnb = lb.nnb;
 	a.max_nb = lb.max_nb;
@@ -278,6 +284,7 @@ extern "C" int oxgb_verlet_update(oxgb_verlet *h, const void *d_poss, void *d_li
 	if(!h || !d_poss || !d_list_poss || !d_bonds) return fail(OXGB_E_INVALID, "null argument");
 	ListArgs a = list_args(h->lb, h->N, (const float4 *) d_poss, (float) h->box, h->rverlet, (const int2 *) d_bonds,
 			(float4 *) d_list_poss, h->d_status, h->d_flag, 0);
+	a.col_major = 1;  // matrix_neighs[k * N + i], the layout NEXT_NEIGHBOUR reads
 	CK(launch_list_build(a, (cudaStream_t) stream));
 	return OXGB_OK;
 }
@@ -336,10 +343,12 @@ struct oxgb_md {
 	int *status = nullptr, *flag = nullptr;
 	long long *step = nullptr;
 	double *esplit = nullptr, *scratch = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
+	unsigned *bussi_done = nullptr;
 	int bussi_blocks = 0;
 	double pt = 0, pr = 0;
 
-	cudaStream_t stream = nullptr, side = nullptr;
+	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 	cudaGraphExec_t gexec = nullptr;
 	int graph_steps = 0;
 	bool conditional_ok = true;
@@ -351,12 +360,15 @@ struct oxgb_md {
 		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
 					(void *) fback, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, bond_f,
 					bond_tp, bond_tq, d_tab, (void *) status, (void *) flag, (void *) step, (void *) esplit, (void *) scratch,
-					(void *) bussi_partials, (void *) bussi_state, (void *) d_rebuilds})
+					(void *) bussi_partials, (void *) bussi_state, (void *) bussi_done, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
 		if(stream) cudaStreamDestroy(stream);
 		if(side) cudaStreamDestroy(side);
+		if(noise) cudaStreamDestroy(noise);
+		if(ev_fork) cudaEventDestroy(ev_fork);
+		if(ev_join) cudaEventDestroy(ev_join);
 	}
 };
 
@@ -393,6 +405,7 @@ static StepArgs step_args(oxgb_md *h) {
 	a.bussi_c = std::exp(-(double) a.newtonian_steps / h->md.bussi_tau);
 	a.bussi_partials = h->bussi_partials;
 	a.bussi_state = h->bussi_state;
+	a.bussi_done = h->bussi_done;
 	a.bussi_blocks = h->bussi_blocks;
 	return a;
 }
@@ -477,6 +490,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	h->dna.assign(dna, dna + n_systems);
 	h->md = *md;
 	if(h->md.steps_per_graph <= 0) h->md.steps_per_graph = 16;
+	h->conditional_ok = h->md.list_rebuild_node == 0;
 	h->dbl = md->precision == OXGB_PRECISION_DOUBLE;
 	const size_t v4 = h->dbl ? sizeof(double4_32a) : sizeof(float4);
 	auto bail = [&](int rc) {
@@ -484,7 +498,10 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 		return rc;
 	};
 	if(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
-			cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess)
+			cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+			cudaStreamCreateWithFlags(&h->noise, cudaStreamNonBlocking) != cudaSuccess ||
+			cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+			cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
 		return bail(fail(OXGB_E_CUDA, "stream creation failed"));
 	bool ok = true;
 	ok &= cudaMalloc(&h->posd, sizeof(double4_32a) * N) == cudaSuccess;
@@ -513,13 +530,15 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->scratch, sizeof(double) * 8 * n_systems) == cudaSuccess;
 	h->bussi_blocks = std::max(1, std::min(1024, (N + 255) / 256));
 	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * h->bussi_blocks) == cudaSuccess;
-	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 8) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
 	if(!ok) return bail(fail(OXGB_E_NOMEM, "device allocation failed"));
 	cudaMemset(h->status, 0, sizeof(int));
 	cudaMemset(h->flag, 0, sizeof(int));
 	cudaMemset(h->step, 0, sizeof(long long));
 	cudaMemset(h->d_rebuilds, 0, sizeof(unsigned long long));
+	cudaMemset(h->bussi_done, 0, sizeof(unsigned));
 	int rc = upload_tables(h);
 	if(rc) return bail(rc);
 	h->rverlet = (float) h->rcut + 2.f * (float) h->md.verlet_skin;
@@ -531,7 +550,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	rc = h->tl.alloc(N, std::min(std::max(N - 1, 1), 128), std::min(std::max(N - 1, 1), 64), std::min(std::max(N - 1, 1), 64));
 	if(rc) return bail(rc);
 	// Bussi running kinetic energies start at their targets (BussiThermostat::init)
-	double bs[8] = {0.5 * 3 * (N - 1) * h->dna[0].T, 0.5 * 3 * N * h->dna[0].T, 1, 1, 0, 0, 0, 0};
+	double bs[16] = {0.5 * 3 * (N - 1) * h->dna[0].T, 0.5 * 3 * N * h->dna[0].T, 1, 1};
 	if(cudaMemcpy(h->bussi_state, bs, sizeof(bs), cudaMemcpyHostToDevice) != cudaSuccess) return bail(fail(OXGB_E_CUDA, "upload"));
 	*out = h;
 	return OXGB_OK;
@@ -718,10 +737,27 @@ extern "C" int oxgb_md_get_state(oxgb_md *h, double *pos, double *quat, double *
 	return OXGB_OK;
 }
 
+// The Bussi noise draws depend only on (seed, step): they run on a second stream (a parallel
+// branch of the step graph) while the forces are evaluated, and join before the thermostat.
+static cudaError_t fork_noise(oxgb_md *h, const StepArgs &sa) {
+	if(sa.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
+	cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
+	if(e == cudaSuccess) e = cudaStreamWaitEvent(h->noise, h->ev_fork, 0);
+	if(e == cudaSuccess) e = launch_bussi_noise(sa, h->noise);
+	if(e == cudaSuccess) e = cudaEventRecord(h->ev_join, h->noise);
+	return e;
+}
+
+static cudaError_t join_noise(oxgb_md *h, const StepArgs &sa) {
+	if(sa.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
+	return cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+}
+
 // one MD step on h->stream (captured into the graph)
 static int enqueue_step(oxgb_md *h, cudaGraph_t capturing) {
 	StepArgs sa = step_args(h);
 	CK(launch_first_step(sa, h->dbl, h->stream));
+	CK(fork_noise(h, sa));
 	ListArgs la = md_list_args(h, h->conditional_ok ? 0 : 1);
 	if(h->conditional_ok) {
 		cudaGraphConditionalHandle hc;
@@ -753,6 +789,7 @@ static int enqueue_step(oxgb_md *h, cudaGraph_t capturing) {
 	}
 	ForceArgs fa = force_args(h);
 	CK(launch_forces_split(fa, h->dbl, false, true, h->stream));
+	CK(join_noise(h, sa));
 	CK(launch_thermostat(sa, h->stream));
 	CK(launch_step_advance(sa, h->stream));
 	return OXGB_OK;
@@ -808,10 +845,12 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 	for(; done < nsteps; done++) {
 		StepArgs sa = step_args(h);
 		CK(launch_first_step(sa, h->dbl, h->stream));
+		CK(fork_noise(h, sa));
 		ListArgs la = md_list_args(h, 1);
 		CK(launch_list_build(la, h->stream));
 		ForceArgs fa = force_args(h);
 		CK(launch_forces_split(fa, h->dbl, false, true, h->stream));
+		CK(join_noise(h, sa));
 		CK(launch_thermostat(sa, h->stream));
 		CK(launch_step_advance(sa, h->stream));
 	}

@@ -116,10 +116,17 @@ __device__ double sum_noises(Stream &st, int nn) {
 	return 2.0 * gamdev(st, (nn - 1) / 2) + r * r;
 }
 
-__device__ void update_K(Stream &st, double &K, int dof, double T, double c) {
+// the two draws of one kinetic-energy update (BussiThermostat::_update_K, BussiThermostat.cpp:
+// 55-65): the Gaussian r, then the sum of dof - 1 squared Gaussians; they do not depend on the
+// state, so they are drawn apart from (and concurrently with) the force evaluation
+__device__ void bussi_draws(Stream &st, int dof, double &sum, double &rr) {
+	rr = st.gauss();
+	sum = sum_noises(st, dof - 1);
+}
+
+__device__ void update_K(double &K, int dof, double T, double c, double sum, double rr) {
 	const double Kt = 0.5 * dof * T;
-	const double rr = st.gauss();
-	const double dK = (1.0 - c) * (Kt * (sum_noises(st, dof - 1) + rr * rr) / dof - K) + 2.0 * rr * sqrt(K * Kt / dof * (1.0 - c) * c);
+	const double dK = (1.0 - c) * (Kt * (sum + rr * rr) / dof - K) + 2.0 * rr * sqrt(K * Kt / dof * (1.0 - c) * c);
 	K += dK;
 }
 
@@ -191,18 +198,32 @@ __global__ void k_first_step(StepArgs a) {
 	L.y += (double) T.y * hdt;
 	L.z += (double) T.z * hdt;
 	// rotation by dt|L| about L (body frame): q <- q * (sin(th/2) L^, cos(th/2))
-	const double norm = sqrt(L.x * L.x + L.y * L.y + L.z * L.z);
-	if(norm > 0.0) {
-		double sh, ch;
-		sincos(0.5 * a.dt * norm, &sh, &ch);
-		const double k = sh / norm;
+	const double L2 = L.x * L.x + L.y * L.y + L.z * L.z;
+	if(L2 > 0.0) {
+		const double hd = 0.5 * a.dt, x2 = hd * hd * L2;  // x = th / 2
+		double k, ch;
+		if(x2 < 1e-2) {
+			// sin(x) / x and cos(x) as Taylor series in x^2 (truncation below 1e-20 for |x| < 0.1):
+			// no square root, range reduction or division, which are slow in FP64
+			k = hd * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0) * (1.0 - x2 * (1.0 / 42.0) * (1.0 - x2 * (1.0 / 72.0) * (1.0 - x2 * (1.0 / 110.0))))));
+			ch = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0) * (1.0 - x2 * (1.0 / 56.0) * (1.0 - x2 * (1.0 / 90.0)))));
+		}
+		else {
+			const double norm = sqrt(L2);
+			double sh;
+			sincos(hd * norm, &sh, &ch);
+			k = sh / norm;
+		}
 		const double rx = L.x * k, ry = L.y * k, rz = L.z * k, rw = ch;
 		double4_32a n;
 		n.w = q.w * rw - q.x * rx - q.y * ry - q.z * rz;
 		n.x = q.w * rx + q.x * rw + q.y * rz - q.z * ry;
 		n.y = q.w * ry - q.x * rz + q.y * rw + q.z * rx;
 		n.z = q.w * rz + q.x * ry - q.y * rx + q.z * rw;
-		const double inv = 1.0 / sqrt(n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w);
+		const double nn = n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w;
+		const double d = nn - 1.0;
+		// |n|^2 = 1 + d with |d| at the rounding level: 1/sqrt(1 + d) = 1 - d/2 + 3d^2/8 - ...
+		const double inv = fabs(d) < 1e-6 ? 1.0 - d * (0.5 - 0.375 * d) : 1.0 / sqrt(nn);
 		q = make_double4_32a(n.x * inv, n.y * inv, n.z * inv, n.w * inv);
 	}
 	a.vel[i] = v;
@@ -233,6 +254,22 @@ __global__ void k_brownian(StepArgs a) {
 	if(u01(o0[1]) < a.pr) a.angmom[i] = make_double4_32a(g[3] * a.sqrtT, g[4] * a.sqrtT, g[5] * a.sqrtT, 0.0);
 }
 
+__global__ void k_bussi_noise(StepArgs a) {
+	const long long s = *a.step;
+	if(s % a.newtonian_steps != 0 || (threadIdx.x & 31) != 0) return;
+	// warp 0: translational (channel 0), warp 1: rotational (channel 1)
+	const int w = threadIdx.x >> 5;
+	if(w > 1) return;
+	Stream rs;
+	rs.init(a.seed, s, (unsigned) w);
+	double sum, rr;
+	bussi_draws(rs, w == 0 ? 3 * (a.N - 1) : 3 * a.N, sum, rr);
+	a.bussi_state[8 + 2 * w] = sum;
+	a.bussi_state[9 + 2 * w] = rr;
+}
+
+// per-block sums of v, v^2 and L^2; the last block to finish reduces the block sums in a fixed
+// order (deterministic) and updates the running kinetic energies and the rescaling factors
 __global__ void __launch_bounds__(256) k_bussi_partial(StepArgs a) {
 	const long long s = *a.step;
 	if(s % a.newtonian_steps != 0) return;
@@ -246,6 +283,7 @@ __global__ void __launch_bounds__(256) k_bussi_partial(StepArgs a) {
 		acc[4] += L.x * L.x + L.y * L.y + L.z * L.z;
 	}
 	__shared__ double red[5][8];
+	__shared__ bool last;
 #pragma unroll
 	for(int k = 0; k < 5; k++) {
 		double x = acc[k];
@@ -257,30 +295,45 @@ __global__ void __launch_bounds__(256) k_bussi_partial(StepArgs a) {
 		double x = 0;
 		for(int w = 0; w < (int) (blockDim.x >> 5); w++) x += red[threadIdx.x][w];
 		a.bussi_partials[blockIdx.x * 8 + threadIdx.x] = x;
+		__threadfence();
 	}
-}
-
-__global__ void k_bussi_scalar(StepArgs a) {
-	const long long s = *a.step;
-	if(s % a.newtonian_steps != 0 || threadIdx.x != 0) return;
-	double sum[5] = {0, 0, 0, 0, 0};
-	for(int b = 0; b < a.bussi_blocks; b++)
-		for(int k = 0; k < 5; k++) sum[k] += a.bussi_partials[b * 8 + k];
+	__syncthreads();
+	if(threadIdx.x == 0) last = atomicAdd(a.bussi_done, 1u) == gridDim.x - 1;
+	__syncthreads();
+	if(!last) return;
+	__threadfence();
+	// fixed-order reduction of the block sums: thread t takes blocks t, t + 256, ...
+	double part[5] = {0, 0, 0, 0, 0};
+	for(int b = threadIdx.x; b < a.bussi_blocks; b += blockDim.x)
+#pragma unroll
+		for(int k = 0; k < 5; k++) part[k] += __ldcg(a.bussi_partials + b * 8 + k);
+#pragma unroll
+	for(int k = 0; k < 5; k++) {
+		double x = part[k];
+		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+		if((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = x;
+	}
+	__syncthreads();
+	if(threadIdx.x != 0) return;
+	double sum[5];
+	for(int k = 0; k < 5; k++) {
+		double x = 0;
+		for(int w = 0; w < (int) (blockDim.x >> 5); w++) x += red[k][w];
+		sum[k] = x;
+	}
 	const double N = a.N;
 	const double vc[3] = {sum[0] / N, sum[1] / N, sum[2] / N};
 	const double Kt_now = 0.5 * (sum[3] - N * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
 	const double Kr_now = 0.5 * sum[4];
 	double *st = a.bussi_state;
-	Stream rs;
-	rs.init(a.seed, s, 0u);
-	update_K(rs, st[0], 3 * (a.N - 1), a.T, a.bussi_c);
-	rs.init(a.seed, s, 1u);
-	update_K(rs, st[1], 3 * a.N, a.T, a.bussi_c);
+	update_K(st[0], 3 * (a.N - 1), a.T, a.bussi_c, __ldcg(st + 8), __ldcg(st + 9));
+	update_K(st[1], 3 * a.N, a.T, a.bussi_c, __ldcg(st + 10), __ldcg(st + 11));
 	st[2] = sqrt(st[0] / Kt_now);
 	st[3] = sqrt(st[1] / Kr_now);
 	st[4] = vc[0];
 	st[5] = vc[1];
 	st[6] = vc[2];
+	*a.bussi_done = 0;
 }
 
 __global__ void k_bussi_apply(StepArgs a) {
@@ -330,9 +383,13 @@ cudaError_t launch_thermostat(const StepArgs &a, cudaStream_t s) {
 	if(a.thermostat == 1) k_brownian<<<blocks_for(a.N, 256), 256, 0, s>>>(a);
 	else if(a.thermostat == 2) {
 		k_bussi_partial<<<a.bussi_blocks, 256, 0, s>>>(a);
-		k_bussi_scalar<<<1, 32, 0, s>>>(a);
 		k_bussi_apply<<<blocks_for(a.N, 256), 256, 0, s>>>(a);
 	}
+	return cudaGetLastError();
+}
+
+cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
+	k_bussi_noise<<<1, 64, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

@@ -55,7 +55,9 @@ struct ListArgs {
 	int *cell_count;        // [n_cells]
 	int *cell_start;        // [n_cells + 1]
 	int *cell_cursor;       // [n_cells]
-	int *cell_list;         // [N]
+	int *cell_list;         // [N] particles by cell, by index within a cell
+	int *cell_tmp;          // [N] scatter target before the ordering
+	int *scan_part;         // [scan_tiles(n_cells) + 1]
 	int *nb, *nnb;          // [N * max_nb], [N]
 	int max_nb;
 	float4 *list_pos;       // positions at this build
@@ -76,6 +78,8 @@ struct ListArgs {
 
 // full rebuild: cells (counting sort, deterministic order) then neighbour rows
 cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s);
+// size of ListArgs::scan_part is scan_tiles(n_cells) + 1
+int scan_tiles(int n_cells);
 
 struct StepArgs {
 	int N;
@@ -98,12 +102,16 @@ struct StepArgs {
 	unsigned long long seed;
 	double bussi_c;                        // exp(-newtonian_steps / tau)
 	double *bussi_partials;                // [blocks * 8]
-	double *bussi_state;                   // K_t, K_r, then scratch: factor_t, factor_r, vcom x y z
+	double *bussi_state;                   // [16]: K_t, K_r, factor_t, factor_r, vcom x y z, -,
+	                                       // then the step's noise draws: sum_t, rr_t, sum_r, rr_r
+	unsigned *bussi_done;                  // blocks of k_bussi_partial finished (0 between steps)
 	int bussi_blocks;
 };
 
 cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s);
 cudaError_t launch_thermostat(const StepArgs &a, cudaStream_t s);
+// the Bussi noise draws of the current step (independent of the state: may run beside the forces)
+cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s);
 cudaError_t launch_step_advance(const StepArgs &a, cudaStream_t s);
 // sets the graph conditional to (*flag != 0)
 cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h, cudaStream_t s);

@@ -3,8 +3,8 @@
 // Replaces simple_fill_cells / simple_update_neigh_list (src/CUDA/Lists/CUDA_simple_verlet.cuh:
 // 14-95) and the host control of CUDASimpleVerletList::update (src/CUDA/Lists/
 // CUDASimpleVerletList.cu:231-289).  Cells are filled by a counting sort (count, scan,
-// scatter, then each cell's short segment ordered by index), so there is no per-cell capacity
-// to overflow and the neighbour order is deterministic run to run.  The geometry is the
+// scatter, then each particle placed by its index rank within its cell), so there is no
+// per-cell capacity to overflow and the neighbour order is deterministic run to run.  The geometry is the
 // reference's fp32 geometry: cell coordinate ((x/L - floor(x/L)) * (1 - FLT_EPSILON)) * n and
 // minimum-image squared distance against r_verlet^2, with IEEE division and the fused
 // multiply-adds written out, so that oracle/dna2_oracle.c (oxo_verlet_f32) reproduces the
@@ -60,55 +60,106 @@ __global__ void k_cell_count(ListArgs a) {
 	atomicAdd(a.cell_count + c, 1);
 }
 
-// exclusive scan of the cell counts by one block; each thread owns a contiguous chunk
-__global__ void __launch_bounds__(1024) k_cell_scan(ListArgs a, int n_cells) {
-	SKIP_IF_FRESH(a);
-	__shared__ int part[1024];
-	const int t = threadIdx.x;
-	const int chunk = (n_cells + blockDim.x - 1) / blockDim.x;
-	const int lo = t * chunk, hi = min(lo + chunk, n_cells);
-	int s = 0;
-	for(int c = lo; c < hi; c++) s += a.cell_count[c];
-	part[t] = s;
+// Exclusive scan of the cell counts in three passes: block sums, a scan of the block sums by
+// one block, then each block's own scan plus its offset.  SCAN_TILE cells per block.
+#define SCAN_TPB 512
+#define SCAN_TILE (SCAN_TPB * 4)
+
+__device__ __forceinline__ int block_incl_scan(int v, int *warp_tot) {
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+	for(int off = 1; off < 32; off <<= 1) {
+		const int u = __shfl_up_sync(0xffffffffu, v, off);
+		if(lane >= off) v += u;
+	}
+	if(lane == 31) warp_tot[w] = v;
 	__syncthreads();
-	for(int off = 1; off < blockDim.x; off <<= 1) {
-		const int v = (t >= off) ? part[t - off] : 0;
-		__syncthreads();
-		part[t] += v;
-		__syncthreads();
+	if(w == 0) {
+		int t = lane < (int) (blockDim.x >> 5) ? warp_tot[lane] : 0;
+#pragma unroll
+		for(int off = 1; off < 32; off <<= 1) {
+			const int u = __shfl_up_sync(0xffffffffu, t, off);
+			if(lane >= off) t += u;
+		}
+		warp_tot[lane] = t;  // inclusive over warps
 	}
-	int run = part[t] - s;
-	for(int c = lo; c < hi; c++) {
-		a.cell_start[c] = run;
-		a.cell_cursor[c] = run;
-		run += a.cell_count[c];
-	}
-	if(t == blockDim.x - 1) a.cell_start[n_cells] = part[t];
+	__syncthreads();
+	return v + (w > 0 ? warp_tot[w - 1] : 0);
 }
 
+__global__ void __launch_bounds__(SCAN_TPB) k_scan_tiles(ListArgs a, int n_cells) {
+	SKIP_IF_FRESH(a);
+	__shared__ int wt[32];
+	const int base = blockIdx.x * SCAN_TILE + threadIdx.x * 4;
+	int v = 0;
+#pragma unroll
+	for(int k = 0; k < 4; k++)
+		if(base + k < n_cells) v += a.cell_count[base + k];
+	const int incl = block_incl_scan(v, wt);
+	if(threadIdx.x == blockDim.x - 1) a.scan_part[blockIdx.x] = incl;
+}
+
+// exclusive scan of the tile sums in place (one block, any number of tiles)
+__global__ void __launch_bounds__(SCAN_TPB) k_scan_top(ListArgs a, int n_tiles) {
+	SKIP_IF_FRESH(a);
+	__shared__ int wt[32];
+	__shared__ int carry;
+	if(threadIdx.x == 0) carry = 0;
+	__syncthreads();
+	for(int b = 0; b < n_tiles; b += blockDim.x) {
+		const int t = b + threadIdx.x;
+		const int v = t < n_tiles ? a.scan_part[t] : 0;
+		const int incl = block_incl_scan(v, wt);
+		const int c0 = carry;
+		if(t < n_tiles) a.scan_part[t] = c0 + incl - v;
+		__syncthreads();
+		if(threadIdx.x == blockDim.x - 1) carry = c0 + incl;
+		__syncthreads();
+	}
+	if(threadIdx.x == 0) a.scan_part[n_tiles] = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_TPB) k_scan_apply(ListArgs a, int n_cells, int n_tiles) {
+	SKIP_IF_FRESH(a);
+	__shared__ int wt[32];
+	const int base = blockIdx.x * SCAN_TILE + threadIdx.x * 4;
+	int c[4], v = 0;
+#pragma unroll
+	for(int k = 0; k < 4; k++) {
+		c[k] = base + k < n_cells ? a.cell_count[base + k] : 0;
+		v += c[k];
+	}
+	int run = block_incl_scan(v, wt) - v + a.scan_part[blockIdx.x];
+#pragma unroll
+	for(int k = 0; k < 4; k++) {
+		if(base + k < n_cells) {
+			a.cell_start[base + k] = run;
+			a.cell_cursor[base + k] = run;
+		}
+		run += c[k];
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0) a.cell_start[n_cells] = a.scan_part[n_tiles];
+}
+
+// particles into their cells' segments, in arbitrary order (cell_tmp)
 __global__ void k_cell_scatter(ListArgs a) {
 	SKIP_IF_FRESH(a);
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= a.N) return;
 	const int slot = atomicAdd(a.cell_cursor + a.cell_of[i], 1);
-	a.cell_list[slot] = i;
+	a.cell_tmp[slot] = i;
 }
 
-// order each cell's segment by particle index (segments hold a handful of particles)
-__global__ void k_cell_order(ListArgs a, int n_cells) {
+// each particle's rank by index within its cell gives the deterministic order (cell_list)
+__global__ void k_cell_rank(ListArgs a) {
 	SKIP_IF_FRESH(a);
-	const int c = blockIdx.x * blockDim.x + threadIdx.x;
-	if(c >= n_cells) return;
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= a.N) return;
+	const int c = a.cell_of[i];
 	const int b = a.cell_start[c], e = a.cell_start[c + 1];
-	for(int k = b + 1; k < e; k++) {
-		const int v = a.cell_list[k];
-		int m = k - 1;
-		while(m >= b && a.cell_list[m] > v) {
-			a.cell_list[m + 1] = a.cell_list[m];
-			m--;
-		}
-		a.cell_list[m + 1] = v;
-	}
+	int rank = 0;
+	for(int k = b; k < e; k++) rank += a.cell_tmp[k] < i;
+	a.cell_list[b + rank] = i;
 }
 
 // minimum-image separation vector (the reference's fp32 geometry, explicit fused multiply-adds)
@@ -120,66 +171,109 @@ __device__ __forceinline__ float3 min_image_vec(float4 a, float4 b, float L) {
 	return make_float3(dx, dy, dz);
 }
 
-__global__ void k_neighbours(ListArgs a) {
+__device__ __forceinline__ void put(int *rows, bool col_major, long long N, int stride, int i, int k, int j) {
+	if(col_major) rows[(long long) k * N + i] = j;
+	else rows[(long long) i * stride + k] = j;
+}
+
+// One warp per nucleotide.  The candidates of the 27 cells, in the serial scan order (dz, dy, dx
+// from -1 to 1, each cell's segment by index), are numbered 0..C-1; lane l takes candidates
+// l, l + 32, ... and the hits of every round are compacted in order with a ballot, so each row
+// comes out exactly as a serial scan would write it.
+__global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	SKIP_IF_FRESH(a);
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i >= a.N) return;
+	const int lane = threadIdx.x & 31;
+	const int i = (int) (((long long) blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+	if(i >= a.N) return;  // warp-uniform
 	const float4 r = a.pos[i];
 	const int2 b = a.bonds[i];
 	const int n = a.n_side;
 	const int c = a.cell_of[i];
 	const int cx = c % n, cy = (c / n) % n, cz = c / (n * n);
 	const bool terms = a.ev_nb != nullptr;
+	const long long N = a.N;
+	// lane l < 27 owns the l-th cell of the scan
+	int cs = 0, cn = 0;
+	if(lane < 27) {
+		const int z = (cz + lane / 9 - 1 + n) % n, y = (cy + (lane / 3) % 3 - 1 + n) % n, x = (cx + lane % 3 - 1 + n) % n;
+		const int cc = (z * n + y) * n + x;
+		cs = a.cell_start[cc];
+		cn = a.cell_start[cc + 1] - cs;
+	}
+	int incl = cn;
+#pragma unroll
+	for(int off = 1; off < 32; off <<= 1) {
+		const int u = __shfl_up_sync(0xffffffffu, incl, off);
+		if(lane >= off) incl += u;
+	}
+	const int total = __shfl_sync(0xffffffffu, incl, 31);
+	const int excl = incl - cn;
 	float4 a1i = make_float4(0.f, 0.f, 0.f, 0.f), bki = a1i;
 	if(terms) {
 		a1i = a.fa1[i];
 		bki = a.fback[i];
 	}
-	const long long N = a.N;
+	const unsigned below = (1u << lane) - 1u;
 	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
-	for(int dz = -1; dz <= 1; dz++) {
-		const int z = (cz + dz + n) % n;
-		for(int dy = -1; dy <= 1; dy++) {
-			const int y = (cy + dy + n) % n;
-			for(int dx = -1; dx <= 1; dx++) {
-				const int x = (cx + dx + n) % n;
-				const int cc = (z * n + y) * n + x;
-				const int e = a.cell_start[cc + 1];
-				for(int k = a.cell_start[cc]; k < e; k++) {
-					const int j = a.cell_list[k];
-					if(j == i || j == b.x || j == b.y) continue;
-					const float4 rj = a.pos[j];
-					const float d2 = sqr_min_image(r, rj, a.box);
-					if(d2 < a.rverlet2) {
-						if(cnt < a.max_nb) {
-							if(a.col_major) a.nb[(long long) cnt * N + i] = j;
-							else a.nb[(long long) i * a.max_nb + cnt] = j;
-						}
-						cnt++;
-						if(terms && d2 < a.ev_r2) {
-							if(nev < a.ev_cap) a.ev_nb[(long long) nev * N + i] = j;
-							nev++;
-							const float3 d = min_image_vec(r, rj, a.box);
-							const float4 a1j = a.fa1[j];
-							// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
-							const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
-									bz = d.z + 0.4f * (a1j.z - a1i.z);
-							if(bx * bx + by * by + bz * bz < a.base_r2) {
-								if(nbase < a.base_cap) a.base_nb[(long long) nbase * N + i] = j;
-								nbase++;
-							}
-							const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy = d.y + 0.34f * (a1j.y - a1i.y),
-									sz = d.z + 0.34f * (a1j.z - a1i.z);
-							if(sx * sx + sy * sy + sz * sz < a.stk_r2) {
-								if(nstk < a.stk_cap) a.stk_nb[(long long) nstk * N + i] = j;
-								nstk++;
-							}
-						}
-					}
+	for(int t0 = 0; t0 < total; t0 += 32) {
+		const int t = t0 + lane;
+		// the cell holding candidate t: the first lane whose inclusive count exceeds t
+		int l = 0;
+#pragma unroll
+		for(int step = 16; step > 0; step >>= 1) {
+			const int v = __shfl_sync(0xffffffffu, incl, l + step - 1);
+			if(v <= t) l += step;
+		}
+		const int cs_l = __shfl_sync(0xffffffffu, cs, l & 31), ex_l = __shfl_sync(0xffffffffu, excl, l & 31);
+		bool hit = false, hev = false, hbase = false, hstk = false;
+		int j = -1;
+		if(t < total) {
+			j = a.cell_list[cs_l + (t - ex_l)];
+			if(j != i && j != b.x && j != b.y) {
+				const float4 rj = a.pos[j];
+				const float d2 = sqr_min_image(r, rj, a.box);
+				hit = d2 < a.rverlet2;
+				if(terms && hit && d2 < a.ev_r2) {
+					hev = true;
+					const float3 d = min_image_vec(r, rj, a.box);
+					const float4 a1j = a.fa1[j];
+					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
+					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
+							bz = d.z + 0.4f * (a1j.z - a1i.z);
+					hbase = bx * bx + by * by + bz * bz < a.base_r2;
+					const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy = d.y + 0.34f * (a1j.y - a1i.y),
+							sz = d.z + 0.34f * (a1j.z - a1i.z);
+					hstk = sx * sx + sy * sy + sz * sz < a.stk_r2;
 				}
 			}
 		}
+		const unsigned m = __ballot_sync(0xffffffffu, hit);
+		if(hit) {
+			const int k = cnt + __popc(m & below);
+			if(k < a.max_nb) put(a.nb, a.col_major != 0, N, a.max_nb, i, k, j);
+		}
+		cnt += __popc(m);
+		if(terms) {
+			const unsigned me = __ballot_sync(0xffffffffu, hev), mb = __ballot_sync(0xffffffffu, hbase),
+					ms = __ballot_sync(0xffffffffu, hstk);
+			if(hev) {
+				const int k = nev + __popc(me & below);
+				if(k < a.ev_cap) a.ev_nb[(long long) k * N + i] = j;
+			}
+			if(hbase) {
+				const int k = nbase + __popc(mb & below);
+				if(k < a.base_cap) a.base_nb[(long long) k * N + i] = j;
+			}
+			if(hstk) {
+				const int k = nstk + __popc(ms & below);
+				if(k < a.stk_cap) a.stk_nb[(long long) k * N + i] = j;
+			}
+			nev += __popc(me);
+			nbase += __popc(mb);
+			nstk += __popc(ms);
+		}
 	}
+	if(lane != 0) return;
 	if(cnt > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
 	a.nnb[i] = cnt;
 	a.list_pos[i] = r;
@@ -201,16 +295,22 @@ __global__ void k_list_done(ListArgs a) {
 	*a.flag = 0;
 }
 
+int scan_tiles(int n_cells) { return (n_cells + SCAN_TILE - 1) / SCAN_TILE; }
+
 cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s) {
 	const int n_cells = a.n_side * a.n_side * a.n_side;
 	const int tpb = 256;
 	const int gp = (a.N + tpb - 1) / tpb;
+	const int tiles = scan_tiles(n_cells);
 	k_zero_counts<<<(n_cells + tpb - 1) / tpb, tpb, 0, s>>>(a, n_cells);
 	k_cell_count<<<gp, tpb, 0, s>>>(a);
-	k_cell_scan<<<1, 1024, 0, s>>>(a, n_cells);
+	k_scan_tiles<<<tiles, SCAN_TPB, 0, s>>>(a, n_cells);
+	k_scan_top<<<1, SCAN_TPB, 0, s>>>(a, tiles);
+	k_scan_apply<<<tiles, SCAN_TPB, 0, s>>>(a, n_cells, tiles);
 	k_cell_scatter<<<gp, tpb, 0, s>>>(a);
-	k_cell_order<<<(n_cells + tpb - 1) / tpb, tpb, 0, s>>>(a, n_cells);
-	k_neighbours<<<gp, tpb, 0, s>>>(a);
+	k_cell_rank<<<gp, tpb, 0, s>>>(a);
+	const long long warps = (long long) a.N * 32;
+	k_neighbours<<<(int) ((warps + tpb - 1) / tpb), tpb, 0, s>>>(a);
 	k_list_done<<<1, 32, 0, s>>>(a);
 	return cudaGetLastError();
 }

@@ -46,7 +46,7 @@ def dna2_settings(T: float, salt: float = 0.5, average: bool = True, seq: Option
 def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = "no", newtonian_steps: int = 103,
                 pt: float = 0.0, diff_coeff: float = 2.5, bussi_tau: float = 1000.0, seed: int = 1,
                 precision: str = "mixed", cells_auto_optimisation: bool = True, max_neigh: int = 0,
-                steps_per_graph: int = 16) -> _abi.MDSettings:
+                steps_per_graph: int = 16, list_rebuild_node: str = "conditional") -> _abi.MDSettings:
     m = _abi.MDSettings()
     _abi.lib().oxgb_md_default_settings(C.byref(m))
     m.dt = dt
@@ -61,6 +61,7 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
     m.cells_auto_optimisation = 1 if cells_auto_optimisation else 0
     m.max_neigh = max_neigh
     m.steps_per_graph = steps_per_graph
+    m.list_rebuild_node = {"conditional": 0, "kernel": 1}[list_rebuild_node]
     return m
 
 

@@ -101,6 +101,22 @@ def test_graph_replay_equals_single_steps():
     b.close()
 
 
+def test_rebuild_node_kinds_agree():
+    """The conditional rebuild node and the always-launched rebuild kernels give the same run."""
+    g = load_golden("mixed")
+    a, _ = system_from_golden(g, precision="mixed", dt=0.003, steps_per_graph=10)
+    b, _ = system_from_golden(g, precision="mixed", dt=0.003, steps_per_graph=10, list_rebuild_node="kernel")
+    a.run(300)
+    b.run(300)
+    sa, sb = a.get_state(), b.get_state()
+    assert np.array_equal(sa["pos"], sb["pos"])
+    assert np.array_equal(sa["vel"], sb["vel"])
+    assert np.array_equal(sa["quat"], sb["quat"])
+    assert a.info()["rebuilds"] == b.info()["rebuilds"] >= 2
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("precision", ["mixed", "double"])
 def test_lists_stay_complete_between_rebuilds(precision):
     """Forces from term lists carried over many steps equal forces from freshly built lists."""
