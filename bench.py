@@ -176,7 +176,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain40k", choices=sorted(WORKLOADS))
-    ap.add_argument("--md-steps", type=int, default=100, help="MD steps per timed iteration")
+    ap.add_argument("--md-steps", type=int, default=200, help="MD steps per timed iteration")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -344,7 +344,7 @@ struct oxgb_md {
 	long long *step = nullptr;
 	double *esplit = nullptr, *scratch = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
 	unsigned *bussi_done = nullptr;
-	int bussi_blocks = 0;
+	long long *bussi_stamp = nullptr;
 	double pt = 0, pr = 0;
 
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
@@ -360,7 +360,7 @@ struct oxgb_md {
 		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
 					(void *) fback, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, bond_f,
 					bond_tp, bond_tq, d_tab, (void *) status, (void *) flag, (void *) step, (void *) esplit, (void *) scratch,
-					(void *) bussi_partials, (void *) bussi_state, (void *) bussi_done, (void *) d_rebuilds})
+					(void *) bussi_partials, (void *) bussi_state, (void *) bussi_done, (void *) bussi_stamp, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -371,6 +371,25 @@ struct oxgb_md {
 		if(ev_join) cudaEventDestroy(ev_join);
 	}
 };
+
+static ThermoArgs thermo_args(oxgb_md *h) {
+	ThermoArgs t{};
+	t.N = h->N;
+	t.thermostat = h->md.thermostat;
+	t.newtonian_steps = h->md.newtonian_steps > 0 ? h->md.newtonian_steps : 1;
+	t.pt = h->pt;
+	t.pr = h->pr;
+	t.T = h->dna[0].T;
+	t.sqrtT = std::sqrt(h->dna[0].T);
+	t.seed = h->md.seed;
+	t.bussi_c = std::exp(-(double) t.newtonian_steps / h->md.bussi_tau);
+	t.bussi_partials = h->bussi_partials;
+	t.bussi_state = h->bussi_state;
+	t.bussi_stamp = h->bussi_stamp;
+	t.done = h->bussi_done;
+	t.step = h->step;
+	return t;
+}
 
 static StepArgs step_args(oxgb_md *h) {
 	StepArgs a{};
@@ -394,19 +413,7 @@ static StepArgs step_args(oxgb_md *h) {
 	a.skin2 = (float) h->md.verlet_skin * (float) h->md.verlet_skin;
 	a.flag = h->flag;
 	a.status = h->status;
-	a.step = h->step;
-	a.thermostat = h->md.thermostat;
-	a.newtonian_steps = h->md.newtonian_steps > 0 ? h->md.newtonian_steps : 1;
-	a.pt = h->pt;
-	a.pr = h->pr;
-	a.T = h->dna[0].T;
-	a.sqrtT = std::sqrt(h->dna[0].T);
-	a.seed = h->md.seed;
-	a.bussi_c = std::exp(-(double) a.newtonian_steps / h->md.bussi_tau);
-	a.bussi_partials = h->bussi_partials;
-	a.bussi_state = h->bussi_state;
-	a.bussi_done = h->bussi_done;
-	a.bussi_blocks = h->bussi_blocks;
+	a.th = thermo_args(h);
 	return a;
 }
 
@@ -446,6 +453,7 @@ static ForceArgs force_args(oxgb_md *h) {
 	a.bond_f = h->bond_f;
 	a.bond_tp = h->bond_tp;
 	a.bond_tq = h->bond_tq;
+	a.th = thermo_args(h);
 	return a;
 }
 
@@ -528,8 +536,8 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->esplit, sizeof(double) * 8 * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->scratch, sizeof(double) * 8 * n_systems) == cudaSuccess;
-	h->bussi_blocks = std::max(1, std::min(1024, (N + 255) / 256));
-	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * h->bussi_blocks) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * nonbonded_blocks(N)) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
@@ -539,6 +547,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	cudaMemset(h->step, 0, sizeof(long long));
 	cudaMemset(h->d_rebuilds, 0, sizeof(unsigned long long));
 	cudaMemset(h->bussi_done, 0, sizeof(unsigned));
+	cudaMemset(h->bussi_stamp, 0xff, sizeof(long long));  // -1: no rescaling pending
 	int rc = upload_tables(h);
 	if(rc) return bail(rc);
 	h->rverlet = (float) h->rcut + 2.f * (float) h->md.verlet_skin;
@@ -704,6 +713,7 @@ extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *qu
 	CK(cudaMemcpyAsync(h->quatd, q.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
 	CK(cudaMemcpyAsync(h->veld, v.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
 	CK(cudaMemcpyAsync(h->Ld, l.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
+	CK(cudaMemsetAsync(h->bussi_stamp, 0xff, sizeof(long long), h->stream));  // a new state: nothing pending
 	CK(cudaMemcpyAsync(h->pos_hi, hi.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
 	CK(cudaMemcpyAsync(h->pos_lo, lo.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
 	StepArgs sa = step_args(h);
@@ -737,10 +747,11 @@ extern "C" int oxgb_md_get_state(oxgb_md *h, double *pos, double *quat, double *
 	return OXGB_OK;
 }
 
-// The Bussi noise draws depend only on (seed, step): they run on a second stream (a parallel
-// branch of the step graph) while the forces are evaluated, and join before the thermostat.
+// The Bussi draws depend only on (seed, step): they run on a second stream (a parallel branch
+// of the step graph) beside the first step, the list rebuild and the bonded kernel, and join
+// before the non-bonded kernel, whose epilogue makes the update.
 static cudaError_t fork_noise(oxgb_md *h, const StepArgs &sa) {
-	if(sa.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
+	if(sa.th.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
 	cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
 	if(e == cudaSuccess) e = cudaStreamWaitEvent(h->noise, h->ev_fork, 0);
 	if(e == cudaSuccess) e = launch_bussi_noise(sa, h->noise);
@@ -748,16 +759,15 @@ static cudaError_t fork_noise(oxgb_md *h, const StepArgs &sa) {
 	return e;
 }
 
-static cudaError_t join_noise(oxgb_md *h, const StepArgs &sa) {
-	if(sa.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
-	return cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+static cudaEvent_t join_event(oxgb_md *h, const StepArgs &sa) {
+	return sa.th.thermostat == OXGB_THERMOSTAT_BUSSI ? h->ev_join : nullptr;
 }
 
 // one MD step on h->stream (captured into the graph)
 static int enqueue_step(oxgb_md *h, cudaGraph_t capturing) {
 	StepArgs sa = step_args(h);
-	CK(launch_first_step(sa, h->dbl, h->stream));
 	CK(fork_noise(h, sa));
+	CK(launch_first_step(sa, h->dbl, h->stream));
 	ListArgs la = md_list_args(h, h->conditional_ok ? 0 : 1);
 	if(h->conditional_ok) {
 		cudaGraphConditionalHandle hc;
@@ -788,10 +798,7 @@ static int enqueue_step(oxgb_md *h, cudaGraph_t capturing) {
 		CK(launch_list_build(la, h->stream));
 	}
 	ForceArgs fa = force_args(h);
-	CK(launch_forces_split(fa, h->dbl, false, true, h->stream));
-	CK(join_noise(h, sa));
-	CK(launch_thermostat(sa, h->stream));
-	CK(launch_step_advance(sa, h->stream));
+	CK(launch_forces_split(fa, h->dbl, false, true, h->stream, join_event(h, sa)));
 	return OXGB_OK;
 }
 
@@ -844,15 +851,18 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 	// remainder, eagerly
 	for(; done < nsteps; done++) {
 		StepArgs sa = step_args(h);
-		CK(launch_first_step(sa, h->dbl, h->stream));
 		CK(fork_noise(h, sa));
+		CK(launch_first_step(sa, h->dbl, h->stream));
 		ListArgs la = md_list_args(h, 1);
 		CK(launch_list_build(la, h->stream));
 		ForceArgs fa = force_args(h);
-		CK(launch_forces_split(fa, h->dbl, false, true, h->stream));
-		CK(join_noise(h, sa));
-		CK(launch_thermostat(sa, h->stream));
-		CK(launch_step_advance(sa, h->stream));
+		CK(launch_forces_split(fa, h->dbl, false, true, h->stream, join_event(h, sa)));
+	}
+	// a Bussi rescaling decided by the last step is applied now, so that the state is complete
+	// whenever control returns to the caller
+	if(nsteps > 0 && h->md.thermostat == OXGB_THERMOSTAT_BUSSI) {
+		StepArgs sa = step_args(h);
+		CK(launch_bussi_flush(sa, h->stream));
 	}
 	h->host_step += nsteps;
 	if(sync) return read_status(h);

@@ -15,6 +15,7 @@
 //    int2 bonds and a neighbour matrix of any stride, accumulating into forces and torques
 //    initialised by the caller, exactly the contract of CUDABaseInteraction::compute_forces.
 #include "kernels.h"
+#include "thermo.cuh"
 
 #include <cuda_runtime.h>
 
@@ -487,6 +488,62 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 	return s + err;
 }
 
+// End of the fused step, after every nucleotide's second half kick: the blocks' sums of v,
+// |v|^2 and |L|^2 (Bussi steps only) are written in block order; the last block to finish
+// reduces them in a fixed order (deterministic), makes the Bussi update, and advances the step
+// counter (every block has read it by then).
+__device__ void step_epilogue(const ThermoArgs &t, long long step, bool bussi, const double kin[5]) {
+	__shared__ double red[5][32];
+	__shared__ bool last;
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+	if(bussi) {
+#pragma unroll
+		for(int k = 0; k < 5; k++) {
+			double x = kin[k];
+			for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+			if(lane == 0) red[k][w] = x;
+		}
+		__syncthreads();
+		if(threadIdx.x < 5) {
+			double x = 0;
+			for(int u = 0; u < nw; u++) x += red[threadIdx.x][u];
+			t.bussi_partials[blockIdx.x * 8 + threadIdx.x] = x;
+			__threadfence();
+		}
+	}
+	__syncthreads();
+	if(threadIdx.x == 0) last = atomicAdd(t.done, 1u) == gridDim.x - 1;
+	__syncthreads();
+	if(!last) return;
+	__threadfence();
+	if(bussi) {
+		double part[5] = {0, 0, 0, 0, 0};
+		for(int b = threadIdx.x; b < (int) gridDim.x; b += blockDim.x)
+#pragma unroll
+			for(int k = 0; k < 5; k++) part[k] += __ldcg(t.bussi_partials + b * 8 + k);
+#pragma unroll
+		for(int k = 0; k < 5; k++) {
+			double x = part[k];
+			for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+			if(lane == 0) red[k][w] = x;
+		}
+		__syncthreads();
+		if(threadIdx.x == 0) {
+			double sum[5];
+			for(int k = 0; k < 5; k++) {
+				double x = 0;
+				for(int u = 0; u < nw; u++) x += red[k][u];
+				sum[k] = x;
+			}
+			bussi_update(t, step, sum);
+		}
+	}
+	if(threadIdx.x == 0) {
+		*t.done = 0;
+		*t.step = step + 1;
+	}
+}
+
 // K lanes per nucleotide: lane l of a group takes entries l, l + K, ... of every term list, so a
 // warp holds 32 / K nucleotides and all its lanes run the same term loop
 template <typename R, class Loader, bool SPLIT, bool FUSE_KICK, int K>
@@ -496,12 +553,18 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
 	const long long N = a.N;
 	const int sub = threadIdx.x % K;
-	const int groups = (gridDim.x * blockDim.x) / K;
-	const int g0 = (blockIdx.x * blockDim.x + threadIdx.x) / K;
-	// every lane iterates the same number of times (all lanes take part in the shuffles)
-	const int rounds = (a.N + groups - 1) / groups;
-	for(int rnd = 0; rnd < rounds; rnd++) {
-		const int i_raw = g0 + rnd * groups;
+	// one nucleotide per group of K lanes: the grid covers every nucleotide (nonbonded_blocks);
+	// the lanes of a group past the last nucleotide still take part in the shuffles
+	const int i_raw = (blockIdx.x * blockDim.x + threadIdx.x) / K;
+	// fused step epilogue: thermostat of this step and its Bussi block sums
+	long long step = 0;
+	bool thermo_now = false;
+	double kin[5] = {0, 0, 0, 0, 0};
+	if(FUSE_KICK) {
+		step = *a.th.step;
+		thermo_now = a.th.thermostat != 0 && step % a.th.newtonian_steps == 0;
+	}
+	{
 		const bool live = i_raw < a.N;
 		const int i = live ? i_raw : a.N - 1;
 		Nuc<R> p;
@@ -582,7 +645,7 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 		const v3<R> tl{group_sum_comp<R, K>(acc.T.s.x, acc.T.c.x), group_sum_comp<R, K>(acc.T.s.y, acc.T.c.y),
 				group_sum_comp<R, K>(acc.T.s.z, acc.T.c.z)};
 		const R e = group_sum_comp<R, K>(acc.E, acc.Ec), eh = group_sum_comp<R, K>(acc.Eh, acc.Ehc);
-		if(sub != 0 || !live) continue;
+		if(sub == 0 && live) {
 		V4 fo, to;
 		fo.x = fx;
 		fo.y = fy;
@@ -603,10 +666,20 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 			L.x += (double) to.x * hdt;
 			L.y += (double) to.y * hdt;
 			L.z += (double) to.z * hdt;
+			if(thermo_now && a.th.thermostat == 1) brownian_redraw(a.th, i, step, v, L);
 			a.vel[i] = v;
 			a.angmom[i] = L;
+			if(thermo_now && a.th.thermostat == 2) {
+				kin[0] += v.x;
+				kin[1] += v.y;
+				kin[2] += v.z;
+				kin[3] += v.x * v.x + v.y * v.y + v.z * v.z;
+				kin[4] += L.x * L.x + L.y * L.y + L.z * L.z;
+			}
+		}
 		}
 	}
+	if(FUSE_KICK) step_epilogue(a.th, step, thermo_now && a.th.thermostat == 2, kin);
 }
 
 // lanes per nucleotide in the non-bonded kernel
@@ -614,27 +687,34 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 #define OXGB_NB_LANES 4
 #endif
 
+int nonbonded_blocks(int N) {
+	const long long threads = (long long) (N > 0 ? N : 1) * OXGB_NB_LANES;
+	return (int) ((threads + 127) / 128);
+}
+
 template <typename R, class Loader, bool SPLIT, bool FUSE>
-static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s) {
+static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEvent_t wait) {
 	const int tpb = 128;
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	k_bonded_split<R, Loader, SPLIT><<<blocks, tpb, 0, s>>>(a, ld);
+	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
-	const long long threads = (long long) (a.N > 0 ? a.N : 1) * K;
-	const int nb_blocks = (int) ((threads + tpb - 1) / tpb);
-	k_nonbonded_split<R, Loader, SPLIT, FUSE, K><<<nb_blocks, tpb, 0, s>>>(a, ld);
+	k_nonbonded_split<R, Loader, SPLIT, FUSE, K><<<nonbonded_blocks(a.N), tpb, 0, s>>>(a, ld);
 }
 
-cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s) {
+cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s, cudaEvent_t wait) {
+	if(split && fuse_kick) return cudaErrorInvalidValue;  // the energy split is for force-only calls
 	if(dbl) {
 		SplitDouble ld{a.posd, a.quatd, a.pos_hi, a.pos_lo, a.bonds};
-		if(split) fuse_kick ? launch_split_t<double, SplitDouble, true, true>(a, ld, s) : launch_split_t<double, SplitDouble, true, false>(a, ld, s);
-		else fuse_kick ? launch_split_t<double, SplitDouble, false, true>(a, ld, s) : launch_split_t<double, SplitDouble, false, false>(a, ld, s);
+		if(split) launch_split_t<double, SplitDouble, true, false>(a, ld, s, wait);
+		else if(fuse_kick) launch_split_t<double, SplitDouble, false, true>(a, ld, s, wait);
+		else launch_split_t<double, SplitDouble, false, false>(a, ld, s, wait);
 	}
 	else {
 		SplitMixed ld{a.pos_hi, a.pos_lo, a.fa1, a.fa3, a.fback};
-		if(split) fuse_kick ? launch_split_t<float, SplitMixed, true, true>(a, ld, s) : launch_split_t<float, SplitMixed, true, false>(a, ld, s);
-		else fuse_kick ? launch_split_t<float, SplitMixed, false, true>(a, ld, s) : launch_split_t<float, SplitMixed, false, false>(a, ld, s);
+		if(split) launch_split_t<float, SplitMixed, true, false>(a, ld, s, wait);
+		else if(fuse_kick) launch_split_t<float, SplitMixed, false, true>(a, ld, s, wait);
+		else launch_split_t<float, SplitMixed, false, false>(a, ld, s, wait);
 	}
 	return cudaGetLastError();
 }

@@ -13,6 +13,23 @@
 
 namespace oxgb {
 
+// thermostat state shared by the integrator and the fused force epilogue
+struct ThermoArgs {
+	int N;                                 // nucleotides of the system
+	int thermostat;                        // 0 none, 1 brownian, 2 bussi
+	int newtonian_steps;
+	double pt, pr, sqrtT, T;
+	unsigned long long seed;
+	double bussi_c;                        // exp(-newtonian_steps / tau)
+	double *bussi_partials;                // [blocks * 8] per-block sums of v, |v|^2, |L|^2
+	double *bussi_state;                   // [16]: K_t, K_r, factor_t, factor_r, vcom x y z, -,
+	                                       // then the step's draws: sum_t, rr_t, sum_r, rr_r
+	long long *bussi_stamp;                // step of the last Bussi update (its rescaling is
+	                                       // applied by the next first step); -1 when none pends
+	unsigned *done;                        // blocks of the fused epilogue finished (0 between steps)
+	long long *step;                       // device step counter
+};
+
 struct ForceArgs {
 	int N;
 	const float4 *pos_hi, *pos_lo;         // FP32 mirrors (w of pos_hi: btype<<22 | index, w of pos_lo: type)
@@ -35,6 +52,8 @@ struct ForceArgs {
 	const int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
 	int ev_cap, base_cap, stk_cap;            // capacities (an overflowed list is read up to them)
 	void *bond_f, *bond_tp, *bond_tq;         // per bond owner p (q = n3[p]): f on q with w = energy, torques
+	// fused step epilogue (engine layout, fuse_kick): thermostat of the step, step counter
+	ThermoArgs th;
 };
 
 cudaError_t launch_forces_mixed(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s);
@@ -42,7 +61,12 @@ cudaError_t launch_forces_double(const ForceArgs &a, bool split, bool fuse_kick,
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
 // split path: bonded pairs (one thread per bond, both sides), then non-bonded terms (one
 // thread per nucleotide, one loop per term list) with the bonded results gathered in its epilogue
-cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s);
+// fuse_kick: the step epilogue of the MD engine (second half kick, thermostat, step counter);
+// wait: an event the non-bonded kernel waits for (the Bussi draws), or null
+cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s,
+		cudaEvent_t wait = nullptr);
+// blocks of the split non-bonded kernel for N nucleotides (sizes ThermoArgs::bussi_partials)
+int nonbonded_blocks(int N);
 
 struct ListArgs {
 	int N;
@@ -94,25 +118,14 @@ struct StepArgs {
 	float skin2;
 	int *flag;
 	int *status;
-	long long *step;                       // device step counter
-	// thermostats
-	int thermostat;                        // 0 none, 1 brownian, 2 bussi
-	int newtonian_steps;
-	double pt, pr, sqrtT, T;
-	unsigned long long seed;
-	double bussi_c;                        // exp(-newtonian_steps / tau)
-	double *bussi_partials;                // [blocks * 8]
-	double *bussi_state;                   // [16]: K_t, K_r, factor_t, factor_r, vcom x y z, -,
-	                                       // then the step's noise draws: sum_t, rr_t, sum_r, rr_r
-	unsigned *bussi_done;                  // blocks of k_bussi_partial finished (0 between steps)
-	int bussi_blocks;
+	ThermoArgs th;
 };
 
 cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s);
-cudaError_t launch_thermostat(const StepArgs &a, cudaStream_t s);
-// the Bussi noise draws of the current step (independent of the state: may run beside the forces)
+// the Bussi draws of the current step (they do not depend on the state: run beside the step)
 cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s);
-cudaError_t launch_step_advance(const StepArgs &a, cudaStream_t s);
+// applies a pending Bussi rescaling to the state and clears it (end of a run)
+cudaError_t launch_bussi_flush(const StepArgs &a, cudaStream_t s);
 // sets the graph conditional to (*flag != 0)
 cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h, cudaStream_t s);
 // refresh the FP32 mirrors from the FP64 state (after a host upload)

@@ -1,0 +1,178 @@
+// Random streams and thermostat arithmetic shared by the integrator kernels (integrate.cu)
+// and the thermostat epilogue of the fused force kernel (forces.cu).
+//
+// Random numbers come from a counter-based Philox-4x32-10 stream keyed by (seed, step,
+// particle), so runs are reproducible and graph-replayable; the oracle (oracle/dna2_oracle.c,
+// oxo_philox) draws the same numbers.  The Bussi kinetic-energy update follows
+// src/Backends/Thermostats/BussiThermostat.cpp:44-160 and the Brownian ("john") redraw
+// src/CUDA/Thermostats/CUDABrownianThermostat.cu:15-51.
+#pragma once
+
+#include "kernels.h"
+
+namespace oxgb {
+
+// ---------------------------------------------------------------- Philox-4x32-10
+
+static __device__ __forceinline__ void philox(unsigned k0, unsigned k1, unsigned c0, unsigned c1, unsigned c2, unsigned c3,
+		unsigned out[4]) {
+	const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+	for(int r = 0; r < 10; r++) {
+		const unsigned hi0 = __umulhi(M0, c0), lo0 = M0 * c0;
+		const unsigned hi1 = __umulhi(M1, c2), lo1 = M1 * c2;
+		const unsigned n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+		c0 = n0;
+		c1 = lo1;
+		c2 = n2;
+		c3 = lo0;
+		k0 += W0;
+		k1 += W1;
+	}
+	out[0] = c0;
+	out[1] = c1;
+	out[2] = c2;
+	out[3] = c3;
+}
+
+static __device__ __forceinline__ double u01(unsigned x) { return ((double) x + 1.0) * (1.0 / 4294967296.0); }
+
+static __device__ __forceinline__ void box_muller(unsigned ua, unsigned ub, double &g0, double &g1) {
+	const double r = sqrt(-2.0 * log(u01(ua)));
+	double s, c;
+	sincos(6.283185307179586 * u01(ub), &s, &c);
+	g0 = r * c;
+	g1 = r * s;
+}
+
+#define RNG_BROWNIAN 0x42524f57u
+#define RNG_BUSSI 0x42555353u
+
+struct Stream {
+	unsigned k0, k1, s0, s1, c, blk, idx;
+	unsigned buf[4];
+	__device__ void init(unsigned long long seed, long long s, unsigned channel) {
+		k0 = (unsigned) seed;
+		k1 = (unsigned) (seed >> 32);
+		s0 = (unsigned) s;
+		s1 = (unsigned) ((unsigned long long) s >> 32);
+		c = RNG_BUSSI ^ channel;
+		blk = 0;
+		idx = 4;
+	}
+	__device__ double u() {
+		if(idx == 4) {
+			philox(k0, k1, s0, s1, c, blk++, buf);
+			idx = 0;
+		}
+		return u01(buf[idx++]);
+	}
+	__device__ double gauss() {
+		const double a = u(), b = u();
+		return sqrt(-2.0 * log(a)) * cos(6.283185307179586 * b);
+	}
+};
+
+// gamma deviate of integer order (the Numerical Recipes algorithm the reference uses)
+static __device__ double gamdev(Stream &st, int ia) {
+	if(ia < 6) {
+		double x = 1.0;
+		for(int j = 1; j <= ia; j++) x *= st.u();
+		return -log(x);
+	}
+	const double am = ia - 1, s = sqrt(2.0 * am + 1.0);
+	double x = am, e, y = 0.0, v1, v2;
+	// every rejection loop is bounded; each accepts with probability > 0.5, so the bounds are
+	// never reached by a working random stream
+	for(int guard = 0; guard < 1000; guard++) {
+		bool got = false;
+		for(int g2 = 0; g2 < 1000 && !got; g2++) {
+			for(int g1 = 0; g1 < 1000; g1++) {
+				v1 = st.u();
+				v2 = 2.0 * st.u() - 1.0;
+				if(v1 * v1 + v2 * v2 <= 1.0) break;
+			}
+			y = v2 / v1;
+			x = s * y + am;
+			got = x > 0.0;
+		}
+		if(!got) return am;
+		e = (1.0 + y * y) * exp(am * log(x / am) - s * y);
+		if(st.u() <= e) return x;
+	}
+	return am;
+}
+
+static __device__ double sum_noises(Stream &st, int nn) {
+	if(nn == 0) return 0.0;
+	if(nn == 1) {
+		const double r = st.gauss();
+		return r * r;
+	}
+	if(nn % 2 == 0) return 2.0 * gamdev(st, nn / 2);
+	const double r = st.gauss();
+	return 2.0 * gamdev(st, (nn - 1) / 2) + r * r;
+}
+
+// the two draws of one kinetic-energy update (BussiThermostat::_update_K, BussiThermostat.cpp:
+// 55-65): the Gaussian r, then the sum of dof - 1 squared Gaussians; they do not depend on the
+// state, so they are drawn apart from (and concurrently with) the force evaluation
+static __device__ void bussi_draws(Stream &st, int dof, double &sum, double &rr) {
+	rr = st.gauss();
+	sum = sum_noises(st, dof - 1);
+}
+
+static __device__ void update_K(double &K, int dof, double T, double c, double sum, double rr) {
+	const double Kt = 0.5 * dof * T;
+	const double dK = (1.0 - c) * (Kt * (sum + rr * rr) / dof - K) + 2.0 * rr * sqrt(K * Kt / dof * (1.0 - c) * c);
+	K += dK;
+}
+
+// Brownian ("john") thermostat: every newtonian_steps steps each nucleotide redraws its
+// velocity with probability pt and its angular momentum with probability pr from the
+// Maxwell-Boltzmann distribution at T (unit mass and moment of inertia)
+static __device__ __noinline__ void brownian_redraw(const ThermoArgs &t, int i, long long s, double4_32a &v, double4_32a &L) {
+	unsigned o0[4], o1[4];
+	const unsigned k0 = (unsigned) t.seed, k1 = (unsigned) (t.seed >> 32);
+	const unsigned s0 = (unsigned) s, s1 = (unsigned) ((unsigned long long) s >> 32);
+	philox(k0, k1, s0, s1, RNG_BROWNIAN, (unsigned) (2 * i), o0);
+	philox(k0, k1, s0, s1, RNG_BROWNIAN, (unsigned) (2 * i + 1), o1);
+	double g[6];
+	box_muller(o0[2], o0[3], g[0], g[1]);
+	box_muller(o1[0], o1[1], g[2], g[3]);
+	box_muller(o1[2], o1[3], g[4], g[5]);
+	if(u01(o0[0]) < t.pt) v = make_double4_32a(g[0] * t.sqrtT, g[1] * t.sqrtT, g[2] * t.sqrtT, 0.0);
+	if(u01(o0[1]) < t.pr) L = make_double4_32a(g[3] * t.sqrtT, g[4] * t.sqrtT, g[5] * t.sqrtT, 0.0);
+}
+
+// Bussi: from the sums of v, |v|^2 and |L|^2 over the system, the new running kinetic energies
+// (with the draws of this step) and the rescaling factors; one thread
+static __device__ void bussi_update(const ThermoArgs &t, long long s, const double sum[5]) {
+	const double N = t.N;
+	const double vc[3] = {sum[0] / N, sum[1] / N, sum[2] / N};
+	const double Kt_now = 0.5 * (sum[3] - N * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
+	const double Kr_now = 0.5 * sum[4];
+	double *st = t.bussi_state;
+	update_K(st[0], 3 * (t.N - 1), t.T, t.bussi_c, __ldcg(st + 8), __ldcg(st + 9));
+	update_K(st[1], 3 * t.N, t.T, t.bussi_c, __ldcg(st + 10), __ldcg(st + 11));
+	st[2] = sqrt(st[0] / Kt_now);
+	st[3] = sqrt(st[1] / Kr_now);
+	st[4] = vc[0];
+	st[5] = vc[1];
+	st[6] = vc[2];
+	*t.bussi_stamp = s;
+}
+
+// the rescaling of a Bussi update made at step s, applied to one nucleotide
+static __device__ __forceinline__ void bussi_rescale(const ThermoArgs &t, double4_32a &v, double4_32a &L) {
+	const double *st = t.bussi_state;
+	const double ft = __ldcg(st + 2), fr = __ldcg(st + 3), cx = __ldcg(st + 4), cy = __ldcg(st + 5), cz = __ldcg(st + 6);
+	v.x = (v.x - cx) * ft + cx;
+	v.y = (v.y - cy) * ft + cy;
+	v.z = (v.z - cz) * ft + cz;
+	L.x *= fr;
+	L.y *= fr;
+	L.z *= fr;
+}
+
+}  // namespace oxgb
