@@ -344,7 +344,7 @@ struct oxgb_md {
 	long long *step = nullptr;
 	double *esplit = nullptr, *scratch = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
 	unsigned *bussi_done = nullptr;
-	long long *bussi_stamp = nullptr;
+	long long *bussi_stamp = nullptr, *open_step = nullptr;
 	double pt = 0, pr = 0;
 
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
@@ -360,7 +360,7 @@ struct oxgb_md {
 		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
 					(void *) fback, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, bond_f,
 					bond_tp, bond_tq, d_tab, (void *) status, (void *) flag, (void *) step, (void *) esplit, (void *) scratch,
-					(void *) bussi_partials, (void *) bussi_state, (void *) bussi_done, (void *) bussi_stamp, (void *) d_rebuilds})
+					(void *) bussi_partials, (void *) bussi_state, (void *) bussi_done, (void *) bussi_stamp, (void *) open_step, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -372,9 +372,12 @@ struct oxgb_md {
 	}
 };
 
-static ThermoArgs thermo_args(oxgb_md *h) {
+// step_offset: position of the step in its graph; engine_step: the forces belong to an MD step
+// (the bonded kernel then marks its second half kick pending)
+static ThermoArgs thermo_args(oxgb_md *h, int step_offset = 0, bool engine_step = false) {
 	ThermoArgs t{};
 	t.N = h->N;
+	t.dt = h->md.dt;
 	t.thermostat = h->md.thermostat;
 	t.newtonian_steps = h->md.newtonian_steps > 0 ? h->md.newtonian_steps : 1;
 	t.pt = h->pt;
@@ -387,11 +390,13 @@ static ThermoArgs thermo_args(oxgb_md *h) {
 	t.bussi_state = h->bussi_state;
 	t.bussi_stamp = h->bussi_stamp;
 	t.done = h->bussi_done;
-	t.step = h->step;
+	t.step_base = h->step;
+	t.step_offset = step_offset;
+	t.open_step = engine_step ? h->open_step : nullptr;
 	return t;
 }
 
-static StepArgs step_args(oxgb_md *h) {
+static StepArgs step_args(oxgb_md *h, int step_offset = 0) {
 	StepArgs a{};
 	a.N = h->N;
 	a.dt = h->md.dt;
@@ -413,11 +418,12 @@ static StepArgs step_args(oxgb_md *h) {
 	a.skin2 = (float) h->md.verlet_skin * (float) h->md.verlet_skin;
 	a.flag = h->flag;
 	a.status = h->status;
-	a.th = thermo_args(h);
+	a.th = thermo_args(h, step_offset);
+	a.th.open_step = h->open_step;
 	return a;
 }
 
-static ForceArgs force_args(oxgb_md *h) {
+static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = false) {
 	ForceArgs a{};
 	a.N = h->N;
 	a.pos_hi = h->pos_hi;
@@ -453,7 +459,7 @@ static ForceArgs force_args(oxgb_md *h) {
 	a.bond_f = h->bond_f;
 	a.bond_tp = h->bond_tp;
 	a.bond_tq = h->bond_tq;
-	a.th = thermo_args(h);
+	a.th = thermo_args(h, step_offset, engine_step);
 	return a;
 }
 
@@ -481,6 +487,14 @@ static int upload_tables(oxgb_md *h) {
 	h->pt = pt;
 	h->pr = (2 * T * n * dtf) / (T * n * dtf + 2 * 3 * D);
 	return OXGB_OK;
+}
+
+// nothing pending: no open half kick, no Bussi rescaling (a fresh or newly uploaded state)
+static int clear_pending(oxgb_md *h) {
+	const long long none[1] = {OXGB_NO_STEP};
+	if(cudaMemcpyAsync(h->open_step, none, sizeof(long long), cudaMemcpyHostToDevice, h->stream) != cudaSuccess) return 1;
+	if(cudaMemcpyAsync(h->bussi_stamp, none, sizeof(long long), cudaMemcpyHostToDevice, h->stream) != cudaSuccess) return 1;
+	return cudaStreamSynchronize(h->stream) != cudaSuccess;
 }
 
 extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *box, const oxgb_dna2_settings *dna,
@@ -538,6 +552,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->scratch, sizeof(double) * 8 * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * nonbonded_blocks(N)) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
+	ok &= cudaMalloc(&h->open_step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
@@ -547,7 +562,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	cudaMemset(h->step, 0, sizeof(long long));
 	cudaMemset(h->d_rebuilds, 0, sizeof(unsigned long long));
 	cudaMemset(h->bussi_done, 0, sizeof(unsigned));
-	cudaMemset(h->bussi_stamp, 0xff, sizeof(long long));  // -1: no rescaling pending
+	if(clear_pending(h)) return bail(fail(OXGB_E_CUDA, "upload"));
 	int rc = upload_tables(h);
 	if(rc) return bail(rc);
 	h->rverlet = (float) h->rcut + 2.f * (float) h->md.verlet_skin;
@@ -621,7 +636,7 @@ static int build_list_now(oxgb_md *h) {
 static int compute_forces_now(oxgb_md *h, bool split) {
 	ForceArgs fa = force_args(h);
 	if(split) CK(cudaMemsetAsync(h->esplit, 0, sizeof(double) * 8, h->stream));
-	CK(launch_forces_split(fa, h->dbl, split, false, h->stream));
+	CK(launch_forces_split(fa, h->dbl, split, h->stream));
 	return OXGB_OK;
 }
 
@@ -713,7 +728,7 @@ extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *qu
 	CK(cudaMemcpyAsync(h->quatd, q.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
 	CK(cudaMemcpyAsync(h->veld, v.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
 	CK(cudaMemcpyAsync(h->Ld, l.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
-	CK(cudaMemsetAsync(h->bussi_stamp, 0xff, sizeof(long long), h->stream));  // a new state: nothing pending
+	if(clear_pending(h)) return fail(OXGB_E_CUDA, "upload");  // a new state: nothing pending
 	CK(cudaMemcpyAsync(h->pos_hi, hi.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
 	CK(cudaMemcpyAsync(h->pos_lo, lo.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
 	StepArgs sa = step_args(h);
@@ -748,8 +763,8 @@ extern "C" int oxgb_md_get_state(oxgb_md *h, double *pos, double *quat, double *
 }
 
 // The Bussi draws depend only on (seed, step): they run on a second stream (a parallel branch
-// of the step graph) beside the first step, the list rebuild and the bonded kernel, and join
-// before the non-bonded kernel, whose epilogue makes the update.
+// of the step graph) beside the first step, the list rebuild and the force kernels, and join
+// before the Bussi update.
 static cudaError_t fork_noise(oxgb_md *h, const StepArgs &sa) {
 	if(sa.th.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
 	cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
@@ -759,13 +774,17 @@ static cudaError_t fork_noise(oxgb_md *h, const StepArgs &sa) {
 	return e;
 }
 
-static cudaEvent_t join_event(oxgb_md *h, const StepArgs &sa) {
-	return sa.th.thermostat == OXGB_THERMOSTAT_BUSSI ? h->ev_join : nullptr;
+// after the forces of a Bussi step: join the draws, then the kinetic sums and the update
+static cudaError_t bussi_after_forces(oxgb_md *h, const StepArgs &sa) {
+	if(sa.th.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
+	cudaError_t e = cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+	if(e == cudaSuccess) e = launch_bussi_reduce(sa, h->dbl, h->stream);
+	return e;
 }
 
-// one MD step on h->stream (captured into the graph)
-static int enqueue_step(oxgb_md *h, cudaGraph_t capturing) {
-	StepArgs sa = step_args(h);
+// one MD step on h->stream (captured into the graph at position k)
+static int enqueue_step(oxgb_md *h, cudaGraph_t capturing, int k) {
+	StepArgs sa = step_args(h, k);
 	CK(fork_noise(h, sa));
 	CK(launch_first_step(sa, h->dbl, h->stream));
 	ListArgs la = md_list_args(h, h->conditional_ok ? 0 : 1);
@@ -797,8 +816,9 @@ static int enqueue_step(oxgb_md *h, cudaGraph_t capturing) {
 	else {
 		CK(launch_list_build(la, h->stream));
 	}
-	ForceArgs fa = force_args(h);
-	CK(launch_forces_split(fa, h->dbl, false, true, h->stream, join_event(h, sa)));
+	ForceArgs fa = force_args(h, k, true);
+	CK(launch_forces_split(fa, h->dbl, false, h->stream));
+	CK(bussi_after_forces(h, sa));
 	return OXGB_OK;
 }
 
@@ -815,7 +835,12 @@ static int build_graph(oxgb_md *h) {
 		cudaGraph_t cap;
 		CK(cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &cap, nullptr, nullptr, nullptr));
 		int rc = OXGB_OK;
-		for(int k = 0; k < K && rc == OXGB_OK; k++) rc = enqueue_step(h, cap);
+		for(int k = 0; k < K && rc == OXGB_OK; k++) rc = enqueue_step(h, cap, k);
+		if(rc == OXGB_OK) {
+			StepArgs sa = step_args(h);
+			cudaError_t e = launch_step_advance(sa, K, h->stream);
+			if(e != cudaSuccess) rc = fail(OXGB_E_CUDA, cudaGetErrorString(e));
+		}
 		cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
 		if(rc == OXGB_OK && ee == cudaSuccess) {
 			cudaError_t ie = cudaGraphInstantiate(&h->gexec, g, 0);
@@ -855,14 +880,16 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 		CK(launch_first_step(sa, h->dbl, h->stream));
 		ListArgs la = md_list_args(h, 1);
 		CK(launch_list_build(la, h->stream));
-		ForceArgs fa = force_args(h);
-		CK(launch_forces_split(fa, h->dbl, false, true, h->stream, join_event(h, sa)));
+		ForceArgs fa = force_args(h, 0, true);
+		CK(launch_forces_split(fa, h->dbl, false, h->stream));
+		CK(bussi_after_forces(h, sa));
+		CK(launch_step_advance(sa, 1, h->stream));
 	}
-	// a Bussi rescaling decided by the last step is applied now, so that the state is complete
-	// whenever control returns to the caller
-	if(nsteps > 0 && h->md.thermostat == OXGB_THERMOSTAT_BUSSI) {
+	// the last step's second half kick and thermostat, so that the state is complete whenever
+	// control returns to the caller
+	if(nsteps > 0) {
 		StepArgs sa = step_args(h);
-		CK(launch_bussi_flush(sa, h->stream));
+		CK(launch_step_flush(sa, h->dbl, h->stream));
 	}
 	h->host_step += nsteps;
 	if(sync) return read_status(h);

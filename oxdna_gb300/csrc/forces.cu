@@ -169,7 +169,7 @@ struct Vec4Of<double> {
 
 // ---------------------------------------------------------------- the kernel
 
-template <typename R, class Loader, bool SPLIT, bool ACCUMULATE, bool FUSE_KICK>
+template <typename R, class Loader, bool SPLIT, bool ACCUMULATE>
 __global__ void __launch_bounds__(128) k_forces(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	__shared__ DNA2Table<R> P;
@@ -278,19 +278,6 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, Loader ld) {
 			}
 			F4[i] = fo;
 			T4[i] = to;
-			if(FUSE_KICK) {
-				// second half kick of velocity Verlet, in double (CUDA_mixed.cuh:71-93)
-				const double hdt = 0.5 * a.dt;
-				double4_32a v = a.vel[i], L = a.angmom[i];
-				v.x += (double) fo.x * hdt;
-				v.y += (double) fo.y * hdt;
-				v.z += (double) fo.z * hdt;
-				L.x += (double) to.x * hdt;
-				L.y += (double) to.y * hdt;
-				L.z += (double) to.z * hdt;
-				a.vel[i] = v;
-				a.angmom[i] = L;
-			}
 			if(SPLIT) {
 #pragma unroll
 				for(int k = 0; k < N_TERMS; k++) atomicAdd(a.esplit + k, 0.5 * (double) split[k]);
@@ -306,34 +293,9 @@ static int grid_for(int N, int warps_per_block) {
 	return blocks > 0 ? blocks : 1;
 }
 
-template <bool SPLIT, bool FUSE>
-static cudaError_t launch_mixed(const ForceArgs &a, cudaStream_t s) {
-	LoadMixed ld{a.pos_hi, a.pos_lo, a.fa1, a.fa3};
-	k_forces<float, LoadMixed, SPLIT, false, FUSE><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
-	return cudaGetLastError();
-}
-
-cudaError_t launch_forces_mixed(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s) {
-	if(split) return fuse_kick ? launch_mixed<true, true>(a, s) : launch_mixed<true, false>(a, s);
-	return fuse_kick ? launch_mixed<false, true>(a, s) : launch_mixed<false, false>(a, s);
-}
-
-cudaError_t launch_forces_double(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s) {
-	LoadDouble ld{a.posd, a.quatd, a.pos_hi, a.pos_lo};
-	if(split) {
-		if(fuse_kick) k_forces<double, LoadDouble, true, false, true><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
-		else k_forces<double, LoadDouble, true, false, false><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
-	}
-	else {
-		if(fuse_kick) k_forces<double, LoadDouble, false, false, true><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
-		else k_forces<double, LoadDouble, false, false, false><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
-	}
-	return cudaGetLastError();
-}
-
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s) {
 	LoadRef ld{a.pos_hi, a.quat};
-	k_forces<float, LoadRef, false, true, false><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
+	k_forces<float, LoadRef, false, true><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
 	return cudaGetLastError();
 }
 
@@ -429,6 +391,8 @@ __global__ void __launch_bounds__(128) k_bonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	__shared__ DNA2Table<R> P;
 	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
+	// an MD step: from here on its second half kick is pending (the first step has read the mark)
+	if(a.th.open_step && blockIdx.x == 0 && threadIdx.x == 0) *a.th.open_step = *a.th.step_base + a.th.step_offset;
 	for(int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.N; p += gridDim.x * blockDim.x) {
 		const int q = a.bonds[p].x;
 		if(q < 0) continue;
@@ -488,65 +452,9 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 	return s + err;
 }
 
-// End of the fused step, after every nucleotide's second half kick: the blocks' sums of v,
-// |v|^2 and |L|^2 (Bussi steps only) are written in block order; the last block to finish
-// reduces them in a fixed order (deterministic), makes the Bussi update, and advances the step
-// counter (every block has read it by then).
-__device__ void step_epilogue(const ThermoArgs &t, long long step, bool bussi, const double kin[5]) {
-	__shared__ double red[5][32];
-	__shared__ bool last;
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-	if(bussi) {
-#pragma unroll
-		for(int k = 0; k < 5; k++) {
-			double x = kin[k];
-			for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-			if(lane == 0) red[k][w] = x;
-		}
-		__syncthreads();
-		if(threadIdx.x < 5) {
-			double x = 0;
-			for(int u = 0; u < nw; u++) x += red[threadIdx.x][u];
-			t.bussi_partials[blockIdx.x * 8 + threadIdx.x] = x;
-			__threadfence();
-		}
-	}
-	__syncthreads();
-	if(threadIdx.x == 0) last = atomicAdd(t.done, 1u) == gridDim.x - 1;
-	__syncthreads();
-	if(!last) return;
-	__threadfence();
-	if(bussi) {
-		double part[5] = {0, 0, 0, 0, 0};
-		for(int b = threadIdx.x; b < (int) gridDim.x; b += blockDim.x)
-#pragma unroll
-			for(int k = 0; k < 5; k++) part[k] += __ldcg(t.bussi_partials + b * 8 + k);
-#pragma unroll
-		for(int k = 0; k < 5; k++) {
-			double x = part[k];
-			for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-			if(lane == 0) red[k][w] = x;
-		}
-		__syncthreads();
-		if(threadIdx.x == 0) {
-			double sum[5];
-			for(int k = 0; k < 5; k++) {
-				double x = 0;
-				for(int u = 0; u < nw; u++) x += red[k][u];
-				sum[k] = x;
-			}
-			bussi_update(t, step, sum);
-		}
-	}
-	if(threadIdx.x == 0) {
-		*t.done = 0;
-		*t.step = step + 1;
-	}
-}
-
 // K lanes per nucleotide: lane l of a group takes entries l, l + K, ... of every term list, so a
 // warp holds 32 / K nucleotides and all its lanes run the same term loop
-template <typename R, class Loader, bool SPLIT, bool FUSE_KICK, int K>
+template <typename R, class Loader, bool SPLIT, int K>
 __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	__shared__ DNA2Table<R> P;
@@ -556,14 +464,6 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 	// one nucleotide per group of K lanes: the grid covers every nucleotide (nonbonded_blocks);
 	// the lanes of a group past the last nucleotide still take part in the shuffles
 	const int i_raw = (blockIdx.x * blockDim.x + threadIdx.x) / K;
-	// fused step epilogue: thermostat of this step and its Bussi block sums
-	long long step = 0;
-	bool thermo_now = false;
-	double kin[5] = {0, 0, 0, 0, 0};
-	if(FUSE_KICK) {
-		step = *a.th.step;
-		thermo_now = a.th.thermostat != 0 && step % a.th.newtonian_steps == 0;
-	}
 	{
 		const bool live = i_raw < a.N;
 		const int i = live ? i_raw : a.N - 1;
@@ -646,40 +546,19 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 				group_sum_comp<R, K>(acc.T.s.z, acc.T.c.z)};
 		const R e = group_sum_comp<R, K>(acc.E, acc.Ec), eh = group_sum_comp<R, K>(acc.Eh, acc.Ehc);
 		if(sub == 0 && live) {
-		V4 fo, to;
-		fo.x = fx;
-		fo.y = fy;
-		fo.z = fz;
-		fo.w = e;
-		to.x = dot(p.a1, tl);
-		to.y = dot(p.a2, tl);
-		to.z = dot(p.a3, tl);
-		to.w = eh;
-		reinterpret_cast<V4 *>(a.forces)[i] = fo;
-		reinterpret_cast<V4 *>(a.torques)[i] = to;
-		if(FUSE_KICK) {
-			const double hdt = 0.5 * a.dt;
-			double4_32a v = a.vel[i], L = a.angmom[i];
-			v.x += (double) fo.x * hdt;
-			v.y += (double) fo.y * hdt;
-			v.z += (double) fo.z * hdt;
-			L.x += (double) to.x * hdt;
-			L.y += (double) to.y * hdt;
-			L.z += (double) to.z * hdt;
-			if(thermo_now && a.th.thermostat == 1) brownian_redraw(a.th, i, step, v, L);
-			a.vel[i] = v;
-			a.angmom[i] = L;
-			if(thermo_now && a.th.thermostat == 2) {
-				kin[0] += v.x;
-				kin[1] += v.y;
-				kin[2] += v.z;
-				kin[3] += v.x * v.x + v.y * v.y + v.z * v.z;
-				kin[4] += L.x * L.x + L.y * L.y + L.z * L.z;
-			}
-		}
+			V4 fo, to;
+			fo.x = fx;
+			fo.y = fy;
+			fo.z = fz;
+			fo.w = e;
+			to.x = dot(p.a1, tl);
+			to.y = dot(p.a2, tl);
+			to.z = dot(p.a3, tl);
+			to.w = eh;
+			reinterpret_cast<V4 *>(a.forces)[i] = fo;
+			reinterpret_cast<V4 *>(a.torques)[i] = to;
 		}
 	}
-	if(FUSE_KICK) step_epilogue(a.th, step, thermo_now && a.th.thermostat == 2, kin);
 }
 
 // lanes per nucleotide in the non-bonded kernel
@@ -692,29 +571,26 @@ int nonbonded_blocks(int N) {
 	return (int) ((threads + 127) / 128);
 }
 
-template <typename R, class Loader, bool SPLIT, bool FUSE>
+template <typename R, class Loader, bool SPLIT>
 static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEvent_t wait) {
 	const int tpb = 128;
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	k_bonded_split<R, Loader, SPLIT><<<blocks, tpb, 0, s>>>(a, ld);
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
-	k_nonbonded_split<R, Loader, SPLIT, FUSE, K><<<nonbonded_blocks(a.N), tpb, 0, s>>>(a, ld);
+	k_nonbonded_split<R, Loader, SPLIT, K><<<nonbonded_blocks(a.N), tpb, 0, s>>>(a, ld);
 }
 
-cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s, cudaEvent_t wait) {
-	if(split && fuse_kick) return cudaErrorInvalidValue;  // the energy split is for force-only calls
+cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, cudaStream_t s, cudaEvent_t wait) {
 	if(dbl) {
 		SplitDouble ld{a.posd, a.quatd, a.pos_hi, a.pos_lo, a.bonds};
-		if(split) launch_split_t<double, SplitDouble, true, false>(a, ld, s, wait);
-		else if(fuse_kick) launch_split_t<double, SplitDouble, false, true>(a, ld, s, wait);
-		else launch_split_t<double, SplitDouble, false, false>(a, ld, s, wait);
+		if(split) launch_split_t<double, SplitDouble, true>(a, ld, s, wait);
+		else launch_split_t<double, SplitDouble, false>(a, ld, s, wait);
 	}
 	else {
 		SplitMixed ld{a.pos_hi, a.pos_lo, a.fa1, a.fa3, a.fback};
-		if(split) launch_split_t<float, SplitMixed, true, false>(a, ld, s, wait);
-		else if(fuse_kick) launch_split_t<float, SplitMixed, false, true>(a, ld, s, wait);
-		else launch_split_t<float, SplitMixed, false, false>(a, ld, s, wait);
+		if(split) launch_split_t<float, SplitMixed, true>(a, ld, s, wait);
+		else launch_split_t<float, SplitMixed, false>(a, ld, s, wait);
 	}
 	return cudaGetLastError();
 }

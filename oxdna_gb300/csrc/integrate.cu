@@ -9,10 +9,11 @@
 // random numbers come from a counter-based Philox-4x32-10 stream keyed by (seed, step,
 // particle) so that runs are reproducible and graph-replayable, and the Bussi kinetic-energy
 // update runs on the device (its gamma deviate uses the same algorithm as the reference).
-// The second half kick, both thermostats and the step counter are fused into the epilogue of
-// the non-bonded force kernel (forces.cu); a Bussi rescaling is applied by the next first step
-// (or by launch_bussi_flush at the end of a run), and the Bussi draws of a step are made by
-// k_bussi_noise on a parallel branch of the step graph.
+// The second half kick of a step and its thermostat are deferred to the next first step (or
+// to the flush at the end of a run), where they run one thread per nucleotide next to the
+// first half kick; the Bussi sums run after the forces (k_bussi_reduce) and its draws on a
+// parallel branch of the step graph (k_bussi_noise).  No FP64 work is left in the force
+// kernels, whose lanes are mostly idle at the epilogue.
 #include "thermo.cuh"
 
 namespace oxgb {
@@ -67,16 +68,34 @@ __global__ void k_make_mirrors(StepArgs a) {
 
 // ---------------------------------------------------------------- first half step
 
+__device__ __forceinline__ long long step_of(const ThermoArgs &t) { return *t.step_base + t.step_offset; }
+
+// completes step sp of nucleotide i: its second half kick (CUDA_mixed.cuh:71-93) and its
+// thermostat (Brownian redraw or Bussi rescaling)
+template <typename V4>
+__device__ __forceinline__ void complete_step(const ThermoArgs &t, int i, long long sp, const V4 &F, const V4 &T,
+		double4_32a &v, double4_32a &L) {
+	const double hdt = 0.5 * t.dt;
+	v.x += (double) F.x * hdt;
+	v.y += (double) F.y * hdt;
+	v.z += (double) F.z * hdt;
+	L.x += (double) T.x * hdt;
+	L.y += (double) T.y * hdt;
+	L.z += (double) T.z * hdt;
+	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) brownian_redraw(t, i, sp, v, L);
+	else if(t.thermostat == 2 && *t.bussi_stamp == sp) bussi_rescale(t, v, L);
+}
+
 template <typename V4>
 __global__ void k_first_step(StepArgs a) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= a.N) return;
+	const long long s = step_of(a.th);
 	const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
 	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 	const double hdt = 0.5 * a.dt;
 	double4_32a v = a.vel[i], r = a.pos[i], L = a.angmom[i], q = a.quat[i];
-	// the Bussi rescaling decided at the end of the previous step
-	if(a.th.thermostat == 2 && *a.th.bussi_stamp == *a.th.step - 1) bussi_rescale(a.th, v, L);
+	if(*a.th.open_step == s - 1) complete_step(a.th, i, s - 1, F, T, v, L);
 	v.x += (double) F.x * hdt;
 	v.y += (double) F.y * hdt;
 	v.z += (double) F.z * hdt;
@@ -128,7 +147,7 @@ __global__ void k_first_step(StepArgs a) {
 
 // the Bussi draws of the current step: warp 0 translational (channel 0), warp 1 rotational
 __global__ void k_bussi_noise(StepArgs a) {
-	const long long s = *a.th.step;
+	const long long s = step_of(a.th);
 	if(s % a.th.newtonian_steps != 0 || (threadIdx.x & 31) != 0) return;
 	const int w = threadIdx.x >> 5;
 	if(w > 1) return;
@@ -140,19 +159,98 @@ __global__ void k_bussi_noise(StepArgs a) {
 	a.th.bussi_state[9 + 2 * w] = rr;
 }
 
-// applies a pending rescaling (made at the step before the current one) ...
-__global__ void k_bussi_flush_apply(StepArgs a) {
+// Bussi step s, after its forces: sums of v, |v|^2 and |L|^2 over the completed velocities
+// v + dt/2 F (computed here, stored by the next first step), per block; the last block to
+// finish reduces the block sums in a fixed order (deterministic) and makes the update
+template <typename V4>
+__global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
+	const long long s = step_of(a.th);
+	if(s % a.th.newtonian_steps != 0) return;
+	const double hdt = 0.5 * a.dt;
+	double acc[5] = {0, 0, 0, 0, 0};
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
+		const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
+		double4_32a v = a.vel[i], L = a.angmom[i];
+		v.x += (double) F.x * hdt;
+		v.y += (double) F.y * hdt;
+		v.z += (double) F.z * hdt;
+		L.x += (double) T.x * hdt;
+		L.y += (double) T.y * hdt;
+		L.z += (double) T.z * hdt;
+		acc[0] += v.x;
+		acc[1] += v.y;
+		acc[2] += v.z;
+		acc[3] += v.x * v.x + v.y * v.y + v.z * v.z;
+		acc[4] += L.x * L.x + L.y * L.y + L.z * L.z;
+	}
+	__shared__ double red[5][8];
+	__shared__ bool last;
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+	for(int k = 0; k < 5; k++) {
+		double x = acc[k];
+		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+		if(lane == 0) red[k][w] = x;
+	}
+	__syncthreads();
+	if(threadIdx.x < 5) {
+		double x = 0;
+		for(int u = 0; u < nw; u++) x += red[threadIdx.x][u];
+		a.th.bussi_partials[blockIdx.x * 8 + threadIdx.x] = x;
+		__threadfence();
+	}
+	__syncthreads();
+	if(threadIdx.x == 0) last = atomicAdd(a.th.done, 1u) == gridDim.x - 1;
+	__syncthreads();
+	if(!last) return;
+	__threadfence();
+	double part[5] = {0, 0, 0, 0, 0};
+	for(int b = threadIdx.x; b < (int) gridDim.x; b += blockDim.x)
+#pragma unroll
+		for(int k = 0; k < 5; k++) part[k] += __ldcg(a.th.bussi_partials + b * 8 + k);
+#pragma unroll
+	for(int k = 0; k < 5; k++) {
+		double x = part[k];
+		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+		if(lane == 0) red[k][w] = x;
+	}
+	__syncthreads();
+	if(threadIdx.x != 0) return;
+	double sum[5];
+	for(int k = 0; k < 5; k++) {
+		double x = 0;
+		for(int u = 0; u < nw; u++) x += red[k][u];
+		sum[k] = x;
+	}
+	bussi_update(a.th, s, sum);
+	*a.th.done = 0;
+}
+
+__global__ void k_step_advance(StepArgs a, int K) {
+	if(threadIdx.x == 0 && blockIdx.x == 0) *a.th.step_base += K;
+}
+
+// end of a run: the last step's second half kick and thermostat ...
+template <typename V4>
+__global__ void k_step_flush(StepArgs a) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i >= a.N || *a.th.bussi_stamp != *a.th.step - 1) return;
+	const long long sp = *a.th.step_base - 1;
+	if(i >= a.N || *a.th.open_step != sp) return;
+	const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
+	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 	double4_32a v = a.vel[i], L = a.angmom[i];
-	bussi_rescale(a.th, v, L);
+	complete_step(a.th, i, sp, F, T, v, L);
 	a.vel[i] = v;
 	a.angmom[i] = L;
 }
 
-// ... and marks it applied
-__global__ void k_bussi_flush_clear(StepArgs a) {
-	if(threadIdx.x == 0 && blockIdx.x == 0) *a.th.bussi_stamp = -1;
+// ... after which nothing is pending
+__global__ void k_step_flush_clear(StepArgs a) {
+	if(threadIdx.x == 0 && blockIdx.x == 0) {
+		*a.th.open_step = OXGB_NO_STEP;
+		*a.th.bussi_stamp = OXGB_NO_STEP;
+	}
 }
 
 __global__ void k_set_conditional(const int *flag, cudaGraphConditionalHandle h) {
@@ -182,9 +280,21 @@ cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
 	return cudaGetLastError();
 }
 
-cudaError_t launch_bussi_flush(const StepArgs &a, cudaStream_t s) {
-	k_bussi_flush_apply<<<blocks_for(a.N, 256), 256, 0, s>>>(a);
-	k_bussi_flush_clear<<<1, 32, 0, s>>>(a);
+cudaError_t launch_bussi_reduce(const StepArgs &a, bool double_forces, cudaStream_t s) {
+	if(double_forces) k_bussi_reduce<double4_32a><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	else k_bussi_reduce<float4><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_step_advance(const StepArgs &a, int K, cudaStream_t s) {
+	k_step_advance<<<1, 32, 0, s>>>(a, K);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_step_flush(const StepArgs &a, bool double_forces, cudaStream_t s) {
+	if(double_forces) k_step_flush<double4_32a><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	else k_step_flush<float4><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	k_step_flush_clear<<<1, 32, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

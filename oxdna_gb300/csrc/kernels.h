@@ -13,21 +13,31 @@
 
 namespace oxgb {
 
-// thermostat state shared by the integrator and the fused force epilogue
+// Thermostat and step bookkeeping of the MD engine.  The step number of a kernel is
+// *step_base + step_offset: a graph of K steps bakes offsets 0..K-1 and advances the base by K
+// at its end, so no kernel of a step changes the number the others read.  Velocity Verlet
+// runs with a deferred second half kick: the forces of step s are computed at the end of step
+// s, and the next first step (or the flush at the end of a run) completes v(s+1) = v + dt/2 F,
+// applies the thermostat of step s to it, then makes its own half kick and drift.
+#define OXGB_NO_STEP (-4611686018427387904LL)  // "no step" mark of open_step / bussi_stamp
+
 struct ThermoArgs {
 	int N;                                 // nucleotides of the system
 	int thermostat;                        // 0 none, 1 brownian, 2 bussi
 	int newtonian_steps;
+	double dt;
 	double pt, pr, sqrtT, T;
 	unsigned long long seed;
 	double bussi_c;                        // exp(-newtonian_steps / tau)
 	double *bussi_partials;                // [blocks * 8] per-block sums of v, |v|^2, |L|^2
 	double *bussi_state;                   // [16]: K_t, K_r, factor_t, factor_r, vcom x y z, -,
 	                                       // then the step's draws: sum_t, rr_t, sum_r, rr_r
-	long long *bussi_stamp;                // step of the last Bussi update (its rescaling is
-	                                       // applied by the next first step); -1 when none pends
-	unsigned *done;                        // blocks of the fused epilogue finished (0 between steps)
-	long long *step;                       // device step counter
+	long long *bussi_stamp;                // step of the last Bussi update (-1: none pending)
+	long long *open_step;                  // step whose second half kick is pending (-1: none);
+	                                       // null in force-only calls
+	unsigned *done;                        // blocks of the Bussi reduction finished (0 between steps)
+	long long *step_base;                  // device step counter of the current graph
+	int step_offset;
 };
 
 struct ForceArgs {
@@ -52,19 +62,15 @@ struct ForceArgs {
 	const int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
 	int ev_cap, base_cap, stk_cap;            // capacities (an overflowed list is read up to them)
 	void *bond_f, *bond_tp, *bond_tq;         // per bond owner p (q = n3[p]): f on q with w = energy, torques
-	// fused step epilogue (engine layout, fuse_kick): thermostat of the step, step counter
+	// MD-step bookkeeping (engine layout): the bonded kernel marks the step's half kick pending
 	ThermoArgs th;
 };
 
-cudaError_t launch_forces_mixed(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s);
-cudaError_t launch_forces_double(const ForceArgs &a, bool split, bool fuse_kick, cudaStream_t s);
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
 // split path: bonded pairs (one thread per bond, both sides), then non-bonded terms (one
 // thread per nucleotide, one loop per term list) with the bonded results gathered in its epilogue
-// fuse_kick: the step epilogue of the MD engine (second half kick, thermostat, step counter);
-// wait: an event the non-bonded kernel waits for (the Bussi draws), or null
-cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool fuse_kick, cudaStream_t s,
-		cudaEvent_t wait = nullptr);
+// wait: an event the non-bonded kernel waits for, or null
+cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, cudaStream_t s, cudaEvent_t wait = nullptr);
 // blocks of the split non-bonded kernel for N nucleotides (sizes ThermoArgs::bussi_partials)
 int nonbonded_blocks(int N);
 
@@ -121,12 +127,17 @@ struct StepArgs {
 	ThermoArgs th;
 };
 
+// first half of an MD step: completes a pending half kick and the previous step's thermostat,
+// then half kick, drift, rotation, FP32 mirrors and the list-staleness flag
 cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s);
 // the Bussi draws of the current step (they do not depend on the state: run beside the step)
 cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s);
-// applies a pending Bussi rescaling to the state and clears it (end of a run)
-cudaError_t launch_bussi_flush(const StepArgs &a, cudaStream_t s);
-// sets the graph conditional to (*flag != 0)
+// Bussi kinetic-energy sums over the completed velocities and the update (after the forces)
+cudaError_t launch_bussi_reduce(const StepArgs &a, bool double_forces, cudaStream_t s);
+// end of a graph of K steps: the step base advances by K
+cudaError_t launch_step_advance(const StepArgs &a, int K, cudaStream_t s);
+// end of a run: completes the pending half kick and thermostat so the state is whole
+cudaError_t launch_step_flush(const StepArgs &a, bool double_forces, cudaStream_t s);
 cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h, cudaStream_t s);
 // refresh the FP32 mirrors from the FP64 state (after a host upload)
 cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s);
