@@ -118,6 +118,24 @@ int oxgb_verlet_create(int N, double box, double rcut, double skin, int cells_au
  * oxgb_verlet_status after the stream is synchronised.
  */
 int oxgb_verlet_update(oxgb_verlet *h, const void *d_poss, void *d_list_poss, const void *d_bonds, void *stream);
+/*
+ * No counterpart in the reference.  The same list build as oxgb_verlet_update into caller-owned
+ * d_matrix_neighs (column-major, int[max_neigh * N]), d_number_neighs (int[N]) and
+ * d_list_poss, with no device allocation at all: the scratch (cells, segments, scan tiles,
+ * status) is a fixed static device array of the library, so the call never runs
+ * cudaMalloc/cudaFree (which synchronise the device and can fail under a caching allocator
+ * that holds the free memory), and needs no handle with a lifetime.  Limits: N <=
+ * OXGB_NOALLOC_MAX_N and at most OXGB_NOALLOC_MAX_CELLS cells; larger requests return
+ * OXGB_E_INVALID before any launch.  The scratch is shared by all calls on a device: calls
+ * that overlap in time race and must be serialised by the caller.  The first call on a device
+ * looks the scratch up (and may load the module), so it should precede any stream capture.
+ * Synchronises `stream` to read the status: OXGB_E_NEIGH_OVERFLOW if a row exceeded max_neigh.
+ */
+#define OXGB_NOALLOC_MAX_N 65536
+#define OXGB_NOALLOC_MAX_CELLS 32768
+int oxgb_verlet_build_noalloc(int N, double box, double rcut, double skin, int cells_auto_optimisation,
+		const void *d_poss, void *d_list_poss, const void *d_bonds, int *d_matrix_neighs, int *d_number_neighs,
+		int max_neigh, void *stream);
 /* device pointers of the neighbour rows (int[N * max_neigh]) and counts (int[N]) */
 int oxgb_verlet_buffers(oxgb_verlet *h, int **d_matrix_neighs, int **d_number_neighs, int *max_neigh, int *n_cells_side);
 int oxgb_verlet_status(oxgb_verlet *h);

@@ -18,6 +18,9 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "FENE bond broken", 4: "nei
           5: "non-finite coordinates", 6: "out of device memory"}
 
 THERMOSTATS = {"no": 0, "none": 0, "john": 1, "brownian": 1, "bussi": 2}
+# limits of oxgb_verlet_build_noalloc (OXGB_NOALLOC_MAX_N / OXGB_NOALLOC_MAX_CELLS in oxgb.h)
+NOALLOC_MAX_N = 65536
+NOALLOC_MAX_CELLS = 32768
 
 
 class OxgbError(RuntimeError):
@@ -64,6 +67,8 @@ SIGNATURES = {
     "oxgb_dna2_destroy": (C.c_int, [_VP]),
     "oxgb_verlet_create": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.POINTER(_VP)]),
     "oxgb_verlet_update": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "oxgb_verlet_build_noalloc": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, _VP, _VP, _VP, _VP, _VP,
+                                            C.c_int, _VP]),
     "oxgb_verlet_buffers": (C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "oxgb_verlet_status": (C.c_int, [_VP]),
     "oxgb_verlet_destroy": (C.c_int, [_VP]),

@@ -71,6 +71,13 @@ static std::string status_message(int st) {
 	return m;
 }
 
+// error plumbing for the other translation units of the library
+namespace oxgb {
+int set_error(int code, const std::string &msg) { return fail(code, msg); }
+int list_status_code(int st) { return status_to_code(st); }
+std::string list_status_message(int st) { return status_message(st); }
+}  // namespace oxgb
+
 // ====================================================================== interaction layer
 
 struct oxgb_dna2 {

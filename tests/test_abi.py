@@ -38,3 +38,12 @@ def test_version_and_defaults_need_no_gpu():
     assert s.average == 1 and s.dh_half_charged_ends == 1 and abs(s.dh_lambda - 0.3616455) < 1e-12
     m = ox.md_settings(thermostat="bussi")
     assert m.thermostat == 2 and m.steps_per_graph == 16
+
+
+def test_noalloc_limits_match_header():
+    import re
+
+    from oxdna_gb300 import _abi
+    text = open(HEADER).read()
+    assert int(re.search(r"#define OXGB_NOALLOC_MAX_N (\d+)", text).group(1)) == _abi.NOALLOC_MAX_N
+    assert int(re.search(r"#define OXGB_NOALLOC_MAX_CELLS (\d+)", text).group(1)) == _abi.NOALLOC_MAX_CELLS
