@@ -557,7 +557,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->esplit, sizeof(double) * 8 * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->scratch, sizeof(double) * 8 * n_systems) == cudaSuccess;
-	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * nonbonded_blocks(N)) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * ((N + 63) / 64 + 1)) == cudaSuccess;  // blocks of 64
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->open_step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16) == cudaSuccess;

@@ -454,8 +454,13 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 
 // K lanes per nucleotide: lane l of a group takes entries l, l + K, ... of every term list, so a
 // warp holds 32 / K nucleotides and all its lanes run the same term loop
+// minimum resident blocks per SM asked of the register allocator for the non-bonded kernel
+#ifndef OXGB_NB_MINB
+#define OXGB_NB_MINB 6
+#endif
+
 template <typename R, class Loader, bool SPLIT, int K>
-__global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld) {
+__global__ void __launch_bounds__(128, OXGB_NB_MINB) k_nonbonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	__shared__ DNA2Table<R> P;
 	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
@@ -563,7 +568,7 @@ __global__ void __launch_bounds__(128) k_nonbonded_split(ForceArgs a, Loader ld)
 
 // lanes per nucleotide in the non-bonded kernel
 #ifndef OXGB_NB_LANES
-#define OXGB_NB_LANES 4
+#define OXGB_NB_LANES 8
 #endif
 
 int nonbonded_blocks(int N) {

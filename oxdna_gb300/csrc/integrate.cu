@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 	}
 	__shared__ double red[5][8];
 	__shared__ bool last;
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
 	for(int k = 0; k < 5; k++) {
 		double x = acc[k];
@@ -216,15 +216,16 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 		if(lane == 0) red[k][w] = x;
 	}
 	__syncthreads();
-	if(threadIdx.x != 0) return;
+	// translation on thread 0, rotation on thread 32 (another warp: the two chains overlap)
+	if(threadIdx.x != 0 && threadIdx.x != 32) return;
 	double sum[5];
 	for(int k = 0; k < 5; k++) {
 		double x = 0;
 		for(int u = 0; u < nw; u++) x += red[k][u];
 		sum[k] = x;
 	}
-	bussi_update(a.th, s, sum);
-	*a.th.done = 0;
+	bussi_update(a.th, s, threadIdx.x == 0 ? 0 : 1, sum);
+	if(threadIdx.x == 0) *a.th.done = 0;
 }
 
 __global__ void k_step_advance(StepArgs a, int K) {
@@ -270,8 +271,9 @@ __global__ void k_kinetic(StepArgs a, double *out) {
 static inline int blocks_for(int N, int tpb) { return N > 0 ? (N + tpb - 1) / tpb : 1; }
 
 cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s) {
-	if(double_forces) k_first_step<double4_32a><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
-	else k_first_step<float4><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	// small blocks: the FP64 work (1/64 of the FP32 rate) spreads evenly over the SMs
+	if(double_forces) k_first_step<double4_32a><<<blocks_for(a.N, 64), 64, 0, s>>>(a);
+	else k_first_step<float4><<<blocks_for(a.N, 64), 64, 0, s>>>(a);
 	return cudaGetLastError();
 }
 
@@ -281,8 +283,8 @@ cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_bussi_reduce(const StepArgs &a, bool double_forces, cudaStream_t s) {
-	if(double_forces) k_bussi_reduce<double4_32a><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
-	else k_bussi_reduce<float4><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	if(double_forces) k_bussi_reduce<double4_32a><<<blocks_for(a.N, 64), 64, 0, s>>>(a);
+	else k_bussi_reduce<float4><<<blocks_for(a.N, 64), 64, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

@@ -71,7 +71,7 @@ cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
 // thread per nucleotide, one loop per term list) with the bonded results gathered in its epilogue
 // wait: an event the non-bonded kernel waits for, or null
 cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, cudaStream_t s, cudaEvent_t wait = nullptr);
-// blocks of the split non-bonded kernel for N nucleotides (sizes ThermoArgs::bussi_partials)
+// blocks of the split non-bonded kernel for N nucleotides
 int nonbonded_blocks(int N);
 
 struct ListArgs {

@@ -1,5 +1,4 @@
-// Random streams and thermostat arithmetic shared by the integrator kernels (integrate.cu)
-// and the thermostat epilogue of the fused force kernel (forces.cu).
+// Random streams and thermostat arithmetic of the integrator kernels (integrate.cu).
 //
 // Random numbers come from a counter-based Philox-4x32-10 stream keyed by (seed, step,
 // particle), so runs are reproducible and graph-replayable; the oracle (oracle/dna2_oracle.c,
@@ -145,22 +144,27 @@ static __device__ __noinline__ void brownian_redraw(const ThermoArgs &t, int i, 
 	if(u01(o0[1]) < t.pr) L = make_double4_32a(g[3] * t.sqrtT, g[4] * t.sqrtT, g[5] * t.sqrtT, 0.0);
 }
 
-// Bussi: from the sums of v, |v|^2 and |L|^2 over the system, the new running kinetic energies
-// (with the draws of this step) and the rescaling factors; one thread
-static __device__ void bussi_update(const ThermoArgs &t, long long s, const double sum[5]) {
+// Bussi: from the sums of v, |v|^2 and |L|^2 over the system, the new running kinetic energy
+// (with the draws of this step) and the rescaling factor of one kind of motion: which = 0
+// translation (about the centre-of-mass velocity), 1 rotation.  The two run on two threads.
+static __device__ void bussi_update(const ThermoArgs &t, long long s, int which, const double sum[5]) {
 	const double N = t.N;
-	const double vc[3] = {sum[0] / N, sum[1] / N, sum[2] / N};
-	const double Kt_now = 0.5 * (sum[3] - N * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
-	const double Kr_now = 0.5 * sum[4];
 	double *st = t.bussi_state;
-	update_K(st[0], 3 * (t.N - 1), t.T, t.bussi_c, __ldcg(st + 8), __ldcg(st + 9));
-	update_K(st[1], 3 * t.N, t.T, t.bussi_c, __ldcg(st + 10), __ldcg(st + 11));
-	st[2] = sqrt(st[0] / Kt_now);
-	st[3] = sqrt(st[1] / Kr_now);
-	st[4] = vc[0];
-	st[5] = vc[1];
-	st[6] = vc[2];
-	*t.bussi_stamp = s;
+	if(which == 0) {
+		const double vc[3] = {sum[0] / N, sum[1] / N, sum[2] / N};
+		const double Kt_now = 0.5 * (sum[3] - N * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
+		update_K(st[0], 3 * (t.N - 1), t.T, t.bussi_c, __ldcg(st + 8), __ldcg(st + 9));
+		st[2] = sqrt(st[0] / Kt_now);
+		st[4] = vc[0];
+		st[5] = vc[1];
+		st[6] = vc[2];
+		*t.bussi_stamp = s;
+	}
+	else {
+		const double Kr_now = 0.5 * sum[4];
+		update_K(st[1], 3 * t.N, t.T, t.bussi_c, __ldcg(st + 10), __ldcg(st + 11));
+		st[3] = sqrt(st[1] / Kr_now);
+	}
 }
 
 // the rescaling of a Bussi update made at step s, applied to one nucleotide
