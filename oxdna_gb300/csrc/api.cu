@@ -392,7 +392,11 @@ static ThermoArgs thermo_args(oxgb_md *h, int step_offset = 0, bool engine_step 
 	t.T = h->dna[0].T;
 	t.sqrtT = std::sqrt(h->dna[0].T);
 	t.seed = h->md.seed;
-	t.bussi_c = std::exp(-(double) t.newtonian_steps / h->md.bussi_tau);
+	const double c = std::exp(-(double) t.newtonian_steps / h->md.bussi_tau);
+	t.bussi_1mc = 1.0 - c;
+	t.bussi_a = (1.0 - c) * t.T * 0.5;
+	t.bussi_b = std::sqrt(2.0 * t.T * (1.0 - c) * c);
+	t.inv_N = 1.0 / h->N;
 	t.bussi_partials = h->bussi_partials;
 	t.bussi_state = h->bussi_state;
 	t.bussi_stamp = h->bussi_stamp;

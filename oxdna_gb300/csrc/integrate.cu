@@ -95,24 +95,37 @@ __global__ void k_first_step(StepArgs a) {
 	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 	const double hdt = 0.5 * a.dt;
 	double4_32a v = a.vel[i], r = a.pos[i], L = a.angmom[i], q = a.quat[i];
-	if(*a.th.open_step == s - 1) complete_step(a.th, i, s - 1, F, T, v, L);
-	v.x += (double) F.x * hdt;
-	v.y += (double) F.y * hdt;
-	v.z += (double) F.z * hdt;
+	const long long sp = s - 1;
+	const bool open = *a.th.open_step == sp;
+	const bool acted = open && ((a.th.thermostat == 1 && sp % a.th.newtonian_steps == 0) ||
+								(a.th.thermostat == 2 && *a.th.bussi_stamp == sp));
+	// with no thermostat in between, the previous step's second half kick and this step's first
+	// one are a single kick by dt
+	const double kick = (open && !acted) ? a.dt : hdt;
+	if(acted) complete_step(a.th, i, sp, F, T, v, L);
+	v.x += (double) F.x * kick;
+	v.y += (double) F.y * kick;
+	v.z += (double) F.z * kick;
 	r.x += v.x * a.dt;
 	r.y += v.y * a.dt;
 	r.z += v.z * a.dt;
-	L.x += (double) T.x * hdt;
-	L.y += (double) T.y * hdt;
-	L.z += (double) T.z * hdt;
+	L.x += (double) T.x * kick;
+	L.y += (double) T.y * kick;
+	L.z += (double) T.z * kick;
 	// rotation by dt|L| about L (body frame): q <- q * (sin(th/2) L^, cos(th/2))
 	const double L2 = L.x * L.x + L.y * L.y + L.z * L.z;
 	if(L2 > 0.0) {
 		const double hd = 0.5 * a.dt, x2 = hd * hd * L2;  // x = th / 2
 		double k, ch;
-		if(x2 < 1e-2) {
-			// sin(x) / x and cos(x) as Taylor series in x^2 (truncation below 1e-20 for |x| < 0.1):
-			// no square root, range reduction or division, which are slow in FP64
+		if(x2 < 1e-5) {
+			// sin(x) / x and cos(x) as Taylor series in x^2: no square root, range reduction or
+			// division, which are slow in FP64.  The first omitted terms, x^6/5040 and x^8/40320,
+			// are below 2e-19 for x^2 < 1e-5 (a typical step has x^2 ~ 1e-6)
+			k = hd * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0)));
+			ch = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0)));
+		}
+		else if(x2 < 1e-2) {
+			// the same series to x^10 (truncation below 1e-20 for |x| < 0.1)
 			k = hd * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0) * (1.0 - x2 * (1.0 / 42.0) * (1.0 - x2 * (1.0 / 72.0) * (1.0 - x2 * (1.0 / 110.0))))));
 			ch = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0) * (1.0 - x2 * (1.0 / 56.0) * (1.0 - x2 * (1.0 / 90.0)))));
 		}
@@ -283,8 +296,8 @@ cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_bussi_reduce(const StepArgs &a, bool double_forces, cudaStream_t s) {
-	if(double_forces) k_bussi_reduce<double4_32a><<<blocks_for(a.N, 64), 64, 0, s>>>(a);
-	else k_bussi_reduce<float4><<<blocks_for(a.N, 64), 64, 0, s>>>(a);
+	if(double_forces) k_bussi_reduce<double4_32a><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	else k_bussi_reduce<float4><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

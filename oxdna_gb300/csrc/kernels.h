@@ -28,7 +28,9 @@ struct ThermoArgs {
 	double dt;
 	double pt, pr, sqrtT, T;
 	unsigned long long seed;
-	double bussi_c;                        // exp(-newtonian_steps / tau)
+	double bussi_1mc, bussi_a, bussi_b;    // with c = exp(-newtonian_steps / tau): 1 - c,
+	                                       // (1 - c) T / 2 and sqrt(2 T (1 - c) c)
+	double inv_N;
 	double *bussi_partials;                // [blocks * 8] per-block sums of v, |v|^2, |L|^2
 	double *bussi_state;                   // [16]: K_t, K_r, factor_t, factor_r, vcom x y z, -,
 	                                       // then the step's draws: sum_t, rr_t, sum_r, rr_r

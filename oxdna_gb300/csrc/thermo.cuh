@@ -121,10 +121,11 @@ static __device__ void bussi_draws(Stream &st, int dof, double &sum, double &rr)
 	sum = sum_noises(st, dof - 1);
 }
 
-static __device__ void update_K(double &K, int dof, double T, double c, double sum, double rr) {
-	const double Kt = 0.5 * dof * T;
-	const double dK = (1.0 - c) * (Kt * (sum + rr * rr) / dof - K) + 2.0 * rr * sqrt(K * Kt / dof * (1.0 - c) * c);
-	K += dK;
+// K <- K + (1 - c) (K_target (sum + rr^2) / dof - K) + 2 rr sqrt(K K_target / dof (1 - c) c) with
+// K_target = dof T / 2 (BussiThermostat::_update_K), written with the host-side constants
+// a = (1 - c) T / 2 and b = sqrt(2 T (1 - c) c), so that the device chain is short
+static __device__ __forceinline__ void update_K(double &K, double one_minus_c, double a, double b, double sum, double rr) {
+	K += a * (sum + rr * rr) - one_minus_c * K + b * rr * sqrt(K);
 }
 
 // Brownian ("john") thermostat: every newtonian_steps steps each nucleotide redraws its
@@ -148,13 +149,12 @@ static __device__ __noinline__ void brownian_redraw(const ThermoArgs &t, int i, 
 // (with the draws of this step) and the rescaling factor of one kind of motion: which = 0
 // translation (about the centre-of-mass velocity), 1 rotation.  The two run on two threads.
 static __device__ void bussi_update(const ThermoArgs &t, long long s, int which, const double sum[5]) {
-	const double N = t.N;
 	double *st = t.bussi_state;
 	if(which == 0) {
-		const double vc[3] = {sum[0] / N, sum[1] / N, sum[2] / N};
-		const double Kt_now = 0.5 * (sum[3] - N * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
-		update_K(st[0], 3 * (t.N - 1), t.T, t.bussi_c, __ldcg(st + 8), __ldcg(st + 9));
-		st[2] = sqrt(st[0] / Kt_now);
+		const double vc[3] = {sum[0] * t.inv_N, sum[1] * t.inv_N, sum[2] * t.inv_N};
+		const double Kt_now = 0.5 * (sum[3] - (double) t.N * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
+		update_K(st[0], t.bussi_1mc, t.bussi_a, t.bussi_b, __ldcg(st + 8), __ldcg(st + 9));
+		st[2] = sqrt(st[0]) * rsqrt(Kt_now);
 		st[4] = vc[0];
 		st[5] = vc[1];
 		st[6] = vc[2];
@@ -162,8 +162,8 @@ static __device__ void bussi_update(const ThermoArgs &t, long long s, int which,
 	}
 	else {
 		const double Kr_now = 0.5 * sum[4];
-		update_K(st[1], 3 * t.N, t.T, t.bussi_c, __ldcg(st + 10), __ldcg(st + 11));
-		st[3] = sqrt(st[1] / Kr_now);
+		update_K(st[1], t.bussi_1mc, t.bussi_a, t.bussi_b, __ldcg(st + 10), __ldcg(st + 11));
+		st[3] = sqrt(st[1]) * rsqrt(Kr_now);
 	}
 }
 
