@@ -95,23 +95,18 @@ __global__ void k_first_step(StepArgs a) {
 	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 	const double hdt = 0.5 * a.dt;
 	double4_32a v = a.vel[i], r = a.pos[i], L = a.angmom[i], q = a.quat[i];
-	const long long sp = s - 1;
-	const bool open = *a.th.open_step == sp;
-	const bool acted = open && ((a.th.thermostat == 1 && sp % a.th.newtonian_steps == 0) ||
-								(a.th.thermostat == 2 && *a.th.bussi_stamp == sp));
-	// with no thermostat in between, the previous step's second half kick and this step's first
-	// one are a single kick by dt
-	const double kick = (open && !acted) ? a.dt : hdt;
-	if(acted) complete_step(a.th, i, sp, F, T, v, L);
-	v.x += (double) F.x * kick;
-	v.y += (double) F.y * kick;
-	v.z += (double) F.z * kick;
+	// the previous step's second half kick and thermostat (kept as a separate half kick, so that
+	// a state is the same whether or not a run ended at that step)
+	if(*a.th.open_step == s - 1) complete_step(a.th, i, s - 1, F, T, v, L);
+	v.x += (double) F.x * hdt;
+	v.y += (double) F.y * hdt;
+	v.z += (double) F.z * hdt;
 	r.x += v.x * a.dt;
 	r.y += v.y * a.dt;
 	r.z += v.z * a.dt;
-	L.x += (double) T.x * kick;
-	L.y += (double) T.y * kick;
-	L.z += (double) T.z * kick;
+	L.x += (double) T.x * hdt;
+	L.y += (double) T.y * hdt;
+	L.z += (double) T.z * hdt;
 	// rotation by dt|L| about L (body frame): q <- q * (sin(th/2) L^, cos(th/2))
 	const double L2 = L.x * L.x + L.y * L.y + L.z * L.z;
 	if(L2 > 0.0) {
