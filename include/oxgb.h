@@ -173,8 +173,12 @@ void oxgb_md_default_settings(oxgb_md_settings *s);
 /*
  * A batch of n_systems independent systems in one engine (n_systems = 1 for a plain run).
  * offsets[n_systems + 1] partitions the N = offsets[n_systems] nucleotides; system k has its own
- * cubic box box[k] and model settings dna[k] (temperature, salt, ...).  Allocates device memory
- * on the current device.  MD_CUDABackend::get_settings + init (MD_CUDABackend.cu:621-755).
+ * cubic box box[k] and model settings dna[k] (temperature, salt, ...), hence its own cutoff,
+ * cell grid, Verlet lists and thermostat, and its random stream uses the seed md->seed + k
+ * (keyed by the index within the system, so a system evolves exactly as it would alone).  All
+ * systems step together in the same kernels and graphs.  Bonds may not cross systems.
+ * Allocates device memory on the current device.  MD_CUDABackend::get_settings + init
+ * (MD_CUDABackend.cu:621-755).
  */
 int oxgb_md_create(int n_systems, const int *offsets, const double *box, const oxgb_dna2_settings *dna,
 		const oxgb_md_settings *md, oxgb_md **out);
@@ -203,7 +207,9 @@ int oxgb_md_get_forces(oxgb_md *h, double *F, double *T, double *E);
 /* per-system potential energy (FP64 sum of the per-nucleotide energies / 2) and the
  * translational and rotational kinetic energies, each double[n_systems] */
 int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r);
-/* new temperature of system k (parameter tables and thermostat) -- the replica-exchange hook */
+/* new temperature of system k (parameter table, cutoff, thermostat; the Bussi running kinetic
+ * energies scale with T; the lists are rebuilt) -- the replica-exchange hook.  Velocities are
+ * left to the caller (a swap usually rescales them by sqrt(T_new / T_old)). */
 int oxgb_md_set_temperature(oxgb_md *h, int k, double T);
 /* neighbour rows of the last list build: counts nnb[N], rows nb[N * max_neigh] (row-major),
  * cell index of every nucleotide cell[N]; any pointer may be NULL */

@@ -175,11 +175,12 @@ struct ListBuffers {
 	int *cell_tmp = nullptr, *scan_part = nullptr;
 	int *nb = nullptr, *nnb = nullptr;
 
-	int alloc(int N_, int n_side_, int max_nb_) {
+	// n_cells_: cells of all systems of a batch (0: one grid of n_side^3)
+	int alloc(int N_, int n_side_, int max_nb_, int n_cells_ = 0) {
 		free_all();
 		N = N_;
 		n_side = n_side_;
-		n_cells = n_side * n_side * n_side;
+		n_cells = n_cells_ > 0 ? n_cells_ : n_side * n_side * n_side;
 		max_nb = max_nb_;
 		CK(cudaMalloc(&cell_of, sizeof(int) * std::max(N, 1)));
 		CK(cudaMalloc(&cell_count, sizeof(int) * n_cells));
@@ -332,8 +333,13 @@ struct oxgb_md {
 	std::vector<oxgb_dna2_settings> dna;
 	oxgb_md_settings md{};
 	bool dbl = false;
-	double rcut = 0;
-	float rverlet = 0;
+
+	// per-system derived parameters (host copies of the device arrays below)
+	std::vector<double> rcut, par;        // interaction cutoff; SP_STRIDE thermostat values each
+	std::vector<float> rverlet;
+	std::vector<int> nside, cell0;        // cells per side, first cell (cell0[n_systems] = all cells)
+	std::vector<int> chunk_sys, chunk_first, sys_chunk0;  // Bussi / energy chunks of <= 256 nucleotides
+	int n_chunks = 0, tab_span = 1;
 
 	std::vector<int> h_n3, h_n5, h_btype, h_type;
 	bool have_topology = false, have_state = false;
@@ -343,16 +349,20 @@ struct oxgb_md {
 	float4 *list_a1 = nullptr, *list_back = nullptr;
 	int2 *bonds = nullptr;
 	void *F = nullptr, *T = nullptr, *bond_f = nullptr, *bond_tp = nullptr, *bond_tq = nullptr;
-	void *d_tab = nullptr;
+	void *d_tab = nullptr;                // one table per system
+	int *d_sys = nullptr, *d_sys_off = nullptr, *d_sys_nside = nullptr, *d_sys_cell0 = nullptr, *d_cell_sys = nullptr;
+	int *d_sys_stale = nullptr, *d_chunk_sys = nullptr, *d_chunk_first = nullptr, *d_sys_chunk0 = nullptr;
+	float *d_sys_box = nullptr, *d_sys_rv2 = nullptr;
+	double *d_sys_par = nullptr;
+	unsigned long long *d_sys_seed = nullptr;
 	ListBuffers lb;
 	TermLists tl;
 	TermRadii radii{};
 	int *status = nullptr, *flag = nullptr;
 	long long *step = nullptr;
-	double *esplit = nullptr, *scratch = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
+	double *esplit = nullptr, *sums = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
 	unsigned *bussi_done = nullptr;
 	long long *bussi_stamp = nullptr, *open_step = nullptr;
-	double pt = 0, pr = 0;
 
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -362,12 +372,23 @@ struct oxgb_md {
 	long long host_step = 0, n_rebuilds = 0;
 	unsigned long long *d_rebuilds = nullptr;
 
+	void free_layout() {
+		for(void **p : {(void **) &d_sys_nside, (void **) &d_sys_cell0, (void **) &d_cell_sys, (void **) &d_sys_box,
+					(void **) &d_sys_rv2}) {
+			if(*p) cudaFree(*p);
+			*p = nullptr;
+		}
+	}
+
 	~oxgb_md() {
 		if(gexec) cudaGraphExecDestroy(gexec);
+		free_layout();
 		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
 					(void *) fback, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, bond_f,
-					bond_tp, bond_tq, d_tab, (void *) status, (void *) flag, (void *) step, (void *) esplit, (void *) scratch,
-					(void *) bussi_partials, (void *) bussi_state, (void *) bussi_done, (void *) bussi_stamp, (void *) open_step, (void *) d_rebuilds})
+					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
+					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
+					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
+					(void *) bussi_done, (void *) bussi_stamp, (void *) open_step, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -384,26 +405,24 @@ struct oxgb_md {
 static ThermoArgs thermo_args(oxgb_md *h, int step_offset = 0, bool engine_step = false) {
 	ThermoArgs t{};
 	t.N = h->N;
-	t.dt = h->md.dt;
+	t.n_systems = h->n_systems;
 	t.thermostat = h->md.thermostat;
 	t.newtonian_steps = h->md.newtonian_steps > 0 ? h->md.newtonian_steps : 1;
-	t.pt = h->pt;
-	t.pr = h->pr;
-	t.T = h->dna[0].T;
-	t.sqrtT = std::sqrt(h->dna[0].T);
-	t.seed = h->md.seed;
-	const double c = std::exp(-(double) t.newtonian_steps / h->md.bussi_tau);
-	t.bussi_1mc = 1.0 - c;
-	t.bussi_a = (1.0 - c) * t.T * 0.5;
-	t.bussi_b = std::sqrt(2.0 * t.T * (1.0 - c) * c);
-	t.inv_N = 1.0 / h->N;
+	t.dt = h->md.dt;
+	t.sys = h->d_sys;
+	t.sys_off = h->d_sys_off;
+	t.sys_par = h->d_sys_par;
+	t.sys_seed = h->d_sys_seed;
+	t.chunk_sys = h->d_chunk_sys;
+	t.chunk_first = h->d_chunk_first;
+	t.sys_chunk0 = h->d_sys_chunk0;
 	t.bussi_partials = h->bussi_partials;
 	t.bussi_state = h->bussi_state;
-	t.bussi_stamp = h->bussi_stamp;
 	t.done = h->bussi_done;
+	t.bussi_stamp = h->bussi_stamp;
+	t.open_step = engine_step ? h->open_step : nullptr;
 	t.step_base = h->step;
 	t.step_offset = step_offset;
-	t.open_step = engine_step ? h->open_step : nullptr;
 	return t;
 }
 
@@ -428,6 +447,7 @@ static StepArgs step_args(oxgb_md *h, int step_offset = 0) {
 	a.list_back = h->list_back;
 	a.skin2 = (float) h->md.verlet_skin * (float) h->md.verlet_skin;
 	a.flag = h->flag;
+	a.sys_stale = h->d_sys_stale;
 	a.status = h->status;
 	a.th = thermo_args(h, step_offset);
 	a.th.open_step = h->open_step;
@@ -452,11 +472,10 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.forces = h->F;
 	a.torques = h->T;
 	a.table = h->d_tab;
+	a.sys = h->d_sys;
+	a.tab_span = h->tab_span;
 	a.status = h->status;
 	a.esplit = h->esplit;
-	a.dt = h->md.dt;
-	a.vel = h->veld;
-	a.angmom = h->Ld;
 	a.fback = h->fback;
 	a.ev_nb = h->tl.ev_nb;
 	a.ev_n = h->tl.ev_n;
@@ -474,29 +493,85 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	return a;
 }
 
-static int upload_tables(oxgb_md *h) {
-	DNA2Table<double> t64;
+// parameter table, cutoff and thermostat values of system k (host side)
+static int derive_system(oxgb_md *h, int k, DNA2Table<double> &t64) {
 	double rc;
-	if(build_table(h->dna[0], h->box[0], t64, rc)) return fail(OXGB_E_INVALID, "invalid interaction settings");
-	h->rcut = rc;
-	if(h->dbl) {
-		CK(cudaMemcpy(h->d_tab, &t64, sizeof(t64), cudaMemcpyHostToDevice));
-	}
-	else {
-		DNA2Table<float> t32;
-		to_float(t64, h->box[0], t32);
-		CK(cudaMemcpy(h->d_tab, &t32, sizeof(t32), cudaMemcpyHostToDevice));
-	}
+	if(build_table(h->dna[k], h->box[k], t64, rc)) return fail(OXGB_E_INVALID, "invalid interaction settings of system " + std::to_string(k));
+	h->rcut[k] = rc;
+	h->rverlet[k] = (float) rc + 2.f * (float) h->md.verlet_skin;
 	// Brownian probabilities (src/Backends/Thermostats/BrownianThermostat.cpp:43-54); dt and
 	// diff_coeff are read as floats there
-	const double T = h->dna[0].T;
+	const double T = h->dna[k].T;
 	const double dtf = (float) h->md.dt;
 	const int n = h->md.newtonian_steps > 0 ? h->md.newtonian_steps : 1;
-	double pt = h->md.pt > 0 ? (double) (float) h->md.pt : (2 * T * n * dtf) / (T * n * dtf + 2 * (double) (float) h->md.diff_coeff);
+	const double pt = h->md.pt > 0 ? (double) (float) h->md.pt : (2 * T * n * dtf) / (T * n * dtf + 2 * (double) (float) h->md.diff_coeff);
 	if(pt > 1.0) return fail(OXGB_E_INVALID, "pt must be smaller than 1");
 	const double D = T * n * dtf * (1. / pt - 1. / 2.);
-	h->pt = pt;
-	h->pr = (2 * T * n * dtf) / (T * n * dtf + 2 * 3 * D);
+	const double c = std::exp(-(double) n / h->md.bussi_tau);
+	double *p = &h->par[(size_t) k * SP_STRIDE];
+	p[SP_T] = T;
+	p[SP_SQRTT] = std::sqrt(T);
+	p[SP_PT] = pt;
+	p[SP_PR] = (2 * T * n * dtf) / (T * n * dtf + 2 * 3 * D);
+	p[SP_1MC] = 1.0 - c;
+	p[SP_A] = (1.0 - c) * T * 0.5;
+	p[SP_B] = std::sqrt(2.0 * T * (1.0 - c) * c);
+	p[SP_INVN] = 1.0 / (h->offsets[k + 1] - h->offsets[k]);
+	return OXGB_OK;
+}
+
+// uploads the table, cutoff and thermostat values of systems k0 .. k1 - 1
+static int upload_systems(oxgb_md *h, int k0, int k1) {
+	for(int k = k0; k < k1; k++) {
+		DNA2Table<double> t64;
+		int rc = derive_system(h, k, t64);
+		if(rc) return rc;
+		if(h->dbl) {
+			CK(cudaMemcpy(reinterpret_cast<DNA2Table<double> *>(h->d_tab) + k, &t64, sizeof(t64), cudaMemcpyHostToDevice));
+		}
+		else {
+			DNA2Table<float> t32;
+			to_float(t64, h->box[k], t32);
+			CK(cudaMemcpy(reinterpret_cast<DNA2Table<float> *>(h->d_tab) + k, &t32, sizeof(t32), cudaMemcpyHostToDevice));
+		}
+	}
+	CK(cudaMemcpy(h->d_sys_par + (size_t) k0 * SP_STRIDE, &h->par[(size_t) k0 * SP_STRIDE], sizeof(double) * SP_STRIDE * (k1 - k0),
+			cudaMemcpyHostToDevice));
+	return OXGB_OK;
+}
+
+// cell grids of all systems (cells per side from each system's own box and cutoff) and the
+// device copies of the geometry the list kernels read; reallocates the cell buffers
+static int layout_cells(oxgb_md *h) {
+	const int S = h->n_systems;
+	h->nside.assign(S, 0);
+	h->cell0.assign(S + 1, 0);
+	for(int k = 0; k < S; k++) {
+		const int Nk = h->offsets[k + 1] - h->offsets[k];
+		h->nside[k] = cells_per_side(Nk, (float) h->box[k], h->rverlet[k], h->md.cells_auto_optimisation != 0);
+		const long long nc = (long long) h->nside[k] * h->nside[k] * h->nside[k];
+		if(h->cell0[k] + nc >= (1LL << 30)) return fail(OXGB_E_INVALID, "too many cells");
+		h->cell0[k + 1] = h->cell0[k] + (int) nc;
+	}
+	const int n_cells = h->cell0[S];
+	std::vector<int> cell_sys(n_cells);
+	std::vector<float> bx(S), rv2(S);
+	for(int k = 0; k < S; k++) {
+		for(int c = h->cell0[k]; c < h->cell0[k + 1]; c++) cell_sys[c] = k;
+		bx[k] = (float) h->box[k];
+		rv2[k] = h->rverlet[k] * h->rverlet[k];
+	}
+	h->free_layout();
+	CK(cudaMalloc(&h->d_sys_nside, sizeof(int) * S));
+	CK(cudaMalloc(&h->d_sys_cell0, sizeof(int) * (S + 1)));
+	CK(cudaMalloc(&h->d_cell_sys, sizeof(int) * n_cells));
+	CK(cudaMalloc(&h->d_sys_box, sizeof(float) * S));
+	CK(cudaMalloc(&h->d_sys_rv2, sizeof(float) * S));
+	CK(cudaMemcpy(h->d_sys_nside, h->nside.data(), sizeof(int) * S, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->d_sys_cell0, h->cell0.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->d_cell_sys, cell_sys.data(), sizeof(int) * n_cells, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->d_sys_box, bx.data(), sizeof(float) * S, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->d_sys_rv2, rv2.data(), sizeof(float) * S, cudaMemcpyHostToDevice));
 	return OXGB_OK;
 }
 
@@ -508,12 +583,26 @@ static int clear_pending(oxgb_md *h) {
 	return cudaStreamSynchronize(h->stream) != cudaSuccess;
 }
 
+// Bussi running kinetic energies of system k start at their targets (BussiThermostat::init)
+static int reset_bussi(oxgb_md *h, int k) {
+	const int n = h->offsets[k + 1] - h->offsets[k];
+	const double T = h->dna[k].T;
+	double bs[16] = {0.5 * 3 * (n - 1) * T, 0.5 * 3 * n * T, 1, 1};
+	CK(cudaMemcpy(h->bussi_state + 16 * (size_t) k, bs, sizeof(bs), cudaMemcpyHostToDevice));
+	return OXGB_OK;
+}
+
 extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *box, const oxgb_dna2_settings *dna,
 		const oxgb_md_settings *md, oxgb_md **out) {
 	if(n_systems < 1 || !offsets || !box || !dna || !md || !out) return fail(OXGB_E_INVALID, "null argument");
-	if(n_systems != 1) return fail(OXGB_E_INVALID, "this engine runs one system per handle; use the batched engine");
 	const int N = offsets[n_systems] - offsets[0];
 	if(offsets[0] != 0 || N <= 0 || N >= (1 << 22)) return fail(OXGB_E_INVALID, "invalid offsets (1 <= N < 2^22)");
+	for(int k = 0; k < n_systems; k++) {
+		if(offsets[k + 1] <= offsets[k]) return fail(OXGB_E_INVALID, "every system needs at least one nucleotide");
+		if(md->thermostat == OXGB_THERMOSTAT_BUSSI && offsets[k + 1] - offsets[k] < 2)
+			return fail(OXGB_E_INVALID, "the Bussi thermostat needs at least two nucleotides per system");
+		if(!(box[k] > 0)) return fail(OXGB_E_INVALID, "invalid box");
+	}
 	if(!(md->dt > 0) || md->verlet_skin < 0) return fail(OXGB_E_INVALID, "invalid dt or verlet_skin");
 	oxgb_md *h = new oxgb_md();
 	h->n_systems = n_systems;
@@ -525,11 +614,33 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	if(h->md.steps_per_graph <= 0) h->md.steps_per_graph = 16;
 	h->conditional_ok = h->md.list_rebuild_node == 0;
 	h->dbl = md->precision == OXGB_PRECISION_DOUBLE;
+	h->rcut.assign(n_systems, 0.0);
+	h->rverlet.assign(n_systems, 0.f);
+	h->par.assign((size_t) n_systems * SP_STRIDE, 0.0);
 	const size_t v4 = h->dbl ? sizeof(double4_32a) : sizeof(float4);
+	const size_t tab = h->dbl ? sizeof(DNA2Table<double>) : sizeof(DNA2Table<float>);
 	auto bail = [&](int rc) {
 		delete h;
 		return rc;
 	};
+	// system of every nucleotide, Bussi / energy chunks and the widest system span of a block
+	std::vector<int> sys(N);
+	h->sys_chunk0.assign(n_systems + 1, 0);
+	for(int k = 0; k < n_systems; k++) {
+		for(int i = offsets[k]; i < offsets[k + 1]; i++) sys[i] = k;
+		h->sys_chunk0[k] = (int) h->chunk_sys.size();
+		for(int f = offsets[k]; f < offsets[k + 1]; f += 256) {
+			h->chunk_sys.push_back(k);
+			h->chunk_first.push_back(f);
+		}
+	}
+	h->n_chunks = (int) h->chunk_sys.size();
+	h->sys_chunk0[n_systems] = h->n_chunks;
+	for(int b = 0; b < N; b += 128) h->tab_span = std::max(h->tab_span, sys[std::min(N, b + 128) - 1] - sys[b] + 1);
+	if(set_forces_smem(h->dbl, tab * h->tab_span)) return bail(fail(OXGB_E_INVALID, "systems too small: one block would need the tables of " + std::to_string(h->tab_span) + " systems"));
+	std::vector<unsigned long long> seeds(n_systems);
+	for(int k = 0; k < n_systems; k++) seeds[k] = h->md.seed + (unsigned long long) k;
+
 	if(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
 			cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
 			cudaStreamCreateWithFlags(&h->noise, cudaStreamNonBlocking) != cudaSuccess ||
@@ -555,38 +666,53 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->bonds, sizeof(int2) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->F, v4 * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->T, v4 * N) == cudaSuccess;
-	ok &= cudaMalloc(&h->d_tab, h->dbl ? sizeof(DNA2Table<double>) : sizeof(DNA2Table<float>)) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_tab, tab * n_systems) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_sys, sizeof(int) * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_sys_off, sizeof(int) * (n_systems + 1)) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_sys_stale, sizeof(int) * n_systems) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_chunk_sys, sizeof(int) * h->n_chunks) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_chunk_first, sizeof(int) * h->n_chunks) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_sys_chunk0, sizeof(int) * (n_systems + 1)) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_sys_par, sizeof(double) * SP_STRIDE * n_systems) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_sys_seed, sizeof(unsigned long long) * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->status, sizeof(int)) == cudaSuccess;
 	ok &= cudaMalloc(&h->flag, sizeof(int)) == cudaSuccess;
 	ok &= cudaMalloc(&h->step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->esplit, sizeof(double) * 8 * n_systems) == cudaSuccess;
-	ok &= cudaMalloc(&h->scratch, sizeof(double) * 8 * n_systems) == cudaSuccess;
-	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * ((N + 63) / 64 + 1)) == cudaSuccess;  // blocks of 64
+	ok &= cudaMalloc(&h->sums, sizeof(double) * 4 * h->n_chunks) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * h->n_chunks) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16 * n_systems) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned) * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->open_step, sizeof(long long)) == cudaSuccess;
-	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16) == cudaSuccess;
-	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
 	if(!ok) return bail(fail(OXGB_E_NOMEM, "device allocation failed"));
-	cudaMemset(h->status, 0, sizeof(int));
-	cudaMemset(h->flag, 0, sizeof(int));
-	cudaMemset(h->step, 0, sizeof(long long));
-	cudaMemset(h->d_rebuilds, 0, sizeof(unsigned long long));
-	cudaMemset(h->bussi_done, 0, sizeof(unsigned));
+	ok &= cudaMemcpy(h->d_sys, sys.data(), sizeof(int) * N, cudaMemcpyHostToDevice) == cudaSuccess;
+	ok &= cudaMemcpy(h->d_sys_off, offsets, sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice) == cudaSuccess;
+	ok &= cudaMemcpy(h->d_chunk_sys, h->chunk_sys.data(), sizeof(int) * h->n_chunks, cudaMemcpyHostToDevice) == cudaSuccess;
+	ok &= cudaMemcpy(h->d_chunk_first, h->chunk_first.data(), sizeof(int) * h->n_chunks, cudaMemcpyHostToDevice) == cudaSuccess;
+	ok &= cudaMemcpy(h->d_sys_chunk0, h->sys_chunk0.data(), sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice) == cudaSuccess;
+	ok &= cudaMemcpy(h->d_sys_seed, seeds.data(), sizeof(unsigned long long) * n_systems, cudaMemcpyHostToDevice) == cudaSuccess;
+	ok &= cudaMemset(h->d_sys_stale, 0, sizeof(int) * n_systems) == cudaSuccess;
+	ok &= cudaMemset(h->status, 0, sizeof(int)) == cudaSuccess;
+	ok &= cudaMemset(h->flag, 0, sizeof(int)) == cudaSuccess;
+	ok &= cudaMemset(h->step, 0, sizeof(long long)) == cudaSuccess;
+	ok &= cudaMemset(h->d_rebuilds, 0, sizeof(unsigned long long)) == cudaSuccess;
+	ok &= cudaMemset(h->bussi_done, 0, sizeof(unsigned) * n_systems) == cudaSuccess;
+	if(!ok) return bail(fail(OXGB_E_CUDA, "upload"));
 	if(clear_pending(h)) return bail(fail(OXGB_E_CUDA, "upload"));
-	int rc = upload_tables(h);
+	int rc = upload_systems(h, 0, n_systems);
 	if(rc) return bail(rc);
-	h->rverlet = (float) h->rcut + 2.f * (float) h->md.verlet_skin;
-	const int n_side = cells_per_side(N, (float) h->box[0], h->rverlet, h->md.cells_auto_optimisation != 0);
+	rc = layout_cells(h);
+	if(rc) return bail(rc);
 	const int cap = md->max_neigh > 0 ? md->max_neigh : std::min(std::max(N - 1, 1), 512);
-	rc = h->lb.alloc(N, n_side, cap);
+	rc = h->lb.alloc(N, h->nside[0], cap, h->cell0[n_systems]);
 	if(rc) return bail(rc);
 	h->radii = term_radii(h->md.verlet_skin);
 	rc = h->tl.alloc(N, std::min(std::max(N - 1, 1), 128), std::min(std::max(N - 1, 1), 64), std::min(std::max(N - 1, 1), 64));
 	if(rc) return bail(rc);
-	// Bussi running kinetic energies start at their targets (BussiThermostat::init)
-	double bs[16] = {0.5 * 3 * (N - 1) * h->dna[0].T, 0.5 * 3 * N * h->dna[0].T, 1, 1};
-	if(cudaMemcpy(h->bussi_state, bs, sizeof(bs), cudaMemcpyHostToDevice) != cudaSuccess) return bail(fail(OXGB_E_CUDA, "upload"));
+	for(int k = 0; k < n_systems; k++)
+		if((rc = reset_bussi(h, k))) return bail(rc);
 	*out = h;
 	return OXGB_OK;
 }
@@ -595,12 +721,17 @@ extern "C" int oxgb_md_set_topology(oxgb_md *h, const int *n3, const int *n5, co
 	if(!h || !n3 || !n5 || !btype || !type) return fail(OXGB_E_INVALID, "null argument");
 	const int N = h->N;
 	std::vector<int2> b(N);
-	for(int i = 0; i < N; i++) {
-		if(n3[i] < -1 || n3[i] >= N || n5[i] < -1 || n5[i] >= N || n3[i] == i || n5[i] == i)
-			return fail(OXGB_E_INVALID, "topology: bonded neighbour index out of range");
-		if(btype[i] < -512 || btype[i] > 511) return fail(OXGB_E_INVALID, "topology: btype outside [-512, 511]");
-		if(type[i] < 0 || type[i] > 4) return fail(OXGB_E_INVALID, "topology: base type outside 0..4");
-		b[i] = make_int2(n3[i], n5[i]);
+	for(int k = 0; k < h->n_systems; k++) {
+		const int lo = h->offsets[k], hi = h->offsets[k + 1];
+		for(int i = lo; i < hi; i++) {
+			if(n3[i] < -1 || n3[i] >= N || n5[i] < -1 || n5[i] >= N || n3[i] == i || n5[i] == i)
+				return fail(OXGB_E_INVALID, "topology: bonded neighbour index out of range");
+			if((n3[i] >= 0 && (n3[i] < lo || n3[i] >= hi)) || (n5[i] >= 0 && (n5[i] < lo || n5[i] >= hi)))
+				return fail(OXGB_E_INVALID, "topology: a bond crosses two systems");
+			if(btype[i] < -512 || btype[i] > 511) return fail(OXGB_E_INVALID, "topology: btype outside [-512, 511]");
+			if(type[i] < 0 || type[i] > 4) return fail(OXGB_E_INVALID, "topology: base type outside 0..4");
+			b[i] = make_int2(n3[i], n5[i]);
+		}
 	}
 	for(int i = 0; i < N; i++) {
 		if(n3[i] >= 0 && n5[n3[i]] != i) return fail(OXGB_E_INVALID, "topology: n3/n5 are not mutual");
@@ -615,10 +746,20 @@ extern "C" int oxgb_md_set_topology(oxgb_md *h, const int *n3, const int *n5, co
 }
 
 static ListArgs md_list_args(oxgb_md *h, int check_flag) {
-	ListArgs a = list_args(h->lb, h->N, h->pos_hi, (float) h->box[0], h->rverlet, h->bonds, h->list_pos, h->status, h->flag,
+	ListArgs a = list_args(h->lb, h->N, h->pos_hi, (float) h->box[0], h->rverlet[0], h->bonds, h->list_pos, h->status, h->flag,
 			check_flag);
 	a.rebuilds = h->d_rebuilds;
 	a.col_major = 1;
+	// the batch geometry (one grid per system; only requested systems are rebuilt)
+	a.sys = h->d_sys;
+	a.sys_nside = h->d_sys_nside;
+	a.sys_cell0 = h->d_sys_cell0;
+	a.cell_sys = h->d_cell_sys;
+	a.sys_box = h->d_sys_box;
+	a.sys_rv2 = h->d_sys_rv2;
+	a.sys_stale = h->d_sys_stale;
+	a.n_systems = h->n_systems;
+	a.n_cells_total = h->cell0[h->n_systems];
 	a.fa1 = h->fa1;
 	a.fback = h->fback;
 	a.ev_nb = h->tl.ev_nb;
@@ -638,7 +779,9 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	return a;
 }
 
+// rebuilds every system's lists now
 static int build_list_now(oxgb_md *h) {
+	CK(cudaMemsetAsync(h->d_sys_stale, 1, sizeof(int) * h->n_systems, h->stream));  // nonzero: rebuild
 	ListArgs a = md_list_args(h, 0);
 	CK(launch_list_build(a, h->stream));
 	return OXGB_OK;
@@ -646,7 +789,7 @@ static int build_list_now(oxgb_md *h) {
 
 static int compute_forces_now(oxgb_md *h, bool split) {
 	ForceArgs fa = force_args(h);
-	if(split) CK(cudaMemsetAsync(h->esplit, 0, sizeof(double) * 8, h->stream));
+	if(split) CK(cudaMemsetAsync(h->esplit, 0, sizeof(double) * 8 * h->n_systems, h->stream));
 	CK(launch_forces_split(fa, h->dbl, split, h->stream));
 	return OXGB_OK;
 }
@@ -689,7 +832,7 @@ static int size_and_build_list(oxgb_md *h) {
 		rc = h->tl.alloc(h->N, we, wb, ws);
 		if(rc) return rc;
 		want = want > 0 ? want : h->lb.max_nb;
-		rc = h->lb.alloc(h->N, h->lb.n_side, want);
+		rc = h->lb.alloc(h->N, h->lb.n_side, want, h->cell0[h->n_systems]);
 		if(rc) return rc;
 		CK(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
 		rc = build_list_now(h);
@@ -700,7 +843,7 @@ static int size_and_build_list(oxgb_md *h) {
 			cudaGraphExecDestroy(h->gexec);
 			h->gexec = nullptr;
 		}
-		rc = h->lb.alloc(h->N, h->lb.n_side, want);
+		rc = h->lb.alloc(h->N, h->lb.n_side, want, h->cell0[h->n_systems]);
 		if(rc) return rc;
 		CK(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
 		rc = build_list_now(h);
@@ -789,7 +932,7 @@ static cudaError_t fork_noise(oxgb_md *h, const StepArgs &sa) {
 static cudaError_t bussi_after_forces(oxgb_md *h, const StepArgs &sa) {
 	if(sa.th.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
 	cudaError_t e = cudaStreamWaitEvent(h->stream, h->ev_join, 0);
-	if(e == cudaSuccess) e = launch_bussi_reduce(sa, h->dbl, h->stream);
+	if(e == cudaSuccess) e = launch_bussi_reduce(sa, h->n_chunks, h->dbl, h->stream);
 	return e;
 }
 
@@ -919,7 +1062,7 @@ extern "C" int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *
 	if(rc) return rc;
 	rc = download_forces(h, F, T, E);
 	if(rc) return rc;
-	if(E_split) CK(cudaMemcpy(E_split, h->esplit, sizeof(double) * 8, cudaMemcpyDeviceToHost));
+	if(E_split) CK(cudaMemcpy(E_split, h->esplit, sizeof(double) * 8 * h->n_systems, cudaMemcpyDeviceToHost));
 	return OXGB_OK;
 }
 
@@ -956,30 +1099,22 @@ static int download_forces(oxgb_md *h, double *F, double *T, double *E) {
 
 extern "C" int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r) {
 	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
+	StepArgs sa = step_args(h);
+	CK(launch_system_sums(sa, h->n_chunks, h->dbl, h->sums, h->stream));
+	std::vector<double> c((size_t) 4 * h->n_chunks);
+	CK(cudaMemcpyAsync(c.data(), h->sums, sizeof(double) * c.size(), cudaMemcpyDeviceToHost, h->stream));
 	CK(cudaStreamSynchronize(h->stream));
-	const int N = h->N;
-	if(U) {
-		double u = 0;
-		if(h->dbl) {
-			std::vector<double4_32a> f(N);
-			CK(cudaMemcpy(f.data(), h->F, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
-			for(int i = 0; i < N; i++) u += f[i].w;
+	// per system, the chunks in order (deterministic)
+	for(int k = 0; k < h->n_systems; k++) {
+		double u = 0, kt = 0, kr = 0;
+		for(int ch = h->sys_chunk0[k]; ch < h->sys_chunk0[k + 1]; ch++) {
+			u += c[4 * ch];
+			kt += c[4 * ch + 1];
+			kr += c[4 * ch + 2];
 		}
-		else {
-			std::vector<float4> f(N);
-			CK(cudaMemcpy(f.data(), h->F, sizeof(float4) * N, cudaMemcpyDeviceToHost));
-			for(int i = 0; i < N; i++) u += f[i].w;
-		}
-		*U = 0.5 * u;
-	}
-	if(K_t || K_r) {
-		StepArgs sa = step_args(h);
-		CK(launch_kinetic(sa, h->scratch, h->stream));
-		double k[2];
-		CK(cudaMemcpyAsync(k, h->scratch, sizeof(k), cudaMemcpyDeviceToHost, h->stream));
-		CK(cudaStreamSynchronize(h->stream));
-		if(K_t) *K_t = k[0];
-		if(K_r) *K_r = k[1];
+		if(U) U[k] = u;
+		if(K_t) K_t[k] = kt;
+		if(K_r) K_r[k] = kr;
 	}
 	return OXGB_OK;
 }
@@ -987,12 +1122,48 @@ extern "C" int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r)
 extern "C" int oxgb_md_set_temperature(oxgb_md *h, int k, double T) {
 	if(!h || k < 0 || k >= h->n_systems || !(T > 0)) return fail(OXGB_E_INVALID, "invalid argument");
 	CK(cudaStreamSynchronize(h->stream));
+	const double T_old = h->dna[k].T;
 	h->dna[k].T = T;
-	int rc = upload_tables(h);
+	int rc = upload_systems(h, k, k + 1);  // table, cutoff, thermostat values (read by the kernels)
 	if(rc) return rc;
-	if(h->gexec) {  // the thermostat parameters are baked into the captured kernels
-		cudaGraphExecDestroy(h->gexec);
-		h->gexec = nullptr;
+	// the Bussi running kinetic energies follow the temperature
+	double bs[2];
+	CK(cudaMemcpy(bs, h->bussi_state + 16 * (size_t) k, sizeof(bs), cudaMemcpyDeviceToHost));
+	bs[0] *= T / T_old;
+	bs[1] *= T / T_old;
+	CK(cudaMemcpy(h->bussi_state + 16 * (size_t) k, bs, sizeof(bs), cudaMemcpyHostToDevice));
+	// the cutoff moves with T (Debye-Hueckel): a grid whose cells became narrower than the new
+	// r_verlet is laid out again (new buffers, so the step graph is captured again)
+	const bool relaid = (float) h->box[k] / (float) h->nside[k] < h->rverlet[k];
+	if(relaid) {
+		if(h->gexec) {
+			cudaGraphExecDestroy(h->gexec);
+			h->gexec = nullptr;
+		}
+		rc = layout_cells(h);
+		if(rc) return rc;
+		rc = h->lb.alloc(h->N, h->nside[0], h->lb.max_nb, h->cell0[h->n_systems]);
+		if(rc) return rc;
+	}
+	else {
+		const float rv2 = h->rverlet[k] * h->rverlet[k];
+		CK(cudaMemcpy(h->d_sys_rv2 + k, &rv2, sizeof(float), cudaMemcpyHostToDevice));
+	}
+	// system k's lists are rebuilt now (a larger cutoff needs it); a new cell layout rebuilds
+	// every system
+	if(h->have_state) {
+		if(relaid) {
+			rc = build_list_now(h);
+		}
+		else {
+			CK(cudaMemsetAsync(h->d_sys_stale + k, 1, sizeof(int), h->stream));
+			ListArgs a = md_list_args(h, 0);
+			CK(launch_list_build(a, h->stream));
+		}
+		if(rc) return rc;
+		rc = compute_forces_now(h, false);
+		if(rc) return rc;
+		return read_status(h);
 	}
 	return OXGB_OK;
 }

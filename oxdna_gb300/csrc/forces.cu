@@ -15,7 +15,6 @@
 //    int2 bonds and a neighbour matrix of any stride, accumulating into forces and torques
 //    initialised by the caller, exactly the contract of CUDABaseInteraction::compute_forces.
 #include "kernels.h"
-#include "thermo.cuh"
 
 #include <cuda_runtime.h>
 
@@ -66,6 +65,23 @@ __device__ __forceinline__ void load_table(const DNA2Table<R> *g, DNA2Table<R> *
 	for(int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
 	__syncthreads();
 }
+
+// The tables of the systems the nucleotides first .. last of this block belong to, copied into
+// dynamic shared memory (a plain run has one system); returns the first of those systems.
+// The host sizes the shared memory for the largest span of any block (ForceArgs::tab_span).
+template <typename R>
+__device__ __forceinline__ int load_table_span(const ForceArgs &a, int first, int last, DNA2Table<R> *s) {
+	const int s0 = a.sys ? a.sys[first] : 0;
+	const int s1 = a.sys ? a.sys[last] : 0;
+	const int n = (s1 - s0 + 1) * (int) (sizeof(DNA2Table<R>) / sizeof(int));
+	const int *src = reinterpret_cast<const int *>(reinterpret_cast<const DNA2Table<R> *>(a.table) + s0);
+	int *dst = reinterpret_cast<int *>(s);
+	for(int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+	__syncthreads();
+	return s0;
+}
+
+extern __shared__ __align__(16) unsigned char g_tables_smem[];
 
 // ---------------------------------------------------------------- particle loaders
 
@@ -389,13 +405,18 @@ __device__ __forceinline__ void load_dh<SplitMixed, float>(const SplitMixed &ld,
 template <typename R, class Loader, bool SPLIT>
 __global__ void __launch_bounds__(128) k_bonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
-	__shared__ DNA2Table<R> P;
-	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
+	// one bond (owner p, partner q = n3[p]) per thread; the grid covers every nucleotide
+	const int first = blockIdx.x * blockDim.x;
+	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
+	const int s0 = load_table_span<R>(a, first, min(first + (int) blockDim.x, a.N) - 1, Ps);
 	// an MD step: from here on its second half kick is pending (the first step has read the mark)
 	if(a.th.open_step && blockIdx.x == 0 && threadIdx.x == 0) *a.th.open_step = *a.th.step_base + a.th.step_offset;
-	for(int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.N; p += gridDim.x * blockDim.x) {
+	const int p = first + threadIdx.x;
+	if(p < a.N) {
 		const int q = a.bonds[p].x;
-		if(q < 0) continue;
+		if(q < 0) return;
+		const int sy = a.sys ? a.sys[p] : 0;
+		const DNA2Table<R> &P = Ps[sy - s0];
 		Nuc<R> np, nq;
 		V4 ph, pl, qh, ql;
 		load_full<Loader, R>(ld, p, P, np, ph, pl);
@@ -410,9 +431,9 @@ __global__ void __launch_bounds__(128) k_bonded_split(ForceArgs a, Loader ld) {
 		reinterpret_cast<V4 *>(a.bond_tp)[p] = tp;
 		reinterpret_cast<V4 *>(a.bond_tq)[p] = tq;
 		if(SPLIT) {
-			atomicAdd(a.esplit + T_FENE, (double) b.split[0]);
-			atomicAdd(a.esplit + T_BEXC, (double) b.split[1]);
-			atomicAdd(a.esplit + T_STCK, (double) b.split[2]);
+			atomicAdd(a.esplit + 8 * sy + T_FENE, (double) b.split[0]);
+			atomicAdd(a.esplit + 8 * sy + T_BEXC, (double) b.split[1]);
+			atomicAdd(a.esplit + 8 * sy + T_STCK, (double) b.split[2]);
 		}
 	}
 }
@@ -460,18 +481,21 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 #endif
 
 template <typename R, class Loader, bool SPLIT, int K>
-__global__ void __launch_bounds__(128, OXGB_NB_MINB) k_nonbonded_split(ForceArgs a, Loader ld) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonbonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
-	__shared__ DNA2Table<R> P;
-	load_table(reinterpret_cast<const DNA2Table<R> *>(a.table), &P);
 	const long long N = a.N;
 	const int sub = threadIdx.x % K;
 	// one nucleotide per group of K lanes: the grid covers every nucleotide (nonbonded_blocks);
 	// the lanes of a group past the last nucleotide still take part in the shuffles
 	const int i_raw = (blockIdx.x * blockDim.x + threadIdx.x) / K;
+	const int first = blockIdx.x * (blockDim.x / K);
+	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
+	const int s0 = load_table_span<R>(a, first, min(first + (int) (blockDim.x / K), a.N) - 1, Ps);
 	{
 		const bool live = i_raw < a.N;
 		const int i = live ? i_raw : a.N - 1;
+		const int sy = a.sys ? a.sys[i] : 0;
+		const DNA2Table<R> &P = Ps[sy - s0];
 		Nuc<R> p;
 		V4 ph, pl;
 		load_full<Loader, R>(ld, i, P, p, ph, pl);
@@ -524,7 +548,7 @@ __global__ void __launch_bounds__(128, OXGB_NB_MINB) k_nonbonded_split(ForceArgs
 		if(SPLIT && live) {
 #pragma unroll
 			for(int k = 0; k < N_TERMS; k++)
-				if(acc.split[k] != R(0)) atomicAdd(a.esplit + k, 0.5 * (double) acc.split[k]);
+				if(acc.split[k] != R(0)) atomicAdd(a.esplit + 8 * sy + k, 0.5 * (double) acc.split[k]);
 		}
 
 		// bonded pairs of this nucleotide, evaluated by k_bonded_split (first lane of the group)
@@ -580,10 +604,28 @@ template <typename R, class Loader, bool SPLIT>
 static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEvent_t wait) {
 	const int tpb = 128;
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
-	k_bonded_split<R, Loader, SPLIT><<<blocks, tpb, 0, s>>>(a, ld);
+	const size_t smem = sizeof(DNA2Table<R>) * (size_t) (a.tab_span > 0 ? a.tab_span : 1);
+	k_bonded_split<R, Loader, SPLIT><<<blocks, tpb, smem, s>>>(a, ld);
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
-	k_nonbonded_split<R, Loader, SPLIT, K><<<nonbonded_blocks(a.N), tpb, 0, s>>>(a, ld);
+	k_nonbonded_split<R, Loader, SPLIT, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
+}
+
+template <typename R, class Loader>
+static cudaError_t allow_smem(int bytes) {
+	cudaError_t e = cudaFuncSetAttribute(k_bonded_split<R, Loader, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_bonded_split<R, Loader, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	if(e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, false, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	if(e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, true, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	return e;
+}
+
+int set_forces_smem(bool dbl, size_t bytes) {
+	if(bytes <= 48 * 1024) return 0;
+	if(bytes > 160 * 1024) return 1;
+	return (dbl ? allow_smem<double, SplitDouble>((int) bytes) : allow_smem<float, SplitMixed>((int) bytes)) != cudaSuccess;
 }
 
 cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, cudaStream_t s, cudaEvent_t wait) {

@@ -70,10 +70,10 @@ __global__ void k_make_mirrors(StepArgs a) {
 
 __device__ __forceinline__ long long step_of(const ThermoArgs &t) { return *t.step_base + t.step_offset; }
 
-// completes step sp of nucleotide i: its second half kick (CUDA_mixed.cuh:71-93) and its
-// thermostat (Brownian redraw or Bussi rescaling)
+// completes step sp of nucleotide i (system sy): its second half kick (CUDA_mixed.cuh:71-93)
+// and its thermostat (Brownian redraw or Bussi rescaling)
 template <typename V4>
-__device__ __forceinline__ void complete_step(const ThermoArgs &t, int i, long long sp, const V4 &F, const V4 &T,
+__device__ __forceinline__ void complete_step(const ThermoArgs &t, int i, int sy, long long sp, const V4 &F, const V4 &T,
 		double4_32a &v, double4_32a &L) {
 	const double hdt = 0.5 * t.dt;
 	v.x += (double) F.x * hdt;
@@ -82,8 +82,8 @@ __device__ __forceinline__ void complete_step(const ThermoArgs &t, int i, long l
 	L.x += (double) T.x * hdt;
 	L.y += (double) T.y * hdt;
 	L.z += (double) T.z * hdt;
-	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) brownian_redraw(t, i, sp, v, L);
-	else if(t.thermostat == 2 && *t.bussi_stamp == sp) bussi_rescale(t, v, L);
+	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) brownian_redraw(t, sy, i - t.sys_off[sy], sp, v, L);
+	else if(t.thermostat == 2 && *t.bussi_stamp == sp) bussi_rescale(t, sy, v, L);
 }
 
 template <typename V4>
@@ -91,13 +91,14 @@ __global__ void k_first_step(StepArgs a) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= a.N) return;
 	const long long s = step_of(a.th);
+	const int sy = a.th.sys[i];
 	const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
 	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 	const double hdt = 0.5 * a.dt;
 	double4_32a v = a.vel[i], r = a.pos[i], L = a.angmom[i], q = a.quat[i];
 	// the previous step's second half kick and thermostat (kept as a separate half kick, so that
 	// a state is the same whether or not a run ended at that step)
-	if(*a.th.open_step == s - 1) complete_step(a.th, i, s - 1, F, T, v, L);
+	if(*a.th.open_step == s - 1) complete_step(a.th, i, sy, s - 1, F, T, v, L);
 	v.x += (double) F.x * hdt;
 	v.y += (double) F.y * hdt;
 	v.z += (double) F.z * hdt;
@@ -147,36 +148,50 @@ __global__ void k_first_step(StepArgs a) {
 	a.angmom[i] = L;
 	a.quat[i] = q;
 	write_mirror(a, i, r, q);
-	// Verlet list staleness (CUDA_mixed.cuh:68, extended to the interaction sites for the term lists)
-	if(list_stale(a, i, r)) atomicOr(a.flag, 1);
+	// Verlet list staleness (CUDA_mixed.cuh:68, extended to the interaction sites for the term
+	// lists), per system
+	if(list_stale(a, i, r)) {
+		a.sys_stale[sy] = 1;
+		atomicOr(a.flag, 1);
+	}
 }
 
 // ---------------------------------------------------------------- thermostats
 
-// the Bussi draws of the current step: warp 0 translational (channel 0), warp 1 rotational
+// the Bussi draws of the current step for system blockIdx.x: warp 0 translational (channel 0),
+// warp 1 rotational (channel 1)
 __global__ void k_bussi_noise(StepArgs a) {
 	const long long s = step_of(a.th);
+	const int sy = blockIdx.x;
 	if(s % a.th.newtonian_steps != 0 || (threadIdx.x & 31) != 0) return;
 	const int w = threadIdx.x >> 5;
 	if(w > 1) return;
+	const int n = a.th.sys_off[sy + 1] - a.th.sys_off[sy];
 	Stream rs;
-	rs.init(a.th.seed, s, (unsigned) w);
+	rs.init(a.th.sys_seed[sy], s, (unsigned) w);
 	double sum, rr;
-	bussi_draws(rs, w == 0 ? 3 * (a.N - 1) : 3 * a.N, sum, rr);
-	a.th.bussi_state[8 + 2 * w] = sum;
-	a.th.bussi_state[9 + 2 * w] = rr;
+	bussi_draws(rs, w == 0 ? 3 * (n - 1) : 3 * n, sum, rr);
+	a.th.bussi_state[16 * sy + 8 + 2 * w] = sum;
+	a.th.bussi_state[16 * sy + 9 + 2 * w] = rr;
 }
 
 // Bussi step s, after its forces: sums of v, |v|^2 and |L|^2 over the completed velocities
-// v + dt/2 F (computed here, stored by the next first step), per block; the last block to
-// finish reduces the block sums in a fixed order (deterministic) and makes the update
+// v + dt/2 F (computed here, stored by the next first step), one block per chunk of up to 256
+// nucleotides of one system; the last chunk of a system to finish reduces that system's chunk
+// sums in a fixed order (deterministic) and makes its update
 template <typename V4>
 __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 	const long long s = step_of(a.th);
 	if(s % a.th.newtonian_steps != 0) return;
+	const int c = blockIdx.x;
+	const int sy = a.th.chunk_sys[c];
+	const int i = a.th.chunk_first[c] + threadIdx.x;
 	const double hdt = 0.5 * a.dt;
+	// the next first step applies the rescaling of step s (every system updates at the same
+	// steps, and no kernel of this launch reads the mark)
+	if(c == 0 && threadIdx.x == 0) *a.th.bussi_stamp = s;
 	double acc[5] = {0, 0, 0, 0, 0};
-	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+	if(i < a.th.sys_off[sy + 1]) {
 		const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
 		const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 		double4_32a v = a.vel[i], L = a.angmom[i];
@@ -186,11 +201,11 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 		L.x += (double) T.x * hdt;
 		L.y += (double) T.y * hdt;
 		L.z += (double) T.z * hdt;
-		acc[0] += v.x;
-		acc[1] += v.y;
-		acc[2] += v.z;
-		acc[3] += v.x * v.x + v.y * v.y + v.z * v.z;
-		acc[4] += L.x * L.x + L.y * L.y + L.z * L.z;
+		acc[0] = v.x;
+		acc[1] = v.y;
+		acc[2] = v.z;
+		acc[3] = v.x * v.x + v.y * v.y + v.z * v.z;
+		acc[4] = L.x * L.x + L.y * L.y + L.z * L.z;
 	}
 	__shared__ double red[5][8];
 	__shared__ bool last;
@@ -205,18 +220,19 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 	if(threadIdx.x < 5) {
 		double x = 0;
 		for(int u = 0; u < nw; u++) x += red[threadIdx.x][u];
-		a.th.bussi_partials[blockIdx.x * 8 + threadIdx.x] = x;
+		a.th.bussi_partials[c * 8 + threadIdx.x] = x;
 		__threadfence();
 	}
 	__syncthreads();
-	if(threadIdx.x == 0) last = atomicAdd(a.th.done, 1u) == gridDim.x - 1;
+	const int c0 = a.th.sys_chunk0[sy], nc = a.th.sys_chunk0[sy + 1] - c0;
+	if(threadIdx.x == 0) last = atomicAdd(a.th.done + sy, 1u) == (unsigned) (nc - 1);
 	__syncthreads();
 	if(!last) return;
 	__threadfence();
 	double part[5] = {0, 0, 0, 0, 0};
-	for(int b = threadIdx.x; b < (int) gridDim.x; b += blockDim.x)
+	for(int b = threadIdx.x; b < nc; b += blockDim.x)
 #pragma unroll
-		for(int k = 0; k < 5; k++) part[k] += __ldcg(a.th.bussi_partials + b * 8 + k);
+		for(int k = 0; k < 5; k++) part[k] += __ldcg(a.th.bussi_partials + (c0 + b) * 8 + k);
 #pragma unroll
 	for(int k = 0; k < 5; k++) {
 		double x = part[k];
@@ -232,8 +248,8 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 		for(int u = 0; u < nw; u++) x += red[k][u];
 		sum[k] = x;
 	}
-	bussi_update(a.th, s, threadIdx.x == 0 ? 0 : 1, sum);
-	if(threadIdx.x == 0) *a.th.done = 0;
+	bussi_update(a.th, sy, s, threadIdx.x == 0 ? 0 : 1, sum);
+	if(threadIdx.x == 0) a.th.done[sy] = 0;
 }
 
 __global__ void k_step_advance(StepArgs a, int K) {
@@ -249,7 +265,7 @@ __global__ void k_step_flush(StepArgs a) {
 	const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
 	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 	double4_32a v = a.vel[i], L = a.angmom[i];
-	complete_step(a.th, i, sp, F, T, v, L);
+	complete_step(a.th, i, a.th.sys[i], sp, F, T, v, L);
 	a.vel[i] = v;
 	a.angmom[i] = L;
 }
@@ -262,16 +278,38 @@ __global__ void k_step_flush_clear(StepArgs a) {
 	}
 }
 
-__global__ void k_set_conditional(const int *flag, cudaGraphConditionalHandle h) {
-	if(threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, *flag != 0 ? 1u : 0u);
+// per-chunk FP64 sums: potential energy (F.w / 2), translational and rotational kinetic energy
+template <typename V4>
+__global__ void __launch_bounds__(256) k_system_sums(StepArgs a, double *out) {
+	const int c = blockIdx.x;
+	const int sy = a.th.chunk_sys[c];
+	const int i = a.th.chunk_first[c] + threadIdx.x;
+	double acc[3] = {0, 0, 0};
+	if(i < a.th.sys_off[sy + 1]) {
+		const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
+		const double4_32a v = a.vel[i], L = a.angmom[i];
+		acc[0] = 0.5 * (double) F.w;
+		acc[1] = 0.5 * (v.x * v.x + v.y * v.y + v.z * v.z);
+		acc[2] = 0.5 * (L.x * L.x + L.y * L.y + L.z * L.z);
+	}
+	__shared__ double red[3][8];
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+	for(int k = 0; k < 3; k++) {
+		double x = acc[k];
+		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+		if(lane == 0) red[k][w] = x;
+	}
+	__syncthreads();
+	if(threadIdx.x < 3) {
+		double x = 0;
+		for(int u = 0; u < nw; u++) x += red[threadIdx.x][u];
+		out[c * 4 + threadIdx.x] = x;
+	}
 }
 
-__global__ void k_kinetic(StepArgs a, double *out) {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i >= a.N) return;
-	const double4_32a v = a.vel[i], L = a.angmom[i];
-	atomicAdd(out, 0.5 * (v.x * v.x + v.y * v.y + v.z * v.z));
-	atomicAdd(out + 1, 0.5 * (L.x * L.x + L.y * L.y + L.z * L.z));
+__global__ void k_set_conditional(const int *flag, cudaGraphConditionalHandle h) {
+	if(threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, *flag != 0 ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------- launchers
@@ -286,13 +324,13 @@ cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_
 }
 
 cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
-	k_bussi_noise<<<1, 64, 0, s>>>(a);
+	k_bussi_noise<<<a.th.n_systems, 64, 0, s>>>(a);
 	return cudaGetLastError();
 }
 
-cudaError_t launch_bussi_reduce(const StepArgs &a, bool double_forces, cudaStream_t s) {
-	if(double_forces) k_bussi_reduce<double4_32a><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
-	else k_bussi_reduce<float4><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s) {
+	if(double_forces) k_bussi_reduce<double4_32a><<<n_chunks, 256, 0, s>>>(a);
+	else k_bussi_reduce<float4><<<n_chunks, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 
@@ -318,10 +356,9 @@ cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s) {
 	return cudaGetLastError();
 }
 
-cudaError_t launch_kinetic(const StepArgs &a, double *out2, cudaStream_t s) {
-	cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(double), s);
-	if(e != cudaSuccess) return e;
-	k_kinetic<<<blocks_for(a.N, 256), 256, 0, s>>>(a, out2);
+cudaError_t launch_system_sums(const StepArgs &a, int n_chunks, bool double_forces, double *out, cudaStream_t s) {
+	if(double_forces) k_system_sums<double4_32a><<<n_chunks, 256, 0, s>>>(a, out);
+	else k_system_sums<float4><<<n_chunks, 256, 0, s>>>(a, out);
 	return cudaGetLastError();
 }
 

@@ -21,23 +21,35 @@ namespace oxgb {
 // applies the thermostat of step s to it, then makes its own half kick and drift.
 #define OXGB_NO_STEP (-4611686018427387904LL)  // "no step" mark of open_step / bussi_stamp
 
+// per-system thermostat parameters, sys_par[s * SP_STRIDE + k]
+enum { SP_T = 0, SP_SQRTT, SP_PT, SP_PR, SP_1MC, SP_A, SP_B, SP_INVN, SP_STRIDE = 8 };
+
+// Every engine handles a batch of independent systems packed one after the other (a plain run
+// is a batch of one): nucleotide i belongs to system sys[i], whose nucleotides are
+// sys_off[s] .. sys_off[s + 1] - 1.  The random streams are keyed by (system seed, step, index
+// within the system), so a system evolves exactly as it would alone with that seed.
 struct ThermoArgs {
-	int N;                                 // nucleotides of the system
+	int N;                                 // nucleotides of all systems
+	int n_systems;
 	int thermostat;                        // 0 none, 1 brownian, 2 bussi
 	int newtonian_steps;
 	double dt;
-	double pt, pr, sqrtT, T;
-	unsigned long long seed;
-	double bussi_1mc, bussi_a, bussi_b;    // with c = exp(-newtonian_steps / tau): 1 - c,
-	                                       // (1 - c) T / 2 and sqrt(2 T (1 - c) c)
-	double inv_N;
-	double *bussi_partials;                // [blocks * 8] per-block sums of v, |v|^2, |L|^2
-	double *bussi_state;                   // [16]: K_t, K_r, factor_t, factor_r, vcom x y z, -,
-	                                       // then the step's draws: sum_t, rr_t, sum_r, rr_r
-	long long *bussi_stamp;                // step of the last Bussi update (-1: none pending)
-	long long *open_step;                  // step whose second half kick is pending (-1: none);
-	                                       // null in force-only calls
-	unsigned *done;                        // blocks of the Bussi reduction finished (0 between steps)
+	const int *sys, *sys_off;
+	const double *sys_par;                 // [n_systems * SP_STRIDE]: T, sqrt T, pt, pr, and with
+	                                       // c = exp(-newtonian_steps / tau): 1 - c, (1 - c) T / 2,
+	                                       // sqrt(2 T (1 - c) c), 1 / N_s
+	const unsigned long long *sys_seed;    // [n_systems]
+	// Bussi: the kinetic sums run over chunks of up to 256 nucleotides of one system
+	const int *chunk_sys, *chunk_first;    // [chunks]
+	const int *sys_chunk0;                 // [n_systems + 1] first chunk of each system
+	double *bussi_partials;                // [chunks * 8] per-chunk sums of v, |v|^2, |L|^2
+	double *bussi_state;                   // [n_systems * 16]: K_t, K_r, factor_t, factor_r,
+	                                       // vcom x y z, -, then the step's draws: sum_t, rr_t,
+	                                       // sum_r, rr_r
+	unsigned *done;                        // [n_systems] chunks finished (0 between steps)
+	long long *bussi_stamp;                // step of the last Bussi update (OXGB_NO_STEP: none)
+	long long *open_step;                  // step whose second half kick is pending
+	                                       // (OXGB_NO_STEP: none); null in force-only calls
 	long long *step_base;                  // device step counter of the current graph
 	int step_offset;
 };
@@ -53,11 +65,11 @@ struct ForceArgs {
 	int max_nb;
 	long long nb_stride_i, nb_stride_k;   // element (i, k) at nb[i * stride_i + k * stride_k]
 	void *forces, *torques;               // float4 or double4_32a per particle
-	const void *table;                    // DNA2Table<float> or DNA2Table<double>
+	const void *table;                    // DNA2Table<float> or DNA2Table<double>, one per system
+	const int *sys;                       // [N] system of each nucleotide (null: one system)
+	int tab_span;                         // most systems one block of the split kernels touches
 	int *status;
-	double *esplit;                       // 8 system energies (split kernels only)
-	double dt;
-	double4_32a *vel, *angmom;                // second half kick (fused kernels only)
+	double *esplit;                       // [8 * n_systems] energies (split kernels only)
 	// split path (engine layout): backbone-site offsets (w = strand-end flag), term lists
 	// (column-major: element k of nucleotide i at [k * N + i]) and the per-bond buffers
 	const float4 *fback;
@@ -75,6 +87,9 @@ cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
 cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, cudaStream_t s, cudaEvent_t wait = nullptr);
 // blocks of the split non-bonded kernel for N nucleotides
 int nonbonded_blocks(int N);
+// lets the split kernels use `bytes` of dynamic shared memory (per-block system tables);
+// nonzero if that is more than they may have
+int set_forces_smem(bool dbl, size_t bytes);
 
 struct ListArgs {
 	int N;
@@ -106,6 +121,14 @@ struct ListArgs {
 	float ev_r2, base_r2, stk_r2;
 	float4 *list_a1, *list_back;   // body axis a1 and backbone offset at this build
 	int col_major;          // full rows column-major ([k * N + i]) instead of row-major
+	// batch of systems (sys null: one system with the scalar geometry above).  System s has
+	// its own box, cutoff and cell grid (sys_nside^3 cells from sys_cell0); only systems with
+	// sys_stale set are rebuilt (their cells, segments and rows), the others keep theirs
+	const int *sys, *sys_nside, *sys_cell0, *cell_sys;
+	const float *sys_box, *sys_rv2;
+	int *sys_stale;
+	int n_systems;
+	int n_cells_total;      // cells of all systems (0: n_side^3)
 };
 
 // full rebuild: cells (counting sort, deterministic order) then neighbour rows
@@ -125,17 +148,20 @@ struct StepArgs {
 	const float4 *list_a1, *list_back;     // site data of the last list build (null: centres only)
 	float skin2;
 	int *flag;
+	int *sys_stale;                        // [n_systems] per-system rebuild requests
 	int *status;
 	ThermoArgs th;
 };
 
 // first half of an MD step: completes a pending half kick and the previous step's thermostat,
-// then half kick, drift, rotation, FP32 mirrors and the list-staleness flag
+// then half kick, drift, rotation, FP32 mirrors and the list-staleness flags
 cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s);
-// the Bussi draws of the current step (they do not depend on the state: run beside the step)
+// the Bussi draws of the current step, per system (they do not depend on the state: they run
+// beside the step)
 cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s);
-// Bussi kinetic-energy sums over the completed velocities and the update (after the forces)
-cudaError_t launch_bussi_reduce(const StepArgs &a, bool double_forces, cudaStream_t s);
+// Bussi kinetic-energy sums over the completed velocities and the per-system update (after the
+// forces); n_chunks chunks of up to 256 nucleotides
+cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s);
 // end of a graph of K steps: the step base advances by K
 cudaError_t launch_step_advance(const StepArgs &a, int K, cudaStream_t s);
 // end of a run: completes the pending half kick and thermostat so the state is whole
@@ -143,7 +169,8 @@ cudaError_t launch_step_flush(const StepArgs &a, bool double_forces, cudaStream_
 cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h, cudaStream_t s);
 // refresh the FP32 mirrors from the FP64 state (after a host upload)
 cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s);
-// per-particle kinetic energies, translational and rotational (FP64)
-cudaError_t launch_kinetic(const StepArgs &a, double *out2, cudaStream_t s);
+// per-chunk FP64 sums of the potential energy (sum of F.w / 2) and the translational and
+// rotational kinetic energies: out[chunk * 4 + {0, 1, 2}]
+cudaError_t launch_system_sums(const StepArgs &a, int n_chunks, bool double_forces, double *out, cudaStream_t s);
 
 }  // namespace oxgb

@@ -31,31 +31,51 @@ __device__ __forceinline__ float sqr_min_image(float4 a, float4 b, float L) {
 #define SKIP_IF_FRESH(a) \
 	if((a).check_flag && *(a).flag == 0) return
 
+// geometry of system s: box side, r_verlet^2, cells per side, first cell
+struct CellGeo {
+	float box, rv2;
+	int n, cell0;
+};
+
+__device__ __forceinline__ int sys_of(const ListArgs &a, int i) { return a.sys ? a.sys[i] : 0; }
+
+__device__ __forceinline__ CellGeo cell_geo(const ListArgs &a, int s) {
+	if(!a.sys) return CellGeo{a.box, a.rverlet2, a.n_side, 0};
+	return CellGeo{a.sys_box[s], a.sys_rv2[s], a.sys_nside[s], a.sys_cell0[s]};
+}
+
+// system s is rebuilt in this pass (always, unless per-system requests are given)
+__device__ __forceinline__ bool rebuilt(const ListArgs &a, int s) { return !a.sys_stale || a.sys_stale[s] != 0; }
+
 __global__ void k_zero_counts(ListArgs a, int n_cells) {
 	SKIP_IF_FRESH(a);
-	for(int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += gridDim.x * blockDim.x) a.cell_count[c] = 0;
+	for(int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_cells; c += gridDim.x * blockDim.x)
+		if(!a.cell_sys || rebuilt(a, a.cell_sys[c])) a.cell_count[c] = 0;
 }
 
 __global__ void k_cell_count(ListArgs a) {
 	SKIP_IF_FRESH(a);
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= a.N) return;
+	const int s = sys_of(a, i);
+	if(!rebuilt(a, s)) return;
+	const CellGeo g = cell_geo(a, s);
 	const float4 r = a.pos[i];
 	if(!(fabsf(r.x) < 1e7f && fabsf(r.y) < 1e7f && fabsf(r.z) < 1e7f)) {
 		atomicOr(a.status, OXGB_ERR_NONFINITE);
-		a.cell_of[i] = 0;
-		atomicAdd(a.cell_count, 1);
+		a.cell_of[i] = g.cell0;
+		atomicAdd(a.cell_count + g.cell0, 1);
 		return;
 	}
-	const int n = a.n_side;
-	int cx = cell_coord(r.x, a.box, n), cy = cell_coord(r.y, a.box, n), cz = cell_coord(r.z, a.box, n);
+	const int n = g.n;
+	int cx = cell_coord(r.x, g.box, n), cy = cell_coord(r.y, g.box, n), cz = cell_coord(r.z, g.box, n);
 	if(cx < 0 || cx >= n || cy < 0 || cy >= n || cz < 0 || cz >= n) {
 		atomicOr(a.status, OXGB_ERR_CELL);
 		cx = min(max(cx, 0), n - 1);
 		cy = min(max(cy, 0), n - 1);
 		cz = min(max(cz, 0), n - 1);
 	}
-	const int c = (cz * n + cy) * n + cx;
+	const int c = g.cell0 + (cz * n + cy) * n + cx;
 	a.cell_of[i] = c;
 	atomicAdd(a.cell_count + c, 1);
 }
@@ -145,7 +165,7 @@ __global__ void __launch_bounds__(SCAN_TPB) k_scan_apply(ListArgs a, int n_cells
 __global__ void k_cell_scatter(ListArgs a) {
 	SKIP_IF_FRESH(a);
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i >= a.N) return;
+	if(i >= a.N || !rebuilt(a, sys_of(a, i))) return;
 	const int slot = atomicAdd(a.cell_cursor + a.cell_of[i], 1);
 	a.cell_tmp[slot] = i;
 }
@@ -154,7 +174,7 @@ __global__ void k_cell_scatter(ListArgs a) {
 __global__ void k_cell_rank(ListArgs a) {
 	SKIP_IF_FRESH(a);
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i >= a.N) return;
+	if(i >= a.N || !rebuilt(a, sys_of(a, i))) return;
 	const int c = a.cell_of[i];
 	const int b = a.cell_start[c], e = a.cell_start[c + 1];
 	int rank = 0;
@@ -185,10 +205,13 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	const int lane = threadIdx.x & 31;
 	const int i = (int) (((long long) blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 	if(i >= a.N) return;  // warp-uniform
+	const int sy = sys_of(a, i);
+	if(!rebuilt(a, sy)) return;  // warp-uniform
+	const CellGeo g = cell_geo(a, sy);
 	const float4 r = a.pos[i];
 	const int2 b = a.bonds[i];
-	const int n = a.n_side;
-	const int c = a.cell_of[i];
+	const int n = g.n;
+	const int c = a.cell_of[i] - g.cell0;
 	const int cx = c % n, cy = (c / n) % n, cz = c / (n * n);
 	const bool terms = a.ev_nb != nullptr;
 	const long long N = a.N;
@@ -196,7 +219,7 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	int cs = 0, cn = 0;
 	if(lane < 27) {
 		const int z = (cz + lane / 9 - 1 + n) % n, y = (cy + (lane / 3) % 3 - 1 + n) % n, x = (cx + lane % 3 - 1 + n) % n;
-		const int cc = (z * n + y) * n + x;
+		const int cc = g.cell0 + (z * n + y) * n + x;
 		cs = a.cell_start[cc];
 		cn = a.cell_start[cc + 1] - cs;
 	}
@@ -231,11 +254,11 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 			j = a.cell_list[cs_l + (t - ex_l)];
 			if(j != i && j != b.x && j != b.y) {
 				const float4 rj = a.pos[j];
-				const float d2 = sqr_min_image(r, rj, a.box);
-				hit = d2 < a.rverlet2;
+				const float d2 = sqr_min_image(r, rj, g.box);
+				hit = d2 < g.rv2;
 				if(terms && hit && d2 < a.ev_r2) {
 					hev = true;
-					const float3 d = min_image_vec(r, rj, a.box);
+					const float3 d = min_image_vec(r, rj, g.box);
 					const float4 a1j = a.fa1[j];
 					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
 					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
@@ -287,10 +310,13 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	}
 }
 
-// runs after every other list kernel: counts the build and clears the request
+// runs after every other list kernel: counts the build and clears the requests
 __global__ void k_list_done(ListArgs a) {
-	if(threadIdx.x != 0 || blockIdx.x != 0) return;
+	if(blockIdx.x != 0) return;
 	if(a.check_flag && *a.flag == 0) return;
+	if(a.sys_stale)
+		for(int s = threadIdx.x; s < a.n_systems; s += blockDim.x) a.sys_stale[s] = 0;
+	if(threadIdx.x != 0) return;
 	if(a.rebuilds) *a.rebuilds += 1;
 	*a.flag = 0;
 }
@@ -298,7 +324,7 @@ __global__ void k_list_done(ListArgs a) {
 int scan_tiles(int n_cells) { return (n_cells + SCAN_TILE - 1) / SCAN_TILE; }
 
 cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s) {
-	const int n_cells = a.n_side * a.n_side * a.n_side;
+	const int n_cells = a.n_cells_total > 0 ? a.n_cells_total : a.n_side * a.n_side * a.n_side;
 	const int tpb = 256;
 	const int gp = (a.N + tpb - 1) / tpb;
 	const int tiles = scan_tiles(n_cells);
@@ -311,7 +337,7 @@ cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s) {
 	k_cell_rank<<<gp, tpb, 0, s>>>(a);
 	const long long warps = (long long) a.N * 32;
 	k_neighbours<<<(int) ((warps + tpb - 1) / tpb), tpb, 0, s>>>(a);
-	k_list_done<<<1, 32, 0, s>>>(a);
+	k_list_done<<<1, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

@@ -130,46 +130,53 @@ static __device__ __forceinline__ void update_K(double &K, double one_minus_c, d
 
 // Brownian ("john") thermostat: every newtonian_steps steps each nucleotide redraws its
 // velocity with probability pt and its angular momentum with probability pr from the
-// Maxwell-Boltzmann distribution at T (unit mass and moment of inertia)
-static __device__ __noinline__ void brownian_redraw(const ThermoArgs &t, int i, long long s, double4_32a &v, double4_32a &L) {
+// Maxwell-Boltzmann distribution at T (unit mass and moment of inertia).  Keyed by the
+// system's seed, the step and the index within the system.
+static __device__ __noinline__ void brownian_redraw(const ThermoArgs &t, int sy, int i_local, long long s, double4_32a &v,
+		double4_32a &L) {
+	const double *par = t.sys_par + sy * SP_STRIDE;
+	const unsigned long long seed = t.sys_seed[sy];
 	unsigned o0[4], o1[4];
-	const unsigned k0 = (unsigned) t.seed, k1 = (unsigned) (t.seed >> 32);
+	const unsigned k0 = (unsigned) seed, k1 = (unsigned) (seed >> 32);
 	const unsigned s0 = (unsigned) s, s1 = (unsigned) ((unsigned long long) s >> 32);
-	philox(k0, k1, s0, s1, RNG_BROWNIAN, (unsigned) (2 * i), o0);
-	philox(k0, k1, s0, s1, RNG_BROWNIAN, (unsigned) (2 * i + 1), o1);
+	philox(k0, k1, s0, s1, RNG_BROWNIAN, (unsigned) (2 * i_local), o0);
+	philox(k0, k1, s0, s1, RNG_BROWNIAN, (unsigned) (2 * i_local + 1), o1);
 	double g[6];
 	box_muller(o0[2], o0[3], g[0], g[1]);
 	box_muller(o1[0], o1[1], g[2], g[3]);
 	box_muller(o1[2], o1[3], g[4], g[5]);
-	if(u01(o0[0]) < t.pt) v = make_double4_32a(g[0] * t.sqrtT, g[1] * t.sqrtT, g[2] * t.sqrtT, 0.0);
-	if(u01(o0[1]) < t.pr) L = make_double4_32a(g[3] * t.sqrtT, g[4] * t.sqrtT, g[5] * t.sqrtT, 0.0);
+	const double sT = par[SP_SQRTT];
+	if(u01(o0[0]) < par[SP_PT]) v = make_double4_32a(g[0] * sT, g[1] * sT, g[2] * sT, 0.0);
+	if(u01(o0[1]) < par[SP_PR]) L = make_double4_32a(g[3] * sT, g[4] * sT, g[5] * sT, 0.0);
 }
 
-// Bussi: from the sums of v, |v|^2 and |L|^2 over the system, the new running kinetic energy
+// Bussi: from the sums of v, |v|^2 and |L|^2 over system sy, the new running kinetic energy
 // (with the draws of this step) and the rescaling factor of one kind of motion: which = 0
 // translation (about the centre-of-mass velocity), 1 rotation.  The two run on two threads.
-static __device__ void bussi_update(const ThermoArgs &t, long long s, int which, const double sum[5]) {
-	double *st = t.bussi_state;
+static __device__ void bussi_update(const ThermoArgs &t, int sy, long long s, int which, const double sum[5]) {
+	const double *par = t.sys_par + sy * SP_STRIDE;
+	double *st = t.bussi_state + 16 * sy;
 	if(which == 0) {
-		const double vc[3] = {sum[0] * t.inv_N, sum[1] * t.inv_N, sum[2] * t.inv_N};
-		const double Kt_now = 0.5 * (sum[3] - (double) t.N * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
-		update_K(st[0], t.bussi_1mc, t.bussi_a, t.bussi_b, __ldcg(st + 8), __ldcg(st + 9));
+		const double inv_n = par[SP_INVN];
+		const double n = (double) (t.sys_off[sy + 1] - t.sys_off[sy]);
+		const double vc[3] = {sum[0] * inv_n, sum[1] * inv_n, sum[2] * inv_n};
+		const double Kt_now = 0.5 * (sum[3] - n * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
+		update_K(st[0], par[SP_1MC], par[SP_A], par[SP_B], __ldcg(st + 8), __ldcg(st + 9));
 		st[2] = sqrt(st[0]) * rsqrt(Kt_now);
 		st[4] = vc[0];
 		st[5] = vc[1];
 		st[6] = vc[2];
-		*t.bussi_stamp = s;
 	}
 	else {
 		const double Kr_now = 0.5 * sum[4];
-		update_K(st[1], t.bussi_1mc, t.bussi_a, t.bussi_b, __ldcg(st + 10), __ldcg(st + 11));
+		update_K(st[1], par[SP_1MC], par[SP_A], par[SP_B], __ldcg(st + 10), __ldcg(st + 11));
 		st[3] = sqrt(st[1]) * rsqrt(Kr_now);
 	}
 }
 
-// the rescaling of a Bussi update made at step s, applied to one nucleotide
-static __device__ __forceinline__ void bussi_rescale(const ThermoArgs &t, double4_32a &v, double4_32a &L) {
-	const double *st = t.bussi_state;
+// the rescaling of the last Bussi update of system sy, applied to one nucleotide
+static __device__ __forceinline__ void bussi_rescale(const ThermoArgs &t, int sy, double4_32a &v, double4_32a &L) {
+	const double *st = t.bussi_state + 16 * sy;
 	const double ft = __ldcg(st + 2), fr = __ldcg(st + 3), cx = __ldcg(st + 4), cy = __ldcg(st + 5), cz = __ldcg(st + 6);
 	v.x = (v.x - cx) * ft + cx;
 	v.y = (v.y - cy) * ft + cy;

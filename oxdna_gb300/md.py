@@ -66,19 +66,43 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
 
 
 class MDSystem:
-    """One system on the GPU: topology, FP64 state, Verlet lists, integrator and thermostat."""
+    """One system -- or a batch of independent systems -- on the GPU: topology, FP64 state,
+    Verlet lists, integrator and thermostat.
 
-    def __init__(self, box: float, top: oxio.Topology, dna: _abi.DNA2Settings, md: _abi.MDSettings):
+    A batch is given as lists: `box`, `top` and `dna` hold one entry per system.  Its systems are
+    packed one after the other (per-nucleotide arrays of `set_state`/`get_state` are the
+    concatenation, system k at rows `offsets[k]:offsets[k + 1]`); each keeps its own box,
+    temperature, cutoff, cell grid, Verlet lists and thermostat, and its random stream uses the
+    seed `md.seed + k`.  Per-system results (energies, energy split) come back per system.
+    """
+
+    def __init__(self, box, top, dna, md: _abi.MDSettings):
         L = _abi.lib()
-        self.N = top.N
-        self.box = float(box)
+        boxes = [float(b) for b in box] if isinstance(box, (list, tuple, np.ndarray)) else [float(box)]
+        tops = list(top) if isinstance(top, (list, tuple)) else [top]
+        dnas = list(dna) if isinstance(dna, (list, tuple)) else [dna]
+        if not (len(boxes) == len(tops) == len(dnas)):
+            raise ValueError("box, top and dna need one entry per system")
+        self.n_systems = len(tops)
+        self.offsets = np.zeros(self.n_systems + 1, np.int32)
+        for k, t in enumerate(tops):
+            self.offsets[k + 1] = self.offsets[k] + t.N
+        self.N = int(self.offsets[-1])
+        self.box = boxes[0] if self.n_systems == 1 else np.array(boxes)
+        dna_arr = (_abi.DNA2Settings * self.n_systems)(*dnas)
         h = C.c_void_p()
-        offsets = np.array([0, self.N], np.int32)
-        _abi.check(L.oxgb_md_create(1, offsets, np.array([self.box]), C.byref(dna), C.byref(md), C.byref(h)))
+        _abi.check(L.oxgb_md_create(self.n_systems, self.offsets, np.array(boxes, np.float64), dna_arr, C.byref(md),
+                                    C.byref(h)))
         self._h = h
-        _abi.check(L.oxgb_md_set_topology(h, np.ascontiguousarray(top.n3, np.int32), np.ascontiguousarray(top.n5, np.int32),
-                                          np.ascontiguousarray(top.btype, np.int32),
-                                          np.ascontiguousarray(top.type, np.int32)))
+
+        def cat(name, shift):
+            parts = []
+            for k, t in enumerate(tops):
+                a = np.asarray(getattr(t, name), np.int32)
+                parts.append(np.where(a >= 0, a + self.offsets[k], a) if shift else a)
+            return np.ascontiguousarray(np.concatenate(parts), np.int32)
+
+        _abi.check(L.oxgb_md_set_topology(h, cat("n3", True), cat("n5", True), cat("btype", False), cat("type", False)))
 
     def close(self):
         if self._h:
@@ -105,10 +129,12 @@ class MDSystem:
         _abi.check(_abi.lib().oxgb_md_run(self._h, int(nsteps), 1 if sync else 0))
 
     def compute_forces(self):
+        """forces, torques, per-nucleotide energies and the 8-term energy split (per system for a
+        batch) of the current state, from freshly built lists"""
         N = self.N
-        F, T, E, Es = np.zeros((N, 3)), np.zeros((N, 3)), np.zeros(N), np.zeros(8)
+        F, T, E, Es = np.zeros((N, 3)), np.zeros((N, 3)), np.zeros(N), np.zeros(8 * self.n_systems)
         _abi.check(_abi.lib().oxgb_md_compute_forces(self._h, _abi.ptr(F), _abi.ptr(T), _abi.ptr(E), _abi.ptr(Es)))
-        return F, T, E, Es
+        return F, T, E, (Es if self.n_systems == 1 else Es.reshape(self.n_systems, 8))
 
     def get_forces(self):
         """forces, torques and per-nucleotide energies of the last step, not recomputed"""
@@ -118,12 +144,17 @@ class MDSystem:
         return F, T, E
 
     def energies(self):
-        U, Kt, Kr = np.zeros(1), np.zeros(1), np.zeros(1)
+        """potential, translational and rotational kinetic energy (FP64 sums; arrays per system
+        for a batch)"""
+        n = self.n_systems
+        U, Kt, Kr = np.zeros(n), np.zeros(n), np.zeros(n)
         _abi.check(_abi.lib().oxgb_md_energies(self._h, _abi.ptr(U), _abi.ptr(Kt), _abi.ptr(Kr)))
-        return float(U[0]), float(Kt[0]), float(Kr[0])
+        if n == 1:
+            return float(U[0]), float(Kt[0]), float(Kr[0])
+        return U, Kt, Kr
 
-    def set_temperature(self, T: float):
-        _abi.check(_abi.lib().oxgb_md_set_temperature(self._h, 0, float(T)))
+    def set_temperature(self, T: float, k: int = 0):
+        _abi.check(_abi.lib().oxgb_md_set_temperature(self._h, int(k), float(T)))
 
     def neighbours(self):
         N = self.N
