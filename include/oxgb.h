@@ -211,6 +211,9 @@ int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r);
  * energies scale with T; the lists are rebuilt) -- the replica-exchange hook.  Velocities are
  * left to the caller (a swap usually rescales them by sqrt(T_new / T_old)). */
 int oxgb_md_set_temperature(oxgb_md *h, int k, double T);
+/* velocities and angular momenta of system k times f (after a temperature swap: f =
+ * sqrt(T_new / T_old)); no counterpart in the reference's CUDA backend, which has no batches */
+int oxgb_md_scale_momenta(oxgb_md *h, int k, double f);
 /* neighbour rows of the last list build: counts nnb[N], rows nb[N * max_neigh] (row-major),
  * cell index of every nucleotide cell[N]; any pointer may be NULL */
 int oxgb_md_neighbours(oxgb_md *h, int *nnb, int *nb, int max_neigh, int *cell, int *n_cells_side);

@@ -79,6 +79,7 @@ SIGNATURES = {
     "oxgb_md_run": (C.c_int, [_VP, C.c_int, C.c_int]),
     "oxgb_md_compute_forces": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "oxgb_md_get_forces": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "oxgb_md_scale_momenta": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_energies": (C.c_int, [_VP, _VP, _VP, _VP]),
     "oxgb_md_set_temperature": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_neighbours": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),

@@ -1168,6 +1168,13 @@ extern "C" int oxgb_md_set_temperature(oxgb_md *h, int k, double T) {
 	return OXGB_OK;
 }
 
+extern "C" int oxgb_md_scale_momenta(oxgb_md *h, int k, double f) {
+	if(!h || k < 0 || k >= h->n_systems || !(f > 0)) return fail(OXGB_E_INVALID, "invalid argument");
+	StepArgs sa = step_args(h);
+	CK(launch_scale_momenta(sa, h->offsets[k], h->offsets[k + 1], f, h->stream));
+	return OXGB_OK;
+}
+
 extern "C" int oxgb_md_neighbours(oxgb_md *h, int *nnb, int *nb, int max_neigh, int *cell, int *n_cells_side) {
 	if(!h) return fail(OXGB_E_INVALID, "null handle");
 	CK(cudaStreamSynchronize(h->stream));

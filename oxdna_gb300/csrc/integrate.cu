@@ -278,6 +278,21 @@ __global__ void k_step_flush_clear(StepArgs a) {
 	}
 }
 
+// velocities and angular momenta of nucleotides lo .. hi - 1 times f (a replica exchange)
+__global__ void k_scale_momenta(StepArgs a, int lo, int hi, double f) {
+	const int i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= hi) return;
+	double4_32a v = a.vel[i], L = a.angmom[i];
+	v.x *= f;
+	v.y *= f;
+	v.z *= f;
+	L.x *= f;
+	L.y *= f;
+	L.z *= f;
+	a.vel[i] = v;
+	a.angmom[i] = L;
+}
+
 // per-chunk FP64 sums: potential energy (F.w / 2), translational and rotational kinetic energy
 template <typename V4>
 __global__ void __launch_bounds__(256) k_system_sums(StepArgs a, double *out) {
@@ -353,6 +368,11 @@ cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h
 
 cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s) {
 	k_make_mirrors<<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_scale_momenta(const StepArgs &a, int lo, int hi, double f, cudaStream_t s) {
+	if(hi > lo) k_scale_momenta<<<blocks_for(hi - lo, 256), 256, 0, s>>>(a, lo, hi, f);
 	return cudaGetLastError();
 }
 

@@ -169,6 +169,8 @@ cudaError_t launch_step_flush(const StepArgs &a, bool double_forces, cudaStream_
 cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h, cudaStream_t s);
 // refresh the FP32 mirrors from the FP64 state (after a host upload)
 cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s);
+// velocities and angular momenta of nucleotides lo .. hi - 1 times f
+cudaError_t launch_scale_momenta(const StepArgs &a, int lo, int hi, double f, cudaStream_t s);
 // per-chunk FP64 sums of the potential energy (sum of F.w / 2) and the translational and
 // rotational kinetic energies: out[chunk * 4 + {0, 1, 2}]
 cudaError_t launch_system_sums(const StepArgs &a, int n_chunks, bool double_forces, double *out, cudaStream_t s);

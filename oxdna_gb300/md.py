@@ -156,6 +156,34 @@ class MDSystem:
     def set_temperature(self, T: float, k: int = 0):
         _abi.check(_abi.lib().oxgb_md_set_temperature(self._h, int(k), float(T)))
 
+    def scale_momenta(self, f: float, k: int = 0):
+        _abi.check(_abi.lib().oxgb_md_scale_momenta(self._h, int(k), float(f)))
+
+    def replica_exchange(self, temps, rng, parity: int = 0):
+        """One round of parallel-tempering swaps between neighbouring rungs of a temperature
+        ladder.  temps[k] is the current temperature of system k; rungs (r, r + 1) with r of the
+        given parity are tried with the Metropolis rule on the FP64 potential energies,
+        min(1, exp((1/T_r - 1/T_r+1) (U_r - U_r+1))); an accepted pair exchanges temperatures
+        (tables, thermostat) and rescales its momenta by sqrt(T_new / T_old).  Returns the new
+        temperatures and the number of accepted swaps."""
+        temps = np.asarray(temps, np.float64).copy()
+        U, _, _ = self.energies()
+        U = np.atleast_1d(U)
+        order = np.argsort(temps)  # order[r] = system at rung r
+        accepted = 0
+        for r in range(parity, len(order) - 1, 2):
+            i, j = order[r], order[r + 1]
+            d = (1.0 / temps[i] - 1.0 / temps[j]) * (U[i] - U[j])
+            if d >= 0 or rng.uniform() < np.exp(d):
+                Ti, Tj = temps[i], temps[j]
+                self.set_temperature(Tj, i)
+                self.set_temperature(Ti, j)
+                self.scale_momenta(np.sqrt(Tj / Ti), i)
+                self.scale_momenta(np.sqrt(Ti / Tj), j)
+                temps[i], temps[j] = Tj, Ti
+                accepted += 1
+        return temps, accepted
+
     def neighbours(self):
         N = self.N
         nnb = np.zeros(N, np.int32)
