@@ -5,13 +5,15 @@ as ideal B helices at 0.01 nucleotides/unit^3 (cube side 158.74), T = 300 K, 0.5
 dt = 0.003, Bussi thermostat (tau = 1000 steps, applied every step), Verlet skin 0.05, FP32
 forces with FP64 integration.  Inputs are generated from a seed (no dataset is involved).
 
-One bench "step" is one timed iteration of M MD steps (default 100) on state resident in HBM;
+One bench "step" is one timed iteration of M MD steps (default 200) on state resident in HBM;
 L2 is flushed (a 256 MiB write) before every timed iteration, outside the timed interval.
 `value` = nucleotides x MD steps / device time of the K timed iterations.  `e2e` is the same
 metric through the C ABI with host buffers: every iteration uploads the state from host memory,
-runs M steps and downloads the state.  The roofline is that of the force kernel (FP32 CUDA-core
-bound): algorithmic FLOPs per launch (the kernel's own pair physics counted with a counting
-scalar type) / its CUDA-event time, against an FP32 FMA throughput measured on the same GPU.
+runs M steps and downloads the state.  The roofline is that of the force kernels (FP32
+CUDA-core bound): algorithmic FLOPs per launch (the kernels' own pair physics counted with a
+counting scalar type) / their CUDA-event time, against an FP32 FMA throughput measured on the
+same GPU.  `batched` (rank 0, one GPU): the 256-system parallel-tempering workload in one engine
+against the same systems run one at a time through the plain path.
 
 --impl reference times the CPU implementation of the same path on the host cores: the
 reference's C++ CPU backend is not available on the GPU machine, so this is the FP64 oracle
@@ -137,6 +139,84 @@ def oracle_baseline(sysm_data, wl, nsteps, nthreads):
     return N * nsteps / dt, dt
 
 
+def batched_workload(seed):
+    """The 256-system parallel-tempering workload (cached like make_system)."""
+    from oxdna_gb300 import generate as G
+    cache = os.path.join(tempfile.gettempdir(), f"oxgb_batched256_{seed}.npz")
+    from oxdna_gb300 import io as oxio
+    if os.path.exists(cache):
+        d = np.load(cache, allow_pickle=True)
+        return list(d["systems"])
+    systems = G.batched_systems(256, seed=seed)
+    try:
+        np.savez(cache, systems=np.array(systems, dtype=object))
+    except Exception:
+        pass
+    return systems
+
+
+def bench_batched(args, torch, ox, _abi):
+    """256 independent systems (16-4000 nt, duplexes and hairpins, each in its own cube at
+    0.005 nt/unit^3, temperatures on a geometric 280-360 K ladder, 0.5 M, dt 0.003, Bussi tau
+    1000) in one engine, with parallel-tempering swaps every 1000 steps on FP64 energies, against
+    the same systems run one at a time through the plain path.  Wall-clock (host-synchronised)
+    time, since the swaps involve the host."""
+    from oxdna_gb300 import io as oxio
+    systems = batched_workload(args.seed)
+    n_tot = sum(s.N for s in systems)
+    md = dict(dt=0.003, thermostat="bussi", newtonian_steps=1, bussi_tau=1000.0, seed=7, precision="mixed",
+              steps_per_graph=25)
+
+    def state(s):
+        a1, a2, a3 = s.frames()
+        return s.pos, oxio.frame_to_quat(a1, a2, a3), s.vel, s.L
+
+    b = ox.MDSystem([s.box for s in systems], [s.top for s in systems], [ox.dna2_settings(s.T, 0.5) for s in systems],
+                    ox.md_settings(**md))
+    b.set_state(*[np.concatenate(x) for x in zip(*[state(s) for s in systems])])
+    M = args.md_steps
+    for _ in range(args.warmup):
+        b.run(M, sync=False)
+    torch.cuda.synchronize()
+    temps = np.array([s.T for s in systems])
+    rng = np.random.default_rng(args.seed)
+    done, tried, accepted, parity = 0, 0, 0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.run(M, sync=False)
+        done += M
+        if done % 1000 == 0:
+            temps, acc = b.replica_exchange(temps, rng, parity)
+            tried += len(systems) // 2
+            accepted += acc
+            parity ^= 1
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    _abi.check(_abi.lib().oxgb_md_status(b.handle))
+    b.close()
+    v_batch = n_tot * M * args.steps / t_batch
+
+    # the same systems through the plain path, one engine each, one after the other
+    t_plain = 0.0
+    for k, s in enumerate(systems):
+        m = ox.MDSystem(s.box, s.top, ox.dna2_settings(s.T, 0.5), ox.md_settings(**dict(md, seed=7 + k)))
+        m.set_state(*state(s))
+        m.run(M)  # warm-up and graph capture
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        m.run(M)
+        torch.cuda.synchronize()
+        t_plain += time.perf_counter() - t1
+        m.close()
+    v_plain = n_tot * M / t_plain
+    return {"value": v_batch, "unit": "particle-steps/s", "n_systems": len(systems), "n_nucleotides": n_tot,
+            "md_steps": M * args.steps, "pt_swaps_tried": tried, "pt_swaps_accepted": accepted,
+            "plain_one_at_a_time": v_plain, "speedup_vs_plain": v_batch / v_plain,
+            "description": "256 systems, 16-4000 nt log-uniform, duplexes/hairpins, 0.005 nt/unit^3, "
+                           "280-360 K geometric ladder, Bussi tau 1000, PT swaps every 1000 steps; "
+                           "wall clock including the swaps"}
+
+
 def cpu_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -181,6 +261,7 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-system batched workload")
     ap.add_argument("--list-node", default="conditional", choices=["conditional", "kernel"],
                     help="list rebuild as a conditional graph node, or as always-launched kernels that "
                          "return at once on a fresh list (what a kernel-level profiler can see)")
@@ -324,8 +405,14 @@ def main():
                "d2h_bytes_per_step": h2d, "md_steps_per_step": M}
         assert np.all(np.isfinite(got["pos"]))
 
-    launches_per_step = 1 + 1 + 1 + (3 if wl["thermostat"] == "bussi" else (1 if wl["thermostat"] == "john" else 0)) + 1
-    gpu_launches = steps_total * launches_per_step + rebuilds * 7 + args.steps  # + the L2 flush fills (torch)
+    # our kernels in the timed region: per MD step the first step, the rebuild condition, the
+    # bonded and non-bonded kernels (+ the Bussi draws and sums); per rebuild 9 list kernels; per
+    # graph of 25 steps the step advance; per run the 2-kernel flush
+    per_step = 4 + (2 if wl["thermostat"] == "bussi" else 0)
+    gpu_launches = steps_total * per_step + rebuilds * 9 + (steps_total // 25) + 2 * args.steps
+
+    if rank == 0 and world == 1 and not args.no_batched:
+        line_extra["batched"] = bench_batched(args, torch, ox, _abi)
     line = {
         "metric": "oxDNA2 MD particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
