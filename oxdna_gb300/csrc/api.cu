@@ -205,8 +205,9 @@ struct ListBuffers {
 struct TermLists {
 	int N = 0, ev_cap = 0, base_cap = 0, stk_cap = 0;
 	int *ev_nb = nullptr, *ev_n = nullptr, *base_nb = nullptr, *base_n = nullptr, *stk_nb = nullptr, *stk_n = nullptr;
+	void *base_res = nullptr, *stk_res = nullptr;  // per-slot pair results, two 4-vectors of v4 bytes each
 
-	int alloc(int N_, int ev, int base, int stk) {
+	int alloc(int N_, int ev, int base, int stk, size_t v4) {
 		free_all();
 		N = std::max(N_, 1);
 		ev_cap = ev;
@@ -218,10 +219,16 @@ struct TermLists {
 		CK(cudaMalloc(&ev_n, sizeof(int) * N));
 		CK(cudaMalloc(&base_n, sizeof(int) * N));
 		CK(cudaMalloc(&stk_n, sizeof(int) * N));
+		CK(cudaMalloc(&base_res, 2 * v4 * (size_t) N * base_cap));
+		CK(cudaMalloc(&stk_res, 2 * v4 * (size_t) N * stk_cap));
 		return OXGB_OK;
 	}
 	void free_all() {
 		for(int **p : {&ev_nb, &ev_n, &base_nb, &base_n, &stk_nb, &stk_n}) {
+			if(*p) cudaFree(*p);
+			*p = nullptr;
+		}
+		for(void **p : {&base_res, &stk_res}) {
 			if(*p) cudaFree(*p);
 			*p = nullptr;
 		}
@@ -489,6 +496,8 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.bond_f = h->bond_f;
 	a.bond_tp = h->bond_tp;
 	a.bond_tq = h->bond_tq;
+	a.base_res = h->tl.base_res;
+	a.stk_res = h->tl.stk_res;
 	a.th = thermo_args(h, step_offset, engine_step);
 	return a;
 }
@@ -709,7 +718,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	rc = h->lb.alloc(N, h->nside[0], cap, h->cell0[n_systems]);
 	if(rc) return bail(rc);
 	h->radii = term_radii(h->md.verlet_skin);
-	rc = h->tl.alloc(N, std::min(std::max(N - 1, 1), 128), std::min(std::max(N - 1, 1), 64), std::min(std::max(N - 1, 1), 64));
+	rc = h->tl.alloc(N, std::min(std::max(N - 1, 1), 128), std::min(std::max(N - 1, 1), 64), std::min(std::max(N - 1, 1), 64), v4);
 	if(rc) return bail(rc);
 	for(int k = 0; k < n_systems; k++)
 		if((rc = reset_bussi(h, k))) return bail(rc);
@@ -829,7 +838,7 @@ static int size_and_build_list(oxgb_md *h) {
 			cudaGraphExecDestroy(h->gexec);
 			h->gexec = nullptr;
 		}
-		rc = h->tl.alloc(h->N, we, wb, ws);
+		rc = h->tl.alloc(h->N, we, wb, ws, h->dbl ? sizeof(double4_32a) : sizeof(float4));
 		if(rc) return rc;
 		want = want > 0 ? want : h->lb.max_nb;
 		rc = h->lb.alloc(h->N, h->lb.n_side, want, h->cell0[h->n_systems]);

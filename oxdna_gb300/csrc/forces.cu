@@ -453,7 +453,60 @@ struct SplitAcc {
 			for(int k = 0; k < N_TERMS; k++) split[k] += o.split[k];
 		}
 	}
+	// a pair result of k_pair_slots: (force, energy) and (torque, hydrogen-bonding energy)
+	template <typename V4>
+	__device__ __forceinline__ void add_result(const V4 &f, const V4 &t) {
+		F.add(v3<R>{f.x, f.y, f.z});
+		T.add(v3<R>{t.x, t.y, t.z});
+		KahanV<R>::kadd(E, Ec, f.w);
+		KahanV<R>::kadd(Eh, Ehc, t.w);
+	}
 };
+
+// One thread per slot of the base-base list (blocks 0 .. base_blocks - 1) or of the stack-stack
+// list (the rest): slot k of nucleotide i evaluates hydrogen bonding + cross stacking, or coaxial
+// stacking, for the pair (i, base_nb / stk_nb[k * N + i]) and stores (force, energy) and (torque
+// on i, HB energy) at [2 (k * N + i)] and [2 (k * N + i) + 1] of base_res / stk_res.  Slots are
+// numbered k * n_pad + i with n_pad a multiple of the block size, so a block holds one k and a
+// run of consecutive nucleotides; a warp of slot k = 0 is nearly full, one past every list
+// length exits at once.  These are the costliest terms and their lists are short (a few
+// entries), so a slot per thread keeps the lanes busy where per-nucleotide lanes would idle.
+template <typename R, class Loader, bool SPLIT>
+__global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int base_blocks, int n_pad) {
+	using V4 = typename Vec4Of<R>::T;
+	const bool is_base = (int) blockIdx.x < base_blocks;
+	const long long t = (long long) (is_base ? blockIdx.x : blockIdx.x - base_blocks) * blockDim.x + threadIdx.x;
+	const int k = (int) (t / n_pad), i = (int) (t % n_pad);
+	const int first = (int) ((t - threadIdx.x) % n_pad);
+	if(first >= a.N) return;  // block-uniform: the padding past the last nucleotide
+	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
+	const int s0 = load_table_span<R>(a, first, min(first + (int) blockDim.x, a.N) - 1, Ps);
+	if(i >= a.N) return;
+	const long long N = a.N;
+	const int n = is_base ? min(a.base_n[i], a.base_cap) : min(a.stk_n[i], a.stk_cap);
+	if(k >= n) return;
+	const int j = (is_base ? a.base_nb : a.stk_nb)[(long long) k * N + i];
+	const int sy = a.sys ? a.sys[i] : 0;
+	const DNA2Table<R> &P = Ps[sy - s0];
+	Nuc<R> p, q;
+	V4 ph, pl, qh, ql;
+	load_full<Loader, R>(ld, i, P, p, ph, pl);
+	load_full<Loader, R>(ld, j, P, q, qh, ql);
+	PairOut<R> o{};
+	if(is_base) pair_base<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
+	else pair_stack<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
+	V4 f, tq;
+	f.x = o.F.x, f.y = o.F.y, f.z = o.F.z, f.w = o.E;
+	tq.x = o.T.x, tq.y = o.T.y, tq.z = o.T.z, tq.w = o.Ehb;
+	V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res) + 2 * ((long long) k * N + i);
+	res[0] = f;
+	res[1] = tq;
+	if(SPLIT) {
+#pragma unroll
+		for(int m = 0; m < N_TERMS; m++)
+			if(o.split[m] != R(0)) atomicAdd(a.esplit + 8 * sy + m, 0.5 * (double) o.split[m]);
+	}
+}
 
 // compensated sum over the K lanes of a group (TwoSum at every level); every lane of the group
 // receives it
@@ -523,28 +576,14 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 			pair_ev<R, SPLIT>(p, q, ld.sep(ph, pl, qh, ql, P).plain(), o);
 			acc.add(o);
 		}
-		// hydrogen bonding and cross stacking over base-close pairs
+		// hydrogen bonding + cross stacking and coaxial stacking: evaluated per list slot by
+		// k_pair_slots, gathered here
 		const int nb_ = live ? min(a.base_n[i], a.base_cap) : 0;
-		for(int k = sub; k < nb_; k += K) {
-			const int j = a.base_nb[(long long) k * N + i];
-			Nuc<R> q;
-			V4 qh, ql;
-			load_full<Loader, R>(ld, j, P, q, qh, ql);
-			PairOut<R> o{};
-			pair_base<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
-			acc.add(o);
-		}
-		// coaxial stacking over stack-close pairs
+		for(int k = sub; k < nb_; k += K) acc.add_result(reinterpret_cast<const V4 *>(a.base_res)[2 * ((long long) k * N + i)],
+				reinterpret_cast<const V4 *>(a.base_res)[2 * ((long long) k * N + i) + 1]);
 		const int ns = live ? min(a.stk_n[i], a.stk_cap) : 0;
-		for(int k = sub; k < ns; k += K) {
-			const int j = a.stk_nb[(long long) k * N + i];
-			Nuc<R> q;
-			V4 qh, ql;
-			load_full<Loader, R>(ld, j, P, q, qh, ql);
-			PairOut<R> o{};
-			pair_stack<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
-			acc.add(o);
-		}
+		for(int k = sub; k < ns; k += K) acc.add_result(reinterpret_cast<const V4 *>(a.stk_res)[2 * ((long long) k * N + i)],
+				reinterpret_cast<const V4 *>(a.stk_res)[2 * ((long long) k * N + i) + 1]);
 		if(SPLIT && live) {
 #pragma unroll
 			for(int k = 0; k < N_TERMS; k++)
@@ -606,6 +645,11 @@ static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEv
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	const size_t smem = sizeof(DNA2Table<R>) * (size_t) (a.tab_span > 0 ? a.tab_span : 1);
 	k_bonded_split<R, Loader, SPLIT><<<blocks, tpb, smem, s>>>(a, ld);
+	// slots numbered k * n_pad + i, n_pad a multiple of the block size
+	const int n_pad = ((a.N + tpb - 1) / tpb) * tpb;
+	const int base_blocks = (int) (((long long) a.base_cap * n_pad) / tpb);
+	const int stk_blocks = (int) (((long long) a.stk_cap * n_pad) / tpb);
+	k_pair_slots<R, Loader, SPLIT><<<base_blocks + stk_blocks, tpb, smem, s>>>(a, ld, base_blocks, n_pad);
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
 	k_nonbonded_split<R, Loader, SPLIT, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
@@ -619,6 +663,8 @@ static cudaError_t allow_smem(int bytes) {
 		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, false, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	if(e == cudaSuccess)
 		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, true, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_pair_slots<R, Loader, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_pair_slots<R, Loader, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	return e;
 }
 

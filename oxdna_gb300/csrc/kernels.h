@@ -76,6 +76,7 @@ struct ForceArgs {
 	const int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
 	int ev_cap, base_cap, stk_cap;            // capacities (an overflowed list is read up to them)
 	void *bond_f, *bond_tp, *bond_tq;         // per bond owner p (q = n3[p]): f on q with w = energy, torques
+	void *base_res, *stk_res;                 // per list slot: (force, E), (torque, E_hb) pairs of V4
 	// MD-step bookkeeping (engine layout): the bonded kernel marks the step's half kick pending
 	ThermoArgs th;
 };
