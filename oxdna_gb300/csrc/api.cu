@@ -370,6 +370,7 @@ struct oxgb_md {
 	double *esplit = nullptr, *sums = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
 	unsigned *bussi_done = nullptr;
 	long long *bussi_stamp = nullptr, *open_step = nullptr;
+	int *term_max = nullptr;
 
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -395,7 +396,7 @@ struct oxgb_md {
 					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
-					(void *) bussi_done, (void *) bussi_stamp, (void *) open_step, (void *) d_rebuilds})
+					(void *) bussi_done, (void *) bussi_stamp, (void *) open_step, (void *) term_max, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -498,6 +499,7 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.bond_tq = h->bond_tq;
 	a.base_res = h->tl.base_res;
 	a.stk_res = h->tl.stk_res;
+	a.term_max = h->term_max;
 	a.th = thermo_args(h, step_offset, engine_step);
 	return a;
 }
@@ -695,7 +697,9 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->open_step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
+	ok &= cudaMalloc(&h->term_max, sizeof(int) * 3) == cudaSuccess;
 	if(!ok) return bail(fail(OXGB_E_NOMEM, "device allocation failed"));
+	ok &= cudaMemset(h->term_max, 0, sizeof(int) * 3) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_sys, sys.data(), sizeof(int) * N, cudaMemcpyHostToDevice) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_sys_off, offsets, sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_chunk_sys, h->chunk_sys.data(), sizeof(int) * h->n_chunks, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -785,6 +789,7 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	a.stk_r2 = h->radii.stk2;
 	a.list_a1 = h->list_a1;
 	a.list_back = h->list_back;
+	a.term_max = h->term_max;
 	return a;
 }
 

@@ -479,6 +479,8 @@ __global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int 
 	const int k = (int) (t / n_pad), i = (int) (t % n_pad);
 	const int first = (int) ((t - threadIdx.x) % n_pad);
 	if(first >= a.N) return;  // block-uniform: the padding past the last nucleotide
+	// block-uniform: slot k is past every list of this term (no table load, no pair)
+	if(a.term_max && k >= min(a.term_max[is_base ? 1 : 2], is_base ? a.base_cap : a.stk_cap)) return;
 	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
 	const int s0 = load_table_span<R>(a, first, min(first + (int) blockDim.x, a.N) - 1, Ps);
 	if(i >= a.N) return;

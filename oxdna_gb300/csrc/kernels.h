@@ -77,6 +77,7 @@ struct ForceArgs {
 	int ev_cap, base_cap, stk_cap;            // capacities (an overflowed list is read up to them)
 	void *bond_f, *bond_tp, *bond_tq;         // per bond owner p (q = n3[p]): f on q with w = energy, torques
 	void *base_res, *stk_res;                 // per list slot: (force, E), (torque, E_hb) pairs of V4
+	const int *term_max;                      // [3] longest EV / base / stack list (slots past it are empty)
 	// MD-step bookkeeping (engine layout): the bonded kernel marks the step's half kick pending
 	ThermoArgs th;
 };
@@ -121,6 +122,7 @@ struct ListArgs {
 	int ev_cap, base_cap, stk_cap;
 	float ev_r2, base_r2, stk_r2;
 	float4 *list_a1, *list_back;   // body axis a1 and backbone offset at this build
+	int *term_max;          // [3] longest EV / base / stack list of any build so far (may be null)
 	int col_major;          // full rows column-major ([k * N + i]) instead of row-major
 	// batch of systems (sys null: one system with the scalar geometry above).  System s has
 	// its own box, cutoff and cell grid (sys_nside^3 cells from sys_cell0); only systems with

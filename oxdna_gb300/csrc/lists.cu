@@ -302,6 +302,11 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	a.list_pos[i] = r;
 	if(terms) {
 		if(nev > a.ev_cap || nbase > a.base_cap || nstk > a.stk_cap) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
+		if(a.term_max) {  // read first: the maxima rarely grow, so few atomics reach them
+			if(nev > a.term_max[0]) atomicMax(a.term_max, nev);
+			if(nbase > a.term_max[1]) atomicMax(a.term_max + 1, nbase);
+			if(nstk > a.term_max[2]) atomicMax(a.term_max + 2, nstk);
+		}
 		a.ev_n[i] = nev;
 		a.base_n[i] = nbase;
 		a.stk_n[i] = nstk;
