@@ -201,11 +201,14 @@ int oxgb_md_run(oxgb_md *h, int nsteps, int sync);
  * volume, stacking, non-bonded excluded volume, hydrogen bonding, cross stacking, coaxial
  * stacking, Debye-Hueckel).  Any output pointer may be NULL. */
 int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *E, double *E_split);
-/* forces, torques and per-nucleotide energies left by the last step (or force evaluation),
- * downloaded without recomputing them; the download half of apply_simulation_data_changes */
+/* forces, torques and per-nucleotide energies of the current state; the download half of
+ * apply_simulation_data_changes.  The MD steps compute forces and torques only: when E is asked
+ * for after a run, the energies are evaluated once from the current state and lists (the forces
+ * and torques of that evaluation are the same numbers). */
 int oxgb_md_get_forces(oxgb_md *h, double *F, double *T, double *E);
-/* per-system potential energy (FP64 sum of the per-nucleotide energies / 2) and the
- * translational and rotational kinetic energies, each double[n_systems] */
+/* per-system potential energy (FP64 sum of the per-nucleotide energies / 2, evaluated on
+ * request as for oxgb_md_get_forces) and the translational and rotational kinetic energies,
+ * each double[n_systems] */
 int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r);
 /* new temperature of system k (parameter table, cutoff, thermostat; the Bussi running kinetic
  * energies scale with T; the lists are rebuilt) -- the replica-exchange hook.  Velocities are

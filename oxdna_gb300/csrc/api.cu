@@ -371,6 +371,7 @@ struct oxgb_md {
 	unsigned *bussi_done = nullptr;
 	long long *bussi_stamp = nullptr, *open_step = nullptr;
 	int *term_max = nullptr;
+	bool energies_fresh = false;  // F.w / T.w hold the energies of the current state
 
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -801,11 +802,20 @@ static int build_list_now(oxgb_md *h) {
 	return OXGB_OK;
 }
 
+// forces, torques and energies of the current state with the current lists
 static int compute_forces_now(oxgb_md *h, bool split) {
 	ForceArgs fa = force_args(h);
 	if(split) CK(cudaMemsetAsync(h->esplit, 0, sizeof(double) * 8 * h->n_systems, h->stream));
-	CK(launch_forces_split(fa, h->dbl, split, h->stream));
+	CK(launch_forces_split(fa, h->dbl, split, true, h->stream));
+	h->energies_fresh = true;
 	return OXGB_OK;
+}
+
+// the steps compute forces and torques only; the per-nucleotide energies (F.w, T.w) are made
+// on request from the same state and lists
+static int ensure_energies(oxgb_md *h) {
+	if(h->energies_fresh) return OXGB_OK;
+	return compute_forces_now(h, false);
 }
 
 static int read_status(oxgb_md *h) {
@@ -985,7 +995,7 @@ static int enqueue_step(oxgb_md *h, cudaGraph_t capturing, int k) {
 		CK(launch_list_build(la, h->stream));
 	}
 	ForceArgs fa = force_args(h, k, true);
-	CK(launch_forces_split(fa, h->dbl, false, h->stream));
+	CK(launch_forces_split(fa, h->dbl, false, false, h->stream));
 	CK(bussi_after_forces(h, sa));
 	return OXGB_OK;
 }
@@ -1032,6 +1042,7 @@ static int build_graph(oxgb_md *h) {
 
 extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 	if(!h || !h->have_state || nsteps < 0) return fail(OXGB_E_INVALID, "invalid call");
+	if(nsteps > 0) h->energies_fresh = false;
 	if(!h->gexec) {
 		int rc = build_graph(h);
 		if(rc) return rc;
@@ -1049,7 +1060,7 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 		ListArgs la = md_list_args(h, 1);
 		CK(launch_list_build(la, h->stream));
 		ForceArgs fa = force_args(h, 0, true);
-		CK(launch_forces_split(fa, h->dbl, false, h->stream));
+		CK(launch_forces_split(fa, h->dbl, false, false, h->stream));
 		CK(bussi_after_forces(h, sa));
 		CK(launch_step_advance(sa, 1, h->stream));
 	}
@@ -1082,6 +1093,10 @@ extern "C" int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *
 
 extern "C" int oxgb_md_get_forces(oxgb_md *h, double *F, double *T, double *E) {
 	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
+	if(E) {
+		int rc = ensure_energies(h);
+		if(rc) return rc;
+	}
 	CK(cudaStreamSynchronize(h->stream));
 	return download_forces(h, F, T, E);
 }
@@ -1113,6 +1128,10 @@ static int download_forces(oxgb_md *h, double *F, double *T, double *E) {
 
 extern "C" int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r) {
 	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
+	if(U) {
+		int rc = ensure_energies(h);
+		if(rc) return rc;
+	}
 	StepArgs sa = step_args(h);
 	CK(launch_system_sums(sa, h->n_chunks, h->dbl, h->sums, h->stream));
 	std::vector<double> c((size_t) 4 * h->n_chunks);

@@ -402,7 +402,7 @@ __device__ __forceinline__ void load_dh<SplitMixed, float>(const SplitMixed &ld,
 	ld.dh(j, n, h, l);
 }
 
-template <typename R, class Loader, bool SPLIT>
+template <typename R, class Loader, bool SPLIT, bool ENERGY>
 __global__ void __launch_bounds__(128) k_bonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	// one bond (owner p, partner q = n3[p]) per thread; the grid covers every nucleotide
@@ -424,7 +424,7 @@ __global__ void __launch_bounds__(128) k_bonded_split(ForceArgs a, Loader ld) {
 		BondOut<R> b;
 		if(!bonded_both(P, np, nq, ld.diff(ph, pl, qh, ql), b)) atomicOr(a.status, OXGB_ERR_FENE);
 		V4 f, tp, tq;
-		f.x = b.f.x, f.y = b.f.y, f.z = b.f.z, f.w = b.E;
+		f.x = b.f.x, f.y = b.f.y, f.z = b.f.z, f.w = ENERGY ? b.E : R(0);
 		tp.x = b.tp.x, tp.y = b.tp.y, tp.z = b.tp.z, tp.w = R(0);
 		tq.x = b.tq.x, tq.y = b.tq.y, tq.z = b.tq.z, tq.w = R(0);
 		reinterpret_cast<V4 *>(a.bond_f)[p] = f;
@@ -438,7 +438,10 @@ __global__ void __launch_bounds__(128) k_bonded_split(ForceArgs a, Loader ld) {
 	}
 }
 
-template <typename R, bool SPLIT>
+// per-lane compensated sums of a nucleotide's pair terms; ENERGY = false leaves the energies out
+// (an MD step needs only forces and torques: the energy arithmetic of the pair functions is then
+// dead code)
+template <typename R, bool SPLIT, bool ENERGY = true>
 struct SplitAcc {
 	KahanV<R> F, T;
 	R E, Ec, Eh, Ehc;
@@ -446,8 +449,10 @@ struct SplitAcc {
 	__device__ __forceinline__ void add(const PairOut<R> &o) {
 		F.add(o.F);
 		T.add(o.T);
-		KahanV<R>::kadd(E, Ec, o.E);
-		KahanV<R>::kadd(Eh, Ehc, o.Ehb);
+		if(ENERGY) {
+			KahanV<R>::kadd(E, Ec, o.E);
+			KahanV<R>::kadd(Eh, Ehc, o.Ehb);
+		}
 		if(SPLIT) {
 #pragma unroll
 			for(int k = 0; k < N_TERMS; k++) split[k] += o.split[k];
@@ -458,8 +463,10 @@ struct SplitAcc {
 	__device__ __forceinline__ void add_result(const V4 &f, const V4 &t) {
 		F.add(v3<R>{f.x, f.y, f.z});
 		T.add(v3<R>{t.x, t.y, t.z});
-		KahanV<R>::kadd(E, Ec, f.w);
-		KahanV<R>::kadd(Eh, Ehc, t.w);
+		if(ENERGY) {
+			KahanV<R>::kadd(E, Ec, f.w);
+			KahanV<R>::kadd(Eh, Ehc, t.w);
+		}
 	}
 };
 
@@ -471,7 +478,7 @@ struct SplitAcc {
 // run of consecutive nucleotides; a warp of slot k = 0 is nearly full, one past every list
 // length exits at once.  These are the costliest terms and their lists are short (a few
 // entries), so a slot per thread keeps the lanes busy where per-nucleotide lanes would idle.
-template <typename R, class Loader, bool SPLIT>
+template <typename R, class Loader, bool SPLIT, bool ENERGY>
 __global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int base_blocks, int n_pad) {
 	using V4 = typename Vec4Of<R>::T;
 	const bool is_base = (int) blockIdx.x < base_blocks;
@@ -498,8 +505,8 @@ __global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int 
 	if(is_base) pair_base<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
 	else pair_stack<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
 	V4 f, tq;
-	f.x = o.F.x, f.y = o.F.y, f.z = o.F.z, f.w = o.E;
-	tq.x = o.T.x, tq.y = o.T.y, tq.z = o.T.z, tq.w = o.Ehb;
+	f.x = o.F.x, f.y = o.F.y, f.z = o.F.z, f.w = ENERGY ? o.E : R(0);
+	tq.x = o.T.x, tq.y = o.T.y, tq.z = o.T.z, tq.w = ENERGY ? o.Ehb : R(0);
 	V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res) + 2 * ((long long) k * N + i);
 	res[0] = f;
 	res[1] = tq;
@@ -535,7 +542,7 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 #define OXGB_NB_MINB 6
 #endif
 
-template <typename R, class Loader, bool SPLIT, int K>
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int K>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonbonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	const long long N = a.N;
@@ -554,7 +561,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 		Nuc<R> p;
 		V4 ph, pl;
 		load_full<Loader, R>(ld, i, P, p, ph, pl);
-		SplitAcc<R, SPLIT> acc{};
+		SplitAcc<R, SPLIT, ENERGY> acc{};
 
 		// Debye-Hueckel over the full Verlet row
 		const int ndh = live ? min(a.nnb[i], a.max_nb) : 0;
@@ -600,13 +607,13 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 				const V4 f = bf[i], t = reinterpret_cast<const V4 *>(a.bond_tp)[i];
 				acc.F.add(v3<R>{-f.x, -f.y, -f.z});
 				acc.T.add(v3<R>{t.x, t.y, t.z});
-				KahanV<R>::kadd(acc.E, acc.Ec, f.w);
+				if(ENERGY) KahanV<R>::kadd(acc.E, acc.Ec, f.w);
 			}
 			if(bi.y >= 0) {
 				const V4 f = bf[bi.y], t = reinterpret_cast<const V4 *>(a.bond_tq)[bi.y];
 				acc.F.add(v3<R>{f.x, f.y, f.z});
 				acc.T.add(v3<R>{t.x, t.y, t.z});
-				KahanV<R>::kadd(acc.E, acc.Ec, f.w);
+				if(ENERGY) KahanV<R>::kadd(acc.E, acc.Ec, f.w);
 			}
 		}
 
@@ -614,7 +621,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 				fz = group_sum_comp<R, K>(acc.F.s.z, acc.F.c.z);
 		const v3<R> tl{group_sum_comp<R, K>(acc.T.s.x, acc.T.c.x), group_sum_comp<R, K>(acc.T.s.y, acc.T.c.y),
 				group_sum_comp<R, K>(acc.T.s.z, acc.T.c.z)};
-		const R e = group_sum_comp<R, K>(acc.E, acc.Ec), eh = group_sum_comp<R, K>(acc.Eh, acc.Ehc);
+		const R e = ENERGY ? group_sum_comp<R, K>(acc.E, acc.Ec) : R(0);
+		const R eh = ENERGY ? group_sum_comp<R, K>(acc.Eh, acc.Ehc) : R(0);
 		if(sub == 0 && live) {
 			V4 fo, to;
 			fo.x = fx;
@@ -641,32 +649,36 @@ int nonbonded_blocks(int N) {
 	return (int) ((threads + 127) / 128);
 }
 
-template <typename R, class Loader, bool SPLIT>
+template <typename R, class Loader, bool SPLIT, bool ENERGY>
 static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEvent_t wait) {
 	const int tpb = 128;
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	const size_t smem = sizeof(DNA2Table<R>) * (size_t) (a.tab_span > 0 ? a.tab_span : 1);
-	k_bonded_split<R, Loader, SPLIT><<<blocks, tpb, smem, s>>>(a, ld);
+	k_bonded_split<R, Loader, SPLIT, ENERGY><<<blocks, tpb, smem, s>>>(a, ld);
 	// slots numbered k * n_pad + i, n_pad a multiple of the block size
 	const int n_pad = ((a.N + tpb - 1) / tpb) * tpb;
 	const int base_blocks = (int) (((long long) a.base_cap * n_pad) / tpb);
 	const int stk_blocks = (int) (((long long) a.stk_cap * n_pad) / tpb);
-	k_pair_slots<R, Loader, SPLIT><<<base_blocks + stk_blocks, tpb, smem, s>>>(a, ld, base_blocks, n_pad);
+	k_pair_slots<R, Loader, SPLIT, ENERGY><<<base_blocks + stk_blocks, tpb, smem, s>>>(a, ld, base_blocks, n_pad);
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
-	k_nonbonded_split<R, Loader, SPLIT, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
+	k_nonbonded_split<R, Loader, SPLIT, ENERGY, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
+}
+
+template <typename R, class Loader, bool SPLIT, bool ENERGY>
+static cudaError_t allow_smem_t(int bytes) {
+	cudaError_t e = cudaFuncSetAttribute(k_bonded_split<R, Loader, SPLIT, ENERGY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	if(e == cudaSuccess)
+		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, SPLIT, ENERGY, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_pair_slots<R, Loader, SPLIT, ENERGY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	return e;
 }
 
 template <typename R, class Loader>
 static cudaError_t allow_smem(int bytes) {
-	cudaError_t e = cudaFuncSetAttribute(k_bonded_split<R, Loader, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_bonded_split<R, Loader, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-	if(e == cudaSuccess)
-		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, false, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-	if(e == cudaSuccess)
-		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, true, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_pair_slots<R, Loader, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_pair_slots<R, Loader, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaError_t e = allow_smem_t<R, Loader, true, true>(bytes);
+	if(e == cudaSuccess) e = allow_smem_t<R, Loader, false, true>(bytes);
+	if(e == cudaSuccess) e = allow_smem_t<R, Loader, false, false>(bytes);
 	return e;
 }
 
@@ -676,16 +688,18 @@ int set_forces_smem(bool dbl, size_t bytes) {
 	return (dbl ? allow_smem<double, SplitDouble>((int) bytes) : allow_smem<float, SplitMixed>((int) bytes)) != cudaSuccess;
 }
 
-cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, cudaStream_t s, cudaEvent_t wait) {
+cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool energy, cudaStream_t s, cudaEvent_t wait) {
 	if(dbl) {
 		SplitDouble ld{a.posd, a.quatd, a.pos_hi, a.pos_lo, a.bonds};
-		if(split) launch_split_t<double, SplitDouble, true>(a, ld, s, wait);
-		else launch_split_t<double, SplitDouble, false>(a, ld, s, wait);
+		if(split) launch_split_t<double, SplitDouble, true, true>(a, ld, s, wait);
+		else if(energy) launch_split_t<double, SplitDouble, false, true>(a, ld, s, wait);
+		else launch_split_t<double, SplitDouble, false, false>(a, ld, s, wait);
 	}
 	else {
 		SplitMixed ld{a.pos_hi, a.pos_lo, a.fa1, a.fa3, a.fback};
-		if(split) launch_split_t<float, SplitMixed, true>(a, ld, s, wait);
-		else launch_split_t<float, SplitMixed, false>(a, ld, s, wait);
+		if(split) launch_split_t<float, SplitMixed, true, true>(a, ld, s, wait);
+		else if(energy) launch_split_t<float, SplitMixed, false, true>(a, ld, s, wait);
+		else launch_split_t<float, SplitMixed, false, false>(a, ld, s, wait);
 	}
 	return cudaGetLastError();
 }

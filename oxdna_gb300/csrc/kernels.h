@@ -86,7 +86,9 @@ cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
 // split path: bonded pairs (one thread per bond, both sides), then non-bonded terms (one
 // thread per nucleotide, one loop per term list) with the bonded results gathered in its epilogue
 // wait: an event the non-bonded kernel waits for, or null
-cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, cudaStream_t s, cudaEvent_t wait = nullptr);
+// energy = false: forces and torques only (w of F and T left 0), what an MD step needs
+cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool energy, cudaStream_t s,
+		cudaEvent_t wait = nullptr);
 // blocks of the split non-bonded kernel for N nucleotides
 int nonbonded_blocks(int N);
 // lets the split kernels use `bytes` of dynamic shared memory (per-block system tables);
