@@ -60,6 +60,23 @@ struct Sep {
 	OXGB_HD v3<R> plain() const { return hi + lo; }
 };
 
+// a * b - c * d from error-free products (Kahan's algorithm: within 1.5 ulp of the exact value)
+template <typename R>
+OXGB_HD R diff_of_products(R a, R b, R c, R d) {
+	const R w = c * d;
+	const R e = m_fma(-c, d, w);
+	const R f = m_fma(a, b, -w);
+	return f + e;
+}
+
+// (hi + lo) x b, the hi part with accurate 2x2 differences
+template <typename R>
+OXGB_HD v3<R> cross_accurate(const Sep<R> &a, const v3<R> &b) {
+	const v3<R> h{diff_of_products(a.hi.y, b.z, a.hi.z, b.y), diff_of_products(a.hi.z, b.x, a.hi.x, b.z),
+			diff_of_products(a.hi.x, b.y, a.hi.y, b.x)};
+	return h + cross(a.lo, b);
+}
+
 template <typename R>
 OXGB_HD void two_sum(R a, R b, R &s, R &e) {
 	s = a + b;

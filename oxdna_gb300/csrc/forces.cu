@@ -458,14 +458,32 @@ struct SplitAcc {
 			for(int k = 0; k < N_TERMS; k++) split[k] += o.split[k];
 		}
 	}
-	// a pair result of k_pair_slots: (force, energy) and (torque, hydrogen-bonding energy)
+	// entry k of nucleotide i's list, evaluated by k_pair_slots in the slot of the lower
+	// nucleotide: its own (force, torque) or, from the partner's slot, (-force, partner torque)
 	template <typename V4>
-	__device__ __forceinline__ void add_result(const V4 &f, const V4 &t) {
-		F.add(v3<R>{f.x, f.y, f.z});
-		T.add(v3<R>{t.x, t.y, t.z});
-		if(ENERGY) {
-			KahanV<R>::kadd(E, Ec, f.w);
-			KahanV<R>::kadd(Eh, Ehc, t.w);
+	__device__ __forceinline__ void add_slot(const int *nb, const int *rev, const V4 *res, long long N, int i, int k) {
+		const long long s = (long long) k * N + i;
+		const int j = nb[s];
+		if(j > i) {
+			const V4 f = res[3 * s], t = res[3 * s + 1];
+			F.add(v3<R>{f.x, f.y, f.z});
+			T.add(v3<R>{t.x, t.y, t.z});
+			if(ENERGY) {
+				KahanV<R>::kadd(E, Ec, f.w);
+				KahanV<R>::kadd(Eh, Ehc, t.w);
+			}
+		}
+		else {
+			const int m = rev[s];
+			if(m < 0) return;  // flagged by the list build
+			const long long sj = (long long) m * N + j;
+			const V4 f = res[3 * sj], ti = res[3 * sj + 1], t = res[3 * sj + 2];
+			F.add(v3<R>{-f.x, -f.y, -f.z});
+			T.add(v3<R>{t.x, t.y, t.z});
+			if(ENERGY) {
+				KahanV<R>::kadd(E, Ec, f.w);
+				KahanV<R>::kadd(Eh, Ehc, ti.w);
+			}
 		}
 	}
 };
@@ -495,25 +513,32 @@ __global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int 
 	const int n = is_base ? min(a.base_n[i], a.base_cap) : min(a.stk_n[i], a.stk_cap);
 	if(k >= n) return;
 	const int j = (is_base ? a.base_nb : a.stk_nb)[(long long) k * N + i];
+	if(j < i) return;  // evaluated in the slot of j
 	const int sy = a.sys ? a.sys[i] : 0;
 	const DNA2Table<R> &P = Ps[sy - s0];
 	Nuc<R> p, q;
 	V4 ph, pl, qh, ql;
 	load_full<Loader, R>(ld, i, P, p, ph, pl);
 	load_full<Loader, R>(ld, j, P, q, qh, ql);
+	const Sep<R> d = ld.sep(ph, pl, qh, ql, P);
 	PairOut<R> o{};
-	if(is_base) pair_base<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
-	else pair_stack<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P), o);
-	V4 f, tq;
+	if(is_base) pair_base<R, SPLIT>(P, p, q, d, o);
+	else pair_stack<R, SPLIT>(P, p, q, d, o);
+	// the potential is invariant under rigid rotations, so the torques balance:
+	// T_j = -T_i + (r_j - r_i) x F_i, the cross product with error-free products
+	const v3<R> c = cross_accurate(d, o.F);
+	V4 f, ti, tj;
 	f.x = o.F.x, f.y = o.F.y, f.z = o.F.z, f.w = ENERGY ? o.E : R(0);
-	tq.x = o.T.x, tq.y = o.T.y, tq.z = o.T.z, tq.w = ENERGY ? o.Ehb : R(0);
-	V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res) + 2 * ((long long) k * N + i);
+	ti.x = o.T.x, ti.y = o.T.y, ti.z = o.T.z, ti.w = ENERGY ? o.Ehb : R(0);
+	tj.x = c.x - o.T.x, tj.y = c.y - o.T.y, tj.z = c.z - o.T.z, tj.w = R(0);
+	V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res) + 3 * ((long long) k * N + i);
 	res[0] = f;
-	res[1] = tq;
+	res[1] = ti;
+	res[2] = tj;
 	if(SPLIT) {
 #pragma unroll
 		for(int m = 0; m < N_TERMS; m++)
-			if(o.split[m] != R(0)) atomicAdd(a.esplit + 8 * sy + m, 0.5 * (double) o.split[m]);
+			if(o.split[m] != R(0)) atomicAdd(a.esplit + 8 * sy + m, (double) o.split[m]);
 	}
 }
 
@@ -588,11 +613,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 		// hydrogen bonding + cross stacking and coaxial stacking: evaluated per list slot by
 		// k_pair_slots, gathered here
 		const int nb_ = live ? min(a.base_n[i], a.base_cap) : 0;
-		for(int k = sub; k < nb_; k += K) acc.add_result(reinterpret_cast<const V4 *>(a.base_res)[2 * ((long long) k * N + i)],
-				reinterpret_cast<const V4 *>(a.base_res)[2 * ((long long) k * N + i) + 1]);
+		for(int k = sub; k < nb_; k += K) acc.add_slot(a.base_nb, a.base_rev, reinterpret_cast<const V4 *>(a.base_res), N, i, k);
 		const int ns = live ? min(a.stk_n[i], a.stk_cap) : 0;
-		for(int k = sub; k < ns; k += K) acc.add_result(reinterpret_cast<const V4 *>(a.stk_res)[2 * ((long long) k * N + i)],
-				reinterpret_cast<const V4 *>(a.stk_res)[2 * ((long long) k * N + i) + 1]);
+		for(int k = sub; k < ns; k += K) acc.add_slot(a.stk_nb, a.stk_rev, reinterpret_cast<const V4 *>(a.stk_res), N, i, k);
 		if(SPLIT && live) {
 #pragma unroll
 			for(int k = 0; k < N_TERMS; k++)

@@ -332,9 +332,9 @@ __global__ void k_set_conditional(const int *flag, cudaGraphConditionalHandle h)
 static inline int blocks_for(int N, int tpb) { return N > 0 ? (N + tpb - 1) / tpb : 1; }
 
 cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s) {
-	// small blocks: the FP64 work (1/64 of the FP32 rate) spreads evenly over the SMs
-	if(double_forces) k_first_step<double4_32a><<<blocks_for(a.N, 64), 64, 0, s>>>(a);
-	else k_first_step<float4><<<blocks_for(a.N, 64), 64, 0, s>>>(a);
+	// one-warp blocks: the FP64 work (1/64 of the FP32 rate) spreads evenly over the SMs
+	if(double_forces) k_first_step<double4_32a><<<blocks_for(a.N, 32), 32, 0, s>>>(a);
+	else k_first_step<float4><<<blocks_for(a.N, 32), 32, 0, s>>>(a);
 	return cudaGetLastError();
 }
 
