@@ -371,7 +371,6 @@ struct oxgb_md {
 	int *status = nullptr, *flag = nullptr;
 	long long *step = nullptr;
 	double *esplit = nullptr, *sums = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
-	unsigned *bussi_done = nullptr;
 	long long *bussi_stamp = nullptr, *open_step = nullptr;
 	int *term_max = nullptr;
 	bool energies_fresh = false;  // F.w / T.w hold the energies of the current state
@@ -400,7 +399,7 @@ struct oxgb_md {
 					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
-					(void *) bussi_done, (void *) bussi_stamp, (void *) open_step, (void *) term_max, (void *) d_rebuilds})
+					(void *) bussi_stamp, (void *) open_step, (void *) term_max, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -430,7 +429,6 @@ static ThermoArgs thermo_args(oxgb_md *h, int step_offset = 0, bool engine_step 
 	t.sys_chunk0 = h->d_sys_chunk0;
 	t.bussi_partials = h->bussi_partials;
 	t.bussi_state = h->bussi_state;
-	t.done = h->bussi_done;
 	t.bussi_stamp = h->bussi_stamp;
 	t.open_step = engine_step ? h->open_step : nullptr;
 	t.step_base = h->step;
@@ -699,7 +697,6 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->sums, sizeof(double) * 4 * h->n_chunks) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * h->n_chunks) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16 * n_systems) == cudaSuccess;
-	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned) * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->open_step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
@@ -717,7 +714,6 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMemset(h->flag, 0, sizeof(int)) == cudaSuccess;
 	ok &= cudaMemset(h->step, 0, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMemset(h->d_rebuilds, 0, sizeof(unsigned long long)) == cudaSuccess;
-	ok &= cudaMemset(h->bussi_done, 0, sizeof(unsigned) * n_systems) == cudaSuccess;
 	if(!ok) return bail(fail(OXGB_E_CUDA, "upload"));
 	if(clear_pending(h)) return bail(fail(OXGB_E_CUDA, "upload"));
 	int rc = upload_systems(h, 0, n_systems);
@@ -854,7 +850,9 @@ static int size_and_build_list(oxgb_md *h) {
 		const int m = *std::max_element(v.begin(), v.end());
 		return ((std::max(16, m + m / 2 + 8) + 7) / 8) * 8;
 	};
-	const int we = cap_of(ce), wb = cap_of(cb), ws = cap_of(cs);
+	// base / stack rows at most 64 long (the pair kernel keeps a row's owned entries in a 64-bit
+	// mask; physically a nucleotide has a handful)
+	const int we = cap_of(ce), wb = std::min(64, cap_of(cb)), ws = std::min(64, cap_of(cs));
 	if(we != h->tl.ev_cap || wb != h->tl.base_cap || ws != h->tl.stk_cap) {
 		if(h->gexec) {
 			cudaGraphExecDestroy(h->gexec);

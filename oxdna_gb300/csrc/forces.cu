@@ -488,57 +488,89 @@ struct SplitAcc {
 	}
 };
 
-// One thread per slot of the base-base list (blocks 0 .. base_blocks - 1) or of the stack-stack
-// list (the rest): slot k of nucleotide i evaluates hydrogen bonding + cross stacking, or coaxial
-// stacking, for the pair (i, base_nb / stk_nb[k * N + i]) and stores (force, energy) and (torque
-// on i, HB energy) at [2 (k * N + i)] and [2 (k * N + i) + 1] of base_res / stk_res.  Slots are
-// numbered k * n_pad + i with n_pad a multiple of the block size, so a block holds one k and a
-// run of consecutive nucleotides; a warp of slot k = 0 is nearly full, one past every list
-// length exits at once.  These are the costliest terms and their lists are short (a few
-// entries), so a slot per thread keeps the lanes busy where per-nucleotide lanes would idle.
+// Base-base pairs (hydrogen bonding + cross stacking; blocks 0 .. base_blocks - 1) and
+// stack-stack pairs (coaxial stacking; the other blocks), each evaluated once, in the slot of
+// its lower nucleotide i (partner j > i): slot k of i stores (force on i, E), (torque on i,
+// E_hb) and (torque on j, 0) at [3 (k N + i) + 0..2] of base_res / stk_res.  These are the
+// costliest terms and their lists are short, so the owned slots of a warp's 32 nucleotides
+// are queued (a warp prefix sum over the per-lane counts) and dealt 32 at a time: every lane
+// works on a pair in every round but the last.
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
-__global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int base_blocks, int n_pad) {
+__global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int base_blocks) {
 	using V4 = typename Vec4Of<R>::T;
 	const bool is_base = (int) blockIdx.x < base_blocks;
-	const long long t = (long long) (is_base ? blockIdx.x : blockIdx.x - base_blocks) * blockDim.x + threadIdx.x;
-	const int k = (int) (t / n_pad), i = (int) (t % n_pad);
-	const int first = (int) ((t - threadIdx.x) % n_pad);
-	if(first >= a.N) return;  // block-uniform: the padding past the last nucleotide
-	// block-uniform: slot k is past every list of this term (no table load, no pair)
-	if(a.term_max && k >= min(a.term_max[is_base ? 1 : 2], is_base ? a.base_cap : a.stk_cap)) return;
+	const int first = (is_base ? blockIdx.x : blockIdx.x - base_blocks) * blockDim.x;
 	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
 	const int s0 = load_table_span<R>(a, first, min(first + (int) blockDim.x, a.N) - 1, Ps);
-	if(i >= a.N) return;
 	const long long N = a.N;
-	const int n = is_base ? min(a.base_n[i], a.base_cap) : min(a.stk_n[i], a.stk_cap);
-	if(k >= n) return;
-	const int j = (is_base ? a.base_nb : a.stk_nb)[(long long) k * N + i];
-	if(j < i) return;  // evaluated in the slot of j
-	const int sy = a.sys ? a.sys[i] : 0;
-	const DNA2Table<R> &P = Ps[sy - s0];
-	Nuc<R> p, q;
-	V4 ph, pl, qh, ql;
-	load_full<Loader, R>(ld, i, P, p, ph, pl);
-	load_full<Loader, R>(ld, j, P, q, qh, ql);
-	const Sep<R> d = ld.sep(ph, pl, qh, ql, P);
-	PairOut<R> o{};
-	if(is_base) pair_base<R, SPLIT>(P, p, q, d, o);
-	else pair_stack<R, SPLIT>(P, p, q, d, o);
-	// the potential is invariant under rigid rotations, so the torques balance:
-	// T_j = -T_i + (r_j - r_i) x F_i, the cross product with error-free products
-	const v3<R> c = cross_accurate(d, o.F);
-	V4 f, ti, tj;
-	f.x = o.F.x, f.y = o.F.y, f.z = o.F.z, f.w = ENERGY ? o.E : R(0);
-	ti.x = o.T.x, ti.y = o.T.y, ti.z = o.T.z, ti.w = ENERGY ? o.Ehb : R(0);
-	tj.x = c.x - o.T.x, tj.y = c.y - o.T.y, tj.z = c.z - o.T.z, tj.w = R(0);
-	V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res) + 3 * ((long long) k * N + i);
-	res[0] = f;
-	res[1] = ti;
-	res[2] = tj;
-	if(SPLIT) {
+	const int lane = threadIdx.x & 31;
+	const int wbase = first + (threadIdx.x & ~31);
+	if(wbase >= a.N) return;  // warp-uniform
+	const int cap = is_base ? a.base_cap : a.stk_cap;
+	const int *nb = is_base ? a.base_nb : a.stk_nb;
+	// this lane's nucleotide: which of its entries it owns (partner above it), as a bit mask
+	const int il = wbase + lane;
+	unsigned lo = 0u, hi = 0u;
+	if(il < a.N) {
+		const int n = min(min(is_base ? a.base_n[il] : a.stk_n[il], cap), 64);
+		for(int k = 0; k < n; k++)
+			if(nb[(long long) k * N + il] > il) {
+				if(k < 32) lo |= 1u << k;
+				else hi |= 1u << (k - 32);
+			}
+	}
+	const int own = __popc(lo) + __popc(hi);
+	int incl = own;
 #pragma unroll
-		for(int m = 0; m < N_TERMS; m++)
-			if(o.split[m] != R(0)) atomicAdd(a.esplit + 8 * sy + m, (double) o.split[m]);
+	for(int off = 1; off < 32; off <<= 1) {
+		const int u = __shfl_up_sync(0xffffffffu, incl, off);
+		if(lane >= off) incl += u;
+	}
+	const int total = __shfl_sync(0xffffffffu, incl, 31);
+	const int excl = incl - own;
+	for(int q0 = 0; q0 < total; q0 += 32) {
+		const int q = q0 + lane;
+		// the lane that owns queue entry q: the first whose inclusive count exceeds q
+		int l = 0;
+#pragma unroll
+		for(int step = 16; step > 0; step >>= 1) {
+			const int v = __shfl_sync(0xffffffffu, incl, l + step - 1);
+			if(v <= q) l += step;
+		}
+		const int ex_l = __shfl_sync(0xffffffffu, excl, l & 31);
+		const unsigned lo_l = __shfl_sync(0xffffffffu, lo, l & 31), hi_l = __shfl_sync(0xffffffffu, hi, l & 31);
+		if(q >= total) continue;
+		// the r-th owned entry of nucleotide i
+		const int r = q - ex_l, nlo = __popc(lo_l);
+		const int k = r < nlo ? (int) __fns(lo_l, 0u, r + 1) : 32 + (int) __fns(hi_l, 0u, r - nlo + 1);
+		const int i = wbase + l;
+		const int j = nb[(long long) k * N + i];
+		const int sy = a.sys ? a.sys[i] : 0;
+		const DNA2Table<R> &P = Ps[sy - s0];
+		Nuc<R> p, qn;
+		V4 ph, pl, qh, ql;
+		load_full<Loader, R>(ld, i, P, p, ph, pl);
+		load_full<Loader, R>(ld, j, P, qn, qh, ql);
+		const Sep<R> d = ld.sep(ph, pl, qh, ql, P);
+		PairOut<R> o{};
+		if(is_base) pair_base<R, SPLIT>(P, p, qn, d, o);
+		else pair_stack<R, SPLIT>(P, p, qn, d, o);
+		// the potential is invariant under rigid rotations, so the torques balance:
+		// T_j = -T_i + (r_j - r_i) x F_i, the cross product with error-free products
+		const v3<R> c = cross_accurate(d, o.F);
+		V4 f, ti, tj;
+		f.x = o.F.x, f.y = o.F.y, f.z = o.F.z, f.w = ENERGY ? o.E : R(0);
+		ti.x = o.T.x, ti.y = o.T.y, ti.z = o.T.z, ti.w = ENERGY ? o.Ehb : R(0);
+		tj.x = c.x - o.T.x, tj.y = c.y - o.T.y, tj.z = c.z - o.T.z, tj.w = R(0);
+		V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res) + 3 * ((long long) k * N + i);
+		res[0] = f;
+		res[1] = ti;
+		res[2] = tj;
+		if(SPLIT) {
+#pragma unroll
+			for(int m = 0; m < N_TERMS; m++)
+				if(o.split[m] != R(0)) atomicAdd(a.esplit + 8 * sy + m, (double) o.split[m]);
+		}
 	}
 }
 
@@ -678,11 +710,8 @@ static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEv
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	const size_t smem = sizeof(DNA2Table<R>) * (size_t) (a.tab_span > 0 ? a.tab_span : 1);
 	k_bonded_split<R, Loader, SPLIT, ENERGY><<<blocks, tpb, smem, s>>>(a, ld);
-	// slots numbered k * n_pad + i, n_pad a multiple of the block size
-	const int n_pad = ((a.N + tpb - 1) / tpb) * tpb;
-	const int base_blocks = (int) (((long long) a.base_cap * n_pad) / tpb);
-	const int stk_blocks = (int) (((long long) a.stk_cap * n_pad) / tpb);
-	k_pair_slots<R, Loader, SPLIT, ENERGY><<<base_blocks + stk_blocks, tpb, smem, s>>>(a, ld, base_blocks, n_pad);
+	// one block of 128 nucleotides per term
+	k_pair_slots<R, Loader, SPLIT, ENERGY><<<2 * blocks, tpb, smem, s>>>(a, ld, blocks);
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
 	k_nonbonded_split<R, Loader, SPLIT, ENERGY, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);

@@ -11,8 +11,8 @@
 // update runs on the device (its gamma deviate uses the same algorithm as the reference).
 // The second half kick of a step and its thermostat are deferred to the next first step (or
 // to the flush at the end of a run), where they run one thread per nucleotide next to the
-// first half kick; the Bussi sums run after the forces (k_bussi_reduce) and its draws on a
-// parallel branch of the step graph (k_bussi_noise).  No FP64 work is left in the force
+// first half kick; the Bussi sums run after the forces (k_bussi_sums, k_bussi_update) and its
+// draws on a parallel branch of the step graph (k_bussi_noise).  No FP64 work is left in the force
 // kernels, whose lanes are mostly idle at the epilogue.
 #include "thermo.cuh"
 
@@ -177,19 +177,15 @@ __global__ void k_bussi_noise(StepArgs a) {
 
 // Bussi step s, after its forces: sums of v, |v|^2 and |L|^2 over the completed velocities
 // v + dt/2 F (computed here, stored by the next first step), one block per chunk of up to 256
-// nucleotides of one system; the last chunk of a system to finish reduces that system's chunk
-// sums in a fixed order (deterministic) and makes its update
+// nucleotides of one system
 template <typename V4>
-__global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
+__global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 	const long long s = step_of(a.th);
 	if(s % a.th.newtonian_steps != 0) return;
 	const int c = blockIdx.x;
 	const int sy = a.th.chunk_sys[c];
 	const int i = a.th.chunk_first[c] + threadIdx.x;
 	const double hdt = 0.5 * a.dt;
-	// the next first step applies the rescaling of step s (every system updates at the same
-	// steps, and no kernel of this launch reads the mark)
-	if(c == 0 && threadIdx.x == 0) *a.th.bussi_stamp = s;
 	double acc[5] = {0, 0, 0, 0, 0};
 	if(i < a.th.sys_off[sy + 1]) {
 		const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
@@ -208,7 +204,6 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 		acc[4] = L.x * L.x + L.y * L.y + L.z * L.z;
 	}
 	__shared__ double red[5][8];
-	__shared__ bool last;
 	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
 	for(int k = 0; k < 5; k++) {
@@ -221,18 +216,24 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 		double x = 0;
 		for(int u = 0; u < nw; u++) x += red[threadIdx.x][u];
 		a.th.bussi_partials[c * 8 + threadIdx.x] = x;
-		__threadfence();
 	}
-	__syncthreads();
+}
+
+// the update of system blockIdx.x: its chunk sums reduced in a fixed order (deterministic),
+// translation on thread 0 and rotation on thread 32 (two warps: the chains overlap)
+__global__ void __launch_bounds__(256) k_bussi_update(StepArgs a) {
+	const long long s = step_of(a.th);
+	if(s % a.th.newtonian_steps != 0) return;
+	const int sy = blockIdx.x;
+	// the next first step applies the rescaling of step s (every system updates at the same steps)
+	if(sy == 0 && threadIdx.x == 0) *a.th.bussi_stamp = s;
 	const int c0 = a.th.sys_chunk0[sy], nc = a.th.sys_chunk0[sy + 1] - c0;
-	if(threadIdx.x == 0) last = atomicAdd(a.th.done + sy, 1u) == (unsigned) (nc - 1);
-	__syncthreads();
-	if(!last) return;
-	__threadfence();
 	double part[5] = {0, 0, 0, 0, 0};
 	for(int b = threadIdx.x; b < nc; b += blockDim.x)
 #pragma unroll
-		for(int k = 0; k < 5; k++) part[k] += __ldcg(a.th.bussi_partials + (c0 + b) * 8 + k);
+		for(int k = 0; k < 5; k++) part[k] += a.th.bussi_partials[(c0 + b) * 8 + k];
+	__shared__ double red[5][8];
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
 	for(int k = 0; k < 5; k++) {
 		double x = part[k];
@@ -240,7 +241,6 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 		if(lane == 0) red[k][w] = x;
 	}
 	__syncthreads();
-	// translation on thread 0, rotation on thread 32 (another warp: the two chains overlap)
 	if(threadIdx.x != 0 && threadIdx.x != 32) return;
 	double sum[5];
 	for(int k = 0; k < 5; k++) {
@@ -249,7 +249,6 @@ __global__ void __launch_bounds__(256) k_bussi_reduce(StepArgs a) {
 		sum[k] = x;
 	}
 	bussi_update(a.th, sy, s, threadIdx.x == 0 ? 0 : 1, sum);
-	if(threadIdx.x == 0) a.th.done[sy] = 0;
 }
 
 __global__ void k_step_advance(StepArgs a, int K) {
@@ -344,8 +343,9 @@ cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s) {
-	if(double_forces) k_bussi_reduce<double4_32a><<<n_chunks, 256, 0, s>>>(a);
-	else k_bussi_reduce<float4><<<n_chunks, 256, 0, s>>>(a);
+	if(double_forces) k_bussi_sums<double4_32a><<<n_chunks, 256, 0, s>>>(a);
+	else k_bussi_sums<float4><<<n_chunks, 256, 0, s>>>(a);
+	k_bussi_update<<<a.th.n_systems, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

@@ -316,31 +316,32 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 }
 
 // For every base / stack list entry (k, i) with partner j < i: where i sits in j's list (the
-// lists are symmetric: the pair criteria are exactly symmetric in FP32).  One thread per slot,
-// numbered k * n_pad + i as in the pair kernels.
-__global__ void k_term_rev(ListArgs a, int base_blocks, int n_pad) {
+// lists are symmetric: the pair criteria are exactly symmetric in FP32).  One thread per
+// nucleotide and term (blocks 0 .. base_blocks - 1: base lists).
+__global__ void k_term_rev(ListArgs a, int base_blocks) {
 	SKIP_IF_FRESH(a);
 	const bool is_base = (int) blockIdx.x < base_blocks;
-	const long long t = (long long) (is_base ? blockIdx.x : blockIdx.x - base_blocks) * blockDim.x + threadIdx.x;
-	const int k = (int) (t / n_pad), i = (int) (t % n_pad);
+	const int i = (is_base ? blockIdx.x : blockIdx.x - base_blocks) * blockDim.x + threadIdx.x;
 	if(i >= a.N || !rebuilt(a, sys_of(a, i))) return;
 	const long long N = a.N;
 	const int cap = is_base ? a.base_cap : a.stk_cap;
 	const int *nb = is_base ? a.base_nb : a.stk_nb;
+	int *rev = is_base ? a.base_rev : a.stk_rev;
 	const int n = min(is_base ? a.base_n[i] : a.stk_n[i], cap);
-	if(k >= n) return;
-	const int j = nb[(long long) k * N + i];
-	int r = -1;
-	if(j < i) {
-		const int nj = min(is_base ? a.base_n[j] : a.stk_n[j], cap);
-		for(int m = 0; m < nj; m++)
-			if(nb[(long long) m * N + j] == i) {
-				r = m;
-				break;
-			}
-		if(r < 0) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);  // an asymmetric (overflowed) list
+	for(int k = 0; k < n; k++) {
+		const int j = nb[(long long) k * N + i];
+		int r = -1;
+		if(j < i) {
+			const int nj = min(is_base ? a.base_n[j] : a.stk_n[j], cap);
+			for(int m = 0; m < nj; m++)
+				if(nb[(long long) m * N + j] == i) {
+					r = m;
+					break;
+				}
+			if(r < 0) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);  // an asymmetric (overflowed) list
+		}
+		rev[(long long) k * N + i] = r;
 	}
-	(is_base ? a.base_rev : a.stk_rev)[(long long) k * N + i] = r;
 }
 
 // runs after every other list kernel: counts the build and clears the requests
@@ -370,12 +371,7 @@ cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s) {
 	k_cell_rank<<<gp, tpb, 0, s>>>(a);
 	const long long warps = (long long) a.N * 32;
 	k_neighbours<<<(int) ((warps + tpb - 1) / tpb), tpb, 0, s>>>(a);
-	if(a.base_rev && a.stk_rev) {
-		const int n_pad = ((a.N + tpb - 1) / tpb) * tpb;
-		const int base_blocks = (int) (((long long) a.base_cap * n_pad) / tpb);
-		const int stk_blocks = (int) (((long long) a.stk_cap * n_pad) / tpb);
-		k_term_rev<<<base_blocks + stk_blocks, tpb, 0, s>>>(a, base_blocks, n_pad);
-	}
+	if(a.base_rev && a.stk_rev) k_term_rev<<<2 * gp, tpb, 0, s>>>(a, gp);
 	k_list_done<<<1, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
