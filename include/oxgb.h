@@ -201,10 +201,11 @@ int oxgb_md_run(oxgb_md *h, int nsteps, int sync);
  * volume, stacking, non-bonded excluded volume, hydrogen bonding, cross stacking, coaxial
  * stacking, Debye-Hueckel).  Any output pointer may be NULL. */
 int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *E, double *E_split);
-/* forces, torques and per-nucleotide energies of the current state; the download half of
- * apply_simulation_data_changes.  The MD steps compute forces and torques only: when E is asked
- * for after a run, the energies are evaluated once from the current state and lists (the forces
- * and torques of that evaluation are the same numbers). */
+/* forces and torques the dynamics uses (those of the last step, or of the last state upload)
+ * and per-nucleotide energies of the current state; the download half of
+ * apply_simulation_data_changes.  The MD steps compute forces and torques only: E is evaluated
+ * on request from the current state and lists, in separate buffers, so asking for it never
+ * changes a trajectory. */
 int oxgb_md_get_forces(oxgb_md *h, double *F, double *T, double *E);
 /* per-system potential energy (FP64 sum of the per-nucleotide energies / 2, evaluated on
  * request as for oxgb_md_get_forces) and the translational and rotational kinetic energies,
@@ -229,8 +230,9 @@ int oxgb_md_status(oxgb_md *h);
 int oxgb_md_device_buffers(oxgb_md *h, void **pos, void **vel, void **L, void **quat, void **F, void **T);
 /* the CUDA stream all of the engine's work runs on */
 void *oxgb_md_stream(oxgb_md *h);
-/* enqueues one force evaluation on the engine's current buffers and lists, device only (the
- * engine-side equivalent of CUDABaseInteraction::compute_forces; used to time the kernel) */
+/* enqueues one force and energy evaluation of the current state and lists, device only, into
+ * the engine's evaluation buffers (the forces the dynamics uses are left alone): the engine-side
+ * equivalent of CUDABaseInteraction::compute_forces, used to time the kernels */
 int oxgb_md_launch_forces(oxgb_md *h);
 
 /* ------------------------------------------------------------------ diagnostics */

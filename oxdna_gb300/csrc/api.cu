@@ -359,6 +359,7 @@ struct oxgb_md {
 	float4 *list_a1 = nullptr, *list_back = nullptr;
 	int2 *bonds = nullptr;
 	void *F = nullptr, *T = nullptr, *bond_f = nullptr, *bond_tp = nullptr, *bond_tq = nullptr;
+	void *Fe = nullptr, *Te = nullptr;    // forces with energies (w), evaluated on request
 	void *d_tab = nullptr;                // one table per system
 	int *d_sys = nullptr, *d_sys_off = nullptr, *d_sys_nside = nullptr, *d_sys_cell0 = nullptr, *d_cell_sys = nullptr;
 	int *d_sys_stale = nullptr, *d_chunk_sys = nullptr, *d_chunk_first = nullptr, *d_sys_chunk0 = nullptr;
@@ -373,7 +374,7 @@ struct oxgb_md {
 	double *esplit = nullptr, *sums = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
 	long long *bussi_stamp = nullptr, *open_step = nullptr;
 	int *term_max = nullptr;
-	bool energies_fresh = false;  // F.w / T.w hold the energies of the current state
+	bool energies_fresh = false;  // Fe / Te hold the forces and energies of the current state
 
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -395,7 +396,7 @@ struct oxgb_md {
 		if(gexec) cudaGraphExecDestroy(gexec);
 		free_layout();
 		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
-					(void *) fback, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, bond_f,
+					(void *) fback, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, Fe, Te, bond_f,
 					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
@@ -464,7 +465,9 @@ static StepArgs step_args(oxgb_md *h, int step_offset = 0) {
 	return a;
 }
 
-static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = false) {
+// energy_buffers: results into Fe / Te (an evaluation with energies, which leaves the forces the
+// dynamics uses untouched)
+static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = false, bool energy_buffers = false) {
 	ForceArgs a{};
 	a.N = h->N;
 	a.pos_hi = h->pos_hi;
@@ -479,8 +482,8 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.max_nb = h->lb.max_nb;
 	a.nb_stride_i = 1;  // the engine's rows are column-major
 	a.nb_stride_k = h->N;
-	a.forces = h->F;
-	a.torques = h->T;
+	a.forces = energy_buffers ? h->Fe : h->F;
+	a.torques = energy_buffers ? h->Te : h->T;
 	a.table = h->d_tab;
 	a.sys = h->d_sys;
 	a.tab_span = h->tab_span;
@@ -681,6 +684,8 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->bonds, sizeof(int2) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->F, v4 * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->T, v4 * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->Fe, v4 * N) == cudaSuccess;
+	ok &= cudaMalloc(&h->Te, v4 * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_tab, tab * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_sys, sizeof(int) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_sys_off, sizeof(int) * (n_systems + 1)) == cudaSuccess;
@@ -805,20 +810,27 @@ static int build_list_now(oxgb_md *h) {
 	return OXGB_OK;
 }
 
-// forces, torques and energies of the current state with the current lists
-static int compute_forces_now(oxgb_md *h, bool split) {
+// The forces and torques the dynamics uses (F, T) come from one kernel variant only, the one
+// an MD step runs (no energies), so that a state evolves the same whatever the caller asks for
+// in between; evaluations with energies (and the per-term split) go to Fe / Te.
+static int compute_forces_now(oxgb_md *h) {
 	ForceArgs fa = force_args(h);
+	CK(launch_forces_split(fa, h->dbl, false, false, h->stream));
+	h->energies_fresh = false;
+	return OXGB_OK;
+}
+
+static int compute_energies_now(oxgb_md *h, bool split) {
+	ForceArgs fa = force_args(h, 0, false, true);
 	if(split) CK(cudaMemsetAsync(h->esplit, 0, sizeof(double) * 8 * h->n_systems, h->stream));
 	CK(launch_forces_split(fa, h->dbl, split, true, h->stream));
 	h->energies_fresh = true;
 	return OXGB_OK;
 }
 
-// the steps compute forces and torques only; the per-nucleotide energies (F.w, T.w) are made
-// on request from the same state and lists
 static int ensure_energies(oxgb_md *h) {
 	if(h->energies_fresh) return OXGB_OK;
-	return compute_forces_now(h, false);
+	return compute_energies_now(h, false);
 }
 
 static int read_status(oxgb_md *h) {
@@ -918,7 +930,7 @@ extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *qu
 	CK(launch_make_mirrors(sa, h->stream));
 	int rc = size_and_build_list(h);
 	if(rc) return rc;
-	rc = compute_forces_now(h, false);
+	rc = compute_forces_now(h);
 	if(rc) return rc;
 	h->have_state = true;
 	return read_status(h);
@@ -1080,17 +1092,19 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 	return OXGB_OK;
 }
 
-static int download_forces(oxgb_md *h, double *F, double *T, double *E);
+static int download_forces(oxgb_md *h, const void *dF, const void *dT, double *F, double *T, double *E);
 
 extern "C" int oxgb_md_compute_forces(oxgb_md *h, double *F, double *T, double *E, double *E_split) {
 	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
 	int rc = build_list_now(h);
 	if(rc) return rc;
-	rc = compute_forces_now(h, true);
+	rc = compute_forces_now(h);  // the dynamics' forces follow the new lists
+	if(rc) return rc;
+	rc = compute_energies_now(h, true);
 	if(rc) return rc;
 	rc = read_status(h);
 	if(rc) return rc;
-	rc = download_forces(h, F, T, E);
+	rc = download_forces(h, h->Fe, h->Te, F, T, E);
 	if(rc) return rc;
 	if(E_split) CK(cudaMemcpy(E_split, h->esplit, sizeof(double) * 8 * h->n_systems, cudaMemcpyDeviceToHost));
 	return OXGB_OK;
@@ -1103,15 +1117,18 @@ extern "C" int oxgb_md_get_forces(oxgb_md *h, double *F, double *T, double *E) {
 		if(rc) return rc;
 	}
 	CK(cudaStreamSynchronize(h->stream));
-	return download_forces(h, F, T, E);
+	int rc = download_forces(h, h->F, h->T, F, T, nullptr);
+	if(rc == OXGB_OK && E) rc = download_forces(h, h->Fe, h->Te, nullptr, nullptr, E);
+	return rc;
 }
 
-static int download_forces(oxgb_md *h, double *F, double *T, double *E) {
+// F, T from the device buffers dF, dT and E from the w of dF (any output may be NULL)
+static int download_forces(oxgb_md *h, const void *dF, const void *dT, double *F, double *T, double *E) {
 	const int N = h->N;
 	if(h->dbl) {
 		std::vector<double4_32a> f(N), t(N);
-		CK(cudaMemcpy(f.data(), h->F, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
-		CK(cudaMemcpy(t.data(), h->T, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(f.data(), dF, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(t.data(), dT, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
 		for(int i = 0; i < N; i++) {
 			if(F) F[3 * i] = f[i].x, F[3 * i + 1] = f[i].y, F[3 * i + 2] = f[i].z;
 			if(T) T[3 * i] = t[i].x, T[3 * i + 1] = t[i].y, T[3 * i + 2] = t[i].z;
@@ -1120,8 +1137,8 @@ static int download_forces(oxgb_md *h, double *F, double *T, double *E) {
 	}
 	else {
 		std::vector<float4> f(N), t(N);
-		CK(cudaMemcpy(f.data(), h->F, sizeof(float4) * N, cudaMemcpyDeviceToHost));
-		CK(cudaMemcpy(t.data(), h->T, sizeof(float4) * N, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(f.data(), dF, sizeof(float4) * N, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(t.data(), dT, sizeof(float4) * N, cudaMemcpyDeviceToHost));
 		for(int i = 0; i < N; i++) {
 			if(F) F[3 * i] = f[i].x, F[3 * i + 1] = f[i].y, F[3 * i + 2] = f[i].z;
 			if(T) T[3 * i] = t[i].x, T[3 * i + 1] = t[i].y, T[3 * i + 2] = t[i].z;
@@ -1138,6 +1155,7 @@ extern "C" int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r)
 		if(rc) return rc;
 	}
 	StepArgs sa = step_args(h);
+	sa.forces = h->Fe;  // the potential energy: w of the forces evaluated with energies
 	CK(launch_system_sums(sa, h->n_chunks, h->dbl, h->sums, h->stream));
 	std::vector<double> c((size_t) 4 * h->n_chunks);
 	CK(cudaMemcpyAsync(c.data(), h->sums, sizeof(double) * c.size(), cudaMemcpyDeviceToHost, h->stream));
@@ -1199,7 +1217,7 @@ extern "C" int oxgb_md_set_temperature(oxgb_md *h, int k, double T) {
 			CK(launch_list_build(a, h->stream));
 		}
 		if(rc) return rc;
-		rc = compute_forces_now(h, false);
+		rc = compute_forces_now(h);
 		if(rc) return rc;
 		return read_status(h);
 	}
@@ -1273,7 +1291,7 @@ extern "C" int oxgb_md_destroy(oxgb_md *h) {
 
 extern "C" int oxgb_md_launch_forces(oxgb_md *h) {
 	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
-	return compute_forces_now(h, false);
+	return compute_energies_now(h, false);
 }
 
 // ====================================================================== diagnostics
