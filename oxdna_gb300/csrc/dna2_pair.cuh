@@ -24,6 +24,9 @@ struct DNA2Table {
 	R f2_k[2], f2_r0[2], f2_rc[2], f2_blow[2], f2_bhigh[2], f2_rlow[2], f2_rhigh[2], f2_rclow[2], f2_rchigh[2];
 	R f4_a[13], f4_b[13], f4_t0[13], f4_ts[13], f4_tc[13];
 	R f4_sa, f4_sb;
+	// support of f4 type i in cos(theta), slightly widened: outside (f4_clo, f4_chi) the factor
+	// and its derivative are exactly zero, which a pair can be told from without an acos
+	R f4_clo[13], f4_chi[13];
 	R f5_a[4], f5_b[4], f5_xc[4], f5_xs[4];
 	R hb_multiplier;
 	R dh_prefactor, dh_rhigh, dh_rc, dh_b, dh_minus_kappa;
@@ -207,6 +210,12 @@ OXGB_HD void f4_both(const DNA2Table<R> &P, R c, int i, R &f, R &fd) {
 	fd = -dsin;
 }
 
+// f4 of type i can be non-zero at cos(theta) = c
+template <typename R>
+OXGB_HD bool f4_may(const DNA2Table<R> &P, R c, int i) {
+	return c > P.f4_clo[i] && c < P.f4_chi[i];
+}
+
 // f5 of cos(phi) and its derivative (DNAInteraction.cpp:1418-1450)
 template <typename R>
 OXGB_HD void f5_both(const DNA2Table<R> &P, R x, int t, R &f, R &fd) {
@@ -286,6 +295,11 @@ OXGB_HD void pair_base(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, 
 		if(R(OXM_HYDR_RCLOW) < rmod && rmod < R(OXM_HYDR_RCHIGH)) {
 			const v3<R> rd = rhydro * (R(1) / rmod);
 			const R c1 = -dot(a1, b1), c2 = -dot(b1, rd), c3 = dot(a1, rd), c4 = dot(a3, b3), c7 = -dot(b3, rd), c8 = dot(a3, rd);
+			// every angular factor must be able to be non-zero (else the term is exactly zero)
+			if(!(f4_may(P, c1, OXM_F4_HB_T1) && f4_may(P, c2, OXM_F4_HB_T2) && f4_may(P, c3, OXM_F4_HB_T2) &&
+					   f4_may(P, c4, OXM_F4_HB_T4) && f4_may(P, c7, OXM_F4_HB_T7) && f4_may(P, c8, OXM_F4_HB_T7)))
+				goto crst;
+			{
 			const R hbm = (abs(q.btype) >= 300 && abs(p.btype) >= 300) ? P.hb_multiplier : R(1);
 			R F1, F1D, g1, d1, g2, d2, g3, d3, g4, d4, g7, d7, g8, d8;
 			f1_both(P, rmod, OXM_F1_HB, q.type, p.type, F1, F1D);
@@ -316,15 +330,23 @@ OXGB_HD void pair_base(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, 
 				o.F -= force;
 				o.T += tp - cross(p.base, force);
 			}
+			}
 		}
 	}
 
+crst:
 	// cross stacking
 	if(R(OXM_CRST_RCLOW) * R(OXM_CRST_RCLOW) < rh2 && rh2 < R(OXM_CRST_RCHIGH) * R(OXM_CRST_RCHIGH)) {
 		const R rmod = m_sqrt(rh2);
 		if(R(OXM_CRST_RCLOW) < rmod && rmod < R(OXM_CRST_RCHIGH)) {
 			const v3<R> rd = rhydro * (R(1) / rmod);
 			const R c1 = -dot(a1, b1), c2 = -dot(b1, rd), c3 = dot(a1, rd), c4 = dot(a3, b3), c7 = -dot(b3, rd), c8 = dot(a3, rd);
+			// theta4, theta7, theta8 enter through f4(theta) + f4(pi - theta)
+			if(!(f4_may(P, c1, OXM_F4_CR_T1) && f4_may(P, c2, OXM_F4_CR_T2) && f4_may(P, c3, OXM_F4_CR_T2) &&
+					   (f4_may(P, c4, OXM_F4_CR_T4) || f4_may(P, -c4, OXM_F4_CR_T4)) &&
+					   (f4_may(P, c7, OXM_F4_CR_T7) || f4_may(P, -c7, OXM_F4_CR_T7)) &&
+					   (f4_may(P, c8, OXM_F4_CR_T7) || f4_may(P, -c8, OXM_F4_CR_T7))))
+				return;
 			R F2, F2D, g1, d1, g2, d2, g3, d3, g4a, d4a, g4b, d4b, g7a, d7a, g7b, d7b, g8a, d8a, g8b, d8b;
 			f2_both(P, rmod, OXM_F2_CRST, F2, F2D);
 			f4_both(P, c1, OXM_F4_CR_T1, g1, d1);
@@ -371,6 +393,10 @@ OXGB_HD void pair_stack(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q,
 			if(R(OXM_CXST_RCLOW) < rmod && rmod < R(OXM_CXST_RCHIGH)) {
 				const v3<R> rd = rstack * (R(1) / rmod);
 				const R c1 = -dot(a1, b1), c4 = dot(a3, b3), c5 = dot(a3, rd), c6 = -dot(b3, rd);
+				if(!(f4_may(P, c1, OXM_F4_CX_T1) && f4_may(P, c4, OXM_F4_CX_T4) &&
+						   (f4_may(P, c5, OXM_F4_CX_T5) || f4_may(P, -c5, OXM_F4_CX_T5)) &&
+						   (f4_may(P, c6, OXM_F4_CX_T5) || f4_may(P, -c6, OXM_F4_CX_T5))))
+					return;
 				R F2, F2D, g1, d1, g4, d4, g5a, d5a, g5b, d5b, g6a, d6a, g6b, d6b;
 				f2_both(P, rmod, OXM_F2_CXST, F2, F2D);
 				f4_both(P, c1, OXM_F4_CX_T1, g1, d1);

@@ -71,6 +71,17 @@ inline int build_table(const oxgb_dna2_settings &s, double box, DNA2Table<double
 	}
 	P.f4_sa = OXM_CXST_THETA1_SA;
 	P.f4_sb = OXM_CXST_THETA1_SB;
+	// support of each f4 in cos(theta): |theta - t0| < tc, widened by 1e-5 in the cosine (far
+	// more than the FP32 error of an acos); open on a side that reaches 0 or pi
+	const double pi = 3.141592653589793;
+	for(int i = 0; i < OXM_N_F4; i++) {
+		const double lo_t = (double) f4t0[i] - (double) f4tc[i], hi_t = (double) f4t0[i] + (double) f4tc[i];
+		P.f4_chi[i] = lo_t <= 0.0 ? 2.0 : std::cos(lo_t) + 1e-5;
+		P.f4_clo[i] = hi_t >= pi ? -2.0 : std::cos(hi_t) - 1e-5;
+	}
+	// the oxDNA2 pure-harmonic coaxial theta1 term adds for theta >= sb
+	P.f4_clo[OXM_F4_CX_T1] = -2.0;
+	P.f4_chi[OXM_F4_CX_T1] = std::fmax((double) P.f4_chi[OXM_F4_CX_T1], std::cos((double) OXM_CXST_THETA1_SB) + 1e-5);
 	for(int i = 0; i < 4; i++) {
 		P.f5_a[i] = f5a[i];
 		P.f5_b[i] = f5b[i];
