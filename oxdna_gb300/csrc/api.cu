@@ -205,8 +205,8 @@ struct ListBuffers {
 struct TermLists {
 	int N = 0, ev_cap = 0, base_cap = 0, stk_cap = 0;
 	int *ev_nb = nullptr, *ev_n = nullptr, *base_nb = nullptr, *base_n = nullptr, *stk_nb = nullptr, *stk_n = nullptr;
-	void *base_res = nullptr, *stk_res = nullptr;  // per-slot pair results, three 4-vectors of v4 bytes each
-	int *base_rev = nullptr, *stk_rev = nullptr;   // partner's slot of entries with a lower partner
+	void *base_res = nullptr, *stk_res = nullptr;  // per-slot pair results, two 4-vectors of v4 bytes each
+	int *base_pos = nullptr, *stk_pos = nullptr;   // owned entries: the position in the partner's list
 
 	int alloc(int N_, int ev, int base, int stk, size_t v4) {
 		free_all();
@@ -220,14 +220,14 @@ struct TermLists {
 		CK(cudaMalloc(&ev_n, sizeof(int) * N));
 		CK(cudaMalloc(&base_n, sizeof(int) * N));
 		CK(cudaMalloc(&stk_n, sizeof(int) * N));
-		CK(cudaMalloc(&base_res, 3 * v4 * (size_t) N * base_cap));
-		CK(cudaMalloc(&stk_res, 3 * v4 * (size_t) N * stk_cap));
-		CK(cudaMalloc(&base_rev, sizeof(int) * (size_t) N * base_cap));
-		CK(cudaMalloc(&stk_rev, sizeof(int) * (size_t) N * stk_cap));
+		CK(cudaMalloc(&base_res, 2 * v4 * (size_t) N * base_cap));
+		CK(cudaMalloc(&stk_res, 2 * v4 * (size_t) N * stk_cap));
+		CK(cudaMalloc(&base_pos, sizeof(int) * (size_t) N * base_cap));
+		CK(cudaMalloc(&stk_pos, sizeof(int) * (size_t) N * stk_cap));
 		return OXGB_OK;
 	}
 	void free_all() {
-		for(int **p : {&ev_nb, &ev_n, &base_nb, &base_n, &stk_nb, &stk_n, &base_rev, &stk_rev}) {
+		for(int **p : {&ev_nb, &ev_n, &base_nb, &base_n, &stk_nb, &stk_n, &base_pos, &stk_pos}) {
 			if(*p) cudaFree(*p);
 			*p = nullptr;
 		}
@@ -504,8 +504,8 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.bond_tq = h->bond_tq;
 	a.base_res = h->tl.base_res;
 	a.stk_res = h->tl.stk_res;
-	a.base_rev = h->tl.base_rev;
-	a.stk_rev = h->tl.stk_rev;
+	a.base_pos = h->tl.base_pos;
+	a.stk_pos = h->tl.stk_pos;
 	a.term_max = h->term_max;
 	a.th = thermo_args(h, step_offset, engine_step);
 	return a;
@@ -797,8 +797,8 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	a.list_a1 = h->list_a1;
 	a.list_back = h->list_back;
 	a.term_max = h->term_max;
-	a.base_rev = h->tl.base_rev;
-	a.stk_rev = h->tl.stk_rev;
+	a.base_pos = h->tl.base_pos;
+	a.stk_pos = h->tl.stk_pos;
 	return a;
 }
 

@@ -458,40 +458,25 @@ struct SplitAcc {
 			for(int k = 0; k < N_TERMS; k++) split[k] += o.split[k];
 		}
 	}
-	// entry k of nucleotide i's list, evaluated by k_pair_slots in the slot of the lower
-	// nucleotide: its own (force, torque) or, from the partner's slot, (-force, partner torque)
+	// entry k of nucleotide i's list: its result, written by k_pair_slots
 	template <typename V4>
-	__device__ __forceinline__ void add_slot(const int *nb, const int *rev, const V4 *res, long long N, int i, int k) {
+	__device__ __forceinline__ void add_slot(const V4 *res, long long N, int i, int k) {
 		const long long s = (long long) k * N + i;
-		const int j = nb[s];
-		if(j > i) {
-			const V4 f = res[3 * s], t = res[3 * s + 1];
-			F.add(v3<R>{f.x, f.y, f.z});
-			T.add(v3<R>{t.x, t.y, t.z});
-			if(ENERGY) {
-				KahanV<R>::kadd(E, Ec, f.w);
-				KahanV<R>::kadd(Eh, Ehc, t.w);
-			}
-		}
-		else {
-			const int m = rev[s];
-			if(m < 0) return;  // flagged by the list build
-			const long long sj = (long long) m * N + j;
-			const V4 f = res[3 * sj], ti = res[3 * sj + 1], t = res[3 * sj + 2];
-			F.add(v3<R>{-f.x, -f.y, -f.z});
-			T.add(v3<R>{t.x, t.y, t.z});
-			if(ENERGY) {
-				KahanV<R>::kadd(E, Ec, f.w);
-				KahanV<R>::kadd(Eh, Ehc, ti.w);
-			}
+		const V4 f = res[2 * s], t = res[2 * s + 1];
+		F.add(v3<R>{f.x, f.y, f.z});
+		T.add(v3<R>{t.x, t.y, t.z});
+		if(ENERGY) {
+			KahanV<R>::kadd(E, Ec, f.w);
+			KahanV<R>::kadd(Eh, Ehc, t.w);
 		}
 	}
 };
 
 // Base-base pairs (hydrogen bonding + cross stacking; blocks 0 .. base_blocks - 1) and
-// stack-stack pairs (coaxial stacking; the other blocks), each evaluated once, in the slot of
-// its lower nucleotide i (partner j > i): slot k of i stores (force on i, E), (torque on i,
-// E_hb) and (torque on j, 0) at [3 (k N + i) + 0..2] of base_res / stk_res.  These are the
+// stack-stack pairs (coaxial stacking; the other blocks), each evaluated once, by its lower
+// nucleotide i (partner j > i, at position k of i's list and m of j's): slot k of i gets
+// (force on i, E), (torque on i, E_hb) and slot m of j gets (-force, E), (torque on j, E_hb), at
+// [2 (k N + i) + 0..1] of base_res / stk_res.  Every slot of every list is written once.  These are the
 // costliest terms and their lists are short, so the owned slots of a warp's 32 nucleotides
 // are queued (a warp prefix sum over the per-lane counts) and dealt 32 at a time: every lane
 // works on a pair in every round but the last.
@@ -545,6 +530,7 @@ __global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int 
 		const int k = r < nlo ? (int) __fns(lo_l, 0u, r + 1) : 32 + (int) __fns(hi_l, 0u, r - nlo + 1);
 		const int i = wbase + l;
 		const int j = nb[(long long) k * N + i];
+		const int m = (is_base ? a.base_pos : a.stk_pos)[(long long) k * N + i];
 		const int sy = a.sys ? a.sys[i] : 0;
 		const DNA2Table<R> &P = Ps[sy - s0];
 		Nuc<R> p, qn;
@@ -558,14 +544,18 @@ __global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int 
 		// the potential is invariant under rigid rotations, so the torques balance:
 		// T_j = -T_i + (r_j - r_i) x F_i, the cross product with error-free products
 		const v3<R> c = cross_accurate(d, o.F);
-		V4 f, ti, tj;
-		f.x = o.F.x, f.y = o.F.y, f.z = o.F.z, f.w = ENERGY ? o.E : R(0);
+		V4 fi, ti, fj, tj;
+		fi.x = o.F.x, fi.y = o.F.y, fi.z = o.F.z, fi.w = ENERGY ? o.E : R(0);
 		ti.x = o.T.x, ti.y = o.T.y, ti.z = o.T.z, ti.w = ENERGY ? o.Ehb : R(0);
-		tj.x = c.x - o.T.x, tj.y = c.y - o.T.y, tj.z = c.z - o.T.z, tj.w = R(0);
-		V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res) + 3 * ((long long) k * N + i);
-		res[0] = f;
-		res[1] = ti;
-		res[2] = tj;
+		fj.x = -o.F.x, fj.y = -o.F.y, fj.z = -o.F.z, fj.w = fi.w;
+		tj.x = c.x - o.T.x, tj.y = c.y - o.T.y, tj.z = c.z - o.T.z, tj.w = ti.w;
+		V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res);
+		res[2 * ((long long) k * N + i)] = fi;
+		res[2 * ((long long) k * N + i) + 1] = ti;
+		if(m >= 0) {  // (a missing position is flagged by the list build)
+			res[2 * ((long long) m * N + j)] = fj;
+			res[2 * ((long long) m * N + j) + 1] = tj;
+		}
 		if(SPLIT) {
 #pragma unroll
 			for(int m = 0; m < N_TERMS; m++)
@@ -645,9 +635,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 		// hydrogen bonding + cross stacking and coaxial stacking: evaluated per list slot by
 		// k_pair_slots, gathered here
 		const int nb_ = live ? min(a.base_n[i], a.base_cap) : 0;
-		for(int k = sub; k < nb_; k += K) acc.add_slot(a.base_nb, a.base_rev, reinterpret_cast<const V4 *>(a.base_res), N, i, k);
+		for(int k = sub; k < nb_; k += K) acc.add_slot(reinterpret_cast<const V4 *>(a.base_res), N, i, k);
 		const int ns = live ? min(a.stk_n[i], a.stk_cap) : 0;
-		for(int k = sub; k < ns; k += K) acc.add_slot(a.stk_nb, a.stk_rev, reinterpret_cast<const V4 *>(a.stk_res), N, i, k);
+		for(int k = sub; k < ns; k += K) acc.add_slot(reinterpret_cast<const V4 *>(a.stk_res), N, i, k);
 		if(SPLIT && live) {
 #pragma unroll
 			for(int k = 0; k < N_TERMS; k++)

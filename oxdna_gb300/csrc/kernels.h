@@ -75,10 +75,10 @@ struct ForceArgs {
 	const int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
 	int ev_cap, base_cap, stk_cap;            // capacities (an overflowed list is read up to them)
 	void *bond_f, *bond_tp, *bond_tq;         // per bond owner p (q = n3[p]): f on q with w = energy, torques
-	// base / stack pairs are evaluated once, in the slot of their lower nucleotide i (partner
-	// j > i): (force on i, E), (torque on i, E_hb), (torque on j, 0) as three V4 per slot
+	// base / stack pairs are evaluated once, by their lower nucleotide i, which writes slot k of i
+	// and slot pos[k N + i] of its partner j: (force, E), (torque, E_hb) as two V4 per slot
 	void *base_res, *stk_res;
-	const int *base_rev, *stk_rev;            // see ListArgs
+	const int *base_pos, *stk_pos;            // see ListArgs
 	const int *term_max;                      // [3] longest EV / base / stack list (slots past it are empty)
 	// MD-step bookkeeping (engine layout): the bonded kernel marks the step's half kick pending
 	ThermoArgs th;
@@ -123,9 +123,9 @@ struct ListArgs {
 	// list when its stacking sites are closer than stk_r (all thresholds include twice the skin)
 	const float4 *fa1, *fback;
 	int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
-	// for every base / stack entry (k, i) whose partner j is lower: the position of i in j's
-	// list (the pair is evaluated once, in j's slot); -1 otherwise
-	int *base_rev, *stk_rev;
+	// for every base / stack entry (k, i) whose partner j is higher (i owns the pair): the
+	// position of i in j's list, where the pair evaluation also writes j's result; -1 otherwise
+	int *base_pos, *stk_pos;
 	int ev_cap, base_cap, stk_cap;
 	float ev_r2, base_r2, stk_r2;
 	float4 *list_a1, *list_back;   // body axis a1 and backbone offset at this build

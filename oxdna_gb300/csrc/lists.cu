@@ -315,10 +315,10 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	}
 }
 
-// For every base / stack list entry (k, i) with partner j < i: where i sits in j's list (the
-// lists are symmetric: the pair criteria are exactly symmetric in FP32).  One thread per
-// nucleotide and term (blocks 0 .. base_blocks - 1: base lists).
-__global__ void k_term_rev(ListArgs a, int base_blocks) {
+// For every base / stack list entry (k, i) with partner j > i (i owns the pair): where i sits in
+// j's list (the lists are symmetric: the pair criteria are exactly symmetric in FP32).  One
+// thread per nucleotide and term (blocks 0 .. base_blocks - 1: base lists).
+__global__ void k_term_pos(ListArgs a, int base_blocks) {
 	SKIP_IF_FRESH(a);
 	const bool is_base = (int) blockIdx.x < base_blocks;
 	const int i = (is_base ? blockIdx.x : blockIdx.x - base_blocks) * blockDim.x + threadIdx.x;
@@ -326,12 +326,12 @@ __global__ void k_term_rev(ListArgs a, int base_blocks) {
 	const long long N = a.N;
 	const int cap = is_base ? a.base_cap : a.stk_cap;
 	const int *nb = is_base ? a.base_nb : a.stk_nb;
-	int *rev = is_base ? a.base_rev : a.stk_rev;
+	int *pos = is_base ? a.base_pos : a.stk_pos;
 	const int n = min(is_base ? a.base_n[i] : a.stk_n[i], cap);
 	for(int k = 0; k < n; k++) {
 		const int j = nb[(long long) k * N + i];
 		int r = -1;
-		if(j < i) {
+		if(j > i) {
 			const int nj = min(is_base ? a.base_n[j] : a.stk_n[j], cap);
 			for(int m = 0; m < nj; m++)
 				if(nb[(long long) m * N + j] == i) {
@@ -340,7 +340,7 @@ __global__ void k_term_rev(ListArgs a, int base_blocks) {
 				}
 			if(r < 0) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);  // an asymmetric (overflowed) list
 		}
-		rev[(long long) k * N + i] = r;
+		pos[(long long) k * N + i] = r;
 	}
 }
 
@@ -371,7 +371,7 @@ cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s) {
 	k_cell_rank<<<gp, tpb, 0, s>>>(a);
 	const long long warps = (long long) a.N * 32;
 	k_neighbours<<<(int) ((warps + tpb - 1) / tpb), tpb, 0, s>>>(a);
-	if(a.base_rev && a.stk_rev) k_term_rev<<<2 * gp, tpb, 0, s>>>(a, gp);
+	if(a.base_pos && a.stk_pos) k_term_pos<<<2 * gp, tpb, 0, s>>>(a, gp);
 	k_list_done<<<1, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
