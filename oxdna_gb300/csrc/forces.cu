@@ -480,23 +480,32 @@ struct SplitAcc {
 // costliest terms and their lists are short, so the owned slots of a warp's 32 nucleotides
 // are queued (a warp prefix sum over the per-lane counts) and dealt 32 at a time: every lane
 // works on a pair in every round but the last.
+// nucleotides per warp in k_pair_slots: fewer than 32 gives more warps (more latency hidden)
+// for about as many rounds of pairs per warp as a full-warp queue
+#ifndef OXGB_PAIR_NPW
+#define OXGB_PAIR_NPW 16
+#endif
+
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
 __global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int base_blocks) {
 	using V4 = typename Vec4Of<R>::T;
+	constexpr int NPW = OXGB_PAIR_NPW;
 	const bool is_base = (int) blockIdx.x < base_blocks;
-	const int first = (is_base ? blockIdx.x : blockIdx.x - base_blocks) * blockDim.x;
+	const int per_block = (blockDim.x / 32) * NPW;
+	const int first = (is_base ? blockIdx.x : blockIdx.x - base_blocks) * per_block;
 	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
-	const int s0 = load_table_span<R>(a, first, min(first + (int) blockDim.x, a.N) - 1, Ps);
+	const int s0 = load_table_span<R>(a, first, min(first + per_block, a.N) - 1, Ps);
 	const long long N = a.N;
 	const int lane = threadIdx.x & 31;
-	const int wbase = first + (threadIdx.x & ~31);
+	const int wbase = first + (threadIdx.x >> 5) * NPW;
 	if(wbase >= a.N) return;  // warp-uniform
 	const int cap = is_base ? a.base_cap : a.stk_cap;
 	const int *nb = is_base ? a.base_nb : a.stk_nb;
-	// this lane's nucleotide: which of its entries it owns (partner above it), as a bit mask
+	// this lane's nucleotide (lanes below NPW): which of its entries it owns (partner above
+	// it), as a bit mask
 	const int il = wbase + lane;
 	unsigned lo = 0u, hi = 0u;
-	if(il < a.N) {
+	if(lane < NPW && il < a.N) {
 		const int n = min(min(is_base ? a.base_n[il] : a.stk_n[il], cap), 64);
 		for(int k = 0; k < n; k++)
 			if(nb[(long long) k * N + il] > il) {
@@ -700,8 +709,9 @@ static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEv
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	const size_t smem = sizeof(DNA2Table<R>) * (size_t) (a.tab_span > 0 ? a.tab_span : 1);
 	k_bonded_split<R, Loader, SPLIT, ENERGY><<<blocks, tpb, smem, s>>>(a, ld);
-	// one block of 128 nucleotides per term
-	k_pair_slots<R, Loader, SPLIT, ENERGY><<<2 * blocks, tpb, smem, s>>>(a, ld, blocks);
+	// blocks of 4 warps x OXGB_PAIR_NPW nucleotides per term
+	const int pair_blocks = (a.N + 4 * OXGB_PAIR_NPW - 1) / (4 * OXGB_PAIR_NPW);
+	k_pair_slots<R, Loader, SPLIT, ENERGY><<<2 * pair_blocks, tpb, smem, s>>>(a, ld, pair_blocks);
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
 	k_nonbonded_split<R, Loader, SPLIT, ENERGY, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
