@@ -605,7 +605,7 @@ static int clear_pending(oxgb_md *h) {
 static int reset_bussi(oxgb_md *h, int k) {
 	const int n = h->offsets[k + 1] - h->offsets[k];
 	const double T = h->dna[k].T;
-	double bs[16] = {0.5 * 3 * (n - 1) * T, 0.5 * 3 * (n - 1) * T, 0.5 * 3 * n * T, 0.5 * 3 * n * T};
+	double bs[16] = {0.5 * 3 * (n - 1) * T, 0.5 * 3 * n * T, 1, 1};
 	CK(cudaMemcpy(h->bussi_state + 16 * (size_t) k, bs, sizeof(bs), cudaMemcpyHostToDevice));
 	return OXGB_OK;
 }
@@ -1182,10 +1182,11 @@ extern "C" int oxgb_md_set_temperature(oxgb_md *h, int k, double T) {
 	h->dna[k].T = T;
 	int rc = upload_systems(h, k, k + 1);  // table, cutoff, thermostat values (read by the kernels)
 	if(rc) return rc;
-	// the Bussi running kinetic energies (both slots) follow the temperature
-	double bs[4];
+	// the Bussi running kinetic energies follow the temperature
+	double bs[2];
 	CK(cudaMemcpy(bs, h->bussi_state + 16 * (size_t) k, sizeof(bs), cudaMemcpyDeviceToHost));
-	for(double &x : bs) x *= T / T_old;
+	bs[0] *= T / T_old;
+	bs[1] *= T / T_old;
 	CK(cudaMemcpy(h->bussi_state + 16 * (size_t) k, bs, sizeof(bs), cudaMemcpyHostToDevice));
 	// the cutoff moves with T (Debye-Hueckel): a grid whose cells became narrower than the new
 	// r_verlet is laid out again (new buffers, so the step graph is captured again)

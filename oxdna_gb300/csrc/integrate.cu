@@ -71,11 +71,10 @@ __global__ void k_make_mirrors(StepArgs a) {
 __device__ __forceinline__ long long step_of(const ThermoArgs &t) { return *t.step_base + t.step_offset; }
 
 // completes step sp of nucleotide i (system sy): its second half kick (CUDA_mixed.cuh:71-93)
-// and its thermostat (Brownian redraw or Bussi rescaling).  Called by every lane of a warp
-// (the Bussi factors are a warp computation); live = the lane has a nucleotide.
+// and its thermostat (Brownian redraw or Bussi rescaling)
 template <typename V4>
-__device__ __forceinline__ void complete_step(const ThermoArgs &t, bool live, int i, int sy, long long sp, const V4 &F,
-		const V4 &T, double4_32a &v, double4_32a &L) {
+__device__ __forceinline__ void complete_step(const ThermoArgs &t, int i, int sy, long long sp, const V4 &F, const V4 &T,
+		double4_32a &v, double4_32a &L) {
 	const double hdt = 0.5 * t.dt;
 	v.x += (double) F.x * hdt;
 	v.y += (double) F.y * hdt;
@@ -83,20 +82,14 @@ __device__ __forceinline__ void complete_step(const ThermoArgs &t, bool live, in
 	L.x += (double) T.x * hdt;
 	L.y += (double) T.y * hdt;
 	L.z += (double) T.z * hdt;
-	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) {
-		if(live) brownian_redraw(t, sy, i - t.sys_off[sy], sp, v, L);
-	}
-	else if(t.thermostat == 2 && *t.bussi_stamp == sp) {
-		const BussiFactors f = bussi_factors_warp(t, live ? sy : -1, i, sp);
-		if(live) bussi_rescale(f, v, L);
-	}
+	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) brownian_redraw(t, sy, i - t.sys_off[sy], sp, v, L);
+	else if(t.thermostat == 2 && *t.bussi_stamp == sp) bussi_rescale(t, sy, v, L);
 }
 
 template <typename V4>
 __global__ void k_first_step(StepArgs a) {
-	const int i_raw = blockIdx.x * blockDim.x + threadIdx.x;
-	const bool live = i_raw < a.N;
-	const int i = live ? i_raw : a.N - 1;  // lanes past the end join the warp computations only
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= a.N) return;
 	const long long s = step_of(a.th);
 	const int sy = a.th.sys[i];
 	const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
@@ -105,8 +98,7 @@ __global__ void k_first_step(StepArgs a) {
 	double4_32a v = a.vel[i], r = a.pos[i], L = a.angmom[i], q = a.quat[i];
 	// the previous step's second half kick and thermostat (kept as a separate half kick, so that
 	// a state is the same whether or not a run ended at that step)
-	if(*a.th.open_step == s - 1) complete_step(a.th, live, i, sy, s - 1, F, T, v, L);
-	if(!live) return;
+	if(*a.th.open_step == s - 1) complete_step(a.th, i, sy, s - 1, F, T, v, L);
 	v.x += (double) F.x * hdt;
 	v.y += (double) F.y * hdt;
 	v.z += (double) F.z * hdt;
@@ -179,9 +171,8 @@ __global__ void k_bussi_noise(StepArgs a) {
 	rs.init(a.th.sys_seed[sy], s, (unsigned) w);
 	double sum, rr;
 	bussi_draws(rs, w == 0 ? 3 * (n - 1) : 3 * n, sum, rr);
-	double *dr = a.th.bussi_state + 16 * sy + 8 + 4 * bussi_slot(a.th, s);
-	dr[2 * w] = sum;
-	dr[2 * w + 1] = rr;
+	a.th.bussi_state[16 * sy + 8 + 2 * w] = sum;
+	a.th.bussi_state[16 * sy + 9 + 2 * w] = rr;
 }
 
 // Bussi step s, after its forces: sums of v, |v|^2 and |L|^2 over the completed velocities
@@ -195,8 +186,6 @@ __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 	const int sy = a.th.chunk_sys[c];
 	const int i = a.th.chunk_first[c] + threadIdx.x;
 	const double hdt = 0.5 * a.dt;
-	// the next first step (or the flush) makes the update of step s from these sums
-	if(c == 0 && threadIdx.x == 0) *a.th.bussi_stamp = s;
 	double acc[5] = {0, 0, 0, 0, 0};
 	if(i < a.th.sys_off[sy + 1]) {
 		const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
@@ -230,6 +219,38 @@ __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 	}
 }
 
+// the update of system blockIdx.x: its chunk sums reduced in a fixed order (deterministic),
+// translation on thread 0 and rotation on thread 32 (two warps: the chains overlap)
+__global__ void __launch_bounds__(256) k_bussi_update(StepArgs a) {
+	const long long s = step_of(a.th);
+	if(s % a.th.newtonian_steps != 0) return;
+	const int sy = blockIdx.x;
+	// the next first step applies the rescaling of step s (every system updates at the same steps)
+	if(sy == 0 && threadIdx.x == 0) *a.th.bussi_stamp = s;
+	const int c0 = a.th.sys_chunk0[sy], nc = a.th.sys_chunk0[sy + 1] - c0;
+	double part[5] = {0, 0, 0, 0, 0};
+	for(int b = threadIdx.x; b < nc; b += blockDim.x)
+#pragma unroll
+		for(int k = 0; k < 5; k++) part[k] += a.th.bussi_partials[(c0 + b) * 8 + k];
+	__shared__ double red[5][8];
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+	for(int k = 0; k < 5; k++) {
+		double x = part[k];
+		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+		if(lane == 0) red[k][w] = x;
+	}
+	__syncthreads();
+	if(threadIdx.x != 0 && threadIdx.x != 32) return;
+	double sum[5];
+	for(int k = 0; k < 5; k++) {
+		double x = 0;
+		for(int u = 0; u < nw; u++) x += red[k][u];
+		sum[k] = x;
+	}
+	bussi_update(a.th, sy, s, threadIdx.x == 0 ? 0 : 1, sum);
+}
+
 __global__ void k_step_advance(StepArgs a, int K) {
 	if(threadIdx.x == 0 && blockIdx.x == 0) *a.th.step_base += K;
 }
@@ -237,16 +258,13 @@ __global__ void k_step_advance(StepArgs a, int K) {
 // end of a run: the last step's second half kick and thermostat ...
 template <typename V4>
 __global__ void k_step_flush(StepArgs a) {
-	const int i_raw = blockIdx.x * blockDim.x + threadIdx.x;
-	const bool live = i_raw < a.N;
-	const int i = live ? i_raw : a.N - 1;
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	const long long sp = *a.th.step_base - 1;
-	if(*a.th.open_step != sp) return;  // grid-uniform
+	if(i >= a.N || *a.th.open_step != sp) return;
 	const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
 	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 	double4_32a v = a.vel[i], L = a.angmom[i];
-	complete_step(a.th, live, i, a.th.sys[i], sp, F, T, v, L);
-	if(!live) return;
+	complete_step(a.th, i, a.th.sys[i], sp, F, T, v, L);
 	a.vel[i] = v;
 	a.angmom[i] = L;
 }
@@ -327,6 +345,7 @@ cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
 cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s) {
 	if(double_forces) k_bussi_sums<double4_32a><<<n_chunks, 256, 0, s>>>(a);
 	else k_bussi_sums<float4><<<n_chunks, 256, 0, s>>>(a);
+	k_bussi_update<<<a.th.n_systems, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 
@@ -336,8 +355,8 @@ cudaError_t launch_step_advance(const StepArgs &a, int K, cudaStream_t s) {
 }
 
 cudaError_t launch_step_flush(const StepArgs &a, bool double_forces, cudaStream_t s) {
-	if(double_forces) k_step_flush<double4_32a><<<blocks_for(a.N, 32), 32, 0, s>>>(a);
-	else k_step_flush<float4><<<blocks_for(a.N, 32), 32, 0, s>>>(a);
+	if(double_forces) k_step_flush<double4_32a><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	else k_step_flush<float4><<<blocks_for(a.N, 256), 256, 0, s>>>(a);
 	k_step_flush_clear<<<1, 32, 0, s>>>(a);
 	return cudaGetLastError();
 }

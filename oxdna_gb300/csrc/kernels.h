@@ -43,8 +43,9 @@ struct ThermoArgs {
 	const int *chunk_sys, *chunk_first;    // [chunks]
 	const int *sys_chunk0;                 // [n_systems + 1] first chunk of each system
 	double *bussi_partials;                // [chunks * 8] per-chunk sums of v, |v|^2, |L|^2
-	double *bussi_state;                   // [n_systems * 16]: running K_t, K_r and the draws,
-	                                       // two slots each (thermo.cuh, bussi_slot)
+	double *bussi_state;                   // [n_systems * 16]: K_t, K_r, factor_t, factor_r,
+	                                       // vcom x y z, -, then the step's draws: sum_t, rr_t,
+	                                       // sum_r, rr_r
 	long long *bussi_stamp;                // step of the last Bussi update (OXGB_NO_STEP: none)
 	long long *open_step;                  // step whose second half kick is pending
 	                                       // (OXGB_NO_STEP: none); null in force-only calls

@@ -150,79 +150,40 @@ static __device__ __noinline__ void brownian_redraw(const ThermoArgs &t, int sy,
 	if(u01(o0[1]) < par[SP_PR]) L = make_double4_32a(g[3] * sT, g[4] * sT, g[5] * sT, 0.0);
 }
 
-// Bussi state of system sy, 16 doubles: K_t and K_r in two slots each ([0 + u], [2 + u]) and
-// the draws of a step in two slots ([8 + 4u] .. [11 + 4u]: sum_t, rr_t, sum_r, rr_r), where
-// u = (step / newtonian_steps) & 1 is the parity of the update; the update at step s reads
-// the slot of the previous update and writes its own, and the draws of the next step go to
-// the other slot, so no kernel reads what another running kernel writes.
-__device__ __forceinline__ int bussi_slot(const ThermoArgs &t, long long s) { return (int) ((s / t.newtonian_steps) & 1); }
-
-struct BussiFactors {
-	double ft, fr, cx, cy, cz;
-};
-
-// The rescaling of system sy decided by the Bussi update of step s, computed by a whole warp
-// (every lane gets it): the chunk sums of the system (k_bussi_sums) in a fixed order, the new
-// running kinetic energies from the draws of step s, and the factors.  The warp holding the
-// system's first nucleotide (write = true) stores the new kinetic energies.
-__device__ __noinline__ BussiFactors bussi_factors(const ThermoArgs &t, int sy, long long s, bool write) {
-	const int lane = threadIdx.x & 31;
-	const int c0 = t.sys_chunk0[sy], nc = t.sys_chunk0[sy + 1] - c0;
-	double part[5] = {0, 0, 0, 0, 0};
-	for(int b = lane; b < nc; b += 32)
-#pragma unroll
-		for(int k = 0; k < 5; k++) part[k] += t.bussi_partials[(c0 + b) * 8 + k];
-#pragma unroll
-	for(int k = 0; k < 5; k++)
-		for(int off = 16; off > 0; off >>= 1) part[k] += __shfl_xor_sync(0xffffffffu, part[k], off);
+// Bussi: from the sums of v, |v|^2 and |L|^2 over system sy, the new running kinetic energy
+// (with the draws of this step) and the rescaling factor of one kind of motion: which = 0
+// translation (about the centre-of-mass velocity), 1 rotation.  The two run on two threads.
+static __device__ void bussi_update(const ThermoArgs &t, int sy, long long s, int which, const double sum[5]) {
 	const double *par = t.sys_par + sy * SP_STRIDE;
 	double *st = t.bussi_state + 16 * sy;
-	const int u = bussi_slot(t, s);
-	const double *dr = st + 8 + 4 * u;
-	const double inv_n = par[SP_INVN];
-	const double n = (double) (t.sys_off[sy + 1] - t.sys_off[sy]);
-	BussiFactors f;
-	f.cx = part[0] * inv_n;
-	f.cy = part[1] * inv_n;
-	f.cz = part[2] * inv_n;
-	const double Kt_now = 0.5 * (part[3] - n * (f.cx * f.cx + f.cy * f.cy + f.cz * f.cz));
-	const double Kr_now = 0.5 * part[4];
-	double Kt = st[1 - u], Kr = st[3 - u];
-	update_K(Kt, par[SP_1MC], par[SP_A], par[SP_B], dr[0], dr[1]);
-	update_K(Kr, par[SP_1MC], par[SP_A], par[SP_B], dr[2], dr[3]);
-	f.ft = sqrt(Kt) * rsqrt(Kt_now);
-	f.fr = sqrt(Kr) * rsqrt(Kr_now);
-	if(write && lane == 0) {
-		st[u] = Kt;
-		st[2 + u] = Kr;
+	if(which == 0) {
+		const double inv_n = par[SP_INVN];
+		const double n = (double) (t.sys_off[sy + 1] - t.sys_off[sy]);
+		const double vc[3] = {sum[0] * inv_n, sum[1] * inv_n, sum[2] * inv_n};
+		const double Kt_now = 0.5 * (sum[3] - n * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
+		update_K(st[0], par[SP_1MC], par[SP_A], par[SP_B], __ldcg(st + 8), __ldcg(st + 9));
+		st[2] = sqrt(st[0]) * rsqrt(Kt_now);
+		st[4] = vc[0];
+		st[5] = vc[1];
+		st[6] = vc[2];
 	}
-	return f;
+	else {
+		const double Kr_now = 0.5 * sum[4];
+		update_K(st[1], par[SP_1MC], par[SP_A], par[SP_B], __ldcg(st + 10), __ldcg(st + 11));
+		st[3] = sqrt(st[1]) * rsqrt(Kr_now);
+	}
 }
 
-__device__ __forceinline__ void bussi_rescale(const BussiFactors &f, double4_32a &v, double4_32a &L) {
-	v.x = (v.x - f.cx) * f.ft + f.cx;
-	v.y = (v.y - f.cy) * f.ft + f.cy;
-	v.z = (v.z - f.cz) * f.ft + f.cz;
-	L.x *= f.fr;
-	L.y *= f.fr;
-	L.z *= f.fr;
-}
-
-// the factors for the system of this lane's nucleotide, for a warp whose nucleotides may
-// belong to several systems (the distinct systems in turn, warp-uniform); lanes past the last
-// nucleotide pass sy = -1
-__device__ __forceinline__ BussiFactors bussi_factors_warp(const ThermoArgs &t, int sy, int i, long long s) {
-	BussiFactors mine{1.0, 1.0, 0.0, 0.0, 0.0};
-	unsigned todo = __ballot_sync(0xffffffffu, sy >= 0);
-	while(todo) {
-		const int leader = __ffs(todo) - 1;
-		const int cur = __shfl_sync(0xffffffffu, sy, leader);
-		const bool first = __any_sync(0xffffffffu, sy == cur && i == t.sys_off[cur]);
-		const BussiFactors f = bussi_factors(t, cur, s, first);
-		if(sy == cur) mine = f;
-		todo &= ~__ballot_sync(0xffffffffu, sy == cur);
-	}
-	return mine;
+// the rescaling of the last Bussi update of system sy, applied to one nucleotide
+static __device__ __forceinline__ void bussi_rescale(const ThermoArgs &t, int sy, double4_32a &v, double4_32a &L) {
+	const double *st = t.bussi_state + 16 * sy;
+	const double ft = __ldcg(st + 2), fr = __ldcg(st + 3), cx = __ldcg(st + 4), cy = __ldcg(st + 5), cz = __ldcg(st + 6);
+	v.x = (v.x - cx) * ft + cx;
+	v.y = (v.y - cy) * ft + cy;
+	v.z = (v.z - cz) * ft + cz;
+	L.x *= fr;
+	L.y *= fr;
+	L.z *= fr;
 }
 
 }  // namespace oxgb
