@@ -215,6 +215,36 @@ int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r);
  * energies scale with T; the lists are rebuilt) -- the replica-exchange hook.  Velocities are
  * left to the caller (a swap usually rescales them by sqrt(T_new / T_old)). */
 int oxgb_md_set_temperature(oxgb_md *h, int k, double T);
+/*
+ * External forces, the CUDA backend's set_external_forces (src/CUDA/Backends/CUDA_MD.cuh:97-200)
+ * for the force types of src/Forces/{ConstantRateForce,MutualTrap,MovingTrap,LowdimMovingTrap,
+ * RepulsionPlane,AttractionPlane}.cpp.  Each record acts on one nucleotide (global index) and
+ * is evaluated at every force evaluation from the FP64 positions, with `step` the MD step being
+ * computed (0 for a state just uploaded); no torques, no energies (as in the reference).
+ *   CONSTANT:          F += (F0 + rate step) dir, dir -> unit(dir - r) if flags & 1
+ *   MUTUAL_TRAP:       d = r(ref) - r (minimum image if flags & 1), F += d (|d| - (r0 + rate step))
+ *                      (stiff + stiff_rate step) / |d|
+ *   MOVING_TRAP:       F += -stiff (r - (pos0 + rate step dir))
+ *   LOWDIM_TRAP:       the same on the components whose flags bit (2: x, 4: y, 8: z) is set
+ *   REPULSION_PLANE:   p = position + rate step, stopped at r0 (the end position) when rate != 0;
+ *                      d = dir . r + p; F += -d stiff dir where d < 0
+ *   ATTRACTION_PLANE:  d = dir . r + position; F += -d stiff dir where d < 0, else -stiff dir
+ */
+enum {
+	OXGB_FORCE_CONSTANT = 0,
+	OXGB_FORCE_MUTUAL_TRAP = 1,
+	OXGB_FORCE_MOVING_TRAP = 2,
+	OXGB_FORCE_LOWDIM_TRAP = 3,
+	OXGB_FORCE_REPULSION_PLANE = 4,
+	OXGB_FORCE_ATTRACTION_PLANE = 5
+};
+typedef struct oxgb_ext_force {
+	int type, particle, ref_particle, flags;
+	double F0, rate, stiff, stiff_rate, r0, position;
+	double dir[3], pos0[3];
+} oxgb_ext_force;
+/* replaces the engine's external forces by f[0 .. n-1] (n = 0 removes them) */
+int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_force *f);
 /* velocities and angular momenta of system k times f (after a temperature swap: f =
  * sqrt(T_new / T_old)); no counterpart in the reference's CUDA backend, which has no batches */
 int oxgb_md_scale_momenta(oxgb_md *h, int k, double f);

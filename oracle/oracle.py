@@ -191,3 +191,53 @@ def md_run(params: Params, md: MD, state: dict, n3, n5, typ, btype, L: float, st
                           _c(typ, np.int32), _c(btype, np.int32), float(L), state["F"].reshape(-1),
                           state["T"].reshape(-1), int(step0), int(nsteps), Es, nthreads)
     return rc, Es
+
+
+def external_forces(pos, step, forces, box):
+    """Forces of the external-force records on every nucleotide, as the reference CUDA backend's
+    set_external_forces computes them (src/CUDA/Backends/CUDA_MD.cuh:97-200: CUDA_TRAP_CONSTANT
+    :114-130, CUDA_TRAP_MUTUAL :131-143, CUDA_TRAP_MOVING :144-153, CUDA_TRAP_MOVING_LOWDIM
+    :154-163, CUDA_REPULSION_PLANE :164-177, CUDA_ATTRACTION_PLANE :178-190), in FP64.  `forces`
+    are the dicts MDSystem.set_external_forces takes."""
+    pos = np.asarray(pos, np.float64)
+    F = np.zeros_like(pos)
+    st = float(step)
+    for d in forces:
+        i = int(d["particle"])
+        r = pos[i]
+        t = d["type"]
+        direction = np.asarray(d.get("dir", (0.0, 0.0, 0.0)), np.float64)
+        if t in ("constant", "string"):
+            inten = d.get("F0", 0.0) + st * d.get("rate", 0.0)
+            dv = direction.copy()
+            if d.get("dir_as_centre"):
+                dv = dv - r
+                dv = dv / np.linalg.norm(dv)
+            F[i] += dv * inten
+        elif t == "mutual_trap":
+            dr = pos[int(d["ref_particle"])] - r
+            if d.get("PBC"):
+                dr = dr - np.rint(dr / box) * box
+            dm = np.linalg.norm(dr)
+            F[i] += dr * ((dm - (d.get("r0", 0.0) + d.get("rate", 0.0) * st)) *
+                          (d.get("stiff", 0.0) + st * d.get("stiff_rate", 0.0)) / dm)
+        elif t in ("trap", "moving_trap", "lowdim_trap"):
+            tgt = np.asarray(d.get("pos0", (0.0, 0.0, 0.0)), np.float64) + d.get("rate", 0.0) * st * direction
+            f = -d.get("stiff", 0.0) * (r - tgt)
+            if t == "lowdim_trap":
+                f = f * np.asarray(d.get("visibility", (True, True, True)), np.float64)
+            F[i] += f
+        elif t == "repulsion_plane":
+            p0, end = d.get("position", 0.0), d.get("r0", 0.0)
+            p = p0 + d.get("rate", 0.0) * st
+            if end > p0 and p > end:
+                p = end
+            if end < p0 and p < end:
+                p = end
+            dist = direction @ r + p
+            if dist < 0:
+                F[i] += -dist * d.get("stiff", 0.0) * direction
+        elif t == "attraction_plane":
+            dist = direction @ r + d.get("position", 0.0)
+            F[i] += (-dist if dist < 0 else -1.0) * d.get("stiff", 0.0) * direction
+    return F

@@ -39,6 +39,18 @@ class DNA2Settings(C.Structure):
     ]
 
 
+class ExtForce(C.Structure):
+    _fields_ = [
+        ("type", C.c_int), ("particle", C.c_int), ("ref_particle", C.c_int), ("flags", C.c_int),
+        ("F0", C.c_double), ("rate", C.c_double), ("stiff", C.c_double), ("stiff_rate", C.c_double),
+        ("r0", C.c_double), ("position", C.c_double), ("dir", C.c_double * 3), ("pos0", C.c_double * 3),
+    ]
+
+
+FORCE_TYPES = {"constant": 0, "string": 0, "mutual_trap": 1, "trap": 2, "moving_trap": 2, "lowdim_trap": 3,
+               "repulsion_plane": 4, "attraction_plane": 5}
+
+
 class MDSettings(C.Structure):
     _fields_ = [
         ("dt", C.c_double), ("verlet_skin", C.c_double), ("thermostat", C.c_int), ("newtonian_steps", C.c_int),
@@ -80,6 +92,7 @@ SIGNATURES = {
     "oxgb_md_compute_forces": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "oxgb_md_get_forces": (C.c_int, [_VP, _VP, _VP, _VP]),
     "oxgb_md_scale_momenta": (C.c_int, [_VP, C.c_int, C.c_double]),
+    "oxgb_md_set_external_forces": (C.c_int, [_VP, C.c_int, C.POINTER(ExtForce)]),
     "oxgb_md_energies": (C.c_int, [_VP, _VP, _VP, _VP]),
     "oxgb_md_set_temperature": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_neighbours": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),

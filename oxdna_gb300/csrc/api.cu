@@ -374,6 +374,9 @@ struct oxgb_md {
 	double *esplit = nullptr, *sums = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
 	long long *bussi_stamp = nullptr, *open_step = nullptr;
 	int *term_max = nullptr;
+	void *ext_rec = nullptr;              // external forces grouped by nucleotide
+	int *ext_nuc = nullptr, *ext_off = nullptr;
+	int ext_n = 0;
 	bool energies_fresh = false;  // Fe / Te hold the forces and energies of the current state
 
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
@@ -400,7 +403,7 @@ struct oxgb_md {
 					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
-					(void *) bussi_stamp, (void *) open_step, (void *) term_max, (void *) d_rebuilds})
+					(void *) bussi_stamp, (void *) open_step, (void *) term_max, ext_rec, (void *) ext_nuc, (void *) ext_off, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -507,6 +510,12 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.base_pos = h->tl.base_pos;
 	a.stk_pos = h->tl.stk_pos;
 	a.term_max = h->term_max;
+	a.ext_rec = h->ext_rec;
+	a.ext_nuc = h->ext_nuc;
+	a.ext_off = h->ext_off;
+	a.ext_n = h->ext_n;
+	a.box = (float) h->box[0];
+	a.sys_box = h->n_systems > 1 ? h->d_sys_box : nullptr;
 	a.th = thermo_args(h, step_offset, engine_step);
 	return a;
 }
@@ -1218,6 +1227,63 @@ extern "C" int oxgb_md_set_temperature(oxgb_md *h, int k, double T) {
 		}
 		if(rc) return rc;
 		rc = compute_forces_now(h);
+		if(rc) return rc;
+		return read_status(h);
+	}
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_force *f) {
+	if(!h || n < 0 || (n > 0 && !f)) return fail(OXGB_E_INVALID, "invalid argument");
+	for(int m = 0; m < n; m++) {
+		const oxgb_ext_force &e = f[m];
+		if(e.type < OXGB_FORCE_CONSTANT || e.type > OXGB_FORCE_ATTRACTION_PLANE)
+			return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": unknown type");
+		if(e.particle < 0 || e.particle >= h->N) return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": particle out of range");
+		if(e.type == OXGB_FORCE_MUTUAL_TRAP) {
+			if(e.ref_particle < 0 || e.ref_particle >= h->N || e.ref_particle == e.particle)
+				return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": invalid ref_particle");
+			const auto sys_of = [&](int i) { return (int) (std::upper_bound(h->offsets.begin(), h->offsets.end(), i) - h->offsets.begin()) - 1; };
+			if(sys_of(e.ref_particle) != sys_of(e.particle))
+				return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": a mutual trap crosses two systems");
+		}
+	}
+	CK(cudaStreamSynchronize(h->stream));
+	if(h->gexec) {  // the record count is part of the captured launches
+		cudaGraphExecDestroy(h->gexec);
+		h->gexec = nullptr;
+	}
+	for(void *p : {h->ext_rec, (void *) h->ext_nuc, (void *) h->ext_off})
+		if(p) cudaFree(p);
+	h->ext_rec = nullptr;
+	h->ext_nuc = h->ext_off = nullptr;
+	h->ext_n = 0;
+	if(n == 0) return OXGB_OK;
+	// records grouped by nucleotide, in the given order within a nucleotide
+	std::vector<int> order(n);
+	for(int m = 0; m < n; m++) order[m] = m;
+	std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return f[x].particle < f[y].particle; });
+	std::vector<oxgb_ext_force> rec(n);
+	std::vector<int> nuc, off;
+	for(int m = 0; m < n; m++) {
+		rec[m] = f[order[m]];
+		if(nuc.empty() || nuc.back() != rec[m].particle) {
+			nuc.push_back(rec[m].particle);
+			off.push_back(m);
+		}
+	}
+	off.push_back(n);
+	CK(cudaMalloc(&h->ext_rec, sizeof(oxgb_ext_force) * n));
+	CK(cudaMalloc(&h->ext_nuc, sizeof(int) * nuc.size()));
+	CK(cudaMalloc(&h->ext_off, sizeof(int) * off.size()));
+	CK(cudaMemcpy(h->ext_rec, rec.data(), sizeof(oxgb_ext_force) * n, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->ext_nuc, nuc.data(), sizeof(int) * nuc.size(), cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->ext_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+	h->ext_n = (int) nuc.size();
+	h->energies_fresh = false;
+	// the forces of the current state now include them
+	if(h->have_state) {
+		int rc = compute_forces_now(h);
 		if(rc) return rc;
 		return read_status(h);
 	}

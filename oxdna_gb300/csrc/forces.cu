@@ -703,6 +703,80 @@ int nonbonded_blocks(int N) {
 	return (int) ((threads + 127) / 128);
 }
 
+// External forces (CUDA_MD.cuh:97-200): one thread per nucleotide that has some, its records
+// in order (deterministic), added to the force the pair kernels left; FP64 positions.
+template <typename V4>
+__global__ void k_external(ForceArgs a) {
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= a.ext_n) return;
+	const int i = a.ext_nuc[k];
+	const long long step = a.th.step_base ? *a.th.step_base + a.th.step_offset : 0;
+	const double st = (double) step;
+	const oxgb_ext_force *rec = reinterpret_cast<const oxgb_ext_force *>(a.ext_rec);
+	const double4_32a r = a.posd[i];
+	double fx = 0, fy = 0, fz = 0;
+	for(int m = a.ext_off[k]; m < a.ext_off[k + 1]; m++) {
+		const oxgb_ext_force &e = rec[m];
+		switch(e.type) {
+		case OXGB_FORCE_CONSTANT: {
+			const double in = e.F0 + st * e.rate;
+			double dx = e.dir[0], dy = e.dir[1], dz = e.dir[2];
+			if(e.flags & 1) {
+				dx -= r.x, dy -= r.y, dz -= r.z;
+				const double n = sqrt(dx * dx + dy * dy + dz * dz);
+				dx /= n, dy /= n, dz /= n;
+			}
+			fx += dx * in, fy += dy * in, fz += dz * in;
+			break;
+		}
+		case OXGB_FORCE_MUTUAL_TRAP: {
+			const double4_32a q = a.posd[e.ref_particle];
+			double dx = q.x - r.x, dy = q.y - r.y, dz = q.z - r.z;
+			if(e.flags & 1) {
+				const double L = a.sys_box ? (double) a.sys_box[a.sys ? a.sys[i] : 0] : (double) a.box;
+				dx -= rint(dx / L) * L, dy -= rint(dy / L) * L, dz -= rint(dz / L) * L;
+			}
+			const double d = sqrt(dx * dx + dy * dy + dz * dz);
+			const double c = (d - (e.r0 + e.rate * st)) * (e.stiff + st * e.stiff_rate) / d;
+			fx += dx * c, fy += dy * c, fz += dz * c;
+			break;
+		}
+		case OXGB_FORCE_MOVING_TRAP:
+		case OXGB_FORCE_LOWDIM_TRAP: {
+			const double tx = e.pos0[0] + e.rate * st * e.dir[0], ty = e.pos0[1] + e.rate * st * e.dir[1],
+						 tz = e.pos0[2] + e.rate * st * e.dir[2];
+			const bool all = e.type == OXGB_FORCE_MOVING_TRAP;
+			if(all || (e.flags & 2)) fx += -e.stiff * (r.x - tx);
+			if(all || (e.flags & 4)) fy += -e.stiff * (r.y - ty);
+			if(all || (e.flags & 8)) fz += -e.stiff * (r.z - tz);
+			break;
+		}
+		case OXGB_FORCE_REPULSION_PLANE: {
+			double p = e.position + e.rate * st;
+			if(e.r0 > e.position && p > e.r0) p = e.r0;
+			if(e.r0 < e.position && p < e.r0) p = e.r0;
+			const double d = e.dir[0] * r.x + e.dir[1] * r.y + e.dir[2] * r.z + p;
+			if(d < 0.0) fx += -d * e.stiff * e.dir[0], fy += -d * e.stiff * e.dir[1], fz += -d * e.stiff * e.dir[2];
+			break;
+		}
+		case OXGB_FORCE_ATTRACTION_PLANE: {
+			const double d = e.dir[0] * r.x + e.dir[1] * r.y + e.dir[2] * r.z + e.position;
+			if(d < 0.0) fx += -d * e.stiff * e.dir[0], fy += -d * e.stiff * e.dir[1], fz += -d * e.stiff * e.dir[2];
+			else fx += -e.stiff * e.dir[0], fy += -e.stiff * e.dir[1], fz += -e.stiff * e.dir[2];
+			break;
+		}
+		default:
+			break;
+		}
+	}
+	V4 *F = reinterpret_cast<V4 *>(a.forces);
+	V4 f = F[i];
+	f.x += fx;
+	f.y += fy;
+	f.z += fz;
+	F[i] = f;
+}
+
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
 static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEvent_t wait) {
 	const int tpb = 128;
@@ -715,6 +789,7 @@ static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEv
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
 	k_nonbonded_split<R, Loader, SPLIT, ENERGY, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
+	if(a.ext_n > 0) k_external<typename Vec4Of<R>::T><<<(a.ext_n + tpb - 1) / tpb, tpb, 0, s>>>(a);
 }
 
 template <typename R, class Loader, bool SPLIT, bool ENERGY>

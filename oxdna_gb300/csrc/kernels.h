@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/oxgb.h"
 #include "dna2_pair.cuh"
 
 // device status bits (OR-ed by kernels, read by the host between launches)
@@ -82,6 +83,13 @@ struct ForceArgs {
 	const int *term_max;                      // [3] longest EV / base / stack list (slots past it are empty)
 	// MD-step bookkeeping (engine layout): the bonded kernel marks the step's half kick pending
 	ThermoArgs th;
+	// external forces (oxgb_ext_force records grouped by nucleotide): ext_n nucleotides
+	// ext_nuc[k] with records ext_off[k] .. ext_off[k + 1] - 1
+	const void *ext_rec;
+	const int *ext_nuc, *ext_off;
+	int ext_n;
+	float box;                                // cubic box of the (single-system) engine
+	const float *sys_box;                     // per system (batches), or null
 };
 
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);

@@ -156,6 +156,34 @@ class MDSystem:
     def set_temperature(self, T: float, k: int = 0):
         _abi.check(_abi.lib().oxgb_md_set_temperature(self._h, int(k), float(T)))
 
+    def set_external_forces(self, forces):
+        """External forces (oxgb_md_set_external_forces): a list of dicts with 'type' (constant /
+        string, mutual_trap, trap / moving_trap, lowdim_trap, repulsion_plane, attraction_plane),
+        'particle' and the parameters of oxgb_ext_force ('ref_particle', 'F0', 'rate', 'stiff',
+        'stiff_rate', 'r0', 'position', 'dir', 'pos0', and 'dir_as_centre' / 'PBC' / 'visibility'
+        for the flags).  Particle indices are global (offsets[k] + index within system k)."""
+        arr = (_abi.ExtForce * max(1, len(forces)))()
+        for m, d in enumerate(forces):
+            e = arr[m]
+            e.type = _abi.FORCE_TYPES[d["type"]]
+            e.particle = int(d["particle"])
+            e.ref_particle = int(d.get("ref_particle", -1))
+            flags = 0
+            if d.get("dir_as_centre") or d.get("PBC"):
+                flags |= 1
+            vis = d.get("visibility", (True, True, True))
+            for bit, on in zip((2, 4, 8), vis):
+                if on:
+                    flags |= bit
+            e.flags = flags
+            for key in ("F0", "rate", "stiff", "stiff_rate", "r0", "position"):
+                setattr(e, key, float(d.get(key, 0.0)))
+            for key in ("dir", "pos0"):
+                v = d.get(key, (0.0, 0.0, 0.0))
+                for c in range(3):
+                    getattr(e, key)[c] = float(v[c])
+        _abi.check(_abi.lib().oxgb_md_set_external_forces(self._h, len(forces), arr))
+
     def scale_momenta(self, f: float, k: int = 0):
         _abi.check(_abi.lib().oxgb_md_scale_momenta(self._h, int(k), float(f)))
 
