@@ -405,11 +405,19 @@ def main():
                "d2h_bytes_per_step": h2d, "md_steps_per_step": M}
         assert np.all(np.isfinite(got["pos"]))
 
-    # our kernels in the timed region: per MD step the first step, the rebuild condition, the
-    # bonded and non-bonded kernels (+ the Bussi draws and sums); per rebuild 9 list kernels; per
-    # graph of 25 steps the step advance; per run the 2-kernel flush
-    per_step = 4 + (2 if wl["thermostat"] == "bussi" else 0)
-    gpu_launches = steps_total * per_step + rebuilds * 9 + (steps_total // 25) + 2 * args.steps
+    # our kernels in the timed region: per MD step the first step, the bonded, pair and
+    # non-bonded kernels, the Bussi draws, sums and update, and either the rebuild condition
+    # (conditional node: 10 list kernels per rebuild) or the 10 list kernels themselves (kernel
+    # node: they return at once unless a system is stale); per graph of 25 steps the step
+    # advance; per run the 2-kernel flush
+    per_step = 4 + (3 if wl["thermostat"] == "bussi" else 0)
+    if args.list_node == "conditional":
+        per_step += 1
+        list_launches = rebuilds * 10
+    else:
+        per_step += 10
+        list_launches = 0
+    gpu_launches = steps_total * per_step + list_launches + (steps_total // 25) + 2 * args.steps
 
     if rank == 0 and world == 1 and not args.no_batched:
         line_extra["batched"] = bench_batched(args, torch, ox, _abi)

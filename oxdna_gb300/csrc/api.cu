@@ -1233,6 +1233,31 @@ extern "C" int oxgb_md_set_temperature(oxgb_md *h, int k, double T) {
 	return OXGB_OK;
 }
 
+// records grouped by nucleotide, in the given order within a nucleotide
+static int upload_external_forces(oxgb_md *h, int n, const oxgb_ext_force *f) {
+	std::vector<int> order(n);
+	for(int m = 0; m < n; m++) order[m] = m;
+	std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return f[x].particle < f[y].particle; });
+	std::vector<oxgb_ext_force> rec(n);
+	std::vector<int> nuc, off;
+	for(int m = 0; m < n; m++) {
+		rec[m] = f[order[m]];
+		if(nuc.empty() || nuc.back() != rec[m].particle) {
+			nuc.push_back(rec[m].particle);
+			off.push_back(m);
+		}
+	}
+	off.push_back(n);
+	CK(cudaMalloc(&h->ext_rec, sizeof(oxgb_ext_force) * n));
+	CK(cudaMalloc(&h->ext_nuc, sizeof(int) * nuc.size()));
+	CK(cudaMalloc(&h->ext_off, sizeof(int) * off.size()));
+	CK(cudaMemcpy(h->ext_rec, rec.data(), sizeof(oxgb_ext_force) * n, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->ext_nuc, nuc.data(), sizeof(int) * nuc.size(), cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->ext_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+	h->ext_n = (int) nuc.size();
+	return OXGB_OK;
+}
+
 extern "C" int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_force *f) {
 	if(!h || n < 0 || (n > 0 && !f)) return fail(OXGB_E_INVALID, "invalid argument");
 	for(int m = 0; m < n; m++) {
@@ -1258,30 +1283,12 @@ extern "C" int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_for
 	h->ext_rec = nullptr;
 	h->ext_nuc = h->ext_off = nullptr;
 	h->ext_n = 0;
-	if(n == 0) return OXGB_OK;
-	// records grouped by nucleotide, in the given order within a nucleotide
-	std::vector<int> order(n);
-	for(int m = 0; m < n; m++) order[m] = m;
-	std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return f[x].particle < f[y].particle; });
-	std::vector<oxgb_ext_force> rec(n);
-	std::vector<int> nuc, off;
-	for(int m = 0; m < n; m++) {
-		rec[m] = f[order[m]];
-		if(nuc.empty() || nuc.back() != rec[m].particle) {
-			nuc.push_back(rec[m].particle);
-			off.push_back(m);
-		}
+	if(n > 0) {
+		int rc = upload_external_forces(h, n, f);
+		if(rc) return rc;
 	}
-	off.push_back(n);
-	CK(cudaMalloc(&h->ext_rec, sizeof(oxgb_ext_force) * n));
-	CK(cudaMalloc(&h->ext_nuc, sizeof(int) * nuc.size()));
-	CK(cudaMalloc(&h->ext_off, sizeof(int) * off.size()));
-	CK(cudaMemcpy(h->ext_rec, rec.data(), sizeof(oxgb_ext_force) * n, cudaMemcpyHostToDevice));
-	CK(cudaMemcpy(h->ext_nuc, nuc.data(), sizeof(int) * nuc.size(), cudaMemcpyHostToDevice));
-	CK(cudaMemcpy(h->ext_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
-	h->ext_n = (int) nuc.size();
 	h->energies_fresh = false;
-	// the forces of the current state now include them
+	// the forces of the current state now include them (or no longer do)
 	if(h->have_state) {
 		int rc = compute_forces_now(h);
 		if(rc) return rc;
@@ -1289,6 +1296,7 @@ extern "C" int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_for
 	}
 	return OXGB_OK;
 }
+
 
 extern "C" int oxgb_md_scale_momenta(oxgb_md *h, int k, double f) {
 	if(!h || k < 0 || k >= h->n_systems || !(f > 0)) return fail(OXGB_E_INVALID, "invalid argument");
