@@ -373,6 +373,7 @@ struct oxgb_md {
 	long long *step = nullptr;
 	double *esplit = nullptr, *sums = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
 	long long *bussi_stamp = nullptr, *open_step = nullptr;
+	unsigned *bussi_done = nullptr;
 	int *term_max = nullptr;
 	void *ext_rec = nullptr;              // external forces grouped by nucleotide
 	int *ext_nuc = nullptr, *ext_off = nullptr;
@@ -403,7 +404,7 @@ struct oxgb_md {
 					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
-					(void *) bussi_stamp, (void *) open_step, (void *) term_max, ext_rec, (void *) ext_nuc, (void *) ext_off, (void *) d_rebuilds})
+					(void *) bussi_stamp, (void *) open_step, (void *) bussi_done, (void *) term_max, ext_rec, (void *) ext_nuc, (void *) ext_off, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -434,6 +435,7 @@ static ThermoArgs thermo_args(oxgb_md *h, int step_offset = 0, bool engine_step 
 	t.bussi_partials = h->bussi_partials;
 	t.bussi_state = h->bussi_state;
 	t.bussi_stamp = h->bussi_stamp;
+	t.bussi_done = h->bussi_done;
 	t.open_step = engine_step ? h->open_step : nullptr;
 	t.step_base = h->step;
 	t.step_offset = step_offset;
@@ -712,6 +714,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * h->n_chunks) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16 * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned) * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->open_step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->term_max, sizeof(int) * 3) == cudaSuccess;
@@ -724,6 +727,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMemcpy(h->d_sys_chunk0, h->sys_chunk0.data(), sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_sys_seed, seeds.data(), sizeof(unsigned long long) * n_systems, cudaMemcpyHostToDevice) == cudaSuccess;
 	ok &= cudaMemset(h->d_sys_stale, 0, sizeof(int) * n_systems) == cudaSuccess;
+	ok &= cudaMemset(h->bussi_done, 0, sizeof(unsigned) * n_systems) == cudaSuccess;
 	ok &= cudaMemset(h->status, 0, sizeof(int)) == cudaSuccess;
 	ok &= cudaMemset(h->flag, 0, sizeof(int)) == cudaSuccess;
 	ok &= cudaMemset(h->step, 0, sizeof(long long)) == cudaSuccess;

@@ -402,15 +402,16 @@ __device__ __forceinline__ void load_dh<SplitMixed, float>(const SplitMixed &ld,
 	ld.dh(j, n, h, l);
 }
 
+// bonded block b: one bond (owner p, partner q = n3[p]) per thread; the bonded blocks cover
+// every nucleotide
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
-__global__ void __launch_bounds__(128) k_bonded_split(ForceArgs a, Loader ld) {
+__device__ __forceinline__ void bonded_block(const ForceArgs &a, const Loader &ld, int b) {
 	using V4 = typename Vec4Of<R>::T;
-	// one bond (owner p, partner q = n3[p]) per thread; the grid covers every nucleotide
-	const int first = blockIdx.x * blockDim.x;
+	const int first = b * blockDim.x;
 	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
 	const int s0 = load_table_span<R>(a, first, min(first + (int) blockDim.x, a.N) - 1, Ps);
 	// an MD step: from here on its second half kick is pending (the first step has read the mark)
-	if(a.th.open_step && blockIdx.x == 0 && threadIdx.x == 0) *a.th.open_step = *a.th.step_base + a.th.step_offset;
+	if(a.th.open_step && b == 0 && threadIdx.x == 0) *a.th.open_step = *a.th.step_base + a.th.step_offset;
 	const int p = first + threadIdx.x;
 	if(p < a.N) {
 		const int q = a.bonds[p].x;
@@ -458,7 +459,7 @@ struct SplitAcc {
 			for(int k = 0; k < N_TERMS; k++) split[k] += o.split[k];
 		}
 	}
-	// entry k of nucleotide i's list: its result, written by k_pair_slots
+	// entry k of nucleotide i's list: its result, written by the pair blocks of k_bonded_pairs
 	template <typename V4>
 	__device__ __forceinline__ void add_slot(const V4 *res, long long N, int i, int k) {
 		const long long s = (long long) k * N + i;
@@ -480,19 +481,19 @@ struct SplitAcc {
 // costliest terms and their lists are short, so the owned slots of a warp's 32 nucleotides
 // are queued (a warp prefix sum over the per-lane counts) and dealt 32 at a time: every lane
 // works on a pair in every round but the last.
-// nucleotides per warp in k_pair_slots: fewer than 32 gives more warps (more latency hidden)
+// nucleotides per warp in a pair block: fewer than 32 gives more warps (more latency hidden)
 // for about as many rounds of pairs per warp as a full-warp queue
 #ifndef OXGB_PAIR_NPW
 #define OXGB_PAIR_NPW 16
 #endif
 
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
-__global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int base_blocks) {
+__device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld, int b, int base_blocks) {
 	using V4 = typename Vec4Of<R>::T;
 	constexpr int NPW = OXGB_PAIR_NPW;
-	const bool is_base = (int) blockIdx.x < base_blocks;
+	const bool is_base = b < base_blocks;
 	const int per_block = (blockDim.x / 32) * NPW;
-	const int first = (is_base ? blockIdx.x : blockIdx.x - base_blocks) * per_block;
+	const int first = (is_base ? b : b - base_blocks) * per_block;
 	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
 	const int s0 = load_table_span<R>(a, first, min(first + per_block, a.N) - 1, Ps);
 	const long long N = a.N;
@@ -573,6 +574,16 @@ __global__ void __launch_bounds__(128) k_pair_slots(ForceArgs a, Loader ld, int 
 	}
 }
 
+// The bonded and the base/stack pair work are independent (both read the mirrors, each writes
+// its own result buffers), so they share one launch: blocks 0 .. 2 pair_blocks - 1 are pair
+// blocks (the costliest, dispatched first), the rest bonded blocks, which fill the tail.
+template <typename R, class Loader, bool SPLIT, bool ENERGY>
+__global__ void __launch_bounds__(128) k_bonded_pairs(ForceArgs a, Loader ld, int pair_blocks) {
+	const int b = blockIdx.x;
+	if(b < 2 * pair_blocks) pair_block<R, Loader, SPLIT, ENERGY>(a, ld, b, pair_blocks);
+	else bonded_block<R, Loader, SPLIT, ENERGY>(a, ld, b - 2 * pair_blocks);
+}
+
 // compensated sum over the K lanes of a group (TwoSum at every level); every lane of the group
 // receives it
 template <typename R, int K>
@@ -642,7 +653,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 			acc.add(o);
 		}
 		// hydrogen bonding + cross stacking and coaxial stacking: evaluated per list slot by
-		// k_pair_slots, gathered here
+		// the pair blocks of k_bonded_pairs, gathered here
 		const int nb_ = live ? min(a.base_n[i], a.base_cap) : 0;
 		for(int k = sub; k < nb_; k += K) acc.add_slot(reinterpret_cast<const V4 *>(a.base_res), N, i, k);
 		const int ns = live ? min(a.stk_n[i], a.stk_cap) : 0;
@@ -653,7 +664,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 				if(acc.split[k] != R(0)) atomicAdd(a.esplit + 8 * sy + k, 0.5 * (double) acc.split[k]);
 		}
 
-		// bonded pairs of this nucleotide, evaluated by k_bonded_split (first lane of the group)
+		// bonded pairs of this nucleotide, evaluated by the bonded blocks of k_bonded_pairs (first
+		// lane of the group)
 		if(sub == 0 && live) {
 			const int2 bi = a.bonds[i];
 			const V4 *bf = reinterpret_cast<const V4 *>(a.bond_f);
@@ -782,10 +794,10 @@ static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEv
 	const int tpb = 128;
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	const size_t smem = sizeof(DNA2Table<R>) * (size_t) (a.tab_span > 0 ? a.tab_span : 1);
-	k_bonded_split<R, Loader, SPLIT, ENERGY><<<blocks, tpb, smem, s>>>(a, ld);
-	// blocks of 4 warps x OXGB_PAIR_NPW nucleotides per term
+	// pair blocks of 4 warps x OXGB_PAIR_NPW nucleotides per term, then one bonded block per
+	// 128 nucleotides
 	const int pair_blocks = (a.N + 4 * OXGB_PAIR_NPW - 1) / (4 * OXGB_PAIR_NPW);
-	k_pair_slots<R, Loader, SPLIT, ENERGY><<<2 * pair_blocks, tpb, smem, s>>>(a, ld, pair_blocks);
+	k_bonded_pairs<R, Loader, SPLIT, ENERGY><<<2 * pair_blocks + blocks, tpb, smem, s>>>(a, ld, pair_blocks);
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
 	k_nonbonded_split<R, Loader, SPLIT, ENERGY, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
@@ -794,10 +806,9 @@ static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEv
 
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
 static cudaError_t allow_smem_t(int bytes) {
-	cudaError_t e = cudaFuncSetAttribute(k_bonded_split<R, Loader, SPLIT, ENERGY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaError_t e = cudaFuncSetAttribute(k_bonded_pairs<R, Loader, SPLIT, ENERGY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	if(e == cudaSuccess)
 		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, SPLIT, ENERGY, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-	if(e == cudaSuccess) e = cudaFuncSetAttribute(k_pair_slots<R, Loader, SPLIT, ENERGY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	return e;
 }
 

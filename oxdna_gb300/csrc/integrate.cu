@@ -11,7 +11,7 @@
 // update runs on the device (its gamma deviate uses the same algorithm as the reference).
 // The second half kick of a step and its thermostat are deferred to the next first step (or
 // to the flush at the end of a run), where they run one thread per nucleotide next to the
-// first half kick; the Bussi sums run after the forces (k_bussi_sums, k_bussi_update) and its
+// first half kick; the Bussi sums and update run after the forces (k_bussi_sums) and its
 // draws on a parallel branch of the step graph (k_bussi_noise).  No FP64 work is left in the force
 // kernels, whose lanes are mostly idle at the epilogue.
 #include "thermo.cuh"
@@ -175,9 +175,37 @@ __global__ void k_bussi_noise(StepArgs a) {
 	a.th.bussi_state[16 * sy + 9 + 2 * w] = rr;
 }
 
+// the update of system sy from its chunk sums, reduced by the block in a fixed chunk order (the
+// result does not depend on which block runs it): translation on thread 0 and rotation on
+// thread 32 (two warps: the chains overlap).  red is the block's shared scratch.
+__device__ __forceinline__ void bussi_system_update(const StepArgs &a, int sy, long long s, double (*red)[8]) {
+	const int c0 = a.th.sys_chunk0[sy], nc = a.th.sys_chunk0[sy + 1] - c0;
+	double part[5] = {0, 0, 0, 0, 0};
+	for(int b = threadIdx.x; b < nc; b += blockDim.x)
+#pragma unroll
+		for(int k = 0; k < 5; k++) part[k] += __ldcg(a.th.bussi_partials + (c0 + b) * 8 + k);
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+	for(int k = 0; k < 5; k++) {
+		double x = part[k];
+		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+		if(lane == 0) red[k][w] = x;
+	}
+	__syncthreads();
+	if(threadIdx.x != 0 && threadIdx.x != 32) return;
+	double sum[5];
+	for(int k = 0; k < 5; k++) {
+		double x = 0;
+		for(int u = 0; u < nw; u++) x += red[k][u];
+		sum[k] = x;
+	}
+	bussi_update(a.th, sy, s, threadIdx.x == 0 ? 0 : 1, sum);
+}
+
 // Bussi step s, after its forces: sums of v, |v|^2 and |L|^2 over the completed velocities
 // v + dt/2 F (computed here, stored by the next first step), one block per chunk of up to 256
-// nucleotides of one system
+// nucleotides of one system.  The block that finishes a system's last outstanding chunk (a
+// per-system arrival counter) makes that system's update, so there is no separate update launch.
 template <typename V4>
 __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 	const long long s = step_of(a.th);
@@ -204,6 +232,7 @@ __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 		acc[4] = L.x * L.x + L.y * L.y + L.z * L.z;
 	}
 	__shared__ double red[5][8];
+	__shared__ int last;
 	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
 	for(int k = 0; k < 5; k++) {
@@ -216,39 +245,22 @@ __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 		double x = 0;
 		for(int u = 0; u < nw; u++) x += red[threadIdx.x][u];
 		a.th.bussi_partials[c * 8 + threadIdx.x] = x;
-	}
-}
-
-// the update of system blockIdx.x: its chunk sums reduced in a fixed order (deterministic),
-// translation on thread 0 and rotation on thread 32 (two warps: the chains overlap)
-__global__ void __launch_bounds__(256) k_bussi_update(StepArgs a) {
-	const long long s = step_of(a.th);
-	if(s % a.th.newtonian_steps != 0) return;
-	const int sy = blockIdx.x;
-	// the next first step applies the rescaling of step s (every system updates at the same steps)
-	if(sy == 0 && threadIdx.x == 0) *a.th.bussi_stamp = s;
-	const int c0 = a.th.sys_chunk0[sy], nc = a.th.sys_chunk0[sy + 1] - c0;
-	double part[5] = {0, 0, 0, 0, 0};
-	for(int b = threadIdx.x; b < nc; b += blockDim.x)
-#pragma unroll
-		for(int k = 0; k < 5; k++) part[k] += a.th.bussi_partials[(c0 + b) * 8 + k];
-	__shared__ double red[5][8];
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-	for(int k = 0; k < 5; k++) {
-		double x = part[k];
-		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-		if(lane == 0) red[k][w] = x;
+		__threadfence();  // the partial is visible device-wide before this block arrives
 	}
 	__syncthreads();
-	if(threadIdx.x != 0 && threadIdx.x != 32) return;
-	double sum[5];
-	for(int k = 0; k < 5; k++) {
-		double x = 0;
-		for(int u = 0; u < nw; u++) x += red[k][u];
-		sum[k] = x;
+	if(threadIdx.x == 0) {
+		const unsigned nc = (unsigned) (a.th.sys_chunk0[sy + 1] - a.th.sys_chunk0[sy]);
+		last = atomicAdd(a.th.bussi_done + sy, 1u) == nc - 1u;
+		if(last) {
+			a.th.bussi_done[sy] = 0u;  // every chunk has arrived: ready for the next step
+			// the next first step applies the rescaling of step s (every system updates at the same steps)
+			if(sy == 0) *a.th.bussi_stamp = s;
+		}
 	}
-	bussi_update(a.th, sy, s, threadIdx.x == 0 ? 0 : 1, sum);
+	__syncthreads();
+	if(!last) return;
+	__threadfence();
+	bussi_system_update(a, sy, s, red);
 }
 
 __global__ void k_step_advance(StepArgs a, int K) {
@@ -345,7 +357,6 @@ cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
 cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s) {
 	if(double_forces) k_bussi_sums<double4_32a><<<n_chunks, 256, 0, s>>>(a);
 	else k_bussi_sums<float4><<<n_chunks, 256, 0, s>>>(a);
-	k_bussi_update<<<a.th.n_systems, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

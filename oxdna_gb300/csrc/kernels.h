@@ -47,6 +47,7 @@ struct ThermoArgs {
 	double *bussi_state;                   // [n_systems * 16]: K_t, K_r, factor_t, factor_r,
 	                                       // vcom x y z, -, then the step's draws: sum_t, rr_t,
 	                                       // sum_r, rr_r
+	unsigned *bussi_done;                  // [n_systems] chunks arrived in this step's sums (0 between steps)
 	long long *bussi_stamp;                // step of the last Bussi update (OXGB_NO_STEP: none)
 	long long *open_step;                  // step whose second half kick is pending
 	                                       // (OXGB_NO_STEP: none); null in force-only calls

@@ -221,6 +221,13 @@ class _Occupancy:
     def add(self, p, tag):
         self.cells.setdefault(self._key(p), []).append((float(p[0]), float(p[1]), float(p[2]), tag))
 
+    def remove(self, p, tag):
+        cell = self.cells.get(self._key(p), [])
+        for k, e in enumerate(cell):
+            if e[3] == tag:
+                del cell[k]
+                return
+
 
 def random_walk_strand(n: int, rng: np.random.Generator, step: float = FENE_R0, min_sep: float = 0.8,
                        occ: Optional[_Occupancy] = None, start: Optional[np.ndarray] = None,
@@ -258,7 +265,9 @@ def random_walk_strand(n: int, rng: np.random.Generator, step: float = FENE_R0, 
     a1[0] = frame(a3[0], np.cross(a3[0], rng.normal(size=3)))
     occ.add(back[0], (strand_tag, 0))
     occ.add(base_of(back[0], a1[0], a3[0]), (strand_tag, 0))
-    for i in range(1, n):
+    i, backtracks = 1, 0
+    while i < n:
+        ok = False
         for attempt in range(1000):
             trial = d + (0.25 + 0.002 * attempt) * rng.normal(size=3)
             trial /= np.linalg.norm(trial)
@@ -269,11 +278,41 @@ def random_walk_strand(n: int, rng: np.random.Generator, step: float = FENE_R0, 
             bprev = base_of(back[i - 1], a1[i - 1], a3[i - 1])
             if np.linalg.norm(bi - bprev) > 0.45 and np.linalg.norm(bi - back[i - 1]) > 0.6 and \
                     np.linalg.norm(p - bprev) > 0.6 and occ.free(p, (strand_tag, i - 1)) and occ.free(bi, (strand_tag, i - 1)):
+                ok = True
                 break
+        if not ok:
+            # a dead end (every trial overlaps a site placed before): take back the last few
+            # nucleotides, or move the start if the walk is stuck at it, and grow again
+            backtracks += 1
+            if backtracks > 100000:
+                raise RuntimeError("self-avoiding walk: no room left in the box")
+            b = min(i, int(rng.integers(5, 25)))
+            for j in range(i - b, i):
+                occ.remove(back[j], (strand_tag, j))
+                occ.remove(base_of(back[j], a1[j], a3[j]), (strand_tag, j))
+            i -= b
+            if i == 0:
+                for _ in range(100000):
+                    back[0] = rng.uniform(0, occ.box, size=3) if occ.box else back[0] + rng.normal(size=3)
+                    d = rng.normal(size=3)
+                    d /= np.linalg.norm(d)
+                    a3[0] = -d
+                    a1[0] = frame(a3[0], np.cross(a3[0], rng.normal(size=3)))
+                    if occ.free(back[0], None) and occ.free(base_of(back[0], a1[0], a3[0]), None):
+                        break
+                else:
+                    raise RuntimeError("self-avoiding walk: no room left in the box")
+                occ.add(back[0], (strand_tag, 0))
+                occ.add(base_of(back[0], a1[0], a3[0]), (strand_tag, 0))
+                i = 1
+                continue
+            d = -a3[i - 1]
+            continue
         back[i], a3[i], a1[i] = p, t3, t1
         d = trial
         occ.add(p, (strand_tag, i))
         occ.add(base_of(p, t1, t3), (strand_tag, i))
+        i += 1
     a2 = np.cross(a3, a1)
     pos = back - (BACK1 * a1 + BACK2 * a2)
     if own:
