@@ -46,7 +46,7 @@ WORKLOADS = {
     "large250k": dict(cfg=2, scale=1.0, thermostat="john", newtonian_steps=103, diff_coeff=2.5, dt=0.003,
                       relax_steps=1000,
                       desc="250 x 1000-nt random-walk strands (250,000 nt), cube 232.08, Brownian n=103, "
-                           "after 1000 force-capped relaxation steps"),
+                           "after 1000 + 200 force-capped relaxation steps"),
     "duplex24": dict(cfg=0, scale=1.0, thermostat="no", newtonian_steps=1, dt=0.005,
                      desc="one 12-bp duplex (24 nt), cube 20, NVE"),
 }
@@ -71,9 +71,12 @@ def make_system(wl, seed):
 
 
 def relax(s, wl, seed):
-    """Force-capped relaxation of a generated state before it is timed: the backbone force is
-    capped (max_backbone_force = 5, as in the reference's relaxation examples) and a Brownian
-    thermostat refreshes every step.  The relaxed state is cached beside the generated one."""
+    """Force-capped relaxation of a generated state before it is timed: relax_steps steps with
+    the backbone force capped at 5 (max_backbone_force = 5, as in the reference's relaxation
+    examples), then 200 steps capped at 50, under which the bonds that thermal excursions past the
+    soft cap left outside the FENE range return into it; a Brownian thermostat refreshes 10 %
+    of the momenta every step and removes the heat of relaxation.  The relaxed state is cached
+    beside the generated one."""
     from oxdna_gb300 import generate as G
     from oxdna_gb300 import io as oxio
     import oxdna_gb300 as ox
@@ -84,15 +87,18 @@ def relax(s, wl, seed):
     if os.path.exists(cache):
         d = np.load(cache)
         return G.System(s.box, d["pos"], d["a1"], d["a3"], d["vel"], d["L"], s.top, s.T)
-    m = ox.MDSystem(s.box, s.top, ox.dna2_settings(s.T, 0.5, mbf_fmax=5.0),
-                    ox.md_settings(dt=wl["dt"], thermostat="john", newtonian_steps=1, diff_coeff=2.5, seed=seed,
-                                   precision="mixed"))
-    m.set_state(s.pos, s.quats(), s.vel, s.L)
-    m.run(n)
-    st = m.get_state()
-    m.close()
-    a1, _, a3 = oxio.quat_to_frame(st["quat"])
-    out = G.System(s.box, st["pos"], a1, a3, st["vel"], st["Lmom"], s.top, s.T)
+    pos, quat, vel, L = s.pos, s.quats(), s.vel, s.L
+    for fmax, steps in ((5.0, n), (50.0, 200)):
+        m = ox.MDSystem(s.box, s.top, ox.dna2_settings(s.T, 0.5, mbf_fmax=fmax),
+                        ox.md_settings(dt=wl["dt"], thermostat="john", newtonian_steps=1, pt=0.1, seed=seed,
+                                       precision="mixed"))
+        m.set_state(pos, quat, vel, L)
+        m.run(steps)
+        st = m.get_state()
+        m.close()
+        pos, quat, vel, L = st["pos"], st["quat"], st["vel"], st["Lmom"]
+    a1, _, a3 = oxio.quat_to_frame(quat)
+    out = G.System(s.box, pos, a1, a3, vel, L, s.top, s.T)
     np.savez(cache, pos=out.pos, a1=out.a1, a3=out.a3, vel=out.vel, L=out.L)
     return out
 

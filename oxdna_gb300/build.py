@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboxgb.so")
 TOOLS = os.path.join(OUT, "liboxgb_tools.so")
-SOURCES = ["forces.cu", "lists.cu", "integrate.cu", "api.cu", "noalloc.cu", "batched.cu"]
+SOURCES = ["forces.cu", "lists.cu", "integrate.cu", "api.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall,-Wno-unused-function",
          "-Xptxas", "-warn-spills"]

@@ -381,7 +381,8 @@ struct oxgb_md {
 	bool energies_fresh = false;  // Fe / Te hold the forces and energies of the current state
 
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
-	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_first = nullptr;
+	float4 *bussi_vf = nullptr, *bussi_Lf = nullptr;  // Bussi: half-kicked v, L in FP32 (mixed)
 	cudaGraphExec_t gexec = nullptr;
 	int graph_steps = 0;
 	bool conditional_ok = true;
@@ -413,6 +414,9 @@ struct oxgb_md {
 		if(noise) cudaStreamDestroy(noise);
 		if(ev_fork) cudaEventDestroy(ev_fork);
 		if(ev_join) cudaEventDestroy(ev_join);
+		if(ev_first) cudaEventDestroy(ev_first);
+		if(bussi_vf) cudaFree(bussi_vf);
+		if(bussi_Lf) cudaFree(bussi_Lf);
 	}
 };
 
@@ -436,6 +440,8 @@ static ThermoArgs thermo_args(oxgb_md *h, int step_offset = 0, bool engine_step 
 	t.bussi_state = h->bussi_state;
 	t.bussi_stamp = h->bussi_stamp;
 	t.bussi_done = h->bussi_done;
+	t.bussi_vf = h->bussi_vf;
+	t.bussi_Lf = h->bussi_Lf;
 	t.open_step = engine_step ? h->open_step : nullptr;
 	t.step_base = h->step;
 	t.step_offset = step_offset;
@@ -674,7 +680,8 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 			cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
 			cudaStreamCreateWithFlags(&h->noise, cudaStreamNonBlocking) != cudaSuccess ||
 			cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-			cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+			cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+			cudaEventCreateWithFlags(&h->ev_first, cudaEventDisableTiming) != cudaSuccess)
 		return bail(fail(OXGB_E_CUDA, "stream creation failed"));
 	bool ok = true;
 	ok &= cudaMalloc(&h->posd, sizeof(double4_32a) * N) == cudaSuccess;
@@ -711,7 +718,11 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->esplit, sizeof(double) * 8 * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->sums, sizeof(double) * 4 * h->n_chunks) == cudaSuccess;
-	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 8 * h->n_chunks) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_partials, sizeof(double) * 16 * h->n_chunks) == cudaSuccess;
+	if(md->thermostat == OXGB_THERMOSTAT_BUSSI && !h->dbl) {
+		ok &= cudaMalloc(&h->bussi_vf, sizeof(float4) * (size_t) N) == cudaSuccess;
+		ok &= cudaMalloc(&h->bussi_Lf, sizeof(float4) * (size_t) N) == cudaSuccess;
+	}
 	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16 * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned) * n_systems) == cudaSuccess;
@@ -978,11 +989,21 @@ static cudaError_t fork_noise(oxgb_md *h, const StepArgs &sa) {
 	cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
 	if(e == cudaSuccess) e = cudaStreamWaitEvent(h->noise, h->ev_fork, 0);
 	if(e == cudaSuccess) e = launch_bussi_noise(sa, h->noise);
+	return e;
+}
+
+// after the first step of a Bussi step: the FP64 sums of the half-kicked state, on the side
+// branch (after the draws) while the main branch builds lists and evaluates forces
+static cudaError_t bussi_after_first_step(oxgb_md *h, const StepArgs &sa) {
+	if(sa.th.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
+	cudaError_t e = cudaEventRecord(h->ev_first, h->stream);
+	if(e == cudaSuccess) e = cudaStreamWaitEvent(h->noise, h->ev_first, 0);
+	if(e == cudaSuccess) e = launch_bussi_prep(sa, h->n_chunks, h->dbl, h->noise);
 	if(e == cudaSuccess) e = cudaEventRecord(h->ev_join, h->noise);
 	return e;
 }
 
-// after the forces of a Bussi step: join the draws, then the kinetic sums and the update
+// after the forces of a Bussi step: join the side branch, then the force sums and the update
 static cudaError_t bussi_after_forces(oxgb_md *h, const StepArgs &sa) {
 	if(sa.th.thermostat != OXGB_THERMOSTAT_BUSSI) return cudaSuccess;
 	cudaError_t e = cudaStreamWaitEvent(h->stream, h->ev_join, 0);
@@ -995,6 +1016,7 @@ static int enqueue_step(oxgb_md *h, cudaGraph_t capturing, int k) {
 	StepArgs sa = step_args(h, k);
 	CK(fork_noise(h, sa));
 	CK(launch_first_step(sa, h->dbl, h->stream));
+	CK(bussi_after_first_step(h, sa));
 	ListArgs la = md_list_args(h, h->conditional_ok ? 0 : 1);
 	if(h->conditional_ok) {
 		cudaGraphConditionalHandle hc;
@@ -1087,6 +1109,7 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 		StepArgs sa = step_args(h);
 		CK(fork_noise(h, sa));
 		CK(launch_first_step(sa, h->dbl, h->stream));
+		CK(bussi_after_first_step(h, sa));
 		ListArgs la = md_list_args(h, 1);
 		CK(launch_list_build(la, h->stream));
 		ForceArgs fa = force_args(h, 0, true);

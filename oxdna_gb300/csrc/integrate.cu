@@ -11,46 +11,56 @@
 // update runs on the device (its gamma deviate uses the same algorithm as the reference).
 // The second half kick of a step and its thermostat are deferred to the next first step (or
 // to the flush at the end of a run), where they run one thread per nucleotide next to the
-// first half kick; the Bussi sums and update run after the forces (k_bussi_sums) and its
+// first half kick; the Bussi sums run beside (k_bussi_prep) and after (k_bussi_sums, with the update) the forces, and its
 // draws on a parallel branch of the step graph (k_bussi_noise).  No FP64 work is left in the force
 // kernels, whose lanes are mostly idle at the epilogue.
+#include "split.cuh"
 #include "thermo.cuh"
 
 namespace oxgb {
 
 // ---------------------------------------------------------------- FP32 mirrors
 
-__device__ __forceinline__ void write_mirror(const StepArgs &a, int i, const double4_32a &r, const double4_32a &q) {
+// the FP32 mirrors of nucleotide i from its FP64 position and quaternion: the position as hi + lo,
+// the body axes a1, a3 and the grooved backbone offset (src/Particles/DNANucleotide.cpp:79), each
+// rounded once (to within an ulp) from exact values; conversions and products on the FP32 and
+// integer pipes (split.cuh).  Returns the position rounded to FP32, a1 and the backbone offset.
+struct Mirror {
+	float3 r, a1, back;
+};
+
+__device__ __forceinline__ Mirror write_mirror(const StepArgs &a, int i, const double4_32a &r, const double4_32a &q) {
 	float4 hi = a.pos_hi[i], lo = a.pos_lo[i];
-	hi.x = (float) r.x;
-	hi.y = (float) r.y;
-	hi.z = (float) r.z;
-	lo.x = (float) (r.x - (double) hi.x);
-	lo.y = (float) (r.y - (double) hi.y);
-	lo.z = (float) (r.z - (double) hi.z);
+	split_rn(r.x, hi.x, lo.x);
+	split_rn(r.y, hi.y, lo.y);
+	split_rn(r.z, hi.z, lo.z);
 	a.pos_hi[i] = hi;
 	a.pos_lo[i] = lo;
-	// body axes from the FP64 quaternion, each component rounded once
-	v3<double> a1, a2, a3;
-	quat_frame(q.x, q.y, q.z, q.w, a1, a2, a3);
-	a.fa1[i] = make_float4((float) a1.x, (float) a1.y, (float) a1.z, 0.f);
-	a.fa3[i] = make_float4((float) a3.x, (float) a3.y, (float) a3.z, 0.f);
-	// grooved backbone offset (src/Particles/DNANucleotide.cpp:79) and the strand-end flag
+	float qh[4], ql[4], a1[3], a3[3], bk[3];
+	split_rn(q.x, qh[0], ql[0]);
+	split_rn(q.y, qh[1], ql[1]);
+	split_rn(q.z, qh[2], ql[2]);
+	split_rn(q.w, qh[3], ql[3]);
+	frame_mirror(qh, ql, OXM_POS_MM_BACK1, OXM_POS_MM_BACK2, a1, a3, bk);
+	a.fa1[i] = make_float4(a1[0], a1[1], a1[2], 0.f);
+	a.fa3[i] = make_float4(a3[0], a3[1], a3[2], 0.f);
+	// the strand-end flag rides in w
 	if(a.fback) {
-		const double b1 = (double) OXM_POS_MM_BACK1, b2 = (double) OXM_POS_MM_BACK2;
 		const int2 bd = a.bonds[i];
-		a.fback[i] = make_float4((float) (a1.x * b1 + a2.x * b2), (float) (a1.y * b1 + a2.y * b2), (float) (a1.z * b1 + a2.z * b2),
-				(bd.x < 0 || bd.y < 0) ? 1.f : 0.f);
+		a.fback[i] = make_float4(bk[0], bk[1], bk[2], (bd.x < 0 || bd.y < 0) ? 1.f : 0.f);
 	}
+	return Mirror{make_float3(hi.x, hi.y, hi.z), make_float3(a1[0], a1[1], a1[2]), make_float3(bk[0], bk[1], bk[2])};
 }
 
 // true if the centre or any interaction site moved more than the skin since the last list build
-__device__ __forceinline__ bool list_stale(const StepArgs &a, int i, const double4_32a &r) {
+// (m: the new mirrors)
+__device__ __forceinline__ bool list_stale(const StepArgs &a, int i, const Mirror &m) {
 	const float4 lp = a.list_pos[i];
-	const float dx = (float) r.x - lp.x, dy = (float) r.y - lp.y, dz = (float) r.z - lp.z;
+	const float dx = m.r.x - lp.x, dy = m.r.y - lp.y, dz = m.r.z - lp.z;
 	if(dx * dx + dy * dy + dz * dz > a.skin2) return true;
 	if(!a.list_a1) return false;
-	const float4 a1 = a.fa1[i], la1 = a.list_a1[i], bk = a.fback[i], lbk = a.list_back[i];
+	const float3 a1 = m.a1, bk = m.back;
+	const float4 la1 = a.list_a1[i], lbk = a.list_back[i];
 	const float ex = a1.x - la1.x, ey = a1.y - la1.y, ez = a1.z - la1.z;
 	float sx = dx + 0.4f * ex, sy = dy + 0.4f * ey, sz = dz + 0.4f * ez;  // base site
 	if(sx * sx + sy * sy + sz * sz > a.skin2) return true;
@@ -63,7 +73,7 @@ __device__ __forceinline__ bool list_stale(const StepArgs &a, int i, const doubl
 __global__ void k_make_mirrors(StepArgs a) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= a.N) return;
-	write_mirror(a, i, a.pos[i], a.quat[i]);
+	(void) write_mirror(a, i, a.pos[i], a.quat[i]);
 }
 
 // ---------------------------------------------------------------- first half step
@@ -76,12 +86,12 @@ template <typename V4>
 __device__ __forceinline__ void complete_step(const ThermoArgs &t, int i, int sy, long long sp, const V4 &F, const V4 &T,
 		double4_32a &v, double4_32a &L) {
 	const double hdt = 0.5 * t.dt;
-	v.x += (double) F.x * hdt;
-	v.y += (double) F.y * hdt;
-	v.z += (double) F.z * hdt;
-	L.x += (double) T.x * hdt;
-	L.y += (double) T.y * hdt;
-	L.z += (double) T.z * hdt;
+	v.x += widen(F.x) * hdt;
+	v.y += widen(F.y) * hdt;
+	v.z += widen(F.z) * hdt;
+	L.x += widen(T.x) * hdt;
+	L.y += widen(T.y) * hdt;
+	L.z += widen(T.z) * hdt;
 	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) brownian_redraw(t, sy, i - t.sys_off[sy], sp, v, L);
 	else if(t.thermostat == 2 && *t.bussi_stamp == sp) bussi_rescale(t, sy, v, L);
 }
@@ -99,15 +109,15 @@ __global__ void k_first_step(StepArgs a) {
 	// the previous step's second half kick and thermostat (kept as a separate half kick, so that
 	// a state is the same whether or not a run ended at that step)
 	if(*a.th.open_step == s - 1) complete_step(a.th, i, sy, s - 1, F, T, v, L);
-	v.x += (double) F.x * hdt;
-	v.y += (double) F.y * hdt;
-	v.z += (double) F.z * hdt;
+	v.x += widen(F.x) * hdt;
+	v.y += widen(F.y) * hdt;
+	v.z += widen(F.z) * hdt;
 	r.x += v.x * a.dt;
 	r.y += v.y * a.dt;
 	r.z += v.z * a.dt;
-	L.x += (double) T.x * hdt;
-	L.y += (double) T.y * hdt;
-	L.z += (double) T.z * hdt;
+	L.x += widen(T.x) * hdt;
+	L.y += widen(T.y) * hdt;
+	L.z += widen(T.z) * hdt;
 	// rotation by dt|L| about L (body frame): q <- q * (sin(th/2) L^, cos(th/2))
 	const double L2 = L.x * L.x + L.y * L.y + L.z * L.z;
 	if(L2 > 0.0) {
@@ -147,10 +157,10 @@ __global__ void k_first_step(StepArgs a) {
 	a.pos[i] = r;
 	a.angmom[i] = L;
 	a.quat[i] = q;
-	write_mirror(a, i, r, q);
+	const Mirror m = write_mirror(a, i, r, q);
 	// Verlet list staleness (CUDA_mixed.cuh:68, extended to the interaction sites for the term
 	// lists), per system
-	if(list_stale(a, i, r)) {
+	if(list_stale(a, i, m)) {
 		a.sys_stale[sy] = 1;
 		atomicOr(a.flag, 1);
 	}
@@ -175,37 +185,132 @@ __global__ void k_bussi_noise(StepArgs a) {
 	a.th.bussi_state[16 * sy + 9 + 2 * w] = rr;
 }
 
+// ---------------------------------------------------------------- Bussi kinetic sums
+//
+// The update of step s needs, per system, the sums of v, |v|^2 and |L|^2 over the completed
+// momenta v + h F and L + h T (h = dt / 2).  They are split as
+//   sum (v + h F)^2 = sum v^2 + 2 h sum v.F + h^2 sum F^2   (and likewise for L, T):
+// the FP64 sums of the half-kicked state (k_bussi_prep) depend only on the first step and run on
+// a side branch of the step graph while the force kernels run (they use the FP64 pipe, which
+// the FP32 force kernels leave idle); the force terms (k_bussi_sums) are FP32 products of the
+// FP32 forces with the FP32-rounded momenta, summed with compensation, a correction of relative
+// size h |F| / |v| to sums that stay FP64.  Both sums run over the same chunks (up to 256
+// nucleotides of one system, aligned to the system's first nucleotide), so a system reduces the
+// same way in a batch as alone.
+
+__device__ __forceinline__ double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+
+// a float sum with its running error (TwoSum at every addition)
+struct CompF {
+	float s, e;
+};
+__device__ __forceinline__ CompF shfl_xor(CompF v, int m) {
+	return CompF{__shfl_xor_sync(0xffffffffu, v.s, m), __shfl_xor_sync(0xffffffffu, v.e, m)};
+}
+__device__ __forceinline__ CompF comp_add(CompF a, CompF b) {
+	const float t = a.s + b.s, bp = t - a.s;
+	return CompF{t, a.e + b.e + ((a.s - (t - bp)) + (b.s - bp))};
+}
+
+// sum over a warp of 8 values per lane by a transposed butterfly (9 additions where 8
+// separate reductions take 40); every lane returns the total of value (lane >> 2) & 7.  The
+// order is fixed.
+template <typename T, typename Add>
+__device__ __forceinline__ T warp_transpose_sum8(const T (&x)[8], Add add) {
+	const int lane = threadIdx.x & 31;
+	const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+	T w[4], u[2];
+#pragma unroll
+	for(int k = 0; k < 4; k++) w[k] = add(h16 ? x[k + 4] : x[k], shfl_xor(h16 ? x[k] : x[k + 4], 16));
+#pragma unroll
+	for(int k = 0; k < 2; k++) u[k] = add(h8 ? w[k + 2] : w[k], shfl_xor(h8 ? w[k] : w[k + 2], 8));
+	T t = add(h4 ? u[1] : u[0], shfl_xor(h4 ? u[0] : u[1], 4));
+	t = add(t, shfl_xor(t, 2));
+	return add(t, shfl_xor(t, 1));
+}
+
+// the 8 per-thread values of a block summed in a fixed order into red[0..7] (a 256-thread block)
+__device__ __forceinline__ void block_sum8(const double (&x)[8], double *red) {
+	__shared__ double part[8][8];
+	const double t = warp_transpose_sum8(x, [](double p, double q) { return p + q; });
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	if((lane & 3) == 0) part[lane >> 2][w] = t;
+	__syncthreads();
+	if(threadIdx.x < 8) {
+		double r = 0;
+		for(int u = 0; u < 8; u++) r += part[threadIdx.x][u];
+		red[threadIdx.x] = r;
+	}
+}
+
+__device__ __forceinline__ void block_sum8(const CompF (&x)[8], double *red) {
+	__shared__ CompF part[8][8];
+	const CompF t = warp_transpose_sum8(x, comp_add);
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	if((lane & 3) == 0) part[lane >> 2][w] = t;
+	__syncthreads();
+	if(threadIdx.x < 8) {
+		CompF r{0.f, 0.f};
+		for(int u = 0; u < 8; u++) r = comp_add(r, part[threadIdx.x][u]);
+		red[threadIdx.x] = (double) r.s + (double) r.e;
+	}
+}
+
+// Bussi step s, after the first step: per chunk, the FP64 sums of the half-kicked v, |v|^2 and
+// |L|^2 (and, in mixed precision, v and L rounded to FP32 for the force terms)
+template <typename V4>
+__global__ void __launch_bounds__(256) k_bussi_prep(StepArgs a) {
+	const long long s = step_of(a.th);
+	if(s % a.th.newtonian_steps != 0) return;
+	const int c = blockIdx.x;
+	const int sy = a.th.chunk_sys[c];
+	const int i = a.th.chunk_first[c] + threadIdx.x;
+	double x[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	if(i < a.th.sys_off[sy + 1]) {
+		const double4_32a v = a.vel[i], L = a.angmom[i];
+		x[0] = v.x;
+		x[1] = v.y;
+		x[2] = v.z;
+		x[3] = v.x * v.x + v.y * v.y + v.z * v.z;
+		x[4] = L.x * L.x + L.y * L.y + L.z * L.z;
+		if(sizeof(V4) == sizeof(float4)) {
+			a.th.bussi_vf[i] = make_float4(narrow(v.x), narrow(v.y), narrow(v.z), 0.f);
+			a.th.bussi_Lf[i] = make_float4(narrow(L.x), narrow(L.y), narrow(L.z), 0.f);
+		}
+	}
+	block_sum8(x, a.th.bussi_partials + 16 * c);
+}
+
 // the update of system sy from its chunk sums, reduced by the block in a fixed chunk order (the
 // result does not depend on which block runs it): translation on thread 0 and rotation on
-// thread 32 (two warps: the chains overlap).  red is the block's shared scratch.
-__device__ __forceinline__ void bussi_system_update(const StepArgs &a, int sy, long long s, double (*red)[8]) {
+// thread 32 (two warps: the chains overlap)
+__device__ __forceinline__ void bussi_system_update(const StepArgs &a, int sy, long long s) {
+	__shared__ double tot[16];
 	const int c0 = a.th.sys_chunk0[sy], nc = a.th.sys_chunk0[sy + 1] - c0;
-	double part[5] = {0, 0, 0, 0, 0};
-	for(int b = threadIdx.x; b < nc; b += blockDim.x)
+	double x[8] = {0, 0, 0, 0, 0, 0, 0, 0}, y[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	for(int b = threadIdx.x; b < nc; b += blockDim.x) {
+		const double *p = a.th.bussi_partials + 16 * (c0 + b);
 #pragma unroll
-		for(int k = 0; k < 5; k++) part[k] += __ldcg(a.th.bussi_partials + (c0 + b) * 8 + k);
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+		for(int k = 0; k < 5; k++) x[k] += __ldcg(p + k);
 #pragma unroll
-	for(int k = 0; k < 5; k++) {
-		double x = part[k];
-		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-		if(lane == 0) red[k][w] = x;
+		for(int k = 0; k < 7; k++) y[k] += __ldcg(p + 8 + k);
 	}
+	__syncthreads();  // the block's scratch is reused
+	block_sum8(x, tot);
+	__syncthreads();
+	block_sum8(y, tot + 8);
 	__syncthreads();
 	if(threadIdx.x != 0 && threadIdx.x != 32) return;
-	double sum[5];
-	for(int k = 0; k < 5; k++) {
-		double x = 0;
-		for(int u = 0; u < nw; u++) x += red[k][u];
-		sum[k] = x;
-	}
+	const double h = 0.5 * a.dt;
+	const double sum[5] = {tot[0] + h * tot[8], tot[1] + h * tot[9], tot[2] + h * tot[10],
+			tot[3] + 2.0 * h * tot[11] + h * h * tot[12], tot[4] + 2.0 * h * tot[13] + h * h * tot[14]};
 	bussi_update(a.th, sy, s, threadIdx.x == 0 ? 0 : 1, sum);
 }
 
-// Bussi step s, after its forces: sums of v, |v|^2 and |L|^2 over the completed velocities
-// v + dt/2 F (computed here, stored by the next first step), one block per chunk of up to 256
-// nucleotides of one system.  The block that finishes a system's last outstanding chunk (a
-// per-system arrival counter) makes that system's update, so there is no separate update launch.
+// Bussi step s, after its forces: per chunk the sums of F, v.F, |F|^2, L.T and |T|^2 (FP32
+// products, compensated sums; FP64 in double precision).  The block that brings a system's last
+// chunk (a per-system arrival counter) makes that system's update, so there is no separate
+// update launch.
 template <typename V4>
 __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 	const long long s = step_of(a.th);
@@ -213,40 +318,42 @@ __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 	const int c = blockIdx.x;
 	const int sy = a.th.chunk_sys[c];
 	const int i = a.th.chunk_first[c] + threadIdx.x;
-	const double hdt = 0.5 * a.dt;
-	double acc[5] = {0, 0, 0, 0, 0};
-	if(i < a.th.sys_off[sy + 1]) {
-		const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
-		const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
-		double4_32a v = a.vel[i], L = a.angmom[i];
-		v.x += (double) F.x * hdt;
-		v.y += (double) F.y * hdt;
-		v.z += (double) F.z * hdt;
-		L.x += (double) T.x * hdt;
-		L.y += (double) T.y * hdt;
-		L.z += (double) T.z * hdt;
-		acc[0] = v.x;
-		acc[1] = v.y;
-		acc[2] = v.z;
-		acc[3] = v.x * v.x + v.y * v.y + v.z * v.z;
-		acc[4] = L.x * L.x + L.y * L.y + L.z * L.z;
-	}
-	__shared__ double red[5][8];
-	__shared__ int last;
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+	const bool live = i < a.th.sys_off[sy + 1];
+	if(sizeof(V4) == sizeof(float4)) {
+		CompF x[8];
 #pragma unroll
-	for(int k = 0; k < 5; k++) {
-		double x = acc[k];
-		for(int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-		if(lane == 0) red[k][w] = x;
+		for(int k = 0; k < 8; k++) x[k] = CompF{0.f, 0.f};
+		if(live) {
+			const float4 F = reinterpret_cast<const float4 *>(a.forces)[i], T = reinterpret_cast<const float4 *>(a.torques)[i];
+			const float4 v = a.th.bussi_vf[i], L = a.th.bussi_Lf[i];
+			x[0].s = F.x;
+			x[1].s = F.y;
+			x[2].s = F.z;
+			x[3].s = v.x * F.x + v.y * F.y + v.z * F.z;
+			x[4].s = F.x * F.x + F.y * F.y + F.z * F.z;
+			x[5].s = L.x * T.x + L.y * T.y + L.z * T.z;
+			x[6].s = T.x * T.x + T.y * T.y + T.z * T.z;
+		}
+		block_sum8(x, a.th.bussi_partials + 16 * c + 8);
 	}
-	__syncthreads();
-	if(threadIdx.x < 5) {
-		double x = 0;
-		for(int u = 0; u < nw; u++) x += red[threadIdx.x][u];
-		a.th.bussi_partials[c * 8 + threadIdx.x] = x;
-		__threadfence();  // the partial is visible device-wide before this block arrives
+	else {
+		double x[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+		if(live) {
+			const double4_32a F = reinterpret_cast<const double4_32a *>(a.forces)[i],
+							  T = reinterpret_cast<const double4_32a *>(a.torques)[i];
+			const double4_32a v = a.vel[i], L = a.angmom[i];
+			x[0] = F.x;
+			x[1] = F.y;
+			x[2] = F.z;
+			x[3] = v.x * F.x + v.y * F.y + v.z * F.z;
+			x[4] = F.x * F.x + F.y * F.y + F.z * F.z;
+			x[5] = L.x * T.x + L.y * T.y + L.z * T.z;
+			x[6] = T.x * T.x + T.y * T.y + T.z * T.z;
+		}
+		block_sum8(x, a.th.bussi_partials + 16 * c + 8);
 	}
+	__shared__ int last;
+	if(threadIdx.x < 8) __threadfence();  // the partials are visible device-wide before this block arrives
 	__syncthreads();
 	if(threadIdx.x == 0) {
 		const unsigned nc = (unsigned) (a.th.sys_chunk0[sy + 1] - a.th.sys_chunk0[sy]);
@@ -260,7 +367,7 @@ __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 	__syncthreads();
 	if(!last) return;
 	__threadfence();
-	bussi_system_update(a, sy, s, red);
+	bussi_system_update(a, sy, s);
 }
 
 __global__ void k_step_advance(StepArgs a, int K) {
@@ -351,6 +458,12 @@ cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_
 
 cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
 	k_bussi_noise<<<a.th.n_systems, 64, 0, s>>>(a);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_bussi_prep(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s) {
+	if(double_forces) k_bussi_prep<double4_32a><<<n_chunks, 256, 0, s>>>(a);
+	else k_bussi_prep<float4><<<n_chunks, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

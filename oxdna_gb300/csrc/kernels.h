@@ -43,7 +43,10 @@ struct ThermoArgs {
 	// Bussi: the kinetic sums run over chunks of up to 256 nucleotides of one system
 	const int *chunk_sys, *chunk_first;    // [chunks]
 	const int *sys_chunk0;                 // [n_systems + 1] first chunk of each system
-	double *bussi_partials;                // [chunks * 8] per-chunk sums of v, |v|^2, |L|^2
+	double *bussi_partials;                // [chunks * 16] per-chunk sums: 0-4 of the half-kicked
+	                                       // state (v, |v|^2, |L|^2), 8-14 of the force terms
+	                                       // (F, v.F, |F|^2, L.T, |T|^2)
+	float4 *bussi_vf, *bussi_Lf;           // [N] half-kicked v and L rounded to FP32 (mixed precision)
 	double *bussi_state;                   // [n_systems * 16]: K_t, K_r, factor_t, factor_r,
 	                                       // vcom x y z, -, then the step's draws: sum_t, rr_t,
 	                                       // sum_r, rr_r
@@ -178,8 +181,10 @@ cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_
 // the Bussi draws of the current step, per system (they do not depend on the state: they run
 // beside the step)
 cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s);
-// Bussi kinetic-energy sums over the completed velocities and the per-system update (after the
-// forces); n_chunks chunks of up to 256 nucleotides
+// Bussi kinetic-energy sums of the half-kicked state (after the first step, beside the forces)
+// and of the force terms with the per-system update (after the forces); n_chunks chunks of up to
+// 256 nucleotides
+cudaError_t launch_bussi_prep(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s);
 cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s);
 // end of a graph of K steps: the step base advances by K
 cudaError_t launch_step_advance(const StepArgs &a, int K, cudaStream_t s);

@@ -1,0 +1,70 @@
+// Host check of the integer-pipe conversions and the FP32 error-free frame (split.cuh): the
+// split and the widening are bit-identical to the C casts (round to nearest, like the device's
+// cvt.rn), and the frame is within half an ulp of 1 of the exact frame, like the FP64 frame
+// rounded once.  Built with g++ -ffp-contract=off by tests/test_split.py; exits non-zero on a
+// failure.
+#include "split.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+
+using namespace oxgb;
+
+int main(int argc, char **argv) {
+	const long n = argc > 1 ? std::atol(argv[1]) : 1000000;
+	std::mt19937_64 g(1);
+	std::uniform_real_distribution<double> U(-1, 1);
+	long bad = 0, fast = 0;
+	auto check = [&](double r) {
+		float h, l;
+		const bool f = split_rn_int(r, h, l);
+		const float h2 = (float) r, l2 = (float) (r - (double) h2);
+		if(f) {
+			fast++;
+			if(f32_bits(h) != f32_bits(h2) || f32_bits(l) != f32_bits(l2)) bad++;
+		}
+		split_rn(r, h, l);
+		if(f32_bits(h) != f32_bits(h2) || f32_bits(l) != f32_bits(l2)) bad++;
+	};
+	for(long i = 0; i < n; i++) check(U(g) * std::ldexp(1.0, (int) (g() % 200) - 90));
+	for(long i = 0; i < n / 10; i++) {
+		// exact ties between two floats and their neighbours
+		const float f = (float) U(g) * 1000.f, f2 = f32_from_bits(f32_bits(f) + 1);
+		const double mid = ((double) f + (double) f2) / 2;
+		check(mid), check(std::nextafter(mid, 0.0)), check(std::nextafter(mid, 1e300)), check((double) f), check(-mid);
+	}
+	for(double r : {1.0, -1.0, 0.5, 1.0 - 1e-17, 3.0e38, 1e-22, 5e-23, 0.0, -0.0}) check(r);
+	long wbad = 0;
+	for(long i = 0; i < n; i++) {
+		const float f = f32_from_bits((unsigned) g());
+		const double a = widen(f), b = (double) f;
+		if(f64_bits(a) != f64_bits(b) && !(std::isnan(a) && std::isnan(b))) wbad++;
+	}
+	for(float f : {0.f, -0.f, 1e-40f, -1e-45f, 1.f, -3.5e38f}) wbad += f64_bits(widen(f)) != f64_bits((double) f);
+	std::normal_distribution<double> N(0, 1);
+	double worst = 0;
+	for(long t = 0; t < n / 10; t++) {
+		double q[4], nn = 0;
+		for(int k = 0; k < 4; k++) q[k] = N(g), nn += q[k] * q[k];
+		nn = std::sqrt(nn);
+		for(int k = 0; k < 4; k++) q[k] /= nn;
+		if(t % 7 == 0) q[g() % 4] *= 1e-6;
+		const long double X = q[0], Y = q[1], Z = q[2], W = q[3];
+		const long double E1[3] = {X * X - Y * Y - Z * Z + W * W, 2 * (X * Y + Z * W), 2 * (X * Z - Y * W)};
+		const long double E2[3] = {2 * (X * Y - Z * W), -X * X + Y * Y - Z * Z + W * W, 2 * (Y * Z + X * W)};
+		const long double E3[3] = {2 * (X * Z + Y * W), 2 * (Y * Z - X * W), -X * X - Y * Y + Z * Z + W * W};
+		float qh[4], ql[4], a1[3], a3[3], bk[3];
+		for(int k = 0; k < 4; k++) split_rn(q[k], qh[k], ql[k]);
+		const float b1 = -0.34f, b2 = 0.3408f;
+		frame_mirror(qh, ql, b1, b2, a1, a3, bk);
+		for(int k = 0; k < 3; k++) {
+			const long double eb = E1[k] * (long double) b1 + E2[k] * (long double) b2;
+			for(long double d : {(long double) a1[k] - E1[k], (long double) a3[k] - E3[k], (long double) bk[k] - eb})
+				worst = std::fmax(worst, (double) std::fabs(d) * std::ldexp(1.0, 24));
+		}
+	}
+	std::printf("split: %ld fast, %ld mismatches; widen: %ld mismatches; frame: max error %.4f x 2^-24\n", fast, bad, wbad, worst);
+	return (bad || wbad || worst > 0.5001) ? 1 : 0;
+}
