@@ -282,149 +282,188 @@ OXGB_HD void pair_ev(const Nuc<R> &p, const Nuc<R> &q, const v3<R> r, PairOut<R>
 	}
 }
 
-// hydrogen bonding and cross stacking, both on the base-base vector (DNAInteraction.cpp:779-1021)
-template <typename R, bool SPLIT>
-OXGB_HD void pair_base(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
-	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3;
+// The base-base vector of a pair and the cosines of its angles, shared by hydrogen bonding and
+// cross stacking (DNAInteraction.cpp:779-1021), with which of the two can be non-zero: each
+// needs its distance window and every angular factor inside its support (f4_may; else the term
+// is exactly zero).
+template <typename R>
+struct BaseGeo {
+	R rmod, c1, c2, c3, c4, c7, c8;
+	v3<R> rd;
+	bool hb, crst;
+};
+
+template <typename R>
+OXGB_HD BaseGeo<R> base_geo(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep) {
+	BaseGeo<R> g;
+	g.hb = g.crst = false;
 	const v3<R> rhydro = site_vec(sep, q.base, p.base);
 	const R rh2 = dot(rhydro, rhydro);
+	const bool hb_range = p.btype + q.btype == 3 && R(OXM_HYDR_RCLOW) * R(OXM_HYDR_RCLOW) < rh2 &&
+			rh2 < R(OXM_HYDR_RCHIGH) * R(OXM_HYDR_RCHIGH);
+	const bool cr_range = R(OXM_CRST_RCLOW) * R(OXM_CRST_RCLOW) < rh2 && rh2 < R(OXM_CRST_RCHIGH) * R(OXM_CRST_RCHIGH);
+	if(!hb_range && !cr_range) return g;
+	g.rmod = m_sqrt(rh2);
+	g.rd = rhydro * (R(1) / g.rmod);
+	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3;
+	g.c1 = -dot(a1, b1), g.c2 = -dot(b1, g.rd), g.c3 = dot(a1, g.rd), g.c4 = dot(a3, b3), g.c7 = -dot(b3, g.rd), g.c8 = dot(a3, g.rd);
+	g.hb = hb_range && R(OXM_HYDR_RCLOW) < g.rmod && g.rmod < R(OXM_HYDR_RCHIGH) && f4_may(P, g.c1, OXM_F4_HB_T1) &&
+			f4_may(P, g.c2, OXM_F4_HB_T2) && f4_may(P, g.c3, OXM_F4_HB_T2) && f4_may(P, g.c4, OXM_F4_HB_T4) &&
+			f4_may(P, g.c7, OXM_F4_HB_T7) && f4_may(P, g.c8, OXM_F4_HB_T7);
+	// theta4, theta7, theta8 of cross stacking enter through f4(theta) + f4(pi - theta)
+	g.crst = cr_range && R(OXM_CRST_RCLOW) < g.rmod && g.rmod < R(OXM_CRST_RCHIGH) && f4_may(P, g.c1, OXM_F4_CR_T1) &&
+			f4_may(P, g.c2, OXM_F4_CR_T2) && f4_may(P, g.c3, OXM_F4_CR_T2) &&
+			(f4_may(P, g.c4, OXM_F4_CR_T4) || f4_may(P, -g.c4, OXM_F4_CR_T4)) &&
+			(f4_may(P, g.c7, OXM_F4_CR_T7) || f4_may(P, -g.c7, OXM_F4_CR_T7)) &&
+			(f4_may(P, g.c8, OXM_F4_CR_T7) || f4_may(P, -g.c8, OXM_F4_CR_T7));
+	return g;
+}
 
-	// hydrogen bonding
-	if(p.btype + q.btype == 3 && R(OXM_HYDR_RCLOW) * R(OXM_HYDR_RCLOW) < rh2 && rh2 < R(OXM_HYDR_RCHIGH) * R(OXM_HYDR_RCHIGH)) {
-		const R rmod = m_sqrt(rh2);
-		if(R(OXM_HYDR_RCLOW) < rmod && rmod < R(OXM_HYDR_RCHIGH)) {
-			const v3<R> rd = rhydro * (R(1) / rmod);
-			const R c1 = -dot(a1, b1), c2 = -dot(b1, rd), c3 = dot(a1, rd), c4 = dot(a3, b3), c7 = -dot(b3, rd), c8 = dot(a3, rd);
-			// every angular factor must be able to be non-zero (else the term is exactly zero)
-			if(!(f4_may(P, c1, OXM_F4_HB_T1) && f4_may(P, c2, OXM_F4_HB_T2) && f4_may(P, c3, OXM_F4_HB_T2) &&
-					   f4_may(P, c4, OXM_F4_HB_T4) && f4_may(P, c7, OXM_F4_HB_T7) && f4_may(P, c8, OXM_F4_HB_T7)))
-				goto crst;
-			{
-			const R hbm = (abs(q.btype) >= 300 && abs(p.btype) >= 300) ? P.hb_multiplier : R(1);
-			R F1, F1D, g1, d1, g2, d2, g3, d3, g4, d4, g7, d7, g8, d8;
-			f1_both(P, rmod, OXM_F1_HB, q.type, p.type, F1, F1D);
-			F1 *= hbm;
-			F1D *= hbm;
-			f4_both(P, c1, OXM_F4_HB_T1, g1, d1);
-			f4_both(P, c2, OXM_F4_HB_T2, g2, d2);
-			f4_both(P, c3, OXM_F4_HB_T2, g3, d3);
-			f4_both(P, c4, OXM_F4_HB_T4, g4, d4);
-			f4_both(P, c7, OXM_F4_HB_T7, g7, d7);
-			f4_both(P, c8, OXM_F4_HB_T7, g8, d8);
-			d3 = -d3;
-			d4 = -d4;
-			d8 = -d8;
-			const R e = F1 * g1 * g2 * g3 * g4 * g7 * g8;
-			if(e != R(0)) {
-				add_e<R, SPLIT>(o, T_HB, e);
-				o.Ehb += e;
-				v3<R> force = rd * (-(F1D * g1 * g2 * g3 * g4 * g7 * g8));
-				v3<R> tp = cross(a3, b3) * (F1 * g1 * g2 * g3 * d4 * g7 * g8);   // theta4: -= dir * (-..)
-				tp += cross(a1, b1) * (F1 * d1 * g2 * g3 * g4 * g7 * g8);         // theta1
-				force += (b1 + rd * c2) * (F1 * g1 * d2 * g3 * g4 * g7 * g8 / rmod);
-				force += (a1 - rd * c3) * (F1 * g1 * g2 * d3 * g4 * g7 * g8 / rmod);
-				tp += cross(rd, a1) * (-(F1 * g1 * g2 * d3 * g4 * g7 * g8));      // theta3
-				force += (b3 + rd * c7) * (F1 * g1 * g2 * g3 * g4 * d7 * g8 / rmod);
-				force += (a3 - rd * c8) * (F1 * g1 * g2 * g3 * g4 * g7 * d8 / rmod);
-				tp += cross(rd, a3) * (-(F1 * g1 * g2 * g3 * g4 * g7 * d8));      // theta8
-				o.F -= force;
-				o.T += tp - cross(p.base, force);
-			}
-			}
-		}
-	}
-
-crst:
-	// cross stacking
-	if(R(OXM_CRST_RCLOW) * R(OXM_CRST_RCLOW) < rh2 && rh2 < R(OXM_CRST_RCHIGH) * R(OXM_CRST_RCHIGH)) {
-		const R rmod = m_sqrt(rh2);
-		if(R(OXM_CRST_RCLOW) < rmod && rmod < R(OXM_CRST_RCHIGH)) {
-			const v3<R> rd = rhydro * (R(1) / rmod);
-			const R c1 = -dot(a1, b1), c2 = -dot(b1, rd), c3 = dot(a1, rd), c4 = dot(a3, b3), c7 = -dot(b3, rd), c8 = dot(a3, rd);
-			// theta4, theta7, theta8 enter through f4(theta) + f4(pi - theta)
-			if(!(f4_may(P, c1, OXM_F4_CR_T1) && f4_may(P, c2, OXM_F4_CR_T2) && f4_may(P, c3, OXM_F4_CR_T2) &&
-					   (f4_may(P, c4, OXM_F4_CR_T4) || f4_may(P, -c4, OXM_F4_CR_T4)) &&
-					   (f4_may(P, c7, OXM_F4_CR_T7) || f4_may(P, -c7, OXM_F4_CR_T7)) &&
-					   (f4_may(P, c8, OXM_F4_CR_T7) || f4_may(P, -c8, OXM_F4_CR_T7))))
-				return;
-			R F2, F2D, g1, d1, g2, d2, g3, d3, g4a, d4a, g4b, d4b, g7a, d7a, g7b, d7b, g8a, d8a, g8b, d8b;
-			f2_both(P, rmod, OXM_F2_CRST, F2, F2D);
-			f4_both(P, c1, OXM_F4_CR_T1, g1, d1);
-			f4_both(P, c2, OXM_F4_CR_T2, g2, d2);
-			f4_both(P, c3, OXM_F4_CR_T2, g3, d3);
-			f4_both(P, c4, OXM_F4_CR_T4, g4a, d4a);
-			f4_both(P, -c4, OXM_F4_CR_T4, g4b, d4b);
-			f4_both(P, c7, OXM_F4_CR_T7, g7a, d7a);
-			f4_both(P, -c7, OXM_F4_CR_T7, g7b, d7b);
-			f4_both(P, c8, OXM_F4_CR_T7, g8a, d8a);
-			f4_both(P, -c8, OXM_F4_CR_T7, g8b, d8b);
-			const R g4 = g4a + g4b, g7 = g7a + g7b, g8 = g8a + g8b;
-			d3 = -d3;
-			const R d4 = -d4a + d4b, d7 = d7a - d7b, d8 = -d8a + d8b;
-			const R e = F2 * g1 * g2 * g3 * g4 * g7 * g8;
-			if(e != R(0)) {
-				add_e<R, SPLIT>(o, T_CRST, e);
-				v3<R> force = rd * (-(F2D * g1 * g2 * g3 * g4 * g7 * g8));
-				v3<R> tp = cross(a1, b1) * (F2 * d1 * g2 * g3 * g4 * g7 * g8);
-				force += (b1 + rd * c2) * (F2 * g1 * d2 * g3 * g4 * g7 * g8 / rmod);
-				force += (a1 - rd * c3) * (F2 * g1 * g2 * d3 * g4 * g7 * g8 / rmod);
-				tp += cross(rd, a1) * (-(F2 * g1 * g2 * d3 * g4 * g7 * g8));
-				tp += cross(a3, b3) * (F2 * g1 * g2 * g3 * d4 * g7 * g8);
-				force += (b3 + rd * c7) * (F2 * g1 * g2 * g3 * g4 * d7 * g8 / rmod);
-				force += (a3 - rd * c8) * (F2 * g1 * g2 * g3 * g4 * g7 * d8 / rmod);
-				tp += cross(rd, a3) * (-(F2 * g1 * g2 * g3 * g4 * g7 * d8));
-				o.F -= force;
-				o.T += tp - cross(p.base, force);
-			}
-		}
+// hydrogen bonding of a pair whose geometry admits it (g.hb)
+template <typename R, bool SPLIT>
+OXGB_HD void hb_term(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const BaseGeo<R> &g, PairOut<R> &o) {
+	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3, rd = g.rd;
+	const R rmod = g.rmod, c2 = g.c2, c3 = g.c3, c7 = g.c7, c8 = g.c8;
+	const R hbm = (abs(q.btype) >= 300 && abs(p.btype) >= 300) ? P.hb_multiplier : R(1);
+	R F1, F1D, g1, d1, g2, d2, g3, d3, g4, d4, g7, d7, g8, d8;
+	f1_both(P, rmod, OXM_F1_HB, q.type, p.type, F1, F1D);
+	F1 *= hbm;
+	F1D *= hbm;
+	f4_both(P, g.c1, OXM_F4_HB_T1, g1, d1);
+	f4_both(P, c2, OXM_F4_HB_T2, g2, d2);
+	f4_both(P, c3, OXM_F4_HB_T2, g3, d3);
+	f4_both(P, g.c4, OXM_F4_HB_T4, g4, d4);
+	f4_both(P, c7, OXM_F4_HB_T7, g7, d7);
+	f4_both(P, c8, OXM_F4_HB_T7, g8, d8);
+	d3 = -d3;
+	d4 = -d4;
+	d8 = -d8;
+	const R e = F1 * g1 * g2 * g3 * g4 * g7 * g8;
+	if(e != R(0)) {
+		add_e<R, SPLIT>(o, T_HB, e);
+		o.Ehb += e;
+		v3<R> force = rd * (-(F1D * g1 * g2 * g3 * g4 * g7 * g8));
+		v3<R> tp = cross(a3, b3) * (F1 * g1 * g2 * g3 * d4 * g7 * g8);   // theta4: -= dir * (-..)
+		tp += cross(a1, b1) * (F1 * d1 * g2 * g3 * g4 * g7 * g8);         // theta1
+		force += (b1 + rd * c2) * (F1 * g1 * d2 * g3 * g4 * g7 * g8 / rmod);
+		force += (a1 - rd * c3) * (F1 * g1 * g2 * d3 * g4 * g7 * g8 / rmod);
+		tp += cross(rd, a1) * (-(F1 * g1 * g2 * d3 * g4 * g7 * g8));      // theta3
+		force += (b3 + rd * c7) * (F1 * g1 * g2 * g3 * g4 * d7 * g8 / rmod);
+		force += (a3 - rd * c8) * (F1 * g1 * g2 * g3 * g4 * g7 * d8 / rmod);
+		tp += cross(rd, a3) * (-(F1 * g1 * g2 * g3 * g4 * g7 * d8));      // theta8
+		o.F -= force;
+		o.T += tp - cross(p.base, force);
 	}
 }
 
+// cross stacking of a pair whose geometry admits it (g.crst)
+template <typename R, bool SPLIT>
+OXGB_HD void crst_term(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const BaseGeo<R> &g, PairOut<R> &o) {
+	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3, rd = g.rd;
+	const R rmod = g.rmod, c2 = g.c2, c3 = g.c3, c4 = g.c4, c7 = g.c7, c8 = g.c8;
+	R F2, F2D, g1, d1, g2, d2, g3, d3, g4a, d4a, g4b, d4b, g7a, d7a, g7b, d7b, g8a, d8a, g8b, d8b;
+	f2_both(P, rmod, OXM_F2_CRST, F2, F2D);
+	f4_both(P, g.c1, OXM_F4_CR_T1, g1, d1);
+	f4_both(P, c2, OXM_F4_CR_T2, g2, d2);
+	f4_both(P, c3, OXM_F4_CR_T2, g3, d3);
+	f4_both(P, c4, OXM_F4_CR_T4, g4a, d4a);
+	f4_both(P, -c4, OXM_F4_CR_T4, g4b, d4b);
+	f4_both(P, c7, OXM_F4_CR_T7, g7a, d7a);
+	f4_both(P, -c7, OXM_F4_CR_T7, g7b, d7b);
+	f4_both(P, c8, OXM_F4_CR_T7, g8a, d8a);
+	f4_both(P, -c8, OXM_F4_CR_T7, g8b, d8b);
+	const R g4 = g4a + g4b, g7 = g7a + g7b, g8 = g8a + g8b;
+	d3 = -d3;
+	const R d4 = -d4a + d4b, d7 = d7a - d7b, d8 = -d8a + d8b;
+	const R e = F2 * g1 * g2 * g3 * g4 * g7 * g8;
+	if(e != R(0)) {
+		add_e<R, SPLIT>(o, T_CRST, e);
+		v3<R> force = rd * (-(F2D * g1 * g2 * g3 * g4 * g7 * g8));
+		v3<R> tp = cross(a1, b1) * (F2 * d1 * g2 * g3 * g4 * g7 * g8);
+		force += (b1 + rd * c2) * (F2 * g1 * d2 * g3 * g4 * g7 * g8 / rmod);
+		force += (a1 - rd * c3) * (F2 * g1 * g2 * d3 * g4 * g7 * g8 / rmod);
+		tp += cross(rd, a1) * (-(F2 * g1 * g2 * d3 * g4 * g7 * g8));
+		tp += cross(a3, b3) * (F2 * g1 * g2 * g3 * d4 * g7 * g8);
+		force += (b3 + rd * c7) * (F2 * g1 * g2 * g3 * g4 * d7 * g8 / rmod);
+		force += (a3 - rd * c8) * (F2 * g1 * g2 * g3 * g4 * g7 * d8 / rmod);
+		tp += cross(rd, a3) * (-(F2 * g1 * g2 * g3 * g4 * g7 * d8));
+		o.F -= force;
+		o.T += tp - cross(p.base, force);
+	}
+}
+
+// hydrogen bonding and cross stacking, both on the base-base vector (DNAInteraction.cpp:779-1021)
+template <typename R, bool SPLIT>
+OXGB_HD void pair_base(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
+	const BaseGeo<R> g = base_geo(P, p, q, sep);
+	if(g.hb) hb_term<R, SPLIT>(P, p, q, g, o);
+	if(g.crst) crst_term<R, SPLIT>(P, p, q, g, o);
+}
+
+// The stacking-site vector of a pair and its cosines, with whether coaxial stacking can be
+// non-zero (distance window and every angular factor inside its support)
+template <typename R>
+struct StackGeo {
+	R rmod, c1, c4, c5, c6;
+	v3<R> rd;
+	bool cxst;
+};
+
+template <typename R>
+OXGB_HD StackGeo<R> stack_geo(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep) {
+	StackGeo<R> g;
+	g.cxst = false;
+	const v3<R> rstack = site_vec(sep, q.stack, p.stack);
+	const R rs2 = dot(rstack, rstack);
+	if(!(R(OXM_CXST_RCLOW) * R(OXM_CXST_RCLOW) < rs2 && rs2 < R(OXM_CXST_RCHIGH) * R(OXM_CXST_RCHIGH))) return g;
+	g.rmod = m_sqrt(rs2);
+	if(!(R(OXM_CXST_RCLOW) < g.rmod && g.rmod < R(OXM_CXST_RCHIGH))) return g;
+	g.rd = rstack * (R(1) / g.rmod);
+	g.c1 = -dot(p.a1, q.a1), g.c4 = dot(p.a3, q.a3), g.c5 = dot(p.a3, g.rd), g.c6 = -dot(q.a3, g.rd);
+	g.cxst = f4_may(P, g.c1, OXM_F4_CX_T1) && f4_may(P, g.c4, OXM_F4_CX_T4) &&
+			(f4_may(P, g.c5, OXM_F4_CX_T5) || f4_may(P, -g.c5, OXM_F4_CX_T5)) &&
+			(f4_may(P, g.c6, OXM_F4_CX_T5) || f4_may(P, -g.c6, OXM_F4_CX_T5));
+	return g;
+}
+
 // coaxial stacking, oxDNA2 form: no phi3 factor, pure-harmonic theta1 term
-// (DNA2Interaction.cpp:214-306)
+// (DNA2Interaction.cpp:214-306), of a pair whose geometry admits it (g.cxst)
+template <typename R, bool SPLIT>
+OXGB_HD void cxst_term(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const StackGeo<R> &g, PairOut<R> &o) {
+	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3, rd = g.rd;
+	const R rmod = g.rmod, c5 = g.c5, c6 = g.c6;
+	R F2, F2D, g1, d1, g4, d4, g5a, d5a, g5b, d5b, g6a, d6a, g6b, d6b;
+	f2_both(P, rmod, OXM_F2_CXST, F2, F2D);
+	f4_both(P, g.c1, OXM_F4_CX_T1, g1, d1);
+	f4_both(P, g.c4, OXM_F4_CX_T4, g4, d4);
+	f4_both(P, c5, OXM_F4_CX_T5, g5a, d5a);
+	f4_both(P, -c5, OXM_F4_CX_T5, g5b, d5b);
+	f4_both(P, c6, OXM_F4_CX_T5, g6a, d6a);
+	f4_both(P, -c6, OXM_F4_CX_T5, g6b, d6b);
+	const R g5 = g5a + g5b, g6 = g6a + g6b;
+	d4 = -d4;
+	const R d5 = -d5a + d5b, d6 = d6a - d6b;
+	const R e = F2 * g1 * g4 * g5 * g6;
+	if(e != R(0)) {
+		add_e<R, SPLIT>(o, T_CXST, e);
+		v3<R> force = rd * (-(F2D * g1 * g4 * g5 * g6));
+		v3<R> tp = cross(a1, b1) * (F2 * d1 * g4 * g5 * g6);
+		tp += cross(a3, b3) * (F2 * g1 * d4 * g5 * g6);
+		const R f5 = F2 * g1 * g4 * d5 * g6;
+		force += (a3 - rd * c5) * (f5 / rmod);
+		tp -= cross(rd, a3) * f5;
+		const R f6 = F2 * g1 * g4 * g5 * d6;
+		force += (b3 + rd * c6) * (f6 / rmod);
+		o.F -= force;
+		o.T += tp - cross(p.stack, force);
+	}
+}
+
+// coaxial stacking of a pair
 template <typename R, bool SPLIT>
 OXGB_HD void pair_stack(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const Sep<R> &sep, PairOut<R> &o) {
-	const v3<R> a1 = p.a1, a3 = p.a3, b1 = q.a1, b3 = q.a3;
-	{
-		const v3<R> rstack = site_vec(sep, q.stack, p.stack);
-		const R rs2 = dot(rstack, rstack);
-		if(R(OXM_CXST_RCLOW) * R(OXM_CXST_RCLOW) < rs2 && rs2 < R(OXM_CXST_RCHIGH) * R(OXM_CXST_RCHIGH)) {
-			const R rmod = m_sqrt(rs2);
-			if(R(OXM_CXST_RCLOW) < rmod && rmod < R(OXM_CXST_RCHIGH)) {
-				const v3<R> rd = rstack * (R(1) / rmod);
-				const R c1 = -dot(a1, b1), c4 = dot(a3, b3), c5 = dot(a3, rd), c6 = -dot(b3, rd);
-				if(!(f4_may(P, c1, OXM_F4_CX_T1) && f4_may(P, c4, OXM_F4_CX_T4) &&
-						   (f4_may(P, c5, OXM_F4_CX_T5) || f4_may(P, -c5, OXM_F4_CX_T5)) &&
-						   (f4_may(P, c6, OXM_F4_CX_T5) || f4_may(P, -c6, OXM_F4_CX_T5))))
-					return;
-				R F2, F2D, g1, d1, g4, d4, g5a, d5a, g5b, d5b, g6a, d6a, g6b, d6b;
-				f2_both(P, rmod, OXM_F2_CXST, F2, F2D);
-				f4_both(P, c1, OXM_F4_CX_T1, g1, d1);
-				f4_both(P, c4, OXM_F4_CX_T4, g4, d4);
-				f4_both(P, c5, OXM_F4_CX_T5, g5a, d5a);
-				f4_both(P, -c5, OXM_F4_CX_T5, g5b, d5b);
-				f4_both(P, c6, OXM_F4_CX_T5, g6a, d6a);
-				f4_both(P, -c6, OXM_F4_CX_T5, g6b, d6b);
-				const R g5 = g5a + g5b, g6 = g6a + g6b;
-				d4 = -d4;
-				const R d5 = -d5a + d5b, d6 = d6a - d6b;
-				const R e = F2 * g1 * g4 * g5 * g6;
-				if(e != R(0)) {
-					add_e<R, SPLIT>(o, T_CXST, e);
-					v3<R> force = rd * (-(F2D * g1 * g4 * g5 * g6));
-					v3<R> tp = cross(a1, b1) * (F2 * d1 * g4 * g5 * g6);
-					tp += cross(a3, b3) * (F2 * g1 * d4 * g5 * g6);
-					const R f5 = F2 * g1 * g4 * d5 * g6;
-					force += (a3 - rd * c5) * (f5 / rmod);
-					tp -= cross(rd, a3) * f5;
-					const R f6 = F2 * g1 * g4 * g5 * d6;
-					force += (b3 + rd * c6) * (f6 / rmod);
-					o.F -= force;
-					o.T += tp - cross(p.stack, force);
-				}
-			}
-		}
-	}
+	const StackGeo<R> g = stack_geo(P, p, q, sep);
+	if(g.cxst) cxst_term<R, SPLIT>(P, p, q, g, o);
 }
 
 // Debye-Hueckel between backbone sites, halved charges at strand ends (DNA2Interaction.cpp:157-212).

@@ -442,11 +442,42 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, const Loader &l
 // per-lane compensated sums of a nucleotide's pair terms; ENERGY = false leaves the energies out
 // (an MD step needs only forces and torques: the energy arithmetic of the pair functions is then
 // dead code)
+// Terms of bounded size (Debye-Hueckel, excluded volume) go to a plain per-lane sum when
+// OXGB_NB_PLAIN_SHORT is set: a lane adds only a few of them, whose rounding is far below the
+// compensated sums of the large bonded and pair terms; they join the compensated sum before the
+// group reduction.
+#ifndef OXGB_NB_PLAIN_SHORT
+#define OXGB_NB_PLAIN_SHORT 0
+#endif
+
 template <typename R, bool SPLIT, bool ENERGY = true>
 struct SplitAcc {
 	KahanV<R> F, T;
+	v3<R> Fp, Tp;
 	R E, Ec, Eh, Ehc;
 	R split[N_TERMS];
+	__device__ __forceinline__ void add_short(const PairOut<R> &o) {
+		if(!OXGB_NB_PLAIN_SHORT) {
+			add(o);
+			return;
+		}
+		Fp = Fp + o.F;
+		Tp = Tp + o.T;
+		if(ENERGY) {
+			KahanV<R>::kadd(E, Ec, o.E);
+			KahanV<R>::kadd(Eh, Ehc, o.Ehb);
+		}
+		if(SPLIT) {
+#pragma unroll
+			for(int k = 0; k < N_TERMS; k++) split[k] += o.split[k];
+		}
+	}
+	__device__ __forceinline__ void fold_short() {
+		if(OXGB_NB_PLAIN_SHORT) {
+			F.add(Fp);
+			T.add(Tp);
+		}
+	}
 	__device__ __forceinline__ void add(const PairOut<R> &o) {
 		F.add(o.F);
 		T.add(o.T);
@@ -477,31 +508,102 @@ struct SplitAcc {
 // stack-stack pairs (coaxial stacking; the other blocks), each evaluated once, by its lower
 // nucleotide i (partner j > i, at position k of i's list and m of j's): slot k of i gets
 // (force on i, E), (torque on i, E_hb) and slot m of j gets (-force, E), (torque on j, E_hb), at
-// [2 (k N + i) + 0..1] of base_res / stk_res.  Every slot of every list is written once.  These are the
-// costliest terms and their lists are short, so the owned slots of a warp's 32 nucleotides
-// are queued (a warp prefix sum over the per-lane counts) and dealt 32 at a time: every lane
-// works on a pair in every round but the last.
+// [2 (k N + i) + 0..1] of base_res / stk_res.  Every slot of every list is written by its pair
+// alone.  These are the costliest terms and their lists are short, so the owned slots of a
+// warp's nucleotides are queued (a warp prefix sum over the per-lane counts) and dealt 32 at a
+// time: every lane works on a pair in every round but the last.
 // nucleotides per warp in a pair block: fewer than 32 gives more warps (more latency hidden)
 // for about as many rounds of pairs per warp as a full-warp queue
 #ifndef OXGB_PAIR_NPW
 #define OXGB_PAIR_NPW 16
 #endif
 
+__device__ __forceinline__ void atomic_add_v4(float4 *p, const float4 &v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add_v4(double4_32a *p, const double4_32a &v) {
+	atomicAdd(&p->x, v.x);
+	atomicAdd(&p->y, v.y);
+	atomicAdd(&p->z, v.z);
+	atomicAdd(&p->w, v.w);
+}
+
+// one term (0 hydrogen bonding, 1 cross stacking, 2 coaxial stacking; warp-uniform) of the
+// queued pairs t[0 .. n - 1], lane l taking t[l]: the pair's result is added to its two slots
+// (zeroed when the pair was screened).  A slot receives at most two terms (hydrogen bonding and
+// cross stacking of one pair), whose sum does not depend on their order.  Not inlined: it is
+// called from several places, and one compiled copy gives a pair the same rounding wherever
+// its batch is evaluated (inlined copies may contract products into FMAs differently); the term
+// is evaluated only if this copy's own screening admits it.
+template <typename R, class Loader, bool SPLIT, bool ENERGY>
+__device__ __noinline__ void eval_terms(const ForceArgs &a, const Loader &ld, const DNA2Table<R> *Ps, int s0,
+		const int4 *t, int n, int term) {
+	using V4 = typename Vec4Of<R>::T;
+	const int lane = threadIdx.x & 31;
+	if(lane >= n) return;
+	const int4 it = t[lane];
+	const int i = it.x, j = it.y, k = it.z, m = it.w;
+	const long long N = a.N;
+	const int sy = a.sys ? a.sys[i] : 0;
+	const DNA2Table<R> &P = Ps[sy - s0];
+	Nuc<R> p, qn;
+	V4 ph, pl, qh, ql;
+	load_full<Loader, R>(ld, i, P, p, ph, pl);
+	load_full<Loader, R>(ld, j, P, qn, qh, ql);
+	const Sep<R> d = ld.sep(ph, pl, qh, ql, P);
+	PairOut<R> o{};
+	if(term == 2) {
+		const StackGeo<R> g = stack_geo(P, p, qn, d);
+		if(g.cxst) cxst_term<R, SPLIT>(P, p, qn, g, o);
+	}
+	else {
+		const BaseGeo<R> g = base_geo(P, p, qn, d);
+		if(term == 0 && g.hb) hb_term<R, SPLIT>(P, p, qn, g, o);
+		if(term == 1 && g.crst) crst_term<R, SPLIT>(P, p, qn, g, o);
+	}
+	// the potential is invariant under rigid rotations, so the torques balance:
+	// T_j = -T_i + (r_j - r_i) x F_i, the cross product with error-free products
+	const v3<R> c = cross_accurate(d, o.F);
+	V4 fi, ti, fj, tj;
+	fi.x = o.F.x, fi.y = o.F.y, fi.z = o.F.z, fi.w = ENERGY ? o.E : R(0);
+	ti.x = o.T.x, ti.y = o.T.y, ti.z = o.T.z, ti.w = ENERGY ? o.Ehb : R(0);
+	fj.x = -o.F.x, fj.y = -o.F.y, fj.z = -o.F.z, fj.w = fi.w;
+	tj.x = c.x - o.T.x, tj.y = c.y - o.T.y, tj.z = c.z - o.T.z, tj.w = ti.w;
+	V4 *res = reinterpret_cast<V4 *>(term == 2 ? a.stk_res : a.base_res);
+	atomic_add_v4(res + 2 * ((long long) k * N + i), fi);
+	atomic_add_v4(res + 2 * ((long long) k * N + i) + 1, ti);
+	if(m >= 0) {  // (a missing position is flagged by the list build)
+		atomic_add_v4(res + 2 * ((long long) m * N + j), fj);
+		atomic_add_v4(res + 2 * ((long long) m * N + j) + 1, tj);
+	}
+	if(SPLIT) {
+#pragma unroll
+		for(int u = 0; u < N_TERMS; u++)
+			if(o.split[u] != R(0)) atomicAdd(a.esplit + 8 * sy + u, (double) o.split[u]);
+	}
+}
+
+// Pair block b: base-base pairs (hydrogen bonding + cross stacking; blocks 0 .. base_blocks -
+// 1) or stack-stack pairs (coaxial stacking; the other blocks).  Each warp deals the owned pairs
+// of its nucleotides 32 at a time (as above) and screens them (base_geo / stack_geo: distance
+// windows and angular supports); only about a third of the pairs has a non-zero term, so the
+// live terms go to per-warp queues in shared memory and are evaluated 32 at a time, every lane
+// on the same term, instead of on the few lanes of each round whose pair happens to be live.
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
 __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld, int b, int base_blocks) {
 	using V4 = typename Vec4Of<R>::T;
 	constexpr int NPW = OXGB_PAIR_NPW;
+	__shared__ int4 tq[4][2][64];  // per warp: live hydrogen-bonding (or coaxial) and cross-stacking terms
 	const bool is_base = b < base_blocks;
 	const int per_block = (blockDim.x / 32) * NPW;
 	const int first = (is_base ? b : b - base_blocks) * per_block;
 	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
 	const int s0 = load_table_span<R>(a, first, min(first + per_block, a.N) - 1, Ps);
 	const long long N = a.N;
-	const int lane = threadIdx.x & 31;
-	const int wbase = first + (threadIdx.x >> 5) * NPW;
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	const int wbase = first + w * NPW;
 	if(wbase >= a.N) return;  // warp-uniform
 	const int cap = is_base ? a.base_cap : a.stk_cap;
 	const int *nb = is_base ? a.base_nb : a.stk_nb;
+	V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res);
 	// this lane's nucleotide (lanes below NPW): which of its entries it owns (partner above
 	// it), as a bit mask
 	const int il = wbase + lane;
@@ -523,6 +625,9 @@ __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld,
 	}
 	const int total = __shfl_sync(0xffffffffu, incl, 31);
 	const int excl = incl - own;
+	const unsigned below = (1u << lane) - 1u;
+	int n0 = 0, n1 = 0;  // queued terms (warp-uniform)
+	const int term0 = is_base ? 0 : 2;
 	for(int q0 = 0; q0 < total; q0 += 32) {
 		const int q = q0 + lane;
 		// the lane that owns queue entry q: the first whose inclusive count exceeds q
@@ -534,44 +639,60 @@ __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld,
 		}
 		const int ex_l = __shfl_sync(0xffffffffu, excl, l & 31);
 		const unsigned lo_l = __shfl_sync(0xffffffffu, lo, l & 31), hi_l = __shfl_sync(0xffffffffu, hi, l & 31);
-		if(q >= total) continue;
-		// the r-th owned entry of nucleotide i
-		const int r = q - ex_l, nlo = __popc(lo_l);
-		const int k = r < nlo ? (int) __fns(lo_l, 0u, r + 1) : 32 + (int) __fns(hi_l, 0u, r - nlo + 1);
-		const int i = wbase + l;
-		const int j = nb[(long long) k * N + i];
-		const int m = (is_base ? a.base_pos : a.stk_pos)[(long long) k * N + i];
-		const int sy = a.sys ? a.sys[i] : 0;
-		const DNA2Table<R> &P = Ps[sy - s0];
-		Nuc<R> p, qn;
-		V4 ph, pl, qh, ql;
-		load_full<Loader, R>(ld, i, P, p, ph, pl);
-		load_full<Loader, R>(ld, j, P, qn, qh, ql);
-		const Sep<R> d = ld.sep(ph, pl, qh, ql, P);
-		PairOut<R> o{};
-		if(is_base) pair_base<R, SPLIT>(P, p, qn, d, o);
-		else pair_stack<R, SPLIT>(P, p, qn, d, o);
-		// the potential is invariant under rigid rotations, so the torques balance:
-		// T_j = -T_i + (r_j - r_i) x F_i, the cross product with error-free products
-		const v3<R> c = cross_accurate(d, o.F);
-		V4 fi, ti, fj, tj;
-		fi.x = o.F.x, fi.y = o.F.y, fi.z = o.F.z, fi.w = ENERGY ? o.E : R(0);
-		ti.x = o.T.x, ti.y = o.T.y, ti.z = o.T.z, ti.w = ENERGY ? o.Ehb : R(0);
-		fj.x = -o.F.x, fj.y = -o.F.y, fj.z = -o.F.z, fj.w = fi.w;
-		tj.x = c.x - o.T.x, tj.y = c.y - o.T.y, tj.z = c.z - o.T.z, tj.w = ti.w;
-		V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res);
-		res[2 * ((long long) k * N + i)] = fi;
-		res[2 * ((long long) k * N + i) + 1] = ti;
-		if(m >= 0) {  // (a missing position is flagged by the list build)
-			res[2 * ((long long) m * N + j)] = fj;
-			res[2 * ((long long) m * N + j) + 1] = tj;
+		bool live0 = false, live1 = false;
+		int4 item = make_int4(0, 0, 0, -1);
+		if(q < total) {
+			// the r-th owned entry of nucleotide i
+			const int r = q - ex_l, nlo = __popc(lo_l);
+			const int k = r < nlo ? (int) __fns(lo_l, 0u, r + 1) : 32 + (int) __fns(hi_l, 0u, r - nlo + 1);
+			const int i = wbase + l;
+			const int j = nb[(long long) k * N + i];
+			const int m = (is_base ? a.base_pos : a.stk_pos)[(long long) k * N + i];
+			const int sy = a.sys ? a.sys[i] : 0;
+			const DNA2Table<R> &P = Ps[sy - s0];
+			Nuc<R> p, qn;
+			V4 ph, pl, qh, ql;
+			load_full<Loader, R>(ld, i, P, p, ph, pl);
+			load_full<Loader, R>(ld, j, P, qn, qh, ql);
+			const Sep<R> d = ld.sep(ph, pl, qh, ql, P);
+			if(is_base) {
+				const BaseGeo<R> g = base_geo(P, p, qn, d);
+				live0 = g.hb;
+				live1 = g.crst;
+			}
+			else {
+				live0 = stack_geo(P, p, qn, d).cxst;
+			}
+			// both slots start from zero; the live terms add into them
+			V4 z;
+			z.x = z.y = z.z = z.w = R(0);
+			res[2 * ((long long) k * N + i)] = z;
+			res[2 * ((long long) k * N + i) + 1] = z;
+			if(m >= 0) {
+				res[2 * ((long long) m * N + j)] = z;
+				res[2 * ((long long) m * N + j) + 1] = z;
+			}
+			item = make_int4(i, j, k, m);
 		}
-		if(SPLIT) {
-#pragma unroll
-			for(int m = 0; m < N_TERMS; m++)
-				if(o.split[m] != R(0)) atomicAdd(a.esplit + 8 * sy + m, (double) o.split[m]);
+		const unsigned b0 = __ballot_sync(0xffffffffu, live0), b1 = __ballot_sync(0xffffffffu, live1);
+		if(live0) tq[w][0][n0 + __popc(b0 & below)] = item;
+		if(live1) tq[w][1][n1 + __popc(b1 & below)] = item;
+		n0 += __popc(b0);
+		n1 += __popc(b1);
+		__syncwarp();  // the queued items and the zeroed slots are visible to the whole warp
+		if(n0 >= 32) {
+			n0 -= 32;
+			eval_terms<R, Loader, SPLIT, ENERGY>(a, ld, Ps, s0, tq[w][0] + n0, 32, term0);
+			__syncwarp();
+		}
+		if(n1 >= 32) {
+			n1 -= 32;
+			eval_terms<R, Loader, SPLIT, ENERGY>(a, ld, Ps, s0, tq[w][1] + n1, 32, 1);
+			__syncwarp();
 		}
 	}
+	if(n0 > 0) eval_terms<R, Loader, SPLIT, ENERGY>(a, ld, Ps, s0, tq[w][0], n0, term0);
+	if(n1 > 0) eval_terms<R, Loader, SPLIT, ENERGY>(a, ld, Ps, s0, tq[w][1], n1, 1);
 }
 
 // The bonded and the base/stack pair work are independent (both read the mirrors, each writes
@@ -639,7 +760,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 			load_dh<Loader, R>(ld, j, P, q, qh, ql);
 			PairOut<R> o{};
 			pair_dh<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P).plain(), o);
-			acc.add(o);
+			acc.add_short(o);
 		}
 		// excluded volume over centre-close pairs
 		const int nev = live ? min(a.ev_n[i], a.ev_cap) : 0;
@@ -650,7 +771,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 			load_full<Loader, R>(ld, j, P, q, qh, ql);
 			PairOut<R> o{};
 			pair_ev<R, SPLIT>(p, q, ld.sep(ph, pl, qh, ql, P).plain(), o);
-			acc.add(o);
+			acc.add_short(o);
 		}
 		// hydrogen bonding + cross stacking and coaxial stacking: evaluated per list slot by
 		// the pair blocks of k_bonded_pairs, gathered here
@@ -683,6 +804,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 			}
 		}
 
+		acc.fold_short();
 		const R fx = group_sum_comp<R, K>(acc.F.s.x, acc.F.c.x), fy = group_sum_comp<R, K>(acc.F.s.y, acc.F.c.y),
 				fz = group_sum_comp<R, K>(acc.F.s.z, acc.F.c.z);
 		const v3<R> tl{group_sum_comp<R, K>(acc.T.s.x, acc.T.c.x), group_sum_comp<R, K>(acc.T.s.y, acc.T.c.y),

@@ -21,21 +21,22 @@ namespace oxgb {
 
 // ---------------------------------------------------------------- FP32 mirrors
 
-// the FP32 mirrors of nucleotide i from its FP64 position and quaternion: the position as hi + lo,
-// the body axes a1, a3 and the grooved backbone offset (src/Particles/DNANucleotide.cpp:79), each
+// The FP32 mirrors of nucleotide i from its FP64 state: the position as hi + lo, the body
+// axes a1, a3 and the grooved backbone offset (src/Particles/DNANucleotide.cpp:79), each
 // rounded once (to within an ulp) from exact values; conversions and products on the FP32 and
-// integer pipes (split.cuh).  Returns the position rounded to FP32, a1 and the backbone offset.
-struct Mirror {
-	float3 r, a1, back;
-};
-
-__device__ __forceinline__ Mirror write_mirror(const StepArgs &a, int i, const double4_32a &r, const double4_32a &q) {
+// integer pipes (split.cuh).  Each part returns what the staleness test needs.
+__device__ __forceinline__ float3 mirror_position(const StepArgs &a, int i, const double4_32a &r) {
 	float4 hi = a.pos_hi[i], lo = a.pos_lo[i];
 	split_rn(r.x, hi.x, lo.x);
 	split_rn(r.y, hi.y, lo.y);
 	split_rn(r.z, hi.z, lo.z);
 	a.pos_hi[i] = hi;
 	a.pos_lo[i] = lo;
+	return make_float3(hi.x, hi.y, hi.z);
+}
+
+// returns a1 and the backbone offset
+__device__ __forceinline__ void mirror_frame(const StepArgs &a, int i, const double4_32a &q, float3 &a1o, float3 &backo) {
 	float qh[4], ql[4], a1[3], a3[3], bk[3];
 	split_rn(q.x, qh[0], ql[0]);
 	split_rn(q.y, qh[1], ql[1]);
@@ -49,17 +50,17 @@ __device__ __forceinline__ Mirror write_mirror(const StepArgs &a, int i, const d
 		const int2 bd = a.bonds[i];
 		a.fback[i] = make_float4(bk[0], bk[1], bk[2], (bd.x < 0 || bd.y < 0) ? 1.f : 0.f);
 	}
-	return Mirror{make_float3(hi.x, hi.y, hi.z), make_float3(a1[0], a1[1], a1[2]), make_float3(bk[0], bk[1], bk[2])};
+	a1o = make_float3(a1[0], a1[1], a1[2]);
+	backo = make_float3(bk[0], bk[1], bk[2]);
 }
 
 // true if the centre or any interaction site moved more than the skin since the last list build
-// (m: the new mirrors)
-__device__ __forceinline__ bool list_stale(const StepArgs &a, int i, const Mirror &m) {
+// (r: the new centre in FP32, a1 and back: the new axis and backbone offset)
+__device__ __forceinline__ bool list_stale(const StepArgs &a, int i, float3 r, float3 a1, float3 bk) {
 	const float4 lp = a.list_pos[i];
-	const float dx = m.r.x - lp.x, dy = m.r.y - lp.y, dz = m.r.z - lp.z;
+	const float dx = r.x - lp.x, dy = r.y - lp.y, dz = r.z - lp.z;
 	if(dx * dx + dy * dy + dz * dz > a.skin2) return true;
 	if(!a.list_a1) return false;
-	const float3 a1 = m.a1, bk = m.back;
 	const float4 la1 = a.list_a1[i], lbk = a.list_back[i];
 	const float ex = a1.x - la1.x, ey = a1.y - la1.y, ez = a1.z - la1.z;
 	float sx = dx + 0.4f * ex, sy = dy + 0.4f * ey, sz = dz + 0.4f * ez;  // base site
@@ -73,7 +74,9 @@ __device__ __forceinline__ bool list_stale(const StepArgs &a, int i, const Mirro
 __global__ void k_make_mirrors(StepArgs a) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= a.N) return;
-	(void) write_mirror(a, i, a.pos[i], a.quat[i]);
+	float3 a1, bk;
+	(void) mirror_position(a, i, a.pos[i]);
+	mirror_frame(a, i, a.quat[i], a1, bk);
 }
 
 // ---------------------------------------------------------------- first half step
@@ -85,82 +88,118 @@ __device__ __forceinline__ long long step_of(const ThermoArgs &t) { return *t.st
 template <typename V4>
 __device__ __forceinline__ void complete_step(const ThermoArgs &t, int i, int sy, long long sp, const V4 &F, const V4 &T,
 		double4_32a &v, double4_32a &L) {
+	// the half kicks are written as FMAs here and in the first step, so that a step completed at
+	// the end of a run and one completed by the next first step are the same
 	const double hdt = 0.5 * t.dt;
-	v.x += widen(F.x) * hdt;
-	v.y += widen(F.y) * hdt;
-	v.z += widen(F.z) * hdt;
-	L.x += widen(T.x) * hdt;
-	L.y += widen(T.y) * hdt;
-	L.z += widen(T.z) * hdt;
+	v.x = fma(widen(F.x), hdt, v.x);
+	v.y = fma(widen(F.y), hdt, v.y);
+	v.z = fma(widen(F.z), hdt, v.z);
+	L.x = fma(widen(T.x), hdt, L.x);
+	L.y = fma(widen(T.y), hdt, L.y);
+	L.z = fma(widen(T.z), hdt, L.z);
 	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) brownian_redraw(t, sy, i - t.sys_off[sy], sp, v, L);
 	else if(t.thermostat == 2 && *t.bussi_stamp == sp) bussi_rescale(t, sy, v, L);
 }
 
-template <typename V4>
-__global__ void k_first_step(StepArgs a) {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i >= a.N) return;
-	const long long s = step_of(a.th);
-	const int sy = a.th.sys[i];
-	const V4 F = reinterpret_cast<const V4 *>(a.forces)[i];
-	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
-	const double hdt = 0.5 * a.dt;
-	double4_32a v = a.vel[i], r = a.pos[i], L = a.angmom[i], q = a.quat[i];
-	// the previous step's second half kick and thermostat (kept as a separate half kick, so that
-	// a state is the same whether or not a run ended at that step)
-	if(*a.th.open_step == s - 1) complete_step(a.th, i, sy, s - 1, F, T, v, L);
-	v.x += widen(F.x) * hdt;
-	v.y += widen(F.y) * hdt;
-	v.z += widen(F.z) * hdt;
-	r.x += v.x * a.dt;
-	r.y += v.y * a.dt;
-	r.z += v.z * a.dt;
-	L.x += widen(T.x) * hdt;
-	L.y += widen(T.y) * hdt;
-	L.z += widen(T.z) * hdt;
-	// rotation by dt|L| about L (body frame): q <- q * (sin(th/2) L^, cos(th/2))
+// the orientation after a step of dt with angular momentum L (body frame):
+// q <- q * (sin(th/2) L^, cos(th/2)), th = dt |L|, then renormalised
+__device__ __forceinline__ void rotate(double4_32a &q, const double4_32a &L, double dt) {
 	const double L2 = L.x * L.x + L.y * L.y + L.z * L.z;
-	if(L2 > 0.0) {
-		const double hd = 0.5 * a.dt, x2 = hd * hd * L2;  // x = th / 2
-		double k, ch;
-		if(x2 < 1e-5) {
-			// sin(x) / x and cos(x) as Taylor series in x^2: no square root, range reduction or
-			// division, which are slow in FP64.  The first omitted terms, x^6/5040 and x^8/40320,
-			// are below 2e-19 for x^2 < 1e-5 (a typical step has x^2 ~ 1e-6)
-			k = hd * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0)));
-			ch = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0)));
+	if(!(L2 > 0.0)) return;
+	const double hd = 0.5 * dt, x2 = hd * hd * L2;  // x = th / 2
+	double k, ch;
+	if(x2 < 1e-5) {
+		// sin(x) / x and cos(x) as Taylor series in x^2: no square root, range reduction or
+		// division, which are slow in FP64.  The first omitted terms, x^6/5040 and x^8/40320,
+		// are below 2e-19 for x^2 < 1e-5 (a typical step has x^2 ~ 1e-6)
+		k = hd * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0)));
+		ch = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0)));
+	}
+	else if(x2 < 1e-2) {
+		// the same series to x^10 (truncation below 1e-20 for |x| < 0.1)
+		k = hd * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0) * (1.0 - x2 * (1.0 / 42.0) * (1.0 - x2 * (1.0 / 72.0) * (1.0 - x2 * (1.0 / 110.0))))));
+		ch = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0) * (1.0 - x2 * (1.0 / 56.0) * (1.0 - x2 * (1.0 / 90.0)))));
+	}
+	else {
+		const double norm = sqrt(L2);
+		double sh;
+		sincos(hd * norm, &sh, &ch);
+		k = sh / norm;
+	}
+	const double rx = L.x * k, ry = L.y * k, rz = L.z * k, rw = ch;
+	double4_32a n;
+	n.w = q.w * rw - q.x * rx - q.y * ry - q.z * rz;
+	n.x = q.w * rx + q.x * rw + q.y * rz - q.z * ry;
+	n.y = q.w * ry - q.x * rz + q.y * rw + q.z * rx;
+	n.z = q.w * rz + q.x * ry - q.y * rx + q.z * rw;
+	const double nn = n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w;
+	const double d = nn - 1.0;
+	// |n|^2 = 1 + d with |d| at the rounding level: 1/sqrt(1 + d) = 1 - d/2 + 3d^2/8 - ...
+	const double inv = fabs(d) < 1e-6 ? 1.0 - d * (0.5 - 0.375 * d) : 1.0 / sqrt(nn);
+	q = make_double4_32a(n.x * inv, n.y * inv, n.z * inv, n.w * inv);
+}
+
+// First half of step s, two warps per 32 nucleotides: warp 0 of a block the translation (second
+// half kick and thermostat of step s - 1, half kick, drift, position mirror), warp 1 the
+// rotation (the same for the angular momentum, rotation, frame mirror).  The chains of FP64
+// operations are half as long and twice as many warps hide them; a warp never diverges on the
+// kind of motion.
+template <typename V4>
+__global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
+	__shared__ float3 s_a1[32], s_bk[32];
+	const int lane = threadIdx.x & 31;
+	const bool rot = threadIdx.x >= 32;
+	const int i = blockIdx.x * 32 + lane;
+	const bool live = i < a.N;
+	float3 r32 = make_float3(0.f, 0.f, 0.f);
+	int sy = 0;
+	if(live) {
+		const long long s = step_of(a.th);
+		sy = a.th.sys[i];
+		const double hdt = 0.5 * a.dt;
+		// the previous step's second half kick and thermostat (kept as a separate half kick, so
+		// that a state is the same whether or not a run ended at that step)
+		const bool complete = *a.th.open_step == s - 1;
+		const long long sp = s - 1;
+		const bool brownian = complete && a.th.thermostat == 1 && sp % a.th.newtonian_steps == 0;
+		const bool bussi = complete && a.th.thermostat == 2 && *a.th.bussi_stamp == sp;
+		const V4 G = reinterpret_cast<const V4 *>(rot ? a.torques : a.forces)[i];
+		double4_32a x = rot ? a.angmom[i] : a.vel[i];
+		const double gx = widen(G.x), gy = widen(G.y), gz = widen(G.z);
+		if(complete) {
+			x.x = fma(gx, hdt, x.x);
+			x.y = fma(gy, hdt, x.y);
+			x.z = fma(gz, hdt, x.z);
+			if(brownian) brownian_redraw_part(a.th, sy, i - a.th.sys_off[sy], sp, rot ? 1 : 0, x);
+			else if(bussi) bussi_rescale_part(a.th, sy, rot ? 1 : 0, x);
 		}
-		else if(x2 < 1e-2) {
-			// the same series to x^10 (truncation below 1e-20 for |x| < 0.1)
-			k = hd * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0) * (1.0 - x2 * (1.0 / 42.0) * (1.0 - x2 * (1.0 / 72.0) * (1.0 - x2 * (1.0 / 110.0))))));
-			ch = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0) * (1.0 - x2 * (1.0 / 56.0) * (1.0 - x2 * (1.0 / 90.0)))));
+		x.x = fma(gx, hdt, x.x);
+		x.y = fma(gy, hdt, x.y);
+		x.z = fma(gz, hdt, x.z);
+		if(!rot) {
+			double4_32a r = a.pos[i];
+			r.x += x.x * a.dt;
+			r.y += x.y * a.dt;
+			r.z += x.z * a.dt;
+			a.vel[i] = x;
+			a.pos[i] = r;
+			r32 = mirror_position(a, i, r);
 		}
 		else {
-			const double norm = sqrt(L2);
-			double sh;
-			sincos(hd * norm, &sh, &ch);
-			k = sh / norm;
+			double4_32a q = a.quat[i];
+			rotate(q, x, a.dt);
+			a.angmom[i] = x;
+			a.quat[i] = q;
+			float3 a1, bk;
+			mirror_frame(a, i, q, a1, bk);
+			s_a1[lane] = a1;
+			s_bk[lane] = bk;
 		}
-		const double rx = L.x * k, ry = L.y * k, rz = L.z * k, rw = ch;
-		double4_32a n;
-		n.w = q.w * rw - q.x * rx - q.y * ry - q.z * rz;
-		n.x = q.w * rx + q.x * rw + q.y * rz - q.z * ry;
-		n.y = q.w * ry - q.x * rz + q.y * rw + q.z * rx;
-		n.z = q.w * rz + q.x * ry - q.y * rx + q.z * rw;
-		const double nn = n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w;
-		const double d = nn - 1.0;
-		// |n|^2 = 1 + d with |d| at the rounding level: 1/sqrt(1 + d) = 1 - d/2 + 3d^2/8 - ...
-		const double inv = fabs(d) < 1e-6 ? 1.0 - d * (0.5 - 0.375 * d) : 1.0 / sqrt(nn);
-		q = make_double4_32a(n.x * inv, n.y * inv, n.z * inv, n.w * inv);
 	}
-	a.vel[i] = v;
-	a.pos[i] = r;
-	a.angmom[i] = L;
-	a.quat[i] = q;
-	const Mirror m = write_mirror(a, i, r, q);
+	__syncthreads();
 	// Verlet list staleness (CUDA_mixed.cuh:68, extended to the interaction sites for the term
-	// lists), per system
-	if(list_stale(a, i, m)) {
+	// lists), per system, on the translation warp with the rotation warp's a1 and backbone offset
+	if(live && !rot && list_stale(a, i, r32, s_a1[lane], s_bk[lane])) {
 		a.sys_stale[sy] = 1;
 		atomicOr(a.flag, 1);
 	}
@@ -450,9 +489,10 @@ __global__ void k_set_conditional(const int *flag, cudaGraphConditionalHandle h)
 static inline int blocks_for(int N, int tpb) { return N > 0 ? (N + tpb - 1) / tpb : 1; }
 
 cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s) {
-	// one-warp blocks: the FP64 work (1/64 of the FP32 rate) spreads evenly over the SMs
-	if(double_forces) k_first_step<double4_32a><<<blocks_for(a.N, 32), 32, 0, s>>>(a);
-	else k_first_step<float4><<<blocks_for(a.N, 32), 32, 0, s>>>(a);
+	// two-warp blocks of 32 nucleotides: the FP64 work (1/64 of the FP32 rate) spreads evenly over
+	// the SMs
+	if(double_forces) k_first_step<double4_32a><<<blocks_for(a.N, 32), 64, 0, s>>>(a);
+	else k_first_step<float4><<<blocks_for(a.N, 32), 64, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

@@ -150,6 +150,32 @@ static __device__ __noinline__ void brownian_redraw(const ThermoArgs &t, int sy,
 	if(u01(o0[1]) < par[SP_PR]) L = make_double4_32a(g[3] * sT, g[4] * sT, g[5] * sT, 0.0);
 }
 
+// one kind of motion of brownian_redraw (which = 0: the velocity, 1: the angular momentum), with
+// the same draws
+static __device__ __noinline__ void brownian_redraw_part(const ThermoArgs &t, int sy, int i_local, long long s, int which,
+		double4_32a &x) {
+	const double *par = t.sys_par + sy * SP_STRIDE;
+	const unsigned long long seed = t.sys_seed[sy];
+	unsigned o0[4], o1[4];
+	const unsigned k0 = (unsigned) seed, k1 = (unsigned) (seed >> 32);
+	const unsigned s0 = (unsigned) s, s1 = (unsigned) ((unsigned long long) s >> 32);
+	philox(k0, k1, s0, s1, RNG_BROWNIAN, (unsigned) (2 * i_local), o0);
+	philox(k0, k1, s0, s1, RNG_BROWNIAN, (unsigned) (2 * i_local + 1), o1);
+	const double sT = par[SP_SQRTT];
+	double g0, g1, g2, g3;
+	box_muller(o1[0], o1[1], g2, g3);
+	if(which == 0) {
+		if(u01(o0[0]) < par[SP_PT]) {
+			box_muller(o0[2], o0[3], g0, g1);
+			x = make_double4_32a(g0 * sT, g1 * sT, g2 * sT, 0.0);
+		}
+	}
+	else if(u01(o0[1]) < par[SP_PR]) {
+		box_muller(o1[2], o1[3], g0, g1);
+		x = make_double4_32a(g3 * sT, g0 * sT, g1 * sT, 0.0);
+	}
+}
+
 // Bussi: from the sums of v, |v|^2 and |L|^2 over system sy, the new running kinetic energy
 // (with the draws of this step) and the rescaling factor of one kind of motion: which = 0
 // translation (about the centre-of-mass velocity), 1 rotation.  The two run on two threads.
@@ -171,6 +197,23 @@ static __device__ void bussi_update(const ThermoArgs &t, int sy, long long s, in
 		const double Kr_now = 0.5 * sum[4];
 		update_K(st[1], par[SP_1MC], par[SP_A], par[SP_B], __ldcg(st + 10), __ldcg(st + 11));
 		st[3] = sqrt(st[1]) * rsqrt(Kr_now);
+	}
+}
+
+// one kind of motion of bussi_rescale (which = 0: the velocity, 1: the angular momentum)
+static __device__ __forceinline__ void bussi_rescale_part(const ThermoArgs &t, int sy, int which, double4_32a &x) {
+	const double *st = t.bussi_state + 16 * sy;
+	if(which == 0) {
+		const double ft = __ldcg(st + 2), cx = __ldcg(st + 4), cy = __ldcg(st + 5), cz = __ldcg(st + 6);
+		x.x = (x.x - cx) * ft + cx;
+		x.y = (x.y - cy) * ft + cy;
+		x.z = (x.z - cz) * ft + cz;
+	}
+	else {
+		const double fr = __ldcg(st + 3);
+		x.x *= fr;
+		x.y *= fr;
+		x.z *= fr;
 	}
 }
 
