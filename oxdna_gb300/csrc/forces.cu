@@ -700,6 +700,7 @@ __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld,
 // blocks (the costliest, dispatched first), the rest bonded blocks, which fill the tail.
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
 __global__ void __launch_bounds__(128) k_bonded_pairs(ForceArgs a, Loader ld, int pair_blocks) {
+	pdl_trigger();  // the non-bonded kernel may start (it waits before reading these results)
 	const int b = blockIdx.x;
 	if(b < 2 * pair_blocks) pair_block<R, Loader, SPLIT, ENERGY>(a, ld, b, pair_blocks);
 	else bonded_block<R, Loader, SPLIT, ENERGY>(a, ld, b - 2 * pair_blocks);
@@ -774,7 +775,10 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 			acc.add_short(o);
 		}
 		// hydrogen bonding + cross stacking and coaxial stacking: evaluated per list slot by
-		// the pair blocks of k_bonded_pairs, gathered here
+		// the pair blocks of k_bonded_pairs, gathered here (the terms above read only the
+		// mirrors and lists, complete before k_bonded_pairs started)
+		pdl_wait();
+		pdl_trigger();
 		const int nb_ = live ? min(a.base_n[i], a.base_cap) : 0;
 		for(int k = sub; k < nb_; k += K) acc.add_slot(reinterpret_cast<const V4 *>(a.base_res), N, i, k);
 		const int ns = live ? min(a.stk_n[i], a.stk_cap) : 0;
@@ -841,6 +845,8 @@ int nonbonded_blocks(int N) {
 // in order (deterministic), added to the force the pair kernels left; FP64 positions.
 template <typename V4>
 __global__ void k_external(ForceArgs a) {
+	pdl_wait();
+	pdl_trigger();
 	const int k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= a.ext_n) return;
 	const int i = a.ext_nuc[k];
@@ -920,10 +926,13 @@ static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEv
 	// 128 nucleotides
 	const int pair_blocks = (a.N + 4 * OXGB_PAIR_NPW - 1) / (4 * OXGB_PAIR_NPW);
 	k_bonded_pairs<R, Loader, SPLIT, ENERGY><<<2 * pair_blocks + blocks, tpb, smem, s>>>(a, ld, pair_blocks);
+	// the non-bonded kernel starts its Debye-Hueckel and excluded-volume work while the tail of
+	// the bonded and pair blocks runs; the external forces follow it the same way
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
 	constexpr int K = OXGB_NB_LANES;
-	k_nonbonded_split<R, Loader, SPLIT, ENERGY, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
-	if(a.ext_n > 0) k_external<typename Vec4Of<R>::T><<<(a.ext_n + tpb - 1) / tpb, tpb, 0, s>>>(a);
+	if(wait) k_nonbonded_split<R, Loader, SPLIT, ENERGY, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
+	else launch_after(k_nonbonded_split<R, Loader, SPLIT, ENERGY, K>, dim3(nonbonded_blocks(a.N)), dim3(tpb), smem, s, a, ld);
+	if(a.ext_n > 0) launch_after(k_external<typename Vec4Of<R>::T>, dim3((a.ext_n + tpb - 1) / tpb), dim3(tpb), 0, s, a);
 }
 
 template <typename R, class Loader, bool SPLIT, bool ENERGY>

@@ -146,6 +146,8 @@ __device__ __forceinline__ void rotate(double4_32a &q, const double4_32a &L, dou
 // kind of motion.
 template <typename V4>
 __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
+	pdl_wait();  // launched after the previous step's last kernel: its forces and Bussi update
+	pdl_trigger();
 	__shared__ float3 s_a1[32], s_bk[32];
 	const int lane = threadIdx.x & 31;
 	const bool rot = threadIdx.x >= 32;
@@ -352,6 +354,8 @@ __device__ __forceinline__ void bussi_system_update(const StepArgs &a, int sy, l
 // update launch.
 template <typename V4>
 __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
+	pdl_wait();  // launched after the force kernels
+	pdl_trigger();
 	const long long s = step_of(a.th);
 	if(s % a.th.newtonian_steps != 0) return;
 	const int c = blockIdx.x;
@@ -481,6 +485,7 @@ __global__ void __launch_bounds__(256) k_system_sums(StepArgs a, double *out) {
 }
 
 __global__ void k_set_conditional(const int *flag, cudaGraphConditionalHandle h) {
+	pdl_wait();  // launched after the first step, which raises the flag
 	if(threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, *flag != 0 ? 1u : 0u);
 }
 
@@ -491,9 +496,8 @@ static inline int blocks_for(int N, int tpb) { return N > 0 ? (N + tpb - 1) / tp
 cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_t s) {
 	// two-warp blocks of 32 nucleotides: the FP64 work (1/64 of the FP32 rate) spreads evenly over
 	// the SMs
-	if(double_forces) k_first_step<double4_32a><<<blocks_for(a.N, 32), 64, 0, s>>>(a);
-	else k_first_step<float4><<<blocks_for(a.N, 32), 64, 0, s>>>(a);
-	return cudaGetLastError();
+	if(double_forces) return launch_after(k_first_step<double4_32a>, dim3(blocks_for(a.N, 32)), dim3(64), 0, s, a);
+	return launch_after(k_first_step<float4>, dim3(blocks_for(a.N, 32)), dim3(64), 0, s, a);
 }
 
 cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s) {
@@ -508,9 +512,8 @@ cudaError_t launch_bussi_prep(const StepArgs &a, int n_chunks, bool double_force
 }
 
 cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s) {
-	if(double_forces) k_bussi_sums<double4_32a><<<n_chunks, 256, 0, s>>>(a);
-	else k_bussi_sums<float4><<<n_chunks, 256, 0, s>>>(a);
-	return cudaGetLastError();
+	if(double_forces) return launch_after(k_bussi_sums<double4_32a>, dim3(n_chunks), dim3(256), 0, s, a);
+	return launch_after(k_bussi_sums<float4>, dim3(n_chunks), dim3(256), 0, s, a);
 }
 
 cudaError_t launch_step_advance(const StepArgs &a, int K, cudaStream_t s) {
@@ -526,8 +529,7 @@ cudaError_t launch_step_flush(const StepArgs &a, bool double_forces, cudaStream_
 }
 
 cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h, cudaStream_t s) {
-	k_set_conditional<<<1, 32, 0, s>>>(flag, h);
-	return cudaGetLastError();
+	return launch_after(k_set_conditional, dim3(1), dim3(32), 0, s, flag, h);
 }
 
 cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s) {

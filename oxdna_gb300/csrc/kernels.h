@@ -14,6 +14,29 @@
 
 namespace oxgb {
 
+// Programmatic dependent launch.  A kernel launched with launch_after may start while the
+// kernel before it on the stream is still running (once every block of that one has called
+// pdl_trigger or finished); it calls pdl_wait before it reads anything the earlier kernel
+// writes, and may do independent work first.  pdl_wait returns at once in a kernel launched
+// the ordinary way.  Both are hardware waits: they end when the earlier grid completes.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_after(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = block;
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = s;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Thermostat and step bookkeeping of the MD engine.  The step number of a kernel is
 // *step_base + step_offset: a graph of K steps bakes offsets 0..K-1 and advances the base by K
 // at its end, so no kernel of a step changes the number the others read.  Velocity Verlet
