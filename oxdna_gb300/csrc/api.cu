@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <climits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -383,6 +384,8 @@ struct oxgb_md {
 	cudaStream_t stream = nullptr, side = nullptr, noise = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_first = nullptr;
 	float4 *bussi_vf = nullptr, *bussi_Lf = nullptr;  // Bussi: half-kicked v, L in FP32 (mixed)
+	double *h_stage = nullptr, *d_stage = nullptr;   // the state in the caller's layout: pinned host, device
+	int *d_bad = nullptr;                             // lowest nucleotide with a bad quaternion
 	cudaGraphExec_t gexec = nullptr;
 	int graph_steps = 0;
 	bool conditional_ok = true;
@@ -417,6 +420,9 @@ struct oxgb_md {
 		if(ev_first) cudaEventDestroy(ev_first);
 		if(bussi_vf) cudaFree(bussi_vf);
 		if(bussi_Lf) cudaFree(bussi_Lf);
+		if(h_stage) cudaFreeHost(h_stage);
+		if(d_stage) cudaFree(d_stage);
+		if(d_bad) cudaFree(d_bad);
 	}
 };
 
@@ -726,11 +732,14 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16 * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned) * n_systems) == cudaSuccess;
+	ok &= cudaMallocHost(&h->h_stage, sizeof(double) * 13 * (size_t) N) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_stage, sizeof(double) * 13 * (size_t) N) == cudaSuccess;
+	ok &= cudaMalloc(&h->d_bad, sizeof(int)) == cudaSuccess;
 	ok &= cudaMalloc(&h->open_step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
-	ok &= cudaMalloc(&h->term_max, sizeof(int) * 3) == cudaSuccess;
+	ok &= cudaMalloc(&h->term_max, sizeof(int) * 4) == cudaSuccess;
 	if(!ok) return bail(fail(OXGB_E_NOMEM, "device allocation failed"));
-	ok &= cudaMemset(h->term_max, 0, sizeof(int) * 3) == cudaSuccess;
+	ok &= cudaMemset(h->term_max, 0, sizeof(int) * 4) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_sys, sys.data(), sizeof(int) * N, cudaMemcpyHostToDevice) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_sys_off, offsets, sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_chunk_sys, h->chunk_sys.data(), sizeof(int) * h->n_chunks, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -785,6 +794,19 @@ extern "C" int oxgb_md_set_topology(oxgb_md *h, const int *n3, const int *n5, co
 	h->h_btype.assign(btype, btype + N);
 	h->h_type.assign(type, type + N);
 	CK(cudaMemcpy(h->bonds, b.data(), sizeof(int2) * N, cudaMemcpyHostToDevice));
+	// the w words of the position mirrors (btype << 22 | index, and the base type) stay; the
+	// mirror updates rewrite only x, y, z
+	std::vector<float4> hi(N), lo(N);
+	for(int i = 0; i < N; i++) {
+		const int packed = (btype[i] << 22) | (i & 0x003FFFFF), t = type[i];
+		float w, tw;
+		std::memcpy(&w, &packed, 4);
+		std::memcpy(&tw, &t, 4);
+		hi[i] = make_float4(0.f, 0.f, 0.f, w);
+		lo[i] = make_float4(0.f, 0.f, 0.f, tw);
+	}
+	CK(cudaMemcpy(h->pos_hi, hi.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->pos_lo, lo.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
 	h->have_topology = true;
 	return OXGB_OK;
 }
@@ -874,21 +896,17 @@ static int size_and_build_list(oxgb_md *h) {
 	int rc = build_list_now(h);
 	if(rc) return rc;
 	if(h->md.max_neigh > 0) return read_status(h);
-	std::vector<int> cnt(h->N), ce(h->N), cb(h->N), cs(h->N);
-	CK(cudaMemcpyAsync(cnt.data(), h->lb.nnb, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
-	CK(cudaMemcpyAsync(ce.data(), h->tl.ev_n, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
-	CK(cudaMemcpyAsync(cb.data(), h->tl.base_n, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
-	CK(cudaMemcpyAsync(cs.data(), h->tl.stk_n, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
+	// the longest rows of any build so far (kept on the device by the list build: four integers
+	// to read rather than the counts of every nucleotide)
+	int tm[4];
+	CK(cudaMemcpyAsync(tm, h->term_max, sizeof(tm), cudaMemcpyDeviceToHost, h->stream));
 	CK(cudaStreamSynchronize(h->stream));
-	const int mx = *std::max_element(cnt.begin(), cnt.end());
+	const int mx = tm[3];
 	int want = ((std::max(64, mx + mx / 2 + 32) + 31) / 32) * 32;
-	auto cap_of = [](const std::vector<int> &v) {
-		const int m = *std::max_element(v.begin(), v.end());
-		return ((std::max(16, m + m / 2 + 8) + 7) / 8) * 8;
-	};
+	auto cap_of = [](int m) { return ((std::max(16, m + m / 2 + 8) + 7) / 8) * 8; };
 	// base / stack rows at most 64 long (the pair kernel keeps a row's owned entries in a 64-bit
 	// mask; physically a nucleotide has a handful)
-	const int we = cap_of(ce), wb = std::min(64, cap_of(cb)), ws = std::min(64, cap_of(cs));
+	const int we = cap_of(tm[0]), wb = std::min(64, cap_of(tm[1])), ws = std::min(64, cap_of(tm[2]));
 	if(we != h->tl.ev_cap || wb != h->tl.base_cap || ws != h->tl.stk_cap) {
 		if(h->gexec) {
 			cudaGraphExecDestroy(h->gexec);
@@ -923,34 +941,25 @@ static int size_and_build_list(oxgb_md *h) {
 extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *quat, const double *vel, const double *L) {
 	if(!h || !pos || !quat || !vel || !L) return fail(OXGB_E_INVALID, "null argument");
 	if(!h->have_topology) return fail(OXGB_E_INVALID, "set the topology first");
-	const int N = h->N;
-	std::vector<double4_32a> p(N), q(N), v(N), l(N);
-	std::vector<float4> hi(N), lo(N);
-	for(int i = 0; i < N; i++) {
-		p[i] = make_double4_32a(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
-		double n = std::sqrt(quat[4 * i] * quat[4 * i] + quat[4 * i + 1] * quat[4 * i + 1] + quat[4 * i + 2] * quat[4 * i + 2] +
-				quat[4 * i + 3] * quat[4 * i + 3]);
-		if(!(n > 0.5)) return fail(OXGB_E_INVALID, "quaternion of nucleotide " + std::to_string(i) + " is not normalisable");
-		q[i] = make_double4_32a(quat[4 * i] / n, quat[4 * i + 1] / n, quat[4 * i + 2] / n, quat[4 * i + 3] / n);
-		v[i] = make_double4_32a(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.0);
-		l[i] = make_double4_32a(L[3 * i], L[3 * i + 1], L[3 * i + 2], 0.0);
-		int packed = (h->h_btype[i] << 22) | (i & 0x003FFFFF);
-		float w;
-		std::memcpy(&w, &packed, 4);
-		hi[i] = make_float4(0.f, 0.f, 0.f, w);
-		int t = h->h_type[i];
-		float tw;
-		std::memcpy(&tw, &t, 4);
-		lo[i] = make_float4(0.f, 0.f, 0.f, tw);
-	}
-	CK(cudaMemcpyAsync(h->posd, p.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
-	CK(cudaMemcpyAsync(h->quatd, q.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
-	CK(cudaMemcpyAsync(h->veld, v.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
-	CK(cudaMemcpyAsync(h->Ld, l.data(), sizeof(double4_32a) * N, cudaMemcpyHostToDevice, h->stream));
-	if(clear_pending(h)) return fail(OXGB_E_CUDA, "upload");  // a new state: nothing pending
-	CK(cudaMemcpyAsync(h->pos_hi, hi.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
-	CK(cudaMemcpyAsync(h->pos_lo, lo.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
+	const size_t N = (size_t) h->N;
+	// the four arrays into pinned memory, one copy to the device, unpacked there
+	double *st = h->h_stage;
+	std::memcpy(st, pos, sizeof(double) * 3 * N);
+	std::memcpy(st + 3 * N, quat, sizeof(double) * 4 * N);
+	std::memcpy(st + 7 * N, vel, sizeof(double) * 3 * N);
+	std::memcpy(st + 10 * N, L, sizeof(double) * 3 * N);
+	const int none = INT_MAX;
+	CK(cudaMemcpyAsync(h->d_bad, &none, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+	CK(cudaMemcpyAsync(h->d_stage, st, sizeof(double) * 13 * N, cudaMemcpyHostToDevice, h->stream));
 	StepArgs sa = step_args(h);
+	// checked before anything is written, so that a rejected state leaves the current one
+	CK(launch_unpack_state(sa, h->d_stage, h->d_bad, true, h->stream));
+	int bad = INT_MAX;
+	CK(cudaMemcpyAsync(&bad, h->d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+	CK(cudaStreamSynchronize(h->stream));
+	if(bad != INT_MAX) return fail(OXGB_E_INVALID, "quaternion of nucleotide " + std::to_string(bad) + " is not normalisable");
+	CK(launch_unpack_state(sa, h->d_stage, h->d_bad, false, h->stream));
+	if(clear_pending(h)) return fail(OXGB_E_CUDA, "upload");  // a new state: nothing pending
 	CK(launch_make_mirrors(sa, h->stream));
 	int rc = size_and_build_list(h);
 	if(rc) return rc;
@@ -962,22 +971,17 @@ extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *qu
 
 extern "C" int oxgb_md_get_state(oxgb_md *h, double *pos, double *quat, double *vel, double *L) {
 	if(!h || !h->have_state) return fail(OXGB_E_INVALID, "no state");
-	const int N = h->N;
-	std::vector<double4_32a> buf(N);
-	struct {
-		double *dst;
-		double4_32a *src;
-		int width;
-	} items[4] = {{pos, h->posd, 3}, {quat, h->quatd, 4}, {vel, h->veld, 3}, {L, h->Ld, 3}};
-	for(auto &it : items) {
-		if(!it.dst) continue;
-		CK(cudaMemcpyAsync(buf.data(), it.src, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost, h->stream));
-		CK(cudaStreamSynchronize(h->stream));
-		for(int i = 0; i < N; i++) {
-			const double c[4] = {buf[i].x, buf[i].y, buf[i].z, buf[i].w};
-			for(int k = 0; k < it.width; k++) it.dst[it.width * i + k] = c[k];
-		}
-	}
+	const size_t N = (size_t) h->N;
+	// packed into the caller's layout on the device, one copy into pinned memory
+	StepArgs sa = step_args(h);
+	CK(launch_pack_state(sa, h->d_stage, h->stream));
+	CK(cudaMemcpyAsync(h->h_stage, h->d_stage, sizeof(double) * 13 * N, cudaMemcpyDeviceToHost, h->stream));
+	CK(cudaStreamSynchronize(h->stream));
+	const double *st = h->h_stage;
+	if(pos) std::memcpy(pos, st, sizeof(double) * 3 * N);
+	if(quat) std::memcpy(quat, st + 3 * N, sizeof(double) * 4 * N);
+	if(vel) std::memcpy(vel, st + 7 * N, sizeof(double) * 3 * N);
+	if(L) std::memcpy(L, st + 10 * N, sizeof(double) * 3 * N);
 	return OXGB_OK;
 }
 

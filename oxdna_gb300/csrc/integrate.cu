@@ -439,6 +439,44 @@ __global__ void k_step_flush_clear(StepArgs a) {
 	}
 }
 
+// The caller's state arrays (positions, quaternions, velocities, angular momenta: 3, 4, 3 and 3
+// doubles per nucleotide, the four arrays one after the other in `in`) into the FP64 state, each
+// quaternion normalised (sums and products rounded in a fixed order); the lowest nucleotide whose
+// quaternion cannot be normalised is kept in *bad.  With check_only nothing is written but *bad.
+__global__ void k_unpack_state(StepArgs a, const double *in, int *bad, int check_only) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= a.N) return;
+	const long long N = a.N;
+	const double *p = in + 3 * (long long) i, *q = in + 3 * N + 4 * (long long) i, *v = in + 7 * N + 3 * (long long) i,
+				 *l = in + 10 * N + 3 * (long long) i;
+	const double n2 = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(q[0], q[0]), __dmul_rn(q[1], q[1])), __dmul_rn(q[2], q[2])),
+			__dmul_rn(q[3], q[3]));
+	double n = sqrt(n2);
+	if(!(n > 0.5)) {
+		atomicMin(bad, i);
+		n = 1.0;
+	}
+	if(check_only) return;
+	a.pos[i] = make_double4_32a(p[0], p[1], p[2], 0.0);
+	a.quat[i] = make_double4_32a(__ddiv_rn(q[0], n), __ddiv_rn(q[1], n), __ddiv_rn(q[2], n), __ddiv_rn(q[3], n));
+	a.vel[i] = make_double4_32a(v[0], v[1], v[2], 0.0);
+	a.angmom[i] = make_double4_32a(l[0], l[1], l[2], 0.0);
+}
+
+// the FP64 state into the caller's layout (the reverse of k_unpack_state)
+__global__ void k_pack_state(StepArgs a, double *out) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= a.N) return;
+	const long long N = a.N;
+	double *p = out + 3 * (long long) i, *q = out + 3 * N + 4 * (long long) i, *v = out + 7 * N + 3 * (long long) i,
+		   *l = out + 10 * N + 3 * (long long) i;
+	const double4_32a r = a.pos[i], o = a.quat[i], u = a.vel[i], m = a.angmom[i];
+	p[0] = r.x, p[1] = r.y, p[2] = r.z;
+	q[0] = o.x, q[1] = o.y, q[2] = o.z, q[3] = o.w;
+	v[0] = u.x, v[1] = u.y, v[2] = u.z;
+	l[0] = m.x, l[1] = m.y, l[2] = m.z;
+}
+
 // velocities and angular momenta of nucleotides lo .. hi - 1 times f (a replica exchange)
 __global__ void k_scale_momenta(StepArgs a, int lo, int hi, double f) {
 	const int i = lo + blockIdx.x * blockDim.x + threadIdx.x;
@@ -534,6 +572,16 @@ cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h
 
 cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s) {
 	k_make_mirrors<<<blocks_for(a.N, 256), 256, 0, s>>>(a);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_state(const StepArgs &a, const double *in, int *bad, bool check_only, cudaStream_t s) {
+	k_unpack_state<<<blocks_for(a.N, 256), 256, 0, s>>>(a, in, bad, check_only ? 1 : 0);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_pack_state(const StepArgs &a, double *out, cudaStream_t s) {
+	k_pack_state<<<blocks_for(a.N, 256), 256, 0, s>>>(a, out);
 	return cudaGetLastError();
 }
 

@@ -107,7 +107,7 @@ struct ForceArgs {
 	// and slot pos[k N + i] of its partner j: (force, E), (torque, E_hb) as two V4 per slot
 	void *base_res, *stk_res;
 	const int *base_pos, *stk_pos;            // see ListArgs
-	const int *term_max;                      // [3] longest EV / base / stack list (slots past it are empty)
+	const int *term_max;                      // [4] longest EV / base / stack list (slots past it are empty), full row
 	// MD-step bookkeeping (engine layout): the bonded kernel marks the step's half kick pending
 	ThermoArgs th;
 	// external forces (oxgb_ext_force records grouped by nucleotide): ext_n nucleotides
@@ -164,7 +164,7 @@ struct ListArgs {
 	int ev_cap, base_cap, stk_cap;
 	float ev_r2, base_r2, stk_r2;
 	float4 *list_a1, *list_back;   // body axis a1 and backbone offset at this build
-	int *term_max;          // [3] longest EV / base / stack list of any build so far (may be null)
+	int *term_max;          // [4] longest EV / base / stack list and full row of any build so far (may be null)
 	int col_major;          // full rows column-major ([k * N + i]) instead of row-major
 	// batch of systems (sys null: one system with the scalar geometry above).  System s has
 	// its own box, cutoff and cell grid (sys_nside^3 cells from sys_cell0); only systems with
@@ -213,6 +213,11 @@ cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_for
 cudaError_t launch_step_advance(const StepArgs &a, int K, cudaStream_t s);
 // end of a run: completes the pending half kick and thermostat so the state is whole
 cudaError_t launch_step_flush(const StepArgs &a, bool double_forces, cudaStream_t s);
+// the caller's state arrays (3, 4, 3, 3 doubles per nucleotide, back to back) to and from the
+// FP64 state; *bad receives the lowest nucleotide whose quaternion cannot be normalised (with
+// check_only that is all that is written)
+cudaError_t launch_unpack_state(const StepArgs &a, const double *in, int *bad, bool check_only, cudaStream_t s);
+cudaError_t launch_pack_state(const StepArgs &a, double *out, cudaStream_t s);
 cudaError_t launch_set_conditional(const int *flag, cudaGraphConditionalHandle h, cudaStream_t s);
 // refresh the FP32 mirrors from the FP64 state (after a host upload)
 cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s);

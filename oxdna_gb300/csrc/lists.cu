@@ -298,6 +298,7 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	}
 	if(lane != 0) return;
 	if(cnt > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
+	if(a.term_max && cnt > a.term_max[3]) atomicMax(a.term_max + 3, cnt);
 	a.nnb[i] = cnt;
 	a.list_pos[i] = r;
 	if(terms) {

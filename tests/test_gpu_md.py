@@ -132,3 +132,27 @@ def test_lists_stay_complete_between_rebuilds(precision):
         assert np.abs(T1 - T2).max() <= tol * max(1.0, np.abs(T2).max())
     assert sysm.info()["rebuilds"] >= 2
     sysm.close()
+
+
+def test_state_round_trip_and_rejected_state():
+    """set_state then get_state returns the state (quaternions normalised); a state with a
+    quaternion that cannot be normalised is rejected and leaves the current one in place."""
+    from oxdna_gb300._abi import OxgbError
+    g = load_golden("mixed")
+    sysm, _ = system_from_golden(g, precision="mixed", dt=0.002)
+    st = sysm.get_state()
+    q = st["quat"] * 3.0  # scaled: normalised on upload
+    sysm.set_state(st["pos"], q, st["vel"], st["Lmom"])
+    back = sysm.get_state()
+    assert np.array_equal(back["pos"], st["pos"]) and np.array_equal(back["vel"], st["vel"])
+    assert np.array_equal(back["Lmom"], st["Lmom"])
+    assert np.abs(back["quat"] - st["quat"]).max() < 1e-15
+    bad = st["quat"].copy()
+    bad[5] = 0.0
+    with pytest.raises(OxgbError, match="nucleotide 5"):
+        sysm.set_state(st["pos"] + 1.0, bad, st["vel"], st["Lmom"])
+    after = sysm.get_state()
+    assert np.array_equal(after["pos"], back["pos"])
+    sysm.run(10)
+    assert np.all(np.isfinite(sysm.get_state()["pos"]))
+    sysm.close()
