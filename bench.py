@@ -52,6 +52,11 @@ WORKLOADS = {
 }
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of k_bonded_pairs + k_nonbonded_split per force
+# launch, from the ncu --set full capture summarised in profiles/ (cold caches)
+FORCE_TRAFFIC = {"plain40k": 7.303e6 + 7.2e3 + 26.265e6 + 2.6e3}
+
+
 def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -466,7 +471,9 @@ def main():
         "md_steps_per_s": value / (world * s.N),
         "list_rebuilds": rebuilds,
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value, "traffic": None,
+                     "frac": achieved / peak.value, "traffic": FORCE_TRAFFIC.get(args.workload),
+                     "traffic_note": "DRAM bytes (read + write) of one launch of the two force kernels, from an ncu "
+                                     "--set full capture with cold caches; the timed launches find their data in L2",
                      "kernel": "k_bonded_pairs + k_nonbonded_split (FP32 pair math)", "flops_per_launch": flops_launch, "sfu_per_launch": sfu_launch,
                      "launch_ms": t_force * 1e3, "pairs_listed": pairs_listed, "pairs_in_cutoff": pairs_in_range,
                      "peak_source": "measured FP32 FMA probe on this GPU"},
