@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 			x.x = fma(gx, hdt, x.x);
 			x.y = fma(gy, hdt, x.y);
 			x.z = fma(gz, hdt, x.z);
-			if(brownian) brownian_redraw_part(a.th, sy, i - a.th.sys_off[sy], sp, rot ? 1 : 0, x);
+			if(brownian) x = brownian_redraw_part(a.th, sy, i - a.th.sys_off[sy], sp, rot ? 1 : 0, x);
 			else if(bussi) bussi_rescale_part(a.th, sy, rot ? 1 : 0, x);
 		}
 		x.x = fma(gx, hdt, x.x);
@@ -189,7 +189,9 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 		}
 		else {
 			double4_32a q = a.quat[i];
-			rotate(q, x, a.dt);
+			// mixed precision: the small rotation as an FP64 sum of an FP32-pair correction (as
+			// accurate, far fewer FP64 operations); double precision, or a large step: FP64
+			if(!(sizeof(V4) == sizeof(float4) && rotate_small(q.x, q.y, q.z, q.w, x.x, x.y, x.z, 0.5 * a.dt))) rotate(q, x, a.dt);
 			a.angmom[i] = x;
 			a.quat[i] = q;
 			float3 a1, bk;

@@ -190,4 +190,64 @@ OXGB_HD void frame_mirror(const float qh[4], const float ql[4], float b1, float 
 	back[2] = lin2(b1, a1z, b2, a2z);
 }
 
+// ---------------------------------------------------------------- pairs as ~48-bit numbers
+
+// a + b of two pairs, renormalised (|e| <= ulp(s) / 2)
+OXGB_HD F2 add2(F2 a, F2 b) {
+	const F2 t = two_sum(a.s, b.s);
+	const float e = OXGB_FADD(t.e, OXGB_FADD(a.e, b.e));
+	const float s = OXGB_FADD(t.s, e);
+	return F2{s, OXGB_FSUB(e, OXGB_FSUB(s, t.s))};
+}
+
+// a b of two pairs, renormalised
+OXGB_HD F2 mul2(F2 a, F2 b) {
+	const F2 p = prod2(a.s, a.e, b.s, b.e);
+	const float s = OXGB_FADD(p.s, p.e);
+	return F2{s, OXGB_FSUB(p.e, OXGB_FSUB(s, p.s))};
+}
+
+OXGB_HD F2 neg2(F2 a) { return F2{-a.s, -a.e}; }
+
+OXGB_HD F2 split2(double x) {
+	F2 r;
+	split_rn(x, r.s, r.e);
+	return r;
+}
+
+// The rotation of the unit quaternion q = (x, y, z, w) by the angle dt |L| about the body-frame
+// angular momentum L (hd = dt / 2): q <- q (x) (sin(t/2) L^, cos(t/2)), t = dt |L|, written
+// as q + c with the small correction c = q (x) (delta, eps), delta = k L, eps = cos(t/2) - 1,
+// k = sin(t/2) / |L|, computed in FP32 pairs (~48 bits: |c| ~ hd |L|, so its absolute error is
+// below 1e-17, under an ulp of q's FP64 components); only the final additions are FP64.  The
+// norm error of q entering the step is removed with it (q (1 - d / 2), d = |q|^2 - 1), so q
+// stays unit to rounding.  Returns false, leaving q alone, outside the range where this holds
+// (x^2 = (hd |L|)^2 >= 1e-5, or |d| >= 1e-6): the caller then rotates in FP64.
+OXGB_HD bool rotate_small(double &qx, double &qy, double &qz, double &qw, double Lx, double Ly, double Lz, double hd) {
+	const double d = fma(qx, qx, fma(qy, qy, fma(qz, qz, fma(qw, qw, -1.0))));
+	if(!(fabs(d) < 1e-6)) return false;
+	const F2 lx = split2(Lx), ly = split2(Ly), lz = split2(Lz), h = split2(hd);
+	const F2 x2 = mul2(mul2(h, h), add2(add2(mul2(lx, lx), mul2(ly, ly)), mul2(lz, lz)));
+	if(!(x2.s < 1e-5f)) return false;
+	// sin(x) / x = 1 - x^2 / 6 + x^4 / 120 - ..., cos(x) - 1 = -x^2 / 2 + x^4 / 24 - ...; the
+	// omitted terms are below 1e-20 for x^2 < 1e-5, the x^4 terms need only FP32
+	const F2 sixth = split2(1.0 / 6.0);
+	const float x4 = OXGB_FMUL(x2.s, x2.s);
+	const F2 sinc = add2(F2{1.f, 0.f}, add2(neg2(mul2(x2, sixth)), F2{OXGB_FMUL(x4, 1.f / 120.f), 0.f}));
+	const F2 eps = add2(F2{-0.5f * x2.s, -0.5f * x2.e}, F2{OXGB_FMUL(x4, 1.f / 24.f), 0.f});
+	const F2 k = mul2(h, sinc);
+	const F2 dx = mul2(k, lx), dy = mul2(k, ly), dz = mul2(k, lz);
+	const F2 ax = split2(qx), ay = split2(qy), az = split2(qz), aw = split2(qw);
+	const F2 cw = add2(add2(mul2(aw, eps), neg2(mul2(ax, dx))), add2(neg2(mul2(ay, dy)), neg2(mul2(az, dz))));
+	const F2 cx = add2(add2(mul2(aw, dx), mul2(ax, eps)), add2(mul2(ay, dz), neg2(mul2(az, dy))));
+	const F2 cy = add2(add2(mul2(aw, dy), neg2(mul2(ax, dz))), add2(mul2(ay, eps), mul2(az, dx)));
+	const F2 cz = add2(add2(mul2(aw, dz), mul2(ax, dy)), add2(neg2(mul2(ay, dx)), mul2(az, eps)));
+	const double hs = -0.5 * d;
+	qx = (fma(qx, hs, qx) + widen(cx.s)) + widen(cx.e);
+	qy = (fma(qy, hs, qy) + widen(cy.s)) + widen(cy.e);
+	qz = (fma(qz, hs, qz) + widen(cz.s)) + widen(cz.e);
+	qw = (fma(qw, hs, qw) + widen(cw.s)) + widen(cw.e);
+	return true;
+}
+
 }  // namespace oxgb

@@ -151,9 +151,9 @@ static __device__ __noinline__ void brownian_redraw(const ThermoArgs &t, int sy,
 }
 
 // one kind of motion of brownian_redraw (which = 0: the velocity, 1: the angular momentum), with
-// the same draws
-static __device__ __noinline__ void brownian_redraw_part(const ThermoArgs &t, int sy, int i_local, long long s, int which,
-		double4_32a &x) {
+// the same draws; returns x, redrawn or not (by value: no stack frame for the caller)
+static __device__ __noinline__ double4_32a brownian_redraw_part(const ThermoArgs &t, int sy, int i_local, long long s,
+		int which, double4_32a x) {
 	const double *par = t.sys_par + sy * SP_STRIDE;
 	const unsigned long long seed = t.sys_seed[sy];
 	unsigned o0[4], o1[4];
@@ -174,6 +174,7 @@ static __device__ __noinline__ void brownian_redraw_part(const ThermoArgs &t, in
 		box_muller(o1[2], o1[3], g0, g1);
 		x = make_double4_32a(g3 * sT, g0 * sT, g1 * sT, 0.0);
 	}
+	return x;
 }
 
 // Bussi: from the sums of v, |v|^2 and |L|^2 over system sy, the new running kinetic energy

@@ -42,7 +42,7 @@ int main(int argc, char **argv) {
 		const double a = widen(f), b = (double) f;
 		if(f64_bits(a) != f64_bits(b) && !(std::isnan(a) && std::isnan(b))) wbad++;
 	}
-	for(float f : {0.f, -0.f, 1e-40f, -1e-45f, 1.f, -3.5e38f}) wbad += f64_bits(widen(f)) != f64_bits((double) f);
+	for(float f : {0.f, -0.f, 1e-40f, -1e-45f, 1.f, -3.4e38f}) wbad += f64_bits(widen(f)) != f64_bits((double) f);
 	std::normal_distribution<double> N(0, 1);
 	double worst = 0;
 	for(long t = 0; t < n / 10; t++) {
@@ -65,6 +65,44 @@ int main(int argc, char **argv) {
 				worst = std::fmax(worst, (double) std::fabs(d) * std::ldexp(1.0, 24));
 		}
 	}
-	std::printf("split: %ld fast, %ld mismatches; widen: %ld mismatches; frame: max error %.4f x 2^-24\n", fast, bad, wbad, worst);
-	return (bad || wbad || worst > 0.5001) ? 1 : 0;
+	// the small-rotation update against the rotation in extended precision, next to the FP64
+	// formula it replaces
+	double rot_err = 0, f64_err = 0;
+	long rot_used = 0;
+	const double hd = 0.0015;
+	for(long t = 0; t < n / 10; t++) {
+		double q[4], nn = 0;
+		for(int k = 0; k < 4; k++) q[k] = N(g), nn += q[k] * q[k];
+		nn = std::sqrt(nn);
+		for(int k = 0; k < 4; k++) q[k] /= nn;
+		const double sc = std::ldexp(1.0, (int) (g() % 6) - 2);  // |L| from about 0.25 to 8
+		const double L[3] = {N(g) * sc, N(g) * sc, N(g) * sc};
+		const long double L2 = (long double) L[0] * L[0] + (long double) L[1] * L[1] + (long double) L[2] * L[2];
+		const long double nrm = sqrtl(L2), x = hd * nrm;
+		const long double k = sinl(x) / nrm, ch = cosl(x);
+		const long double r[4] = {L[0] * k, L[1] * k, L[2] * k, ch};  // x, y, z, w
+		const long double X = q[0], Y = q[1], Z = q[2], Wq = q[3];
+		long double e[4] = {Wq * r[0] + X * r[3] + Y * r[2] - Z * r[1], Wq * r[1] - X * r[2] + Y * r[3] + Z * r[0],
+				Wq * r[2] + X * r[1] - Y * r[0] + Z * r[3], Wq * r[3] - X * r[0] - Y * r[1] - Z * r[2]};
+		const long double en = sqrtl(e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + e[3] * e[3]);
+		for(int c = 0; c < 4; c++) e[c] /= en;
+		double a[4] = {q[0], q[1], q[2], q[3]};
+		if(!rotate_small(a[0], a[1], a[2], a[3], L[0], L[1], L[2], hd)) continue;
+		rot_used++;
+		// the FP64 formula: series for sin(x)/x and cos(x), product, Newton renormalisation
+		const double L2d = L[0] * L[0] + L[1] * L[1] + L[2] * L[2], x2 = hd * hd * L2d;
+		const double kk = hd * (1.0 - x2 * (1.0 / 6.0) * (1.0 - x2 * (1.0 / 20.0)));
+		const double chd = 1.0 - x2 * 0.5 * (1.0 - x2 * (1.0 / 12.0) * (1.0 - x2 * (1.0 / 30.0)));
+		const double rx = L[0] * kk, ry = L[1] * kk, rz = L[2] * kk;
+		double b[4] = {q[3] * rx + q[0] * chd + q[1] * rz - q[2] * ry, q[3] * ry - q[0] * rz + q[1] * chd + q[2] * rx,
+				q[3] * rz + q[0] * ry - q[1] * rx + q[2] * chd, q[3] * chd - q[0] * rx - q[1] * ry - q[2] * rz};
+		const double dd = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3] - 1.0, inv = 1.0 - dd * (0.5 - 0.375 * dd);
+		for(int c = 0; c < 4; c++) {
+			rot_err = std::fmax(rot_err, (double) fabsl((long double) a[c] - e[c]));
+			f64_err = std::fmax(f64_err, (double) fabsl((long double) (b[c] * inv) - e[c]));
+		}
+	}
+	std::printf("split: %ld fast, %ld mismatches; widen: %ld mismatches; frame: max error %.4f x 2^-24; "
+			"rotation (%ld): max error %.3g (FP64 formula %.3g)\n", fast, bad, wbad, worst, rot_used, rot_err, f64_err);
+	return (bad || wbad || worst > 0.5001 || rot_used == 0 || rot_err > 2.0 * f64_err + 1e-16) ? 1 : 0;
 }

@@ -1,6 +1,8 @@
-"""The first step's integer-pipe FP64<->FP32 conversions and FP32 error-free frame (split.cuh),
-checked on the host: bit-identical to the C casts, and the frame within half an ulp of 1 of the
-exact frame (as accurate as the FP64 frame rounded once).  The device runs the same source with
+"""The first step's integer-pipe FP64<->FP32 conversions, FP32 error-free frame and small-rotation
+quaternion update (split.cuh), checked on the host: the conversions bit-identical to the C casts,
+the frame within half an ulp of 1 of the exact frame (as accurate as the FP64 frame rounded
+once), the rotation within the error of the FP64 formula it replaces (both against extended
+precision).  The device runs the same source with
 the _rn intrinsics, so the GPU tests of the mirrors and forces cover the device side."""
 import os
 import shutil
