@@ -18,6 +18,20 @@
 
 namespace oxgb {
 
+// Products and sums that must not be contracted into FMAs (the error terms depend on their
+// rounding): the _rn intrinsics on the device; host builds use -ffp-contract=off.
+#ifdef __CUDA_ARCH__
+#define OXGB_FMUL(a, b) __fmul_rn(a, b)
+#define OXGB_FADD(a, b) __fadd_rn(a, b)
+#define OXGB_FSUB(a, b) __fsub_rn(a, b)
+#define OXGB_FMAF(a, b, c) __fmaf_rn(a, b, c)
+#else
+#define OXGB_FMUL(a, b) ((a) * (b))
+#define OXGB_FADD(a, b) ((a) + (b))
+#define OXGB_FSUB(a, b) ((a) - (b))
+#define OXGB_FMAF(a, b, c) std::fma(a, b, c)
+#endif
+
 OXGB_HD unsigned long long f64_bits(double x) {
 #ifdef __CUDA_ARCH__
 	return (unsigned long long) __double_as_longlong(x);
@@ -58,6 +72,17 @@ OXGB_HD float f32_from_bits(unsigned u) {
 #endif
 }
 
+// (float) x rounded to nearest for |x| < 2^29 without a conversion instruction (which runs on
+// the slow FP64/conversion pipe): x = 128 q + m with q = x >> 7 (|q| < 2^22) and m = x & 127,
+// each made exactly from the bits of 1.5 * 2^23 + q (or 2^23 + m) less that constant, then one
+// FMA rounds 128 q + m once
+OXGB_HD float int_to_float(int x) {
+	const int q = x >> 7, m = x & 127;
+	const float fq = OXGB_FSUB(f32_from_bits(0x4B400000u + (unsigned) q), 12582912.f);
+	const float fm = OXGB_FSUB(f32_from_bits(0x4B000000u | (unsigned) m), 8388608.f);
+	return OXGB_FMAF(fq, 128.f, fm);
+}
+
 // hi = r rounded to the nearest float (ties to even), lo = the exact remainder r - hi rounded
 // to the nearest float; both are exact in the FP32 normal range: 2^-74 <= |r| < 2^127
 // (biased FP64 exponent 949 .. 1149).  Returns false outside it.
@@ -74,11 +99,11 @@ OXGB_HD bool split_rn_int(double r, float &hi, float &lo) {
 	// the exponent is the correctly rounded result)
 	const unsigned hbits = (unsigned) ((mag >> 29) + (up ? 1u : 0u) - (896ull << 23));
 	hi = f32_from_bits((sign << 31) | hbits);
-	// r - hi = (low - 2^29 [if rounded up]) units of 2^(e - 1075), with the sign of r; the
-	// integer-to-float conversion rounds to nearest and the power-of-two scale is exact
+	// r - hi = (low - 2^29 [if rounded up]) units of 2^(e - 1075), with the sign of r, rounded to
+	// the nearest float (int_to_float) and scaled by the exact power of two
 	const int li = (int) low - (up ? (1 << 29) : 0);
 	const float scale = f32_from_bits((unsigned) (e - 1075 + 127) << 23);
-	lo = (float) (sign ? -li : li) * scale;  // an exact remainder is +0, as r - hi gives
+	lo = int_to_float(sign ? -li : li) * scale;  // an exact remainder is +0, as r - hi gives
 	return true;
 }
 
@@ -114,19 +139,7 @@ OXGB_HD double widen(float f) {
 
 // ---------------------------------------------------------------- FP32 error-free arithmetic
 
-// Products and sums that must not be contracted into FMAs (the error terms depend on their
-// rounding): the _rn intrinsics on the device; host builds use -ffp-contract=off.
-#ifdef __CUDA_ARCH__
-#define OXGB_FMUL(a, b) __fmul_rn(a, b)
-#define OXGB_FADD(a, b) __fadd_rn(a, b)
-#define OXGB_FSUB(a, b) __fsub_rn(a, b)
-#define OXGB_FMAF(a, b, c) __fmaf_rn(a, b, c)
-#else
-#define OXGB_FMUL(a, b) ((a) * (b))
-#define OXGB_FADD(a, b) ((a) + (b))
-#define OXGB_FSUB(a, b) ((a) - (b))
-#define OXGB_FMAF(a, b, c) std::fma(a, b, c)
-#endif
+
 
 // a float pair s + e
 struct F2 {

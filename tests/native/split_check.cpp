@@ -36,6 +36,14 @@ int main(int argc, char **argv) {
 		check(mid), check(std::nextafter(mid, 0.0)), check(std::nextafter(mid, 1e300)), check((double) f), check(-mid);
 	}
 	for(double r : {1.0, -1.0, 0.5, 1.0 - 1e-17, 3.0e38, 1e-22, 5e-23, 0.0, -0.0}) check(r);
+	long ibad = 0;  // the conversion-free int -> float over its range
+	for(long t = 0; t < n; t++) {
+		const int x = (int) (g() % (2u << 29)) - (1 << 29) + 1;
+		ibad += f32_bits(int_to_float(x)) != f32_bits((float) x);
+	}
+	for(int x : {0, 1, -1, 127, -128, 1 << 24, (1 << 24) + 1, (1 << 24) + 3, -(1 << 24) - 1, (1 << 29), -(1 << 29) + 1, (1 << 29) - 1})
+		ibad += f32_bits(int_to_float(x)) != f32_bits((float) x);
+	bad += ibad;
 	long wbad = 0;
 	for(long i = 0; i < n; i++) {
 		const float f = f32_from_bits((unsigned) g());
