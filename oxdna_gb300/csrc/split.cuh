@@ -107,10 +107,30 @@ OXGB_HD bool split_rn_int(double r, float &hi, float &lo) {
 	return true;
 }
 
+// The out-of-range cases on the conversion instructions, in a function of its own: inlined, the
+// compiler would compute them on every call and select (they run on the slow FP64 pipe).
+#ifdef __CUDA_ARCH__
+#define OXGB_COLD __device__ __noinline__
+#else
+#define OXGB_COLD inline
+#endif
+
+struct HiLo {
+	float hi, lo;
+};
+
+OXGB_COLD HiLo split_rn_cold(double r) {
+	const float hi = (float) r;
+	return HiLo{hi, (float) (r - (double) hi)};
+}
+
+OXGB_COLD double widen_cold(float f) { return (double) f; }
+
 OXGB_HD void split_rn(double r, float &hi, float &lo) {
 	if(!split_rn_int(r, hi, lo)) {
-		hi = (float) r;
-		lo = (float) (r - (double) hi);
+		const HiLo c = split_rn_cold(r);
+		hi = c.hi;
+		lo = c.lo;
 	}
 }
 
@@ -130,7 +150,7 @@ OXGB_HD double widen(float f) {
 	const unsigned e = (u >> 23) & 0xffu;
 	if(e == 0u || e == 0xffu) {
 		if((u & 0x7fffffffu) == 0u) return f64_from_bits((unsigned long long) (u >> 31) << 63);
-		return (double) f;
+		return widen_cold(f);
 	}
 	const unsigned long long d = ((unsigned long long) (u >> 31) << 63) | ((unsigned long long) (e + 896u) << 52) |
 			((unsigned long long) (u & 0x7fffffu) << 29);
