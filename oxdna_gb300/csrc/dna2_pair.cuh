@@ -33,6 +33,7 @@ struct DNA2Table {
 	R mbf_fmax, mbf_finf, mbf_xmax, mbf_fene_xmax, mbf_long_xmax;
 	R fene_r0, rcut2;
 	R box_hi, box_lo;  // box side as an unevaluated sum hi + lo (exact FP64 value)
+	R inv_box;         // about 1 / box_hi: picks the periodic image (an integer; see LoadMixed::sep)
 	R pos_base_over_stack;
 	int dh_half_charged_ends, use_mbf, pad0, pad1;
 };

@@ -101,14 +101,18 @@ struct LoadMixed {
 		n.is_end = (b.x < 0 || b.y < 0);
 	}
 	// minimum image of q - p as hi + lo: the hi difference of nearby coordinates and its
-	// shift by a box side are exact (Sterbenz), the low parts and the box remainder go to lo
+	// shift by a box side are exact (Sterbenz), the low parts and the box remainder go to lo.
+	// The image m = round(d / box) of a listed pair (|q - p| < r_verlet, far below box / 2) has
+	// d / box at least 0.4 from a half-integer, so the product with an approximate inverse rounds
+	// to the same integer as the quotient; rounding by the 1.5 * 2^23 addition (|d / box| < 2^22)
+	// keeps it on the FMA pipe.
 	__device__ __forceinline__ Sep<float> sep(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql,
 			const DNA2Table<float> &P) const {
 		float d[3] = {qh.x - ph.x, qh.y - ph.y, qh.z - ph.z};
 		float l[3] = {ql.x - pl.x, ql.y - pl.y, ql.z - pl.z};
 #pragma unroll
 		for(int k = 0; k < 3; k++) {
-			const float m = rintf(d[k] / P.box_hi);
+			const float m = __fsub_rn(__fmaf_rn(d[k], P.inv_box, 12582912.f), 12582912.f);
 			d[k] = fmaf(-m, P.box_hi, d[k]);
 			l[k] = fmaf(-m, P.box_lo, l[k]);
 		}

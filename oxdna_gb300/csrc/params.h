@@ -158,6 +158,7 @@ inline int build_table(const oxgb_dna2_settings &s, double box, DNA2Table<double
 	P.rcut2 = rcut * rcut;
 	P.box_hi = box;
 	P.box_lo = 0.0;
+	P.inv_box = 1.0 / box;
 	P.pos_base_over_stack = (double) OXM_POS_BASE / (double) OXM_POS_STACK;
 	return 0;
 }
@@ -173,6 +174,7 @@ inline void to_float(const DNA2Table<double> &d, double box, DNA2Table<float> &f
 	f.use_mbf = d.use_mbf;
 	f.box_hi = (float) box;
 	f.box_lo = (float) (box - (double) f.box_hi);
+	f.inv_box = (float) (1.0 / (double) f.box_hi);
 }
 
 // pair-distance bounds of the force kernel's term lists: a term can only act within these
