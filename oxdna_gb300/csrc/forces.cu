@@ -732,7 +732,7 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 // warp holds 32 / K nucleotides and all its lanes run the same term loop
 // minimum resident blocks per SM asked of the register allocator for the non-bonded kernel
 #ifndef OXGB_NB_MINB
-#define OXGB_NB_MINB 6
+#define OXGB_NB_MINB 8
 #endif
 
 template <typename R, class Loader, bool SPLIT, bool ENERGY, int K>
@@ -837,7 +837,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 
 // lanes per nucleotide in the non-bonded kernel
 #ifndef OXGB_NB_LANES
-#define OXGB_NB_LANES 8
+#define OXGB_NB_LANES 4
 #endif
 
 int nonbonded_blocks(int N) {
