@@ -702,8 +702,13 @@ __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld,
 // The bonded and the base/stack pair work are independent (both read the mirrors, each writes
 // its own result buffers), so they share one launch: blocks 0 .. 2 pair_blocks - 1 are pair
 // blocks (the costliest, dispatched first), the rest bonded blocks, which fill the tail.
+// minimum resident blocks per SM asked of the register allocator for the bonded/pair kernel
+#ifndef OXGB_PAIR_MINB
+#define OXGB_PAIR_MINB 5
+#endif
+
 template <typename R, class Loader, bool SPLIT, bool ENERGY>
-__global__ void __launch_bounds__(128) k_bonded_pairs(ForceArgs a, Loader ld, int pair_blocks) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_PAIR_MINB : 1) k_bonded_pairs(ForceArgs a, Loader ld, int pair_blocks) {
 	pdl_trigger();  // the non-bonded kernel may start (it waits before reading these results)
 	const int b = blockIdx.x;
 	if(b < 2 * pair_blocks) pair_block<R, Loader, SPLIT, ENERGY>(a, ld, b, pair_blocks);
