@@ -374,7 +374,9 @@ struct oxgb_md {
 	long long *step = nullptr;
 	double *esplit = nullptr, *sums = nullptr, *bussi_partials = nullptr, *bussi_state = nullptr;
 	long long *bussi_stamp = nullptr, *open_step = nullptr;
-	unsigned *bussi_done = nullptr;
+	unsigned *bussi_done = nullptr, *bussi_prep_done = nullptr;
+	double *bussi_tot = nullptr;
+	float2 *bussi_fpart = nullptr;
 	int *term_max = nullptr;
 	void *ext_rec = nullptr;              // external forces grouped by nucleotide
 	int *ext_nuc = nullptr, *ext_off = nullptr;
@@ -408,7 +410,7 @@ struct oxgb_md {
 					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
-					(void *) bussi_stamp, (void *) open_step, (void *) bussi_done, (void *) term_max, ext_rec, (void *) ext_nuc, (void *) ext_off, (void *) d_rebuilds})
+					(void *) bussi_stamp, (void *) open_step, (void *) bussi_done, (void *) bussi_prep_done, (void *) bussi_tot, (void *) bussi_fpart, (void *) term_max, ext_rec, (void *) ext_nuc, (void *) ext_off, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -446,6 +448,9 @@ static ThermoArgs thermo_args(oxgb_md *h, int step_offset = 0, bool engine_step 
 	t.bussi_state = h->bussi_state;
 	t.bussi_stamp = h->bussi_stamp;
 	t.bussi_done = h->bussi_done;
+	t.bussi_prep_done = h->bussi_prep_done;
+	t.bussi_tot = h->bussi_tot;
+	t.bussi_fpart = h->bussi_fpart;
 	t.bussi_vf = h->bussi_vf;
 	t.bussi_Lf = h->bussi_Lf;
 	t.open_step = engine_step ? h->open_step : nullptr;
@@ -732,6 +737,9 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->bussi_state, sizeof(double) * 16 * n_systems) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_stamp, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->bussi_done, sizeof(unsigned) * n_systems) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_prep_done, sizeof(unsigned) * n_systems) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_tot, sizeof(double) * 8 * n_systems) == cudaSuccess;
+	ok &= cudaMalloc(&h->bussi_fpart, sizeof(float2) * 8 * h->n_chunks) == cudaSuccess;
 	ok &= cudaMallocHost(&h->h_stage, sizeof(double) * 13 * (size_t) N) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_stage, sizeof(double) * 13 * (size_t) N) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_bad, sizeof(int)) == cudaSuccess;
@@ -748,6 +756,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMemcpy(h->d_sys_seed, seeds.data(), sizeof(unsigned long long) * n_systems, cudaMemcpyHostToDevice) == cudaSuccess;
 	ok &= cudaMemset(h->d_sys_stale, 0, sizeof(int) * n_systems) == cudaSuccess;
 	ok &= cudaMemset(h->bussi_done, 0, sizeof(unsigned) * n_systems) == cudaSuccess;
+	ok &= cudaMemset(h->bussi_prep_done, 0, sizeof(unsigned) * n_systems) == cudaSuccess;
 	ok &= cudaMemset(h->status, 0, sizeof(int)) == cudaSuccess;
 	ok &= cudaMemset(h->flag, 0, sizeof(int)) == cudaSuccess;
 	ok &= cudaMemset(h->step, 0, sizeof(long long)) == cudaSuccess;

@@ -286,17 +286,28 @@ __device__ __forceinline__ void block_sum8(const double (&x)[8], double *red) {
 	}
 }
 
-__device__ __forceinline__ void block_sum8(const CompF (&x)[8], double *red) {
+__device__ __forceinline__ CompF block_sum8_comp(const CompF (&x)[8]) {
 	__shared__ CompF part[8][8];
 	const CompF t = warp_transpose_sum8(x, comp_add);
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 	if((lane & 3) == 0) part[lane >> 2][w] = t;
 	__syncthreads();
-	if(threadIdx.x < 8) {
-		CompF r{0.f, 0.f};
-		for(int u = 0; u < 8; u++) r = comp_add(r, part[threadIdx.x][u]);
-		red[threadIdx.x] = (double) r.s + (double) r.e;
-	}
+	CompF r{0.f, 0.f};
+	if(threadIdx.x < 8)
+		for(int u = 0; u < nw; u++) r = comp_add(r, part[threadIdx.x][u]);
+	return r;
+}
+
+// the block's compensated sums of 8 values as float pairs (written by threads 0..7)
+__device__ __forceinline__ void block_sum8f(const CompF (&x)[8], float2 *out) {
+	const CompF r = block_sum8_comp(x);
+	if(threadIdx.x < 8) out[threadIdx.x] = make_float2(r.s, r.e);
+}
+
+// the same into doubles (threads 0..7)
+__device__ __forceinline__ void block_sum8(const CompF (&x)[8], double *red) {
+	const CompF r = block_sum8_comp(x);
+	if(threadIdx.x < 8) red[threadIdx.x] = widen(r.s) + widen(r.e);
 }
 
 // Bussi step s, after the first step: per chunk, the FP64 sums of the half-kicked v, |v|^2 and
@@ -322,31 +333,56 @@ __global__ void __launch_bounds__(256) k_bussi_prep(StepArgs a) {
 		}
 	}
 	block_sum8(x, a.th.bussi_partials + 16 * c);
-}
-
-// the update of system sy from its chunk sums, reduced by the block in a fixed chunk order (the
-// result does not depend on which block runs it): translation on thread 0 and rotation on
-// thread 32 (two warps: the chains overlap)
-__device__ __forceinline__ void bussi_system_update(const StepArgs &a, int sy, long long s) {
-	__shared__ double tot[16];
+	// the block that brings a system's last chunk sums them (fixed order) into the system's
+	// totals, still on the side branch
+	__shared__ int last;
+	if(threadIdx.x < 8) __threadfence();
+	__syncthreads();
+	if(threadIdx.x == 0) {
+		const unsigned nc = (unsigned) (a.th.sys_chunk0[sy + 1] - a.th.sys_chunk0[sy]);
+		last = atomicAdd(a.th.bussi_prep_done + sy, 1u) == nc - 1u;
+		if(last) a.th.bussi_prep_done[sy] = 0u;
+	}
+	__syncthreads();
+	if(!last) return;
+	__threadfence();
 	const int c0 = a.th.sys_chunk0[sy], nc = a.th.sys_chunk0[sy + 1] - c0;
-	double x[8] = {0, 0, 0, 0, 0, 0, 0, 0}, y[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	double y[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 	for(int b = threadIdx.x; b < nc; b += blockDim.x) {
 		const double *p = a.th.bussi_partials + 16 * (c0 + b);
 #pragma unroll
-		for(int k = 0; k < 5; k++) x[k] += __ldcg(p + k);
-#pragma unroll
-		for(int k = 0; k < 7; k++) y[k] += __ldcg(p + 8 + k);
+		for(int k = 0; k < 5; k++) y[k] += __ldcg(p + k);
 	}
 	__syncthreads();  // the block's scratch is reused
-	block_sum8(x, tot);
-	__syncthreads();
-	block_sum8(y, tot + 8);
+	block_sum8(y, a.th.bussi_tot + 8 * sy);
+}
+
+// the update of system sy: the totals of the half-kicked state (k_bussi_prep) and the force
+// terms of its chunks, reduced by the block in a fixed chunk order as compensated float pairs
+// (the result does not depend on which block runs it); translation on thread 0 and rotation on
+// thread 32 (two warps: the chains overlap)
+__device__ __forceinline__ void bussi_system_update(const StepArgs &a, int sy, long long s) {
+	__shared__ double tot[8];
+	const int c0 = a.th.sys_chunk0[sy], nc = a.th.sys_chunk0[sy + 1] - c0;
+	CompF y[8];
+#pragma unroll
+	for(int k = 0; k < 8; k++) y[k] = CompF{0.f, 0.f};
+	for(int b = threadIdx.x; b < nc; b += blockDim.x) {
+		const float2 *p = a.th.bussi_fpart + 8 * (c0 + b);
+#pragma unroll
+		for(int k = 0; k < 7; k++) {
+			const float2 v = __ldcg(p + k);
+			y[k] = comp_add(y[k], CompF{v.x, v.y});
+		}
+	}
+	__syncthreads();  // the block's scratch is reused
+	block_sum8(y, tot);
 	__syncthreads();
 	if(threadIdx.x != 0 && threadIdx.x != 32) return;
+	const double *x = a.th.bussi_tot + 8 * sy;
 	const double h = 0.5 * a.dt;
-	const double sum[5] = {tot[0] + h * tot[8], tot[1] + h * tot[9], tot[2] + h * tot[10],
-			tot[3] + 2.0 * h * tot[11] + h * h * tot[12], tot[4] + 2.0 * h * tot[13] + h * h * tot[14]};
+	const double sum[5] = {__ldcg(x) + h * tot[0], __ldcg(x + 1) + h * tot[1], __ldcg(x + 2) + h * tot[2],
+			__ldcg(x + 3) + 2.0 * h * tot[3] + h * h * tot[4], __ldcg(x + 4) + 2.0 * h * tot[5] + h * h * tot[6]};
 	bussi_update(a.th, sy, s, threadIdx.x == 0 ? 0 : 1, sum);
 }
 
@@ -379,7 +415,7 @@ __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 			x[5].s = L.x * T.x + L.y * T.y + L.z * T.z;
 			x[6].s = T.x * T.x + T.y * T.y + T.z * T.z;
 		}
-		block_sum8(x, a.th.bussi_partials + 16 * c + 8);
+		block_sum8f(x, a.th.bussi_fpart + 8 * c);
 	}
 	else {
 		double x[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -395,7 +431,15 @@ __global__ void __launch_bounds__(256) k_bussi_sums(StepArgs a) {
 			x[5] = L.x * T.x + L.y * T.y + L.z * T.z;
 			x[6] = T.x * T.x + T.y * T.y + T.z * T.z;
 		}
-		block_sum8(x, a.th.bussi_partials + 16 * c + 8);
+		// FP64 sums, kept as float pairs like the mixed-precision ones (hi + lo carries 48 bits)
+		__shared__ double red[8];
+		block_sum8(x, red);
+		__syncthreads();
+		if(threadIdx.x < 8) {
+			float hi, lo;
+			split_rn(red[threadIdx.x], hi, lo);
+			a.th.bussi_fpart[8 * c + threadIdx.x] = make_float2(hi, lo);
+		}
 	}
 	__shared__ int last;
 	if(threadIdx.x < 8) __threadfence();  // the partials are visible device-wide before this block arrives

@@ -66,14 +66,17 @@ struct ThermoArgs {
 	// Bussi: the kinetic sums run over chunks of up to 256 nucleotides of one system
 	const int *chunk_sys, *chunk_first;    // [chunks]
 	const int *sys_chunk0;                 // [n_systems + 1] first chunk of each system
-	double *bussi_partials;                // [chunks * 16] per-chunk sums: 0-4 of the half-kicked
-	                                       // state (v, |v|^2, |L|^2), 8-14 of the force terms
-	                                       // (F, v.F, |F|^2, L.T, |T|^2)
+	double *bussi_partials;                // [chunks * 16] per-chunk sums 0-4 of the half-kicked
+	                                       // state (v, |v|^2, |L|^2); the force terms (F, v.F,
+	                                       // |F|^2, L.T, |T|^2) go to bussi_fpart
 	float4 *bussi_vf, *bussi_Lf;           // [N] half-kicked v and L rounded to FP32 (mixed precision)
 	double *bussi_state;                   // [n_systems * 16]: K_t, K_r, factor_t, factor_r,
 	                                       // vcom x y z, -, then the step's draws: sum_t, rr_t,
 	                                       // sum_r, rr_r
 	unsigned *bussi_done;                  // [n_systems] chunks arrived in this step's sums (0 between steps)
+	unsigned *bussi_prep_done;             // the same for the sums of the half-kicked state
+	double *bussi_tot;                     // [n_systems * 8] system totals of the half-kicked state
+	float2 *bussi_fpart;                   // [chunks * 8] per-chunk force-term sums as float pairs
 	long long *bussi_stamp;                // step of the last Bussi update (OXGB_NO_STEP: none)
 	long long *open_step;                  // step whose second half kick is pending
 	                                       // (OXGB_NO_STEP: none); null in force-only calls
