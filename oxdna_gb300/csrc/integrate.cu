@@ -55,13 +55,13 @@ __device__ __forceinline__ void mirror_frame(const StepArgs &a, int i, const dou
 }
 
 // true if the centre or any interaction site moved more than the skin since the last list build
-// (r: the new centre in FP32, a1 and back: the new axis and backbone offset)
-__device__ __forceinline__ bool list_stale(const StepArgs &a, int i, float3 r, float3 a1, float3 bk) {
-	const float4 lp = a.list_pos[i];
+// (lp, la1, lbk: centre, a1 and backbone offset at the last build; r: the new centre in FP32,
+// a1 and back: the new axis and backbone offset)
+__device__ __forceinline__ bool list_stale(const StepArgs &a, const float4 &lp, const float4 &la1, const float4 &lbk, float3 r,
+		float3 a1, float3 bk) {
 	const float dx = r.x - lp.x, dy = r.y - lp.y, dz = r.z - lp.z;
 	if(dx * dx + dy * dy + dz * dz > a.skin2) return true;
 	if(!a.list_a1) return false;
-	const float4 la1 = a.list_a1[i], lbk = a.list_back[i];
 	const float ex = a1.x - la1.x, ey = a1.y - la1.y, ez = a1.z - la1.z;
 	float sx = dx + 0.4f * ex, sy = dy + 0.4f * ey, sz = dz + 0.4f * ez;  // base site
 	if(sx * sx + sy * sy + sz * sz > a.skin2) return true;
@@ -146,8 +146,6 @@ __device__ __forceinline__ void rotate(double4_32a &q, const double4_32a &L, dou
 // kind of motion.
 template <typename V4>
 __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
-	pdl_wait();  // launched after the previous step's last kernel: its forces and Bussi update
-	pdl_trigger();
 	__shared__ float3 s_a1[32], s_bk[32];
 	const int lane = threadIdx.x & 31;
 	const bool rot = threadIdx.x >= 32;
@@ -155,9 +153,31 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 	const bool live = i < a.N;
 	float3 r32 = make_float3(0.f, 0.f, 0.f);
 	int sy = 0;
+	double4_32a x, y;  // (v, r) on the translation warp, (L, q) on the rotation warp
+	float4 lp, la1, lbk;
+	auto load_state = [&]() {
+		if(live) {
+			sy = a.th.sys[i];
+			x = rot ? a.angmom[i] : a.vel[i];
+			y = rot ? a.quat[i] : a.pos[i];
+			if(!rot) {
+				lp = a.list_pos[i];
+				if(a.list_a1) la1 = a.list_a1[i], lbk = a.list_back[i];
+			}
+		}
+	};
+	// Inside a graph of steps (offset > 0) the kernel before this one is the previous step's
+	// last, launched after the FP64 state and the list build's positions were written: they are
+	// read before waiting for it, and only its outputs (the forces, the Bussi update) after.
+	// Otherwise (the first step of a graph or a single step, which may follow any kernel that
+	// writes the state) everything is read after the wait.
+	const bool early = a.th.step_offset > 0;
+	if(early) load_state();
+	pdl_wait();
+	pdl_trigger();
+	if(!early) load_state();
 	if(live) {
 		const long long s = step_of(a.th);
-		sy = a.th.sys[i];
 		const double hdt = 0.5 * a.dt;
 		// the previous step's second half kick and thermostat (kept as a separate half kick, so
 		// that a state is the same whether or not a run ended at that step)
@@ -166,7 +186,6 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 		const bool brownian = complete && a.th.thermostat == 1 && sp % a.th.newtonian_steps == 0;
 		const bool bussi = complete && a.th.thermostat == 2 && *a.th.bussi_stamp == sp;
 		const V4 G = reinterpret_cast<const V4 *>(rot ? a.torques : a.forces)[i];
-		double4_32a x = rot ? a.angmom[i] : a.vel[i];
 		const double gx = widen(G.x), gy = widen(G.y), gz = widen(G.z);
 		if(complete) {
 			x.x = fma(gx, hdt, x.x);
@@ -179,7 +198,7 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 		x.y = fma(gy, hdt, x.y);
 		x.z = fma(gz, hdt, x.z);
 		if(!rot) {
-			double4_32a r = a.pos[i];
+			double4_32a r = y;
 			r.x += x.x * a.dt;
 			r.y += x.y * a.dt;
 			r.z += x.z * a.dt;
@@ -188,7 +207,7 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 			r32 = mirror_position(a, i, r);
 		}
 		else {
-			double4_32a q = a.quat[i];
+			double4_32a q = y;
 			// mixed precision: the small rotation as an FP64 sum of an FP32-pair correction (as
 			// accurate, far fewer FP64 operations); double precision, or a large step: FP64
 			if(!(sizeof(V4) == sizeof(float4) && rotate_small(q.x, q.y, q.z, q.w, x.x, x.y, x.z, 0.5 * a.dt))) rotate(q, x, a.dt);
@@ -203,7 +222,7 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 	__syncthreads();
 	// Verlet list staleness (CUDA_mixed.cuh:68, extended to the interaction sites for the term
 	// lists), per system, on the translation warp with the rotation warp's a1 and backbone offset
-	if(live && !rot && list_stale(a, i, r32, s_a1[lane], s_bk[lane])) {
+	if(live && !rot && list_stale(a, lp, la1, lbk, r32, s_a1[lane], s_bk[lane])) {
 		a.sys_stale[sy] = 1;
 		atomicOr(a.flag, 1);
 	}
