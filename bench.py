@@ -289,6 +289,99 @@ def run_reference_arm(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def precision_study(args):
+    """The precision study on the 40,000-nucleotide system: force, torque and per-term energy
+    errors of the mixed-precision kernels against the same kernels in FP64 over `snapshots`
+    snapshots taken every `every` steps of the Bussi run (and against the FP64 CPU oracle on a
+    few of them), and the NVE energy drift of mixed and double precision, per 10^6 steps."""
+    import torch
+    torch.cuda.set_device(0)
+    import oxdna_gb300 as ox
+    from oxdna_gb300 import io as oxio
+    wl = WORKLOADS["plain40k"]
+    s = make_system(wl, args.seed)
+    a1, a2, a3 = s.frames()
+    quat = oxio.frame_to_quat(a1, a2, a3)
+    dna = ox.dna2_settings(s.T, 0.5)
+
+    def engine(precision, thermostat):
+        m = ox.MDSystem(s.box, s.top, dna, ox.md_settings(dt=wl["dt"], thermostat=thermostat, newtonian_steps=1,
+                                                            bussi_tau=wl["bussi_tau"], seed=args.seed, precision=precision,
+                                                            steps_per_graph=25))
+        m.set_state(s.pos, quat, s.vel, s.L)
+        return m
+
+    run = engine("mixed", "bussi")
+    ref = engine("double", "no")
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+    p_or = oracle.make_params(oracle.make_settings(s.T, 0.5))
+    f_max = t_max = 0.0
+    f_num = f_den = t_num = t_den = 0.0
+    f_rel, t_rel = [], []
+    e_err = np.zeros(8)
+    o_max = o_norm = 0.0
+    for k in range(args.snapshots):
+        run.run(args.every)
+        st = run.get_state()
+        F, T, E, Es = run.compute_forces()
+        ref.set_state(st["pos"], st["quat"], st["vel"], st["Lmom"])
+        Fr, Tr, Er, Esr = ref.compute_forces()
+        n = np.linalg.norm(Fr, axis=1)
+        fl = 0.1 * np.sqrt(np.mean(n ** 2))
+        f_rel.append(np.linalg.norm(F - Fr, axis=1) / np.maximum(n, fl))
+        f_max = max(f_max, float(np.max(f_rel[-1])))
+        nt = np.linalg.norm(Tr, axis=1)
+        tl = 0.1 * np.sqrt(np.mean(nt ** 2))
+        t_rel.append(np.linalg.norm(T - Tr, axis=1) / np.maximum(nt, tl))
+        t_max = max(t_max, float(np.max(t_rel[-1])))
+        f_num += float(np.sum((F - Fr) ** 2)); f_den += float(np.sum(Fr ** 2))
+        t_num += float(np.sum((T - Tr) ** 2)); t_den += float(np.sum(Tr ** 2))
+        e_err = np.maximum(e_err, np.abs(Es - Esr) / abs(float(np.sum(Esr))))
+        if k % max(1, args.snapshots // 5) == 0:
+            f1, f2, f3 = oxio.quat_to_frame(st["quat"])
+            rc, Fo, To, Eso, Epo = oracle.forces(p_or, st["pos"], f1, f2, f3, s.top.n3, s.top.n5, s.top.type, s.top.btype,
+                                                 s.box, nthreads=cpu_cores())
+            no = np.linalg.norm(Fo, axis=1)
+            o_max = max(o_max, float(np.max(np.linalg.norm(F - Fo, axis=1) / np.maximum(no, 0.1 * np.sqrt(np.mean(no ** 2))))))
+            o_norm = max(o_norm, float(np.linalg.norm(F - Fo) / np.linalg.norm(Fo)))
+    run.close()
+    ref.close()
+    pct = [50, 99, 99.9, 99.99]
+    f_pct = np.percentile(np.concatenate(f_rel), pct).tolist()
+    t_pct = np.percentile(np.concatenate(t_rel), pct).tolist()
+
+    drift = {}
+    for precision in ("mixed", "double"):
+        m = engine(precision, "no")
+        ts, es = [], []
+        nsteps = args.nve_steps if precision == "mixed" else args.nve_steps_double
+        for k in range(args.nve_samples + 1):
+            if k:
+                m.run(nsteps // args.nve_samples)
+            U, Kt, Kr = m.energies()
+            ts.append(k * (nsteps // args.nve_samples))
+            es.append((U + Kt + Kr) / s.N)
+        m.close()
+        slope = float(np.polyfit(np.array(ts, float), np.array(es), 1)[0])
+        drift[precision] = {"per_1e6_steps": slope * 1e6, "unit": "total energy per nucleotide (simulation units)",
+                            "relative_per_1e6_steps": slope * 1e6 / abs(es[0]), "steps": ts[-1], "e0": es[0],
+                            "e_end": es[-1]}
+    line = {"study": "precision", "workload": "plain40k", "n_nucleotides": s.N, "snapshots": args.snapshots,
+            "every": args.every,
+            "mixed_vs_fp64_kernels": {"force_normwise": (f_num / f_den) ** 0.5, "force_max_per_particle": f_max,
+                                      "torque_normwise": (t_num / t_den) ** 0.5, "torque_max_per_particle": t_max,
+                                      "per_particle_percentiles": pct, "force_per_particle_at": f_pct,
+                                      "torque_per_particle_at": t_pct,
+                                      "energy_term_max_rel": e_err.tolist(),
+                                      "energy_terms": ["FENE", "BEXC", "STCK", "NEXC", "HB", "CRST", "CXST", "DH"]},
+            "mixed_vs_cpu_oracle": {"force_normwise_max": o_norm, "force_max_per_particle": o_max,
+                                    "snapshots": len(range(0, args.snapshots, max(1, args.snapshots // 5)))},
+            "per_particle_floor": "0.1 x RMS of the FP64 values",
+            "nve_drift": drift}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,7 +398,17 @@ def main():
     ap.add_argument("--list-node", default="conditional", choices=["conditional", "kernel"],
                     help="list rebuild as a conditional graph node, or as always-launched kernels that "
                          "return at once on a fresh list (what a kernel-level profiler can see)")
+    ap.add_argument("--precision-study", action="store_true",
+                    help="instead of the throughput line: force/torque/energy errors over snapshots and NVE drift")
+    ap.add_argument("--snapshots", type=int, default=100)
+    ap.add_argument("--every", type=int, default=1000)
+    ap.add_argument("--nve-steps", type=int, default=100000)
+    ap.add_argument("--nve-steps-double", type=int, default=20000)
+    ap.add_argument("--nve-samples", type=int, default=20)
     args = ap.parse_args()
+    if args.precision_study:
+        precision_study(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]

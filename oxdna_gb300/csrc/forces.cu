@@ -15,6 +15,7 @@
 //    int2 bonds and a neighbour matrix of any stride, accumulating into forces and torques
 //    initialised by the caller, exactly the contract of CUDABaseInteraction::compute_forces.
 #include "kernels.h"
+#include "split.cuh"
 
 #include <cuda_runtime.h>
 
@@ -100,23 +101,42 @@ struct LoadMixed {
 		n.type = __float_as_int(lo.w) & 7;
 		n.is_end = (b.x < 0 || b.y < 0);
 	}
-	// minimum image of q - p as hi + lo: the hi difference of nearby coordinates and its
-	// shift by a box side are exact (Sterbenz), the low parts and the box remainder go to lo.
-	// The image m = round(d / box) of a listed pair (|q - p| < r_verlet, far below box / 2) has
-	// d / box at least 0.4 from a half-integer, so the product with an approximate inverse rounds
-	// to the same integer as the quotient; rounding by the 1.5 * 2^23 addition (|d / box| < 2^22)
-	// keeps it on the FMA pipe.
+	// minimum image of q - p as hi + lo.  The image m = round(d / box) of a listed pair
+	// (|q - p| < r_verlet, far below box / 2) has d / box at least 0.4 from a half-integer, so
+	// the product with an approximate inverse rounds to the same integer as the quotient;
+	// rounding by the 1.5 * 2^23 addition (|d / box| < 2^22) keeps it on the FMA pipe.
+	// In one image (m = 0) the hi difference of two nearby coordinates is within half an ulp
+	// of |d| < r_verlet.  Across images (unwrapped coordinates a box side or more apart) it
+	// rounds at the ulp of the box side, 7.6e-6 for a box of 158, which the stiff excluded
+	// volume (force slope ~10^4) turns into force errors of 1e-2: there the exact remainder of
+	// the hi difference (two_sum) joins the low part.  The shift by m box sides is then exact
+	// (the result is a small multiple of the ulp of d and of box_hi); the box remainder goes
+	// to lo.  Pairs across images are few and sit in the cells at the box faces, so the branch
+	// is taken by few warps.  sep_soft leaves the remainder out, for Debye-Hueckel alone: its
+	// force slope is below 0.1, so the 7.6e-6 moves its force by less than 1e-6.
+	template <bool EXACT = true>
 	__device__ __forceinline__ Sep<float> sep(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql,
 			const DNA2Table<float> &P) const {
 		float d[3] = {qh.x - ph.x, qh.y - ph.y, qh.z - ph.z};
 		float l[3] = {ql.x - pl.x, ql.y - pl.y, ql.z - pl.z};
+		float m[3];
+#pragma unroll
+		for(int k = 0; k < 3; k++) m[k] = __fsub_rn(__fmaf_rn(d[k], P.inv_box, 12582912.f), 12582912.f);
+		if(EXACT && (m[0] != 0.f || m[1] != 0.f || m[2] != 0.f)) {
+			const float qv[3] = {qh.x, qh.y, qh.z}, pv[3] = {ph.x, ph.y, ph.z};
+#pragma unroll
+			for(int k = 0; k < 3; k++) l[k] = __fadd_rn(l[k], two_sum(qv[k], -pv[k]).e);
+		}
 #pragma unroll
 		for(int k = 0; k < 3; k++) {
-			const float m = __fsub_rn(__fmaf_rn(d[k], P.inv_box, 12582912.f), 12582912.f);
-			d[k] = fmaf(-m, P.box_hi, d[k]);
-			l[k] = fmaf(-m, P.box_lo, l[k]);
+			d[k] = fmaf(-m[k], P.box_hi, d[k]);
+			l[k] = fmaf(-m[k], P.box_lo, l[k]);
 		}
 		return Sep<float>{v3<float>{d[0], d[1], d[2]}, v3<float>{l[0], l[1], l[2]}};
+	}
+	__device__ __forceinline__ Sep<float> sep_soft(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql,
+			const DNA2Table<float> &P) const {
+		return sep<false>(ph, pl, qh, ql, P);
 	}
 	// bonded neighbours: no periodic image
 	__device__ __forceinline__ Sep<float> diff(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql) const {
@@ -362,6 +382,10 @@ struct SplitMixed {
 			const DNA2Table<float> &P) const {
 		return LoadMixed{}.sep(ph, pl, qh, ql, P);
 	}
+	__device__ __forceinline__ Sep<float> sep_soft(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql,
+			const DNA2Table<float> &P) const {
+		return LoadMixed{}.sep_soft(ph, pl, qh, ql, P);
+	}
 	__device__ __forceinline__ Sep<float> diff(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql) const {
 		return LoadMixed{}.diff(ph, pl, qh, ql);
 	}
@@ -372,6 +396,10 @@ struct SplitDouble {
 	const float4 *meta, *meta_lo;
 	const int2 *bonds;
 	__device__ __forceinline__ Sep<double> sep(const double4_32a &p, const double4_32a &, const double4_32a &q,
+			const double4_32a &, const DNA2Table<double> &P) const {
+		return LoadDouble{}.sep(p, p, q, q, P);
+	}
+	__device__ __forceinline__ Sep<double> sep_soft(const double4_32a &p, const double4_32a &, const double4_32a &q,
 			const double4_32a &, const DNA2Table<double> &P) const {
 		return LoadDouble{}.sep(p, p, q, q, P);
 	}
@@ -769,7 +797,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 			V4 qh, ql;
 			load_dh<Loader, R>(ld, j, P, q, qh, ql);
 			PairOut<R> o{};
-			pair_dh<R, SPLIT>(P, p, q, ld.sep(ph, pl, qh, ql, P).plain(), o);
+			pair_dh<R, SPLIT>(P, p, q, ld.sep_soft(ph, pl, qh, ql, P).plain(), o);
 			acc.add_short(o);
 		}
 		// excluded volume over centre-close pairs
