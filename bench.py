@@ -398,6 +398,8 @@ def main():
     ap.add_argument("--list-node", default="conditional", choices=["conditional", "kernel"],
                     help="list rebuild as a conditional graph node, or as always-launched kernels that "
                          "return at once on a fresh list (what a kernel-level profiler can see)")
+    ap.add_argument("--sort-every", type=int, default=None,
+                    help="store nucleotides in cell order every k-th list rebuild (default: the workload's)")
     ap.add_argument("--precision-study", action="store_true",
                     help="instead of the throughput line: force/torque/energy errors over snapshots and NVE drift")
     ap.add_argument("--snapshots", type=int, default=100)
@@ -433,9 +435,11 @@ def main():
     a1, a2, a3 = s.frames()
     quat = oxio.frame_to_quat(a1, a2, a3)
     dna = ox.dna2_settings(s.T, 0.5)
+    sort_every = wl.get("sort_every", 0) if args.sort_every is None else args.sort_every
     md = ox.md_settings(dt=wl["dt"], thermostat=wl["thermostat"], newtonian_steps=wl["newtonian_steps"],
                         bussi_tau=wl.get("bussi_tau", 1000.0), diff_coeff=wl.get("diff_coeff", 2.5), seed=1 + rank,
-                        precision="mixed", steps_per_graph=25, list_rebuild_node=args.list_node)
+                        precision="mixed", steps_per_graph=25, list_rebuild_node=args.list_node,
+                        sort_every=sort_every)
     sysm = ox.MDSystem(s.box, s.top, dna, md)
     sysm.set_state(s.pos, quat, s.vel, s.L)
     L = _abi.lib()
@@ -570,7 +574,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "n_nucleotides": s.N, "description": wl["desc"], "md_steps_per_step": M,
                    "l2": "flushed before every timed iteration (256 MiB write)", "precision": "FP32 forces, FP64 state",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU", "sort_every": sort_every},
         "md_steps_per_s": value / (world * s.N),
         "list_rebuilds": rebuilds,
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "TFLOP/s",

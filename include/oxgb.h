@@ -166,6 +166,12 @@ typedef struct oxgb_md_settings {
 	int list_rebuild_node;      /* 0: the list rebuild is a device-side IF node of the step graph;
 	                               1: the rebuild kernels are launched every step and return at once
 	                               while the list is fresh (same results; kernel nodes profilable) */
+	int sort_every;             /* CUDA_sort_every (CUDABaseBackend.cu:263-281): every sort_every-th
+	                               list rebuild stores the nucleotides in cell order, on the device
+	                               (0: never).  Forces, Brownian and NVE trajectories are bit-identical
+	                               to an unsorted run; the state, forces and energies cross this
+	                               interface in the caller's order.  Device buffers and the rows of
+	                               oxgb_md_neighbours are in storage order (oxgb_md_storage_order). */
 } oxgb_md_settings;
 
 void oxgb_md_default_settings(oxgb_md_settings *s);
@@ -253,6 +259,9 @@ int oxgb_md_scale_momenta(oxgb_md *h, int k, double f);
 int oxgb_md_neighbours(oxgb_md *h, int *nnb, int *nb, int max_neigh, int *cell, int *n_cells_side);
 /* number of list rebuilds so far, current step counter, neighbour-row capacity */
 int oxgb_md_info(oxgb_md *h, long long *n_rebuilds, long long *step, int *max_neigh);
+/* id[k] = the caller's index of the nucleotide stored at slot k (the identity until a cell-order
+ * sort, oxgb_md_settings.sort_every) */
+int oxgb_md_storage_order(oxgb_md *h, int *id);
 /* status bits raised by the kernels since the last call (and clears them): 0 = healthy */
 int oxgb_md_status(oxgb_md *h);
 /* device pointers (for zero-copy callers): FP64 positions, velocities, angular momenta and

@@ -56,7 +56,7 @@ class MDSettings(C.Structure):
         ("dt", C.c_double), ("verlet_skin", C.c_double), ("thermostat", C.c_int), ("newtonian_steps", C.c_int),
         ("pt", C.c_double), ("diff_coeff", C.c_double), ("bussi_tau", C.c_double), ("seed", C.c_uint64),
         ("precision", C.c_int), ("cells_auto_optimisation", C.c_int), ("max_neigh", C.c_int),
-        ("steps_per_graph", C.c_int), ("list_rebuild_node", C.c_int),
+        ("steps_per_graph", C.c_int), ("list_rebuild_node", C.c_int), ("sort_every", C.c_int),
     ]
 
 
@@ -97,6 +97,7 @@ SIGNATURES = {
     "oxgb_md_set_temperature": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_neighbours": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
     "oxgb_md_info": (C.c_int, [_VP, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
+    "oxgb_md_storage_order": (C.c_int, [_VP, _VP]),
     "oxgb_md_status": (C.c_int, [_VP]),
     "oxgb_md_device_buffers": (C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP),
                                          C.POINTER(_VP), C.POINTER(_VP)]),

@@ -393,6 +393,12 @@ struct oxgb_md {
 	bool conditional_ok = true;
 	long long host_step = 0, n_rebuilds = 0;
 	unsigned long long *d_rebuilds = nullptr;
+	// cell-order storage (md.sort_every > 0): caller's index of each slot and its inverse, the
+	// sort's scratch, and the bonds in the caller's order
+	int *d_id = nullptr, *d_slot = nullptr, *d_perm = nullptr, *d_inv = nullptr;
+	int2 *bonds0 = nullptr;
+	unsigned char *sort_scratch = nullptr;
+	bool sorting() const { return md.sort_every > 0; }
 
 	void free_layout() {
 		for(void **p : {(void **) &d_sys_nside, (void **) &d_sys_cell0, (void **) &d_cell_sys, (void **) &d_sys_box,
@@ -425,6 +431,8 @@ struct oxgb_md {
 		if(h_stage) cudaFreeHost(h_stage);
 		if(d_stage) cudaFree(d_stage);
 		if(d_bad) cudaFree(d_bad);
+		for(void *p : {(void *) d_id, (void *) d_slot, (void *) d_perm, (void *) d_inv, (void *) bonds0, (void *) sort_scratch})
+			if(p) cudaFree(p);
 	}
 };
 
@@ -456,6 +464,7 @@ static ThermoArgs thermo_args(oxgb_md *h, int step_offset = 0, bool engine_step 
 	t.open_step = engine_step ? h->open_step : nullptr;
 	t.step_base = h->step;
 	t.step_offset = step_offset;
+	t.id = h->d_id;
 	return t;
 }
 
@@ -536,6 +545,8 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.box = (float) h->box[0];
 	a.sys_box = h->n_systems > 1 ? h->d_sys_box : nullptr;
 	a.th = thermo_args(h, step_offset, engine_step);
+	a.id = h->d_id;
+	a.slot = h->d_slot;
 	return a;
 }
 
@@ -658,6 +669,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	h->dna.assign(dna, dna + n_systems);
 	h->md = *md;
 	if(h->md.steps_per_graph <= 0) h->md.steps_per_graph = 16;
+	if(h->md.sort_every < 0) h->md.sort_every = 0;
 	h->conditional_ok = h->md.list_rebuild_node == 0;
 	h->dbl = md->precision == OXGB_PRECISION_DOUBLE;
 	h->rcut.assign(n_systems, 0.0);
@@ -746,7 +758,16 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->open_step, sizeof(long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->d_rebuilds, sizeof(unsigned long long)) == cudaSuccess;
 	ok &= cudaMalloc(&h->term_max, sizeof(int) * 4) == cudaSuccess;
+	if(h->sorting()) {
+		ok &= cudaMalloc(&h->d_id, sizeof(int) * N) == cudaSuccess;
+		ok &= cudaMalloc(&h->d_slot, sizeof(int) * N) == cudaSuccess;
+		ok &= cudaMalloc(&h->d_perm, sizeof(int) * N) == cudaSuccess;
+		ok &= cudaMalloc(&h->d_inv, sizeof(int) * N) == cudaSuccess;
+		ok &= cudaMalloc(&h->bonds0, sizeof(int2) * N) == cudaSuccess;
+		ok &= cudaMalloc(&h->sort_scratch, (size_t) SORT_BYTES * N) == cudaSuccess;
+	}
 	if(!ok) return bail(fail(OXGB_E_NOMEM, "device allocation failed"));
+	if(h->sorting()) ok &= launch_identity_order(h->d_id, h->d_slot, N, nullptr) == cudaSuccess;
 	ok &= cudaMemset(h->term_max, 0, sizeof(int) * 4) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_sys, sys.data(), sizeof(int) * N, cudaMemcpyHostToDevice) == cudaSuccess;
 	ok &= cudaMemcpy(h->d_sys_off, offsets, sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -779,9 +800,37 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	return OXGB_OK;
 }
 
+// The per-slot data that follow the caller's order: the w words of the position mirrors
+// (btype << 22 | index, and the base type; the mirror updates rewrite only x, y, z) and, with
+// cell-order storage, the bonds and the identity map.  A new topology or a new state starts in
+// the caller's order.
+static int caller_order(oxgb_md *h) {
+	const int N = h->N;
+	std::vector<float4> hi(N), lo(N);
+	for(int i = 0; i < N; i++) {
+		const int packed = (h->h_btype[i] << 22) | (i & 0x003FFFFF), t = h->h_type[i];
+		float w, tw;
+		std::memcpy(&w, &packed, 4);
+		std::memcpy(&tw, &t, 4);
+		hi[i] = make_float4(0.f, 0.f, 0.f, w);
+		lo[i] = make_float4(0.f, 0.f, 0.f, tw);
+	}
+	CK(cudaMemcpyAsync(h->pos_hi, hi.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
+	CK(cudaMemcpyAsync(h->pos_lo, lo.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, h->stream));
+	if(h->sorting()) {
+		CK(cudaMemcpyAsync(h->bonds, h->bonds0, sizeof(int2) * N, cudaMemcpyDeviceToDevice, h->stream));
+		CK(launch_identity_order(h->d_id, h->d_slot, N, h->stream));
+	}
+	CK(cudaStreamSynchronize(h->stream));
+	return OXGB_OK;
+}
+
 extern "C" int oxgb_md_set_topology(oxgb_md *h, const int *n3, const int *n5, const int *btype, const int *type) {
 	if(!h || !n3 || !n5 || !btype || !type) return fail(OXGB_E_INVALID, "null argument");
 	const int N = h->N;
+	// a state stored in cell order goes back to the caller's order around the new topology
+	std::vector<double> sp, sq, sv, sl;
+	const bool restate = h->sorting() && h->have_state;
 	std::vector<int2> b(N);
 	for(int k = 0; k < h->n_systems; k++) {
 		const int lo = h->offsets[k], hi = h->offsets[k + 1];
@@ -798,25 +847,21 @@ extern "C" int oxgb_md_set_topology(oxgb_md *h, const int *n3, const int *n5, co
 	for(int i = 0; i < N; i++) {
 		if(n3[i] >= 0 && n5[n3[i]] != i) return fail(OXGB_E_INVALID, "topology: n3/n5 are not mutual");
 	}
+	if(restate) {
+		sp.resize(3 * (size_t) N), sq.resize(4 * (size_t) N), sv.resize(3 * (size_t) N), sl.resize(3 * (size_t) N);
+		const int rc = oxgb_md_get_state(h, sp.data(), sq.data(), sv.data(), sl.data());
+		if(rc) return rc;
+	}
 	h->h_n3.assign(n3, n3 + N);
 	h->h_n5.assign(n5, n5 + N);
 	h->h_btype.assign(btype, btype + N);
 	h->h_type.assign(type, type + N);
 	CK(cudaMemcpy(h->bonds, b.data(), sizeof(int2) * N, cudaMemcpyHostToDevice));
-	// the w words of the position mirrors (btype << 22 | index, and the base type) stay; the
-	// mirror updates rewrite only x, y, z
-	std::vector<float4> hi(N), lo(N);
-	for(int i = 0; i < N; i++) {
-		const int packed = (btype[i] << 22) | (i & 0x003FFFFF), t = type[i];
-		float w, tw;
-		std::memcpy(&w, &packed, 4);
-		std::memcpy(&tw, &t, 4);
-		hi[i] = make_float4(0.f, 0.f, 0.f, w);
-		lo[i] = make_float4(0.f, 0.f, 0.f, tw);
-	}
-	CK(cudaMemcpy(h->pos_hi, hi.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
-	CK(cudaMemcpy(h->pos_lo, lo.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
+	if(h->sorting()) CK(cudaMemcpy(h->bonds0, b.data(), sizeof(int2) * N, cudaMemcpyHostToDevice));
+	const int rc = caller_order(h);
+	if(rc) return rc;
 	h->have_topology = true;
+	if(restate) return oxgb_md_set_state(h, sp.data(), sq.data(), sv.data(), sl.data());
 	return OXGB_OK;
 }
 
@@ -854,6 +899,17 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	a.term_max = h->term_max;
 	a.base_pos = h->tl.base_pos;
 	a.stk_pos = h->tl.stk_pos;
+	if(h->sorting()) {
+		a.sort_every = h->md.sort_every;
+		a.id = h->d_id;
+		a.slot = h->d_slot;
+		a.perm = h->d_perm;
+		a.inv = h->d_inv;
+		a.st[0] = h->posd, a.st[1] = h->veld, a.st[2] = h->Ld, a.st[3] = h->quatd;
+		a.mir[0] = h->pos_hi, a.mir[1] = h->pos_lo, a.mir[2] = h->fa1, a.mir[3] = h->fa3, a.mir[4] = h->fback;
+		a.bonds_rw = h->bonds;
+		a.scratch = h->sort_scratch;
+	}
 	return a;
 }
 
@@ -967,6 +1023,10 @@ extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *qu
 	CK(cudaMemcpyAsync(&bad, h->d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
 	CK(cudaStreamSynchronize(h->stream));
 	if(bad != INT_MAX) return fail(OXGB_E_INVALID, "quaternion of nucleotide " + std::to_string(bad) + " is not normalisable");
+	if(h->sorting()) {
+		const int rc0 = caller_order(h);
+		if(rc0) return rc0;
+	}
 	CK(launch_unpack_state(sa, h->d_stage, h->d_bad, false, h->stream));
 	if(clear_pending(h)) return fail(OXGB_E_CUDA, "upload");  // a new state: nothing pending
 	CK(launch_make_mirrors(sa, h->stream));
@@ -1029,7 +1089,8 @@ static int enqueue_step(oxgb_md *h, cudaGraph_t capturing, int k) {
 	StepArgs sa = step_args(h, k);
 	CK(fork_noise(h, sa));
 	CK(launch_first_step(sa, h->dbl, h->stream));
-	CK(bussi_after_first_step(h, sa));
+	// the side branch reads the state: after the rebuild when a rebuild may move nucleotides
+	if(!h->sorting()) CK(bussi_after_first_step(h, sa));
 	ListArgs la = md_list_args(h, h->conditional_ok ? 0 : 1);
 	if(h->conditional_ok) {
 		cudaGraphConditionalHandle hc;
@@ -1059,6 +1120,7 @@ static int enqueue_step(oxgb_md *h, cudaGraph_t capturing, int k) {
 	else {
 		CK(launch_list_build(la, h->stream));
 	}
+	if(h->sorting()) CK(bussi_after_first_step(h, sa));
 	ForceArgs fa = force_args(h, k, true);
 	CK(launch_forces_split(fa, h->dbl, false, false, h->stream));
 	CK(bussi_after_forces(h, sa));
@@ -1122,9 +1184,10 @@ extern "C" int oxgb_md_run(oxgb_md *h, int nsteps, int sync) {
 		StepArgs sa = step_args(h);
 		CK(fork_noise(h, sa));
 		CK(launch_first_step(sa, h->dbl, h->stream));
-		CK(bussi_after_first_step(h, sa));
+		if(!h->sorting()) CK(bussi_after_first_step(h, sa));
 		ListArgs la = md_list_args(h, 1);
 		CK(launch_list_build(la, h->stream));
+		if(h->sorting()) CK(bussi_after_first_step(h, sa));
 		ForceArgs fa = force_args(h, 0, true);
 		CK(launch_forces_split(fa, h->dbl, false, false, h->stream));
 		CK(bussi_after_forces(h, sa));
@@ -1172,27 +1235,40 @@ extern "C" int oxgb_md_get_forces(oxgb_md *h, double *F, double *T, double *E) {
 }
 
 // F, T from the device buffers dF, dT and E from the w of dF (any output may be NULL)
+// the caller's index of every slot (the identity unless the engine stores in cell order)
+static int storage_order(oxgb_md *h, std::vector<int> &id) {
+	id.resize(h->N);
+	if(!h->sorting()) {
+		for(int i = 0; i < h->N; i++) id[i] = i;
+		return OXGB_OK;
+	}
+	CK(cudaMemcpyAsync(id.data(), h->d_id, sizeof(int) * h->N, cudaMemcpyDeviceToHost, h->stream));
+	CK(cudaStreamSynchronize(h->stream));
+	return OXGB_OK;
+}
+
 static int download_forces(oxgb_md *h, const void *dF, const void *dT, double *F, double *T, double *E) {
 	const int N = h->N;
+	std::vector<int> id;
+	const int rc = storage_order(h, id);
+	if(rc) return rc;
+	auto put = [&](int i, double fx, double fy, double fz, double fw, double tx, double ty, double tz) {
+		const size_t o = (size_t) id[i];
+		if(F) F[3 * o] = fx, F[3 * o + 1] = fy, F[3 * o + 2] = fz;
+		if(T) T[3 * o] = tx, T[3 * o + 1] = ty, T[3 * o + 2] = tz;
+		if(E) E[o] = fw;
+	};
 	if(h->dbl) {
 		std::vector<double4_32a> f(N), t(N);
 		CK(cudaMemcpy(f.data(), dF, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
 		CK(cudaMemcpy(t.data(), dT, sizeof(double4_32a) * N, cudaMemcpyDeviceToHost));
-		for(int i = 0; i < N; i++) {
-			if(F) F[3 * i] = f[i].x, F[3 * i + 1] = f[i].y, F[3 * i + 2] = f[i].z;
-			if(T) T[3 * i] = t[i].x, T[3 * i + 1] = t[i].y, T[3 * i + 2] = t[i].z;
-			if(E) E[i] = f[i].w;
-		}
+		for(int i = 0; i < N; i++) put(i, f[i].x, f[i].y, f[i].z, f[i].w, t[i].x, t[i].y, t[i].z);
 	}
 	else {
 		std::vector<float4> f(N), t(N);
 		CK(cudaMemcpy(f.data(), dF, sizeof(float4) * N, cudaMemcpyDeviceToHost));
 		CK(cudaMemcpy(t.data(), dT, sizeof(float4) * N, cudaMemcpyDeviceToHost));
-		for(int i = 0; i < N; i++) {
-			if(F) F[3 * i] = f[i].x, F[3 * i + 1] = f[i].y, F[3 * i + 2] = f[i].z;
-			if(T) T[3 * i] = t[i].x, T[3 * i + 1] = t[i].y, T[3 * i + 2] = t[i].z;
-			if(E) E[i] = f[i].w;
-		}
+		for(int i = 0; i < N; i++) put(i, f[i].x, f[i].y, f[i].z, f[i].w, t[i].x, t[i].y, t[i].z);
 	}
 	return OXGB_OK;
 }
@@ -1359,6 +1435,15 @@ extern "C" int oxgb_md_neighbours(oxgb_md *h, int *nnb, int *nb, int max_neigh, 
 		for(int i = 0; i < N; i++)
 			for(int k = 0; k < h->lb.max_nb; k++) nb[(size_t) i * max_neigh + k] = rows[(size_t) k * N + i];  // column-major
 	}
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_md_storage_order(oxgb_md *h, int *id) {
+	if(!h || !id) return fail(OXGB_E_INVALID, "null argument");
+	std::vector<int> v;
+	const int rc = storage_order(h, v);
+	if(rc) return rc;
+	std::memcpy(id, v.data(), sizeof(int) * h->N);
 	return OXGB_OK;
 }
 

@@ -637,16 +637,19 @@ __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld,
 	const int *nb = is_base ? a.base_nb : a.stk_nb;
 	V4 *res = reinterpret_cast<V4 *>(is_base ? a.base_res : a.stk_res);
 	// this lane's nucleotide (lanes below NPW): which of its entries it owns (partner above
-	// it), as a bit mask
+	// it by caller's index), as a bit mask
 	const int il = wbase + lane;
 	unsigned lo = 0u, hi = 0u;
 	if(lane < NPW && il < a.N) {
 		const int n = min(min(is_base ? a.base_n[il] : a.stk_n[il], cap), 64);
-		for(int k = 0; k < n; k++)
-			if(nb[(long long) k * N + il] > il) {
+		const int key = a.id ? a.id[il] : il;
+		for(int k = 0; k < n; k++) {
+			const int j = nb[(long long) k * N + il];
+			if((a.id ? a.id[j] : j) > key) {
 				if(k < 32) lo |= 1u << k;
 				else hi |= 1u << (k - 32);
 			}
+		}
 	}
 	const int own = __popc(lo) + __popc(hi);
 	int incl = own;
@@ -886,7 +889,8 @@ __global__ void k_external(ForceArgs a) {
 	pdl_trigger();
 	const int k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= a.ext_n) return;
-	const int i = a.ext_nuc[k];
+	// records name caller's indices
+	const int i = a.slot ? a.slot[a.ext_nuc[k]] : a.ext_nuc[k];
 	const long long step = a.th.step_base ? *a.th.step_base + a.th.step_offset : 0;
 	const double st = (double) step;
 	const oxgb_ext_force *rec = reinterpret_cast<const oxgb_ext_force *>(a.ext_rec);
@@ -907,7 +911,7 @@ __global__ void k_external(ForceArgs a) {
 			break;
 		}
 		case OXGB_FORCE_MUTUAL_TRAP: {
-			const double4_32a q = a.posd[e.ref_particle];
+			const double4_32a q = a.posd[a.slot ? a.slot[e.ref_particle] : e.ref_particle];
 			double dx = q.x - r.x, dy = q.y - r.y, dz = q.z - r.z;
 			if(e.flags & 1) {
 				const double L = a.sys_box ? (double) a.sys_box[a.sys ? a.sys[i] : 0] : (double) a.box;

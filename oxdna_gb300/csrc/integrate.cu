@@ -97,7 +97,7 @@ __device__ __forceinline__ void complete_step(const ThermoArgs &t, int i, int sy
 	L.x = fma(widen(T.x), hdt, L.x);
 	L.y = fma(widen(T.y), hdt, L.y);
 	L.z = fma(widen(T.z), hdt, L.z);
-	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) brownian_redraw(t, sy, i - t.sys_off[sy], sp, v, L);
+	if(t.thermostat == 1 && sp % t.newtonian_steps == 0) brownian_redraw(t, sy, (t.id ? t.id[i] : i) - t.sys_off[sy], sp, v, L);
 	else if(t.thermostat == 2 && *t.bussi_stamp == sp) bussi_rescale(t, sy, v, L);
 }
 
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 			x.x = fma(gx, hdt, x.x);
 			x.y = fma(gy, hdt, x.y);
 			x.z = fma(gz, hdt, x.z);
-			if(brownian) x = brownian_redraw_part(a.th, sy, i - a.th.sys_off[sy], sp, rot ? 1 : 0, x);
+			if(brownian) x = brownian_redraw_part(a.th, sy, (a.th.id ? a.th.id[i] : i) - a.th.sys_off[sy], sp, rot ? 1 : 0, x);
 			else if(bussi) bussi_rescale_part(a.th, sy, rot ? 1 : 0, x);
 		}
 		x.x = fma(gx, hdt, x.x);
@@ -528,13 +528,13 @@ __global__ void k_unpack_state(StepArgs a, const double *in, int *bad, int check
 	a.angmom[i] = make_double4_32a(l[0], l[1], l[2], 0.0);
 }
 
-// the FP64 state into the caller's layout (the reverse of k_unpack_state)
+// the FP64 state into the caller's layout and order (the reverse of k_unpack_state)
 __global__ void k_pack_state(StepArgs a, double *out) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= a.N) return;
 	const long long N = a.N;
-	double *p = out + 3 * (long long) i, *q = out + 3 * N + 4 * (long long) i, *v = out + 7 * N + 3 * (long long) i,
-		   *l = out + 10 * N + 3 * (long long) i;
+	const long long c = a.th.id ? a.th.id[i] : i;  // the caller's index
+	double *p = out + 3 * c, *q = out + 3 * N + 4 * c, *v = out + 7 * N + 3 * c, *l = out + 10 * N + 3 * c;
 	const double4_32a r = a.pos[i], o = a.quat[i], u = a.vel[i], m = a.angmom[i];
 	p[0] = r.x, p[1] = r.y, p[2] = r.z;
 	q[0] = o.x, q[1] = o.y, q[2] = o.z, q[3] = o.w;
@@ -642,6 +642,18 @@ cudaError_t launch_make_mirrors(const StepArgs &a, cudaStream_t s) {
 
 cudaError_t launch_unpack_state(const StepArgs &a, const double *in, int *bad, bool check_only, cudaStream_t s) {
 	k_unpack_state<<<blocks_for(a.N, 256), 256, 0, s>>>(a, in, bad, check_only ? 1 : 0);
+	return cudaGetLastError();
+}
+
+__global__ void k_identity_order(int *id, int *slot, int N) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= N) return;
+	id[i] = i;
+	slot[i] = i;
+}
+
+cudaError_t launch_identity_order(int *id, int *slot, int N, cudaStream_t s) {
+	k_identity_order<<<blocks_for(N, 256), 256, 0, s>>>(id, slot, N);
 	return cudaGetLastError();
 }
 

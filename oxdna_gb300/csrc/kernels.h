@@ -82,6 +82,8 @@ struct ThermoArgs {
 	                                       // (OXGB_NO_STEP: none); null in force-only calls
 	long long *step_base;                  // device step counter of the current graph
 	int step_offset;
+	const int *id;                         // [N] caller's index of the nucleotide at each slot
+	                                       // (null: never sorted, slot = index); keys the draws
 };
 
 struct ForceArgs {
@@ -120,6 +122,10 @@ struct ForceArgs {
 	int ext_n;
 	float box;                                // cubic box of the (single-system) engine
 	const float *sys_box;                     // per system (batches), or null
+	// cell-order storage (null: never sorted): caller's index of each slot, which decides the
+	// owner of a base / stack pair as in an unsorted run, and the slot of each caller's index
+	// (external-force records name caller's indices)
+	const int *id, *slot;
 };
 
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
@@ -177,7 +183,23 @@ struct ListArgs {
 	int *sys_stale;
 	int n_systems;
 	int n_cells_total;      // cells of all systems (0: n_side^3)
+	// Cell-order storage (CUDA_sort_every; sort_every 0 or id null: off).  On every sort_every-th
+	// build the nucleotides of the rebuilt systems move to the slots of their cell order (cell,
+	// then caller's index) before the rows are built: the FP64 state, the mirrors, bonds
+	// (renumbered) and id.  Segments are ordered and pairs owned by caller's index, so the rows
+	// list the same partners in the same order as an unsorted build.
+	int sort_every;
+	int *id, *slot;         // [N] caller's index of each slot, and its inverse
+	int *perm, *inv;        // [N] scratch: old slot of new slot k, new slot of old slot
+	double4_32a *st[4];     // FP64 state: positions, velocities, angular momenta, quaternions
+	float4 *mir[5];         // mirrors: pos_hi, pos_lo, fa1, fa3, fback (any may be null)
+	int2 *bonds_rw;         // the bonds the rows exclude (the array of `bonds`)
+	unsigned char *scratch; // [N * SORT_BYTES]
 };
+
+// bytes per nucleotide of the sort's staging buffer: 4 FP64 vectors, 5 FP32 vectors, bonds,
+// id and cell
+#define SORT_BYTES (4 * 32 + 5 * 16 + 8 + 4 + 4)
 
 // full rebuild: cells (counting sort, deterministic order) then neighbour rows
 cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s);
@@ -212,6 +234,8 @@ cudaError_t launch_bussi_noise(const StepArgs &a, cudaStream_t s);
 // 256 nucleotides
 cudaError_t launch_bussi_prep(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s);
 cudaError_t launch_bussi_reduce(const StepArgs &a, int n_chunks, bool double_forces, cudaStream_t s);
+// id[k] = slot[k] = k: the caller's order (cell-order storage undone)
+cudaError_t launch_identity_order(int *id, int *slot, int N, cudaStream_t s);
 // end of a graph of K steps: the step base advances by K
 cudaError_t launch_step_advance(const StepArgs &a, int K, cudaStream_t s);
 // end of a run: completes the pending half kick and thermostat so the state is whole

@@ -170,16 +170,88 @@ __global__ void k_cell_scatter(ListArgs a) {
 	a.cell_tmp[slot] = i;
 }
 
-// each particle's rank by index within its cell gives the deterministic order (cell_list)
+// the caller's index of slot i (slot i itself while the engine was never sorted)
+__device__ __forceinline__ int id_of(const ListArgs &a, int i) { return a.id ? a.id[i] : i; }
+
+// each particle's rank by caller's index within its cell gives the deterministic order (cell_list)
 __global__ void k_cell_rank(ListArgs a) {
 	SKIP_IF_FRESH(a);
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= a.N || !rebuilt(a, sys_of(a, i))) return;
 	const int c = a.cell_of[i];
 	const int b = a.cell_start[c], e = a.cell_start[c + 1];
+	const int key = id_of(a, i);
 	int rank = 0;
-	for(int k = b; k < e; k++) rank += a.cell_tmp[k] < i;
+	for(int k = b; k < e; k++) rank += id_of(a, a.cell_tmp[k]) < key;
 	a.cell_list[b + rank] = i;
+}
+
+// ---------------------------------------------------------------- cell-order storage
+// (CUDABaseBackend::_sort_particles, CUDABaseBackend.cu:263-281, with the cell order of this
+// build in place of a Hilbert key: the order is the one the counting sort just produced)
+
+// this build moves nucleotides: sorting on, and the build count a multiple of sort_every
+__device__ __forceinline__ bool sort_now(const ListArgs &a) {
+	return a.sort_every > 0 && a.id && (a.rebuilds ? *a.rebuilds : 0ull) % (unsigned long long) a.sort_every == 0ull;
+}
+
+// new slot k takes old slot perm[k] = cell_list[k] (rebuilt systems; the others stay)
+__global__ void k_sort_perm(ListArgs a) {
+	SKIP_IF_FRESH(a);
+	if(!sort_now(a)) return;
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= a.N) return;
+	const int from = rebuilt(a, sys_of(a, k)) ? a.cell_list[k] : k;
+	a.perm[k] = from;
+	a.inv[from] = k;
+}
+
+// everything of old slot perm[k] into the staging buffer at k; bonds renumbered
+__global__ void k_sort_gather(ListArgs a) {
+	SKIP_IF_FRESH(a);
+	if(!sort_now(a)) return;
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= a.N) return;
+	const long long N = a.N;
+	const int from = a.perm[k];
+	double4_32a *sd = reinterpret_cast<double4_32a *>(a.scratch);
+	float4 *sf = reinterpret_cast<float4 *>(a.scratch + 4 * 32 * N);
+	int2 *sb = reinterpret_cast<int2 *>(a.scratch + (4 * 32 + 5 * 16) * N);
+	int *si = reinterpret_cast<int *>(a.scratch + (4 * 32 + 5 * 16 + 8) * N);
+#pragma unroll
+	for(int t = 0; t < 4; t++) sd[t * N + k] = a.st[t][from];
+#pragma unroll
+	for(int t = 0; t < 5; t++)
+		if(a.mir[t]) sf[t * N + k] = a.mir[t][from];
+	const int2 b = a.bonds_rw[from];
+	sb[k] = make_int2(b.x >= 0 ? a.inv[b.x] : -1, b.y >= 0 ? a.inv[b.y] : -1);
+	si[k] = a.id[from];
+	si[N + k] = a.cell_of[from];
+	// segment entries name slots: renamed in place (each k touches its own entry)
+	a.cell_list[k] = a.inv[a.cell_list[k]];
+}
+
+// the staging buffer back into the arrays, and the inverse map
+__global__ void k_sort_scatter(ListArgs a) {
+	SKIP_IF_FRESH(a);
+	if(!sort_now(a)) return;
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= a.N) return;
+	const long long N = a.N;
+	const double4_32a *sd = reinterpret_cast<const double4_32a *>(a.scratch);
+	const float4 *sf = reinterpret_cast<const float4 *>(a.scratch + 4 * 32 * N);
+	const int2 *sb = reinterpret_cast<const int2 *>(a.scratch + (4 * 32 + 5 * 16) * N);
+	const int *si = reinterpret_cast<const int *>(a.scratch + (4 * 32 + 5 * 16 + 8) * N);
+#pragma unroll
+	for(int t = 0; t < 4; t++) a.st[t][k] = sd[t * N + k];
+#pragma unroll
+	for(int t = 0; t < 5; t++)
+		if(a.mir[t]) a.mir[t][k] = sf[t * N + k];
+	a.bonds_rw[k] = sb[k];
+	const int id = si[k];
+	a.id[k] = id;
+	a.slot[id] = k;
+	a.cell_of[k] = si[N + k];
 }
 
 // minimum-image separation vector (the reference's fp32 geometry, explicit fused multiply-adds)
@@ -316,7 +388,8 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	}
 }
 
-// For every base / stack list entry (k, i) with partner j > i (i owns the pair): where i sits in
+// For every base / stack list entry (k, i) with partner j above i by caller's index (i owns the
+// pair, as in an unsorted run): where i sits in
 // j's list (the lists are symmetric: the pair criteria are exactly symmetric in FP32).  One
 // thread per nucleotide and term (blocks 0 .. base_blocks - 1: base lists).
 __global__ void k_term_pos(ListArgs a, int base_blocks) {
@@ -332,7 +405,7 @@ __global__ void k_term_pos(ListArgs a, int base_blocks) {
 	for(int k = 0; k < n; k++) {
 		const int j = nb[(long long) k * N + i];
 		int r = -1;
-		if(j > i) {
+		if(id_of(a, j) > id_of(a, i)) {
 			const int nj = min(is_base ? a.base_n[j] : a.stk_n[j], cap);
 			for(int m = 0; m < nj; m++)
 				if(nb[(long long) m * N + j] == i) {
@@ -370,6 +443,11 @@ cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s) {
 	k_scan_apply<<<tiles, SCAN_TPB, 0, s>>>(a, n_cells, tiles);
 	k_cell_scatter<<<gp, tpb, 0, s>>>(a);
 	k_cell_rank<<<gp, tpb, 0, s>>>(a);
+	if(a.sort_every > 0 && a.id) {
+		k_sort_perm<<<gp, tpb, 0, s>>>(a);
+		k_sort_gather<<<gp, tpb, 0, s>>>(a);
+		k_sort_scatter<<<gp, tpb, 0, s>>>(a);
+	}
 	const long long warps = (long long) a.N * 32;
 	k_neighbours<<<(int) ((warps + tpb - 1) / tpb), tpb, 0, s>>>(a);
 	if(a.base_pos && a.stk_pos) k_term_pos<<<2 * gp, tpb, 0, s>>>(a, gp);

@@ -46,7 +46,7 @@ def dna2_settings(T: float, salt: float = 0.5, average: bool = True, seq: Option
 def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = "no", newtonian_steps: int = 103,
                 pt: float = 0.0, diff_coeff: float = 2.5, bussi_tau: float = 1000.0, seed: int = 1,
                 precision: str = "mixed", cells_auto_optimisation: bool = True, max_neigh: int = 0,
-                steps_per_graph: int = 16, list_rebuild_node: str = "conditional") -> _abi.MDSettings:
+                steps_per_graph: int = 16, list_rebuild_node: str = "conditional", sort_every: int = 0) -> _abi.MDSettings:
     m = _abi.MDSettings()
     _abi.lib().oxgb_md_default_settings(C.byref(m))
     m.dt = dt
@@ -62,6 +62,7 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
     m.max_neigh = max_neigh
     m.steps_per_graph = steps_per_graph
     m.list_rebuild_node = {"conditional": 0, "kernel": 1}[list_rebuild_node]
+    m.sort_every = sort_every
     return m
 
 
@@ -135,6 +136,13 @@ class MDSystem:
         F, T, E, Es = np.zeros((N, 3)), np.zeros((N, 3)), np.zeros(N), np.zeros(8 * self.n_systems)
         _abi.check(_abi.lib().oxgb_md_compute_forces(self._h, _abi.ptr(F), _abi.ptr(T), _abi.ptr(E), _abi.ptr(Es)))
         return F, T, E, (Es if self.n_systems == 1 else Es.reshape(self.n_systems, 8))
+
+    def storage_order(self):
+        """the caller's index of the nucleotide in each storage slot (the identity unless the
+        engine sorts into cell order, md_settings(sort_every=...))"""
+        out = np.zeros(self.N, np.int32)
+        _abi.check(_abi.lib().oxgb_md_storage_order(self._h, _abi.ptr(out)))
+        return out
 
     def get_forces(self):
         """forces, torques and per-nucleotide energies of the last step, not recomputed"""
