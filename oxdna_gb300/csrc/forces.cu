@@ -538,7 +538,7 @@ struct SplitAcc {
 
 // Base-base pairs (hydrogen bonding + cross stacking; blocks 0 .. base_blocks - 1) and
 // stack-stack pairs (coaxial stacking; the other blocks), each evaluated once, by its lower
-// nucleotide i (partner j > i, at position k of i's list and m of j's): slot k of i gets
+// nucleotide i (partner j above i by caller's index, at position k of i's list and m of j's): slot k of i gets
 // (force on i, E), (torque on i, E_hb) and slot m of j gets (-force, E), (torque on j, E_hb), at
 // [2 (k N + i) + 0..1] of base_res / stk_res.  Every slot of every list is written by its pair
 // alone.  These are the costliest terms and their lists are short, so the owned slots of a

@@ -108,7 +108,7 @@ struct ForceArgs {
 	const int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
 	int ev_cap, base_cap, stk_cap;            // capacities (an overflowed list is read up to them)
 	void *bond_f, *bond_tp, *bond_tq;         // per bond owner p (q = n3[p]): f on q with w = energy, torques
-	// base / stack pairs are evaluated once, by their lower nucleotide i, which writes slot k of i
+	// base / stack pairs are evaluated once, by their lower nucleotide i (by caller's index), which writes slot k of i
 	// and slot pos[k N + i] of its partner j: (force, E), (torque, E_hb) as two V4 per slot
 	void *base_res, *stk_res;
 	const int *base_pos, *stk_pos;            // see ListArgs
@@ -152,7 +152,7 @@ struct ListArgs {
 	int *cell_count;        // [n_cells]
 	int *cell_start;        // [n_cells + 1]
 	int *cell_cursor;       // [n_cells]
-	int *cell_list;         // [N] particles by cell, by index within a cell
+	int *cell_list;         // [N] particles by cell, by caller's index within a cell
 	int *cell_tmp;          // [N] scatter target before the ordering
 	int *scan_part;         // [scan_tiles(n_cells) + 1]
 	int *nb, *nnb;          // [N * max_nb], [N]

@@ -3,7 +3,7 @@
 // Replaces simple_fill_cells / simple_update_neigh_list (src/CUDA/Lists/CUDA_simple_verlet.cuh:
 // 14-95) and the host control of CUDASimpleVerletList::update (src/CUDA/Lists/
 // CUDASimpleVerletList.cu:231-289).  Cells are filled by a counting sort (count, scan,
-// scatter, then each particle placed by its index rank within its cell), so there is no
+// scatter, then each particle placed by the rank of its caller's index within its cell), so there is no
 // per-cell capacity to overflow and the neighbour order is deterministic run to run.  The geometry is the
 // reference's fp32 geometry: cell coordinate ((x/L - floor(x/L)) * (1 - FLT_EPSILON)) * n and
 // minimum-image squared distance against r_verlet^2, with IEEE division and the fused
