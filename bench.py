@@ -382,6 +382,48 @@ def precision_study(args):
     print(json.dumps(line), flush=True)
 
 
+def averages_study(args):
+    """Long-run averages of mixed precision against FP64 (the FP64 engine follows the
+    reference's MD to 1e-8): independent Brownian runs of the same duplex system in both
+    precisions; the potential, hydrogen-bonding and stacking energy per nucleotide, sampled every
+    `every` steps, with standard errors from `blocks` block averages, and the z-score of each
+    difference."""
+    import torch
+    torch.cuda.set_device(0)
+    import oxdna_gb300 as ox
+    from oxdna_gb300 import generate as G
+    from oxdna_gb300 import io as oxio
+    s = G.system_for_config(1, seed=args.seed, scale=args.avg_scale)
+    a1, a2, a3 = s.frames()
+    quat = oxio.frame_to_quat(a1, a2, a3)
+    out = {}
+    for precision in ("mixed", "double"):
+        m = ox.MDSystem(s.box, s.top, ox.dna2_settings(s.T, 0.5),
+                        ox.md_settings(dt=0.003, thermostat="john", newtonian_steps=103, diff_coeff=2.5,
+                                       seed=101 if precision == "mixed" else 202, precision=precision,
+                                       steps_per_graph=25))
+        m.set_state(s.pos, quat, s.vel, s.L)
+        m.run(args.avg_equil)
+        rows = []
+        for _ in range(args.avg_samples):
+            m.run(args.every)
+            _, _, _, Es = m.compute_forces()
+            rows.append([Es.sum() / s.N, Es[4] / s.N, Es[2] / s.N])
+        m.close()
+        x = np.array(rows)
+        b = x[: (len(x) // args.blocks) * args.blocks].reshape(args.blocks, -1, 3).mean(axis=1)
+        out[precision] = (x.mean(axis=0), b.std(axis=0, ddof=1) / np.sqrt(args.blocks))
+    names = ["potential", "hydrogen_bonding", "stacking"]
+    res = {}
+    for k, n in enumerate(names):
+        (mm, sm), (md, sd) = (out["mixed"][0][k], out["mixed"][1][k]), (out["double"][0][k], out["double"][1][k])
+        res[n] = {"mixed": mm, "mixed_se": sm, "double": md, "double_se": sd, "z": (mm - md) / np.hypot(sm, sd)}
+    print(json.dumps({"study": "long-run averages", "workload": f"{s.N // 40} x 20-bp duplexes ({s.N} nt), 300 K, Brownian",
+                      "unit": "energy per nucleotide (simulation units)", "equilibration_steps": args.avg_equil,
+                      "samples": args.avg_samples, "every": args.every, "blocks": args.blocks, "averages": res}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -402,6 +444,12 @@ def main():
                     help="store nucleotides in cell order every k-th list rebuild (default: the workload's)")
     ap.add_argument("--precision-study", action="store_true",
                     help="instead of the throughput line: force/torque/energy errors over snapshots and NVE drift")
+    ap.add_argument("--averages-study", action="store_true",
+                    help="instead of the throughput line: long-run energy averages, mixed vs FP64")
+    ap.add_argument("--avg-scale", type=float, default=0.05, help="duplex count of the averages study / 1000")
+    ap.add_argument("--avg-equil", type=int, default=20000)
+    ap.add_argument("--avg-samples", type=int, default=400)
+    ap.add_argument("--blocks", type=int, default=20)
     ap.add_argument("--snapshots", type=int, default=100)
     ap.add_argument("--every", type=int, default=1000)
     ap.add_argument("--nve-steps", type=int, default=100000)
@@ -410,6 +458,9 @@ def main():
     args = ap.parse_args()
     if args.precision_study:
         precision_study(args)
+        return
+    if args.averages_study:
+        averages_study(args)
         return
     if args.warmup < 3:
         args.warmup = 3
