@@ -54,7 +54,7 @@ WORKLOADS = {
 
 # dram__bytes_read.sum + dram__bytes_write.sum of k_bonded_pairs + k_nonbonded_split per force
 # launch, from the ncu --set full capture summarised in profiles/ (cold caches)
-FORCE_TRAFFIC = {"plain40k": 7.292e6 + 2.3e+03 + 26.257e6, "large250k": 26.941e6 + 11.8e3 + 62.385e6 + 0.858e6}
+FORCE_TRAFFIC = {"plain40k": 7.293e6 + 8.4e3 + 26.257e6, "large250k": 26.941e6 + 25.1e3 + 62.383e6 + 0.946e6}
 
 
 def env_rank():
