@@ -146,7 +146,11 @@ int oxgb_verlet_destroy(oxgb_verlet *h);
 typedef struct oxgb_md oxgb_md;
 
 enum { OXGB_THERMOSTAT_NONE = 0, OXGB_THERMOSTAT_BROWNIAN = 1, OXGB_THERMOSTAT_BUSSI = 2 };
-enum { OXGB_PRECISION_MIXED = 0, OXGB_PRECISION_DOUBLE = 1 };
+/* backend_precision (src/Backends/BackendFactory.cpp:50-86): mixed = FP32 forces with FP64
+ * integration (the reference's default, MD_CUDAMixedBackend); double = FP64 throughout; float
+ * = FP32 forces and FP32 integration (src/CUDA/Backends/CUDA_MD.cuh:11-60,556-578: kicks,
+ * drift and rotation in FP32, the state FP32-representable) */
+enum { OXGB_PRECISION_MIXED = 0, OXGB_PRECISION_DOUBLE = 1, OXGB_PRECISION_FLOAT = 2 };
 
 /* MDBackend / thermostat input keys (src/Backends/MDBackend.cpp:25-90,
  * src/Backends/Thermostats/{Brownian,Bussi}Thermostat.cpp get_settings) */
@@ -159,7 +163,7 @@ typedef struct oxgb_md_settings {
 	double diff_coeff;          /* diff_coeff */
 	double bussi_tau;           /* bussi_tau */
 	uint64_t seed;              /* seed of the counter-based random stream */
-	int precision;              /* backend_precision: mixed (FP32 forces, FP64 state) or double */
+	int precision;              /* backend_precision: OXGB_PRECISION_MIXED, _DOUBLE or _FLOAT */
 	int cells_auto_optimisation;/* cells_auto_optimisation */
 	int max_neigh;              /* neighbour-row capacity; 0 = sized from the first build */
 	int steps_per_graph;        /* MD steps captured per CUDA graph launch (0 = 16) */
@@ -172,6 +176,12 @@ typedef struct oxgb_md_settings {
 	                               to an unsorted run; the state, forces and energies cross this
 	                               interface in the caller's order.  Device buffers and the rows of
 	                               oxgb_md_neighbours are in storage order (oxgb_md_storage_order). */
+	int autotune;               /* 1: the first oxgb_md_set_state times every shape of the MD step's
+	                               force kernels on that state and keeps the fastest (cached per size
+	                               class for later engines); 0: the default shape.  Shapes change the
+	                               work distribution, not the arithmetic of a pair.  The reference has
+	                               no counterpart (a fixed 64 threads per block,
+	                               src/CUDA/Backends/CUDABaseBackend.cu:244-261). */
 } oxgb_md_settings;
 
 void oxgb_md_default_settings(oxgb_md_settings *s);
@@ -264,6 +274,14 @@ int oxgb_md_info(oxgb_md *h, long long *n_rebuilds, long long *step, int *max_ne
 int oxgb_md_storage_order(oxgb_md *h, int *id);
 /* status bits raised by the kernels since the last call (and clears them): 0 = healthy */
 int oxgb_md_status(oxgb_md *h);
+/* the shape of the MD step's force kernels: nucleotides per pair-block warp queue, non-bonded
+ * lanes per nucleotide, the register cap as resident blocks per SM, and (autotuned engines) the
+ * measured launch time in microseconds (0 otherwise).  No counterpart in the reference. */
+int oxgb_md_force_shape(oxgb_md *h, int *pair_npw, int *nb_lanes, int *nb_min_blocks, double *launch_us);
+/* pins shape k (0 .. 5; 0 the default) of the MD step's force kernels, e.g. to repeat a tuned run
+ * on another engine; the forces of the current state are recomputed with it.  No counterpart in
+ * the reference. */
+int oxgb_md_set_force_shape(oxgb_md *h, int k);
 /* device pointers (for zero-copy callers): FP64 positions, velocities, angular momenta and
  * quaternions (double4 each), FP32 forces and torques (float4; double4 in double precision) */
 int oxgb_md_device_buffers(oxgb_md *h, void **pos, void **vel, void **L, void **quat, void **F, void **T);

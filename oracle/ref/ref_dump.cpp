@@ -6,8 +6,9 @@
 //     centre-of-mass shift, the orthonormalised frame a1 a2 a3, bonds, types);
 //   * per-particle forces (lab frame) and torques (body frame) from one full force
 //     evaluation, accumulated exactly as MD_CPUBackend::_compute_forces does
-//     (src/Backends/MD_CPUBackend.cpp:146-167): bonded pairs through `affected`, then
-//     every non-bonded pair once with the higher index first (src/Lists/Cells.cpp:168);
+//     (src/Backends/MD_CPUBackend.cpp:146-167): the external forces of the current step, bonded
+//     pairs through `affected`, then every non-bonded pair once with the higher index first
+//     (src/Lists/Cells.cpp:168);
 //   * the per-term energy split (src/Interactions/BaseInteraction.cpp:61-86);
 //   * when the input asks for steps > 0, the state after SimManager::run().
 //
@@ -75,10 +76,14 @@ int main(int argc, char *argv[]) {
 		}
 		dump_state(out, "state", true);
 
+		// forces start from the external forces, as in MD_CPUBackend::_compute_forces
+		// (src/Backends/MD_CPUBackend.cpp:146-155); zero without external forces
 		for(auto p : ps) {
 			p->force = LR_vector(0., 0., 0.);
 			p->torque = LR_vector(0., 0., 0.);
+			p->set_initial_forces(CONFIG_INFO->curr_step, CONFIG_INFO->box);
 		}
+		fprintf(out, "step %lld\n", (long long) CONFIG_INFO->curr_step);
 		inter->begin_energy_and_force_computation();
 		number U = 0.;
 		for(auto p : ps) {

@@ -57,6 +57,7 @@ class MDSettings(C.Structure):
         ("pt", C.c_double), ("diff_coeff", C.c_double), ("bussi_tau", C.c_double), ("seed", C.c_uint64),
         ("precision", C.c_int), ("cells_auto_optimisation", C.c_int), ("max_neigh", C.c_int),
         ("steps_per_graph", C.c_int), ("list_rebuild_node", C.c_int), ("sort_every", C.c_int),
+        ("autotune", C.c_int),
     ]
 
 
@@ -94,6 +95,9 @@ SIGNATURES = {
     "oxgb_md_scale_momenta": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_set_external_forces": (C.c_int, [_VP, C.c_int, C.POINTER(ExtForce)]),
     "oxgb_md_energies": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "oxgb_md_force_shape": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_double)]),
+    "oxgb_md_set_force_shape": (C.c_int, [_VP, C.c_int]),
     "oxgb_md_set_temperature": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_neighbours": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
     "oxgb_md_info": (C.c_int, [_VP, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),

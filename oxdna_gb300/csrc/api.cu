@@ -10,6 +10,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstdio>
 #include <climits>
 #include <cstring>
@@ -357,6 +360,7 @@ struct oxgb_md {
 
 	double4_32a *posd = nullptr, *veld = nullptr, *Ld = nullptr, *quatd = nullptr;
 	float4 *pos_hi = nullptr, *pos_lo = nullptr, *fa1 = nullptr, *fa3 = nullptr, *fback = nullptr, *list_pos = nullptr;
+	float4 *fa1lo = nullptr, *fbacklo = nullptr;  // remainders of fa1 / fback (FP32 engines)
 	float4 *list_a1 = nullptr, *list_back = nullptr;
 	int2 *bonds = nullptr;
 	void *F = nullptr, *T = nullptr, *bond_f = nullptr, *bond_tp = nullptr, *bond_tq = nullptr;
@@ -391,6 +395,10 @@ struct oxgb_md {
 	cudaGraphExec_t gexec = nullptr;
 	int graph_steps = 0;
 	bool conditional_ok = true;
+	// shape of the MD step's force kernels (force_shape_of) and its measured launch time
+	int shape = 0;
+	double shape_us = 0.0;
+	bool tuned = false;
 	long long host_step = 0, n_rebuilds = 0;
 	unsigned long long *d_rebuilds = nullptr;
 	// cell-order storage (md.sort_every > 0): caller's index of each slot and its inverse, the
@@ -412,7 +420,7 @@ struct oxgb_md {
 		if(gexec) cudaGraphExecDestroy(gexec);
 		free_layout();
 		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
-					(void *) fback, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, Fe, Te, bond_f,
+					(void *) fback, (void *) fa1lo, (void *) fbacklo, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, Fe, Te, bond_f,
 					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
@@ -472,6 +480,7 @@ static StepArgs step_args(oxgb_md *h, int step_offset = 0) {
 	StepArgs a{};
 	a.N = h->N;
 	a.dt = h->md.dt;
+	a.f32 = h->md.precision == OXGB_PRECISION_FLOAT;
 	a.pos = h->posd;
 	a.vel = h->veld;
 	a.angmom = h->Ld;
@@ -484,6 +493,8 @@ static StepArgs step_args(oxgb_md *h, int step_offset = 0) {
 	a.torques = h->T;
 	a.list_pos = h->list_pos;
 	a.fback = h->fback;
+	a.fa1lo = h->fa1lo;
+	a.fbacklo = h->fbacklo;
 	a.bonds = h->bonds;
 	a.list_a1 = h->list_a1;
 	a.list_back = h->list_back;
@@ -520,7 +531,10 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.tab_span = h->tab_span;
 	a.status = h->status;
 	a.esplit = h->esplit;
+	a.shape = h->shape;
 	a.fback = h->fback;
+	a.fa1lo = h->fa1lo;
+	a.fbacklo = h->fbacklo;
 	a.ev_nb = h->tl.ev_nb;
 	a.ev_n = h->tl.ev_n;
 	a.base_nb = h->tl.base_nb;
@@ -661,6 +675,8 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 		if(!(box[k] > 0)) return fail(OXGB_E_INVALID, "invalid box");
 	}
 	if(!(md->dt > 0) || md->verlet_skin < 0) return fail(OXGB_E_INVALID, "invalid dt or verlet_skin");
+	if(md->precision < OXGB_PRECISION_MIXED || md->precision > OXGB_PRECISION_FLOAT)
+		return fail(OXGB_E_INVALID, "precision must be mixed, double or float");
 	oxgb_md *h = new oxgb_md();
 	h->n_systems = n_systems;
 	h->N = N;
@@ -717,6 +733,10 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->fa3, sizeof(float4) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->list_pos, sizeof(float4) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->fback, sizeof(float4) * N) == cudaSuccess;
+	if(!h->dbl) {
+		ok &= cudaMalloc(&h->fa1lo, sizeof(float4) * N) == cudaSuccess;
+		ok &= cudaMalloc(&h->fbacklo, sizeof(float4) * N) == cudaSuccess;
+	}
 	ok &= cudaMalloc(&h->list_a1, sizeof(float4) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->list_back, sizeof(float4) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->bond_f, v4 * N) == cudaSuccess;
@@ -907,6 +927,7 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 		a.inv = h->d_inv;
 		a.st[0] = h->posd, a.st[1] = h->veld, a.st[2] = h->Ld, a.st[3] = h->quatd;
 		a.mir[0] = h->pos_hi, a.mir[1] = h->pos_lo, a.mir[2] = h->fa1, a.mir[3] = h->fa3, a.mir[4] = h->fback;
+		a.mir[5] = h->fa1lo, a.mir[6] = h->fbacklo;
 		a.bonds_rw = h->bonds;
 		a.scratch = h->sort_scratch;
 	}
@@ -929,6 +950,80 @@ static int compute_forces_now(oxgb_md *h) {
 	CK(launch_forces_split(fa, h->dbl, false, false, h->stream));
 	h->energies_fresh = false;
 	return OXGB_OK;
+}
+
+// ---------------------------------------------------------------- autotuner
+//
+// The MD step's force kernels come in a few shapes (nucleotides per pair-block warp queue,
+// non-bonded lanes per nucleotide and register cap; force_shape_of).  With md.autotune the first
+// state uploaded picks one: every shape runs the step's force evaluation on that state (its own
+// lists and tables), timed with CUDA events on the engine's stream (median of 3 rounds of 10
+// launches after 2 warm-up launches), and the fastest is kept for the engine's life.  The choice
+// is cached per size class (precision, log2 of the nucleotide count, log2 of the mean system
+// size), so engines of the same class reuse it without timing.
+
+static std::mutex g_tune_mutex;
+static std::map<std::tuple<int, int, int>, std::pair<int, double>> g_tune_cache;
+
+static int ilog2(long long v) {
+	int k = 0;
+	while(v > 1) {
+		v >>= 1;
+		k++;
+	}
+	return k;
+}
+
+static int autotune_shape(oxgb_md *h) {
+	if(h->dbl || h->tuned) return OXGB_OK;
+	const auto key = std::make_tuple(h->md.precision, ilog2(h->N), ilog2(h->N / h->n_systems));
+	{
+		std::lock_guard<std::mutex> lock(g_tune_mutex);
+		auto it = g_tune_cache.find(key);
+		if(it != g_tune_cache.end()) {
+			h->shape = it->second.first;
+			h->shape_us = it->second.second;
+			h->tuned = true;
+			return OXGB_OK;
+		}
+	}
+	cudaEvent_t e0, e1;
+	CK(cudaEventCreate(&e0));
+	CK(cudaEventCreate(&e1));
+	int best = 0;
+	double best_us = 1e30;
+	for(int k = 0; k < force_shape_count(); k++) {
+		ForceArgs fa = force_args(h);
+		fa.shape = k;
+		for(int w = 0; w < 2; w++) CK(launch_forces_split(fa, false, false, false, h->stream));
+		std::vector<double> t;
+		for(int rep = 0; rep < 3; rep++) {
+			CK(cudaEventRecord(e0, h->stream));
+			for(int r = 0; r < 10; r++) CK(launch_forces_split(fa, false, false, false, h->stream));
+			CK(cudaEventRecord(e1, h->stream));
+			CK(cudaEventSynchronize(e1));
+			float ms = 0.f;
+			CK(cudaEventElapsedTime(&ms, e0, e1));
+			t.push_back(ms * 100.0);  // us per launch
+		}
+		std::sort(t.begin(), t.end());
+		if(t[1] < best_us) {
+			best_us = t[1];
+			best = k;
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	h->shape = best;
+	h->shape_us = best_us;
+	h->tuned = true;
+	{
+		std::lock_guard<std::mutex> lock(g_tune_mutex);
+		g_tune_cache[key] = std::make_pair(best, best_us);
+	}
+	// the forces of the state, from the chosen shape (the same values: shapes differ in work
+	// distribution and summation order only)
+	return compute_forces_now(h);
 }
 
 static int compute_energies_now(oxgb_md *h, bool split) {
@@ -1034,8 +1129,33 @@ extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *qu
 	if(rc) return rc;
 	rc = compute_forces_now(h);
 	if(rc) return rc;
+	if(h->md.autotune) {
+		rc = autotune_shape(h);
+		if(rc) return rc;
+	}
 	h->have_state = true;
 	return read_status(h);
+}
+
+extern "C" int oxgb_md_set_force_shape(oxgb_md *h, int k) {
+	if(!h) return fail(OXGB_E_INVALID, "null handle");
+	if(k < 0 || k >= force_shape_count()) return fail(OXGB_E_INVALID, "no such force-kernel shape");
+	if(h->dbl && k != 0) return fail(OXGB_E_INVALID, "double precision has the default shape only");
+	h->shape = k;
+	h->tuned = false;
+	h->shape_us = 0.0;
+	if(h->gexec) {  // the step graph holds the old shape's kernels: captured again at the next run
+		cudaGraphExecDestroy(h->gexec);
+		h->gexec = nullptr;
+	}
+	return h->have_state ? compute_forces_now(h) : OXGB_OK;
+}
+
+extern "C" int oxgb_md_force_shape(oxgb_md *h, int *pair_npw, int *nb_lanes, int *nb_min_blocks, double *launch_us) {
+	if(!h) return fail(OXGB_E_INVALID, "null handle");
+	force_shape_of(h->dbl ? 0 : h->shape, pair_npw, nb_lanes, nb_min_blocks);
+	if(launch_us) *launch_us = h->tuned ? h->shape_us : 0.0;
+	return OXGB_OK;
 }
 
 extern "C" int oxgb_md_get_state(oxgb_md *h, double *pos, double *quat, double *vel, double *L) {

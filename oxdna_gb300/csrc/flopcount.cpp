@@ -41,6 +41,7 @@ inline CF m_exp(CF x) { g_sfu += 1; return CF(std::exp(x.v)); }
 inline CF m_expm1(CF x) { g_sfu += 1; return CF(std::expm1(x.v)); }
 inline CF m_log(CF x) { g_sfu += 1; return CF(std::log(x.v)); }
 inline CF m_acos(CF x) { g_sfu += 1; return CF(std::acos(x.v)); }
+inline CF m_atan2(CF y, CF x) { g_sfu += 1; return CF(std::atan2(y.v, x.v)); }
 inline CF m_fabs(CF x) { return CF(std::fabs(x.v)); }
 inline CF m_fma(CF a, CF b, CF c) { g_flops += 2; return CF(std::fma(a.v, b.v, c.v)); }
 inline CF m_rint(CF x) { return CF(std::rint(x.v)); }
@@ -73,8 +74,12 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 	to_float(P64, box, P32);
 	DNA2Table<CF> P;
 	std::memcpy(&P, &P32, sizeof(P));
-	// the split force path: every bond once (both nucleotides), Debye-Hueckel over the full rows,
-	// the other terms over the pairs their term lists admit (same bounds as the list build)
+	// the algorithmic work of one force evaluation: every bond once (both nucleotides), and every
+	// unordered non-bonded pair once (from its lower index), each term over the pairs its term
+	// list admits (same bounds as the list build).  A pair function forms the force and the
+	// torque on its first nucleotide; the partner's torque, -T_p + d x F, adds 12 FLOPs.  Work
+	// the kernels repeat (Debye-Hueckel and excluded volume are evaluated from both ends of the
+	// full rows) is not counted, so it shows as lost efficiency.
 	const TermRadii tr = term_radii(skin);
 	g_flops = g_sfu = 0;
 	double pairs = 0, in_range = 0;
@@ -100,6 +105,7 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 		const int nn = nnb[i] < max_nb ? nnb[i] : max_nb;
 		for(int k = 0; k < nn; k++) {
 			const int j = nb[(long long) i * max_nb + k];
+			if(j < i) continue;
 			Nuc<CF> q;
 			load(j, q);
 			double d[3];
@@ -115,7 +121,7 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 			PairOut<CF> o{};
 			pair_dh<CF, false>(P, p, q, sp.plain(), o);
 			if(r2 < tr.ev2) {
-				pair_ev<CF, false>(p, q, sp.plain(), o);
+				pair_ev<CF, false>(p, q, sp, o);
 				double bb = 0, ss = 0;
 				for(int c = 0; c < 3; c++) {
 					const double da = a1[3 * j + c] - a1[3 * i + c];
@@ -125,6 +131,7 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 				if(bb < tr.base2) pair_base<CF, false>(P, p, q, sp, o);
 				if(ss < tr.stk2) pair_stack<CF, false>(P, p, q, sp, o);
 			}
+			g_flops += 12;  // the partner's torque
 			pairs += 1;
 			if(r2 < rcut * rcut) in_range += 1;
 		}

@@ -355,8 +355,56 @@ cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s) {
 
 namespace oxgb {
 
+// the remainders of nucleotide k's a1 and backbone offset (written with the mirrors)
+__device__ __forceinline__ SiteLo site_lo(const float4 *a1lo, const float4 *backlo, int k) {
+	const float4 u = __ldg(a1lo + k), v = __ldg(backlo + k);
+	return SiteLo{v3<float>{u.x, u.y, u.z}, v3<float>{v.x, v.y, v.z}};
+}
+
+// the refined excluded volume of a stiff bonded contact (rare): out of line, so that the kernel's
+// register allocation stays that of its common path
+template <int K>
+__device__ __noinline__ float ev_refined_call(const float4 *a1lo, const float4 *backlo, int i, int j, Sep<float> sep,
+		v3<float> ps, v3<float> pa1, int pbase, v3<float> qs, v3<float> qa1, int qbase, v3<float> *f) {
+	v3<float> fo;
+	const float e = ev_refined<K>(sep, ps, pa1, site_lo(a1lo, backlo, i), pbase, qs, qa1, site_lo(a1lo, backlo, j), qbase, fo);
+	*f = fo;
+	return e;
+}
+
+// a non-bonded pair with a site pair inside its excluded-volume cutoff, refined: force and torque
+// on nucleotide i (of p) and the energy (rare; out of line, so that the non-bonded kernel's loops
+// keep their register allocation)
+__device__ __noinline__ float4 ev_pair_refined_call(const float4 *a1lo, const float4 *backlo, int i, int j, float4 sh,
+		float4 sl, float4 pb, float4 pk, float4 pa, float4 qb, float4 qk, float4 qa, float3 *T) {
+	Nuc<float> p, q;
+	p.back = v3<float>{pb.x, pb.y, pb.z}, p.base = v3<float>{pk.x, pk.y, pk.z}, p.a1 = v3<float>{pa.x, pa.y, pa.z};
+	q.back = v3<float>{qb.x, qb.y, qb.z}, q.base = v3<float>{qk.x, qk.y, qk.z}, q.a1 = v3<float>{qa.x, qa.y, qa.z};
+	const Sep<float> sep{v3<float>{sh.x, sh.y, sh.z}, v3<float>{sl.x, sl.y, sl.z}};
+	v3<float> F{0.f, 0.f, 0.f}, t{0.f, 0.f, 0.f};
+	const float e = pair_ev_refined(sep, p, site_lo(a1lo, backlo, i), q, site_lo(a1lo, backlo, j), F, t);
+	*T = make_float3(t.x, t.y, t.z);
+	return make_float4(F.x, F.y, F.z, e);
+}
+
+// refines the FP32 engine path for pair (i, j): the site offsets' remainders for the stiff
+// radial factors, and the stiff excluded-volume contacts
+struct StoredLo {
+	static constexpr bool on = true;
+	const float4 *a1lo, *backlo;
+	int i, j;
+	__device__ __forceinline__ SiteLo lo(int which) const { return site_lo(a1lo, backlo, which ? j : i); }
+	template <int K>
+	__device__ __forceinline__ float ev(const Sep<float> &sep, v3<float> ps, v3<float> pa1, int pbase, v3<float> qs,
+			v3<float> qa1, int qbase, v3<float> &f) const {
+		return ev_refined_call<K>(a1lo, backlo, i, j, sep, ps, pa1, pbase, qs, qa1, qbase, &f);
+	}
+};
+
 struct SplitMixed {
 	const float4 *hi, *lo, *fa1, *fa3, *fback;
+	const float4 *a1lo, *backlo;  // remainders of fa1 / fback (StoredLo)
+	__device__ __forceinline__ StoredLo refine(int i, int j) const { return StoredLo{a1lo, backlo, i, j}; }
 	__device__ __forceinline__ void full(int j, Nuc<float> &n, float4 &h, float4 &l) const {
 		h = __ldg(hi + j);
 		l = __ldg(lo + j);
@@ -395,6 +443,7 @@ struct SplitDouble {
 	const double4_32a *pos, *quat;
 	const float4 *meta, *meta_lo;
 	const int2 *bonds;
+	__device__ __forceinline__ NoRefine refine(int, int) const { return NoRefine{}; }
 	__device__ __forceinline__ Sep<double> sep(const double4_32a &p, const double4_32a &, const double4_32a &q,
 			const double4_32a &, const DNA2Table<double> &P) const {
 		return LoadDouble{}.sep(p, p, q, q, P);
@@ -455,7 +504,7 @@ __device__ __forceinline__ void bonded_block(const ForceArgs &a, const Loader &l
 		load_full<Loader, R>(ld, p, P, np, ph, pl);
 		load_full<Loader, R>(ld, q, P, nq, qh, ql);
 		BondOut<R> b;
-		if(!bonded_both(P, np, nq, ld.diff(ph, pl, qh, ql), b)) atomicOr(a.status, OXGB_ERR_FENE);
+		if(!bonded_both(P, np, nq, ld.diff(ph, pl, qh, ql), b, ld.refine(p, q))) atomicOr(a.status, OXGB_ERR_FENE);
 		V4 f, tp, tq;
 		f.x = b.f.x, f.y = b.f.y, f.z = b.f.z, f.w = ENERGY ? b.E : R(0);
 		tp.x = b.tp.x, tp.y = b.tp.y, tp.z = b.tp.z, tp.w = R(0);
@@ -583,14 +632,24 @@ __device__ __noinline__ void eval_terms(const ForceArgs &a, const Loader &ld, co
 	load_full<Loader, R>(ld, j, P, qn, qh, ql);
 	const Sep<R> d = ld.sep(ph, pl, qh, ql, P);
 	PairOut<R> o{};
+	// FP32 engine path: the remainder of the site distance (the stiff radial factors, see rdiff)
+	const auto x = ld.refine(i, j);
 	if(term == 2) {
 		const StackGeo<R> g = stack_geo(P, p, qn, d);
-		if(g.cxst) cxst_term<R, SPLIT>(P, p, qn, g, o);
+		R rl = R(0);
+		if constexpr(decltype(x)::on) {
+			if(g.cxst) rl = site_dist_remainder(d, p, x.lo(0), qn, x.lo(1), true, g.rmod);
+		}
+		if(g.cxst) cxst_term<R, SPLIT>(P, p, qn, g, o, rl);
 	}
 	else {
 		const BaseGeo<R> g = base_geo(P, p, qn, d);
-		if(term == 0 && g.hb) hb_term<R, SPLIT>(P, p, qn, g, o);
-		if(term == 1 && g.crst) crst_term<R, SPLIT>(P, p, qn, g, o);
+		R rl = R(0);
+		if constexpr(decltype(x)::on) {
+			if((term == 0 && g.hb) || (term == 1 && g.crst)) rl = site_dist_remainder(d, p, x.lo(0), qn, x.lo(1), false, g.rmod);
+		}
+		if(term == 0 && g.hb) hb_term<R, SPLIT>(P, p, qn, g, o, rl);
+		if(term == 1 && g.crst) crst_term<R, SPLIT>(P, p, qn, g, o, rl);
 	}
 	// the potential is invariant under rigid rotations, so the torques balance:
 	// T_j = -T_i + (r_j - r_i) x F_i, the cross product with error-free products
@@ -620,10 +679,9 @@ __device__ __noinline__ void eval_terms(const ForceArgs &a, const Loader &ld, co
 // windows and angular supports); only about a third of the pairs has a non-zero term, so the
 // live terms go to per-warp queues in shared memory and are evaluated 32 at a time, every lane
 // on the same term, instead of on the few lanes of each round whose pair happens to be live.
-template <typename R, class Loader, bool SPLIT, bool ENERGY>
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int NPW>
 __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld, int b, int base_blocks) {
 	using V4 = typename Vec4Of<R>::T;
-	constexpr int NPW = OXGB_PAIR_NPW;
 	__shared__ int4 tq[4][2][64];  // per warp: live hydrogen-bonding (or coaxial) and cross-stacking terms
 	const bool is_base = b < base_blocks;
 	const int per_block = (blockDim.x / 32) * NPW;
@@ -739,11 +797,11 @@ __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld,
 #define OXGB_PAIR_MINB 5
 #endif
 
-template <typename R, class Loader, bool SPLIT, bool ENERGY>
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int NPW = OXGB_PAIR_NPW>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_PAIR_MINB : 1) k_bonded_pairs(ForceArgs a, Loader ld, int pair_blocks) {
 	pdl_trigger();  // the non-bonded kernel may start (it waits before reading these results)
 	const int b = blockIdx.x;
-	if(b < 2 * pair_blocks) pair_block<R, Loader, SPLIT, ENERGY>(a, ld, b, pair_blocks);
+	if(b < 2 * pair_blocks) pair_block<R, Loader, SPLIT, ENERGY, NPW>(a, ld, b, pair_blocks);
 	else bonded_block<R, Loader, SPLIT, ENERGY>(a, ld, b - 2 * pair_blocks);
 }
 
@@ -772,8 +830,8 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 #define OXGB_NB_MINB 8
 #endif
 
-template <typename R, class Loader, bool SPLIT, bool ENERGY, int K>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonbonded_split(ForceArgs a, Loader ld) {
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int K, int MINB = OXGB_NB_MINB>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	const long long N = a.N;
 	const int sub = threadIdx.x % K;
@@ -806,14 +864,53 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 		}
 		// excluded volume over centre-close pairs
 		const int nev = live ? min(a.ev_n[i], a.ev_cap) : 0;
-		for(int k = sub; k < nev; k += K) {
-			const int j = a.ev_nb[(long long) k * N + i];
-			Nuc<R> q;
-			V4 qh, ql;
-			load_full<Loader, R>(ld, j, P, q, qh, ql);
-			PairOut<R> o{};
-			pair_ev<R, SPLIT>(p, q, ld.sep(ph, pl, qh, ql, P).plain(), o);
-			acc.add_short(o);
+		if constexpr(decltype(ld.refine(0, 0))::on) {
+			// FP32: each window of 64 of the lane's entries is screened (a site pair inside its
+			// cutoff: a few in a thousand entries); the pairs found are evaluated refined after the
+			// window, outside the screening loop, and the others contribute nothing
+			for(int w0 = 0; w0 < nev; w0 += 64 * K) {
+				const int wend = min(nev, w0 + 64 * K);
+				unsigned long long stiff = 0ull;
+				int m = 0;
+				for(int k = w0 + sub; k < wend; k += K, m++) {
+					const int j = a.ev_nb[(long long) k * N + i];
+					Nuc<R> q;
+					V4 qh, ql;
+					load_full<Loader, R>(ld, j, P, q, qh, ql);
+					if(ev_contact(p, q, ld.sep(ph, pl, qh, ql, P).plain())) stiff |= 1ull << m;
+				}
+				while(stiff) {
+					const int mm = __ffsll((long long) stiff) - 1;
+					stiff &= stiff - 1ull;
+					const int j = a.ev_nb[(long long) (w0 + sub + mm * K) * N + i];
+					Nuc<R> q;
+					V4 qh, ql;
+					load_full<Loader, R>(ld, j, P, q, qh, ql);
+					PairOut<R> o{};
+					const Sep<R> sp = ld.sep(ph, pl, qh, ql, P);
+					float3 t;
+					const float4 fe = ev_pair_refined_call(
+							ld.a1lo, ld.backlo, i, j, make_float4(sp.hi.x, sp.hi.y, sp.hi.z, 0.f), make_float4(sp.lo.x, sp.lo.y, sp.lo.z, 0.f),
+							make_float4(p.back.x, p.back.y, p.back.z, 0.f), make_float4(p.base.x, p.base.y, p.base.z, 0.f),
+							make_float4(p.a1.x, p.a1.y, p.a1.z, 0.f), make_float4(q.back.x, q.back.y, q.back.z, 0.f),
+							make_float4(q.base.x, q.base.y, q.base.z, 0.f), make_float4(q.a1.x, q.a1.y, q.a1.z, 0.f), &t);
+					o.F = v3<R>{fe.x, fe.y, fe.z};
+					o.T = v3<R>{t.x, t.y, t.z};
+					add_e<R, SPLIT>(o, T_NEXC, fe.w);
+					acc.add_short(o);
+				}
+			}
+		}
+		else {
+			for(int k = sub; k < nev; k += K) {
+				const int j = a.ev_nb[(long long) k * N + i];
+				Nuc<R> q;
+				V4 qh, ql;
+				load_full<Loader, R>(ld, j, P, q, qh, ql);
+				PairOut<R> o{};
+				pair_ev<R, SPLIT>(p, q, ld.sep(ph, pl, qh, ql, P), o);
+				acc.add_short(o);
+			}
 		}
 		// hydrogen bonding + cross stacking and coaxial stacking: evaluated per list slot by
 		// the pair blocks of k_bonded_pairs, gathered here (the terms above read only the
@@ -877,9 +974,28 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_NB_MINB : 1) k_nonb
 #define OXGB_NB_LANES 4
 #endif
 
-int nonbonded_blocks(int N) {
-	const long long threads = (long long) (N > 0 ? N : 1) * OXGB_NB_LANES;
+int nonbonded_blocks(int N, int lanes) {
+	const long long threads = (long long) (N > 0 ? N : 1) * lanes;
 	return (int) ((threads + 127) / 128);
+}
+
+// The shapes of the MD step's force kernels (engine, mixed and float precision) the autotuner
+// chooses among: nucleotides per pair-block warp queue, lanes per nucleotide in the non-bonded
+// kernel and the resident blocks per SM its register cap asks for.  Shape 0 is the default, the
+// best of hand sweeps on the 40k and 250k workloads.
+struct ForceShapeDef {
+	int npw, lanes, minb;
+};
+constexpr ForceShapeDef FORCE_SHAPES[] = {{32, 4, 8}, {16, 4, 8}, {32, 8, 6}, {16, 8, 6}, {32, 2, 8}, {16, 2, 8}};
+constexpr int N_FORCE_SHAPES = sizeof(FORCE_SHAPES) / sizeof(FORCE_SHAPES[0]);
+
+int force_shape_count() { return N_FORCE_SHAPES; }
+
+void force_shape_of(int k, int *npw, int *lanes, int *minb) {
+	const ForceShapeDef &d = FORCE_SHAPES[k >= 0 && k < N_FORCE_SHAPES ? k : 0];
+	if(npw) *npw = d.npw;
+	if(lanes) *lanes = d.lanes;
+	if(minb) *minb = d.minb;
 }
 
 // External forces (CUDA_MD.cuh:97-200): one thread per nucleotide that has some, its records
@@ -959,30 +1075,46 @@ __global__ void k_external(ForceArgs a) {
 	F[i] = f;
 }
 
-template <typename R, class Loader, bool SPLIT, bool ENERGY>
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int NPW = OXGB_PAIR_NPW, int K = OXGB_NB_LANES,
+		int NBMINB = OXGB_NB_MINB>
 static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEvent_t wait) {
 	const int tpb = 128;
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	const size_t smem = sizeof(DNA2Table<R>) * (size_t) (a.tab_span > 0 ? a.tab_span : 1);
-	// pair blocks of 4 warps x OXGB_PAIR_NPW nucleotides per term, then one bonded block per
-	// 128 nucleotides
-	const int pair_blocks = (a.N + 4 * OXGB_PAIR_NPW - 1) / (4 * OXGB_PAIR_NPW);
-	k_bonded_pairs<R, Loader, SPLIT, ENERGY><<<2 * pair_blocks + blocks, tpb, smem, s>>>(a, ld, pair_blocks);
+	// pair blocks of 4 warps x NPW nucleotides per term, then one bonded block per 128
+	// nucleotides
+	const int pair_blocks = (a.N + 4 * NPW - 1) / (4 * NPW);
+	k_bonded_pairs<R, Loader, SPLIT, ENERGY, NPW><<<2 * pair_blocks + blocks, tpb, smem, s>>>(a, ld, pair_blocks);
 	// the non-bonded kernel starts its Debye-Hueckel and excluded-volume work while the tail of
 	// the bonded and pair blocks runs; the external forces follow it the same way
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
-	constexpr int K = OXGB_NB_LANES;
-	if(wait) k_nonbonded_split<R, Loader, SPLIT, ENERGY, K><<<nonbonded_blocks(a.N), tpb, smem, s>>>(a, ld);
-	else launch_after(k_nonbonded_split<R, Loader, SPLIT, ENERGY, K>, dim3(nonbonded_blocks(a.N)), dim3(tpb), smem, s, a, ld);
+	if(wait) k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB><<<nonbonded_blocks(a.N, K), tpb, smem, s>>>(a, ld);
+	else launch_after(k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB>, dim3(nonbonded_blocks(a.N, K)), dim3(tpb), smem, s, a,
+			ld);
 	if(a.ext_n > 0) launch_after(k_external<typename Vec4Of<R>::T>, dim3((a.ext_n + tpb - 1) / tpb), dim3(tpb), 0, s, a);
 }
 
-template <typename R, class Loader, bool SPLIT, bool ENERGY>
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int NPW = OXGB_PAIR_NPW, int K = OXGB_NB_LANES,
+		int NBMINB = OXGB_NB_MINB>
 static cudaError_t allow_smem_t(int bytes) {
-	cudaError_t e = cudaFuncSetAttribute(k_bonded_pairs<R, Loader, SPLIT, ENERGY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaError_t e = cudaFuncSetAttribute(k_bonded_pairs<R, Loader, SPLIT, ENERGY, NPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	if(e == cudaSuccess)
-		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, SPLIT, ENERGY, OXGB_NB_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				bytes);
 	return e;
+}
+
+// the MD step's kernels (mixed / float engine) in shape k of FORCE_SHAPES
+template <int k>
+static void launch_md_shape(const ForceArgs &a, const SplitMixed &ld, cudaStream_t s, cudaEvent_t wait) {
+	constexpr ForceShapeDef d = FORCE_SHAPES[k];
+	launch_split_t<float, SplitMixed, false, false, d.npw, d.lanes, d.minb>(a, ld, s, wait);
+}
+
+template <int k>
+static cudaError_t allow_smem_shape(int bytes) {
+	constexpr ForceShapeDef d = FORCE_SHAPES[k];
+	return allow_smem_t<float, SplitMixed, false, false, d.npw, d.lanes, d.minb>(bytes);
 }
 
 template <typename R, class Loader>
@@ -990,6 +1122,13 @@ static cudaError_t allow_smem(int bytes) {
 	cudaError_t e = allow_smem_t<R, Loader, true, true>(bytes);
 	if(e == cudaSuccess) e = allow_smem_t<R, Loader, false, true>(bytes);
 	if(e == cudaSuccess) e = allow_smem_t<R, Loader, false, false>(bytes);
+	if constexpr(sizeof(R) == 4) {
+		if(e == cudaSuccess) e = allow_smem_shape<1>(bytes);
+		if(e == cudaSuccess) e = allow_smem_shape<2>(bytes);
+		if(e == cudaSuccess) e = allow_smem_shape<3>(bytes);
+		if(e == cudaSuccess) e = allow_smem_shape<4>(bytes);
+		if(e == cudaSuccess) e = allow_smem_shape<5>(bytes);
+	}
 	return e;
 }
 
@@ -1007,10 +1146,20 @@ cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool e
 		else launch_split_t<double, SplitDouble, false, false>(a, ld, s, wait);
 	}
 	else {
-		SplitMixed ld{a.pos_hi, a.pos_lo, a.fa1, a.fa3, a.fback};
+		SplitMixed ld{a.pos_hi, a.pos_lo, a.fa1, a.fa3, a.fback, a.fa1lo, a.fbacklo};
 		if(split) launch_split_t<float, SplitMixed, true, true>(a, ld, s, wait);
 		else if(energy) launch_split_t<float, SplitMixed, false, true>(a, ld, s, wait);
-		else launch_split_t<float, SplitMixed, false, false>(a, ld, s, wait);
+		else {
+			static_assert(N_FORCE_SHAPES == 6, "one case per shape");
+			switch(a.shape) {
+			case 1: launch_md_shape<1>(a, ld, s, wait); break;
+			case 2: launch_md_shape<2>(a, ld, s, wait); break;
+			case 3: launch_md_shape<3>(a, ld, s, wait); break;
+			case 4: launch_md_shape<4>(a, ld, s, wait); break;
+			case 5: launch_md_shape<5>(a, ld, s, wait); break;
+			default: launch_md_shape<0>(a, ld, s, wait); break;
+			}
+		}
 	}
 	return cudaGetLastError();
 }

@@ -35,14 +35,21 @@ __device__ __forceinline__ float3 mirror_position(const StepArgs &a, int i, cons
 	return make_float3(hi.x, hi.y, hi.z);
 }
 
-// returns a1 and the backbone offset
+// returns a1 and the backbone offset; with a.fa1lo also the remainders of a1 and the backbone
+// offset (exact value = mirror + remainder to ~2^-46), which the force kernels use for the stiff
+// radial factors and excluded-volume contacts
 __device__ __forceinline__ void mirror_frame(const StepArgs &a, int i, const double4_32a &q, float3 &a1o, float3 &backo) {
-	float qh[4], ql[4], a1[3], a3[3], bk[3];
+	float qh[4], ql[4], a1[3], a3[3], bk[3], a1l[3], bkl[3];
 	split_rn(q.x, qh[0], ql[0]);
 	split_rn(q.y, qh[1], ql[1]);
 	split_rn(q.z, qh[2], ql[2]);
 	split_rn(q.w, qh[3], ql[3]);
-	frame_mirror(qh, ql, OXM_POS_MM_BACK1, OXM_POS_MM_BACK2, a1, a3, bk);
+	if(a.fa1lo) {
+		frame_mirror_rem(qh, ql, OXM_POS_MM_BACK1, OXM_POS_MM_BACK2, a1, a3, bk, a1l, bkl);
+		a.fa1lo[i] = make_float4(a1l[0], a1l[1], a1l[2], 0.f);
+		a.fbacklo[i] = make_float4(bkl[0], bkl[1], bkl[2], 0.f);
+	}
+	else frame_mirror(qh, ql, OXM_POS_MM_BACK1, OXM_POS_MM_BACK2, a1, a3, bk);
 	a.fa1[i] = make_float4(a1[0], a1[1], a1[2], 0.f);
 	a.fa3[i] = make_float4(a3[0], a3[1], a3[2], 0.f);
 	// the strand-end flag rides in w
@@ -139,12 +146,41 @@ __device__ __forceinline__ void rotate(double4_32a &q, const double4_32a &L, dou
 	q = make_double4_32a(n.x * inv, n.y * inv, n.z * inv, n.w * inv);
 }
 
+// The FP32 rotation of backend_precision = float (CUDA_MD.cuh:11-25): q <- q * (sin(th/2) L^,
+// cos(th/2)), th = dt |L|, in FP32; renormalised in FP32 as well (the reference's float path
+// lets the norm drift)
+__device__ __forceinline__ void rotate_f32(float4 &q, float3 L, float dt) {
+	const float L2 = L.x * L.x + L.y * L.y + L.z * L.z;
+	if(!(L2 > 0.f)) return;
+	const float norm = sqrtf(L2);
+	float sh, ch;
+	sincosf(0.5f * dt * norm, &sh, &ch);
+	const float k = sh / norm;
+	const float rx = L.x * k, ry = L.y * k, rz = L.z * k, rw = ch;
+	float4 n;
+	n.w = q.w * rw - q.x * rx - q.y * ry - q.z * rz;
+	n.x = q.w * rx + q.x * rw + q.y * rz - q.z * ry;
+	n.y = q.w * ry - q.x * rz + q.y * rw + q.z * rx;
+	n.z = q.w * rz + q.x * ry - q.y * rx + q.z * rw;
+	const float inv = rsqrtf(n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w);
+	q = make_float4(n.x * inv, n.y * inv, n.z * inv, n.w * inv);
+}
+
+__device__ __forceinline__ double4_32a widen4(float x, float y, float z, float w) {
+	return make_double4_32a(widen(x), widen(y), widen(z), widen(w));
+}
+
+// a state vector rounded to FP32 (backend_precision = float keeps the state FP32-representable)
+__device__ __forceinline__ double4_32a round4(const double4_32a &v) {
+	return widen4(narrow(v.x), narrow(v.y), narrow(v.z), narrow(v.w));
+}
+
 // First half of step s, two warps per 32 nucleotides: warp 0 of a block the translation (second
 // half kick and thermostat of step s - 1, half kick, drift, position mirror), warp 1 the
 // rotation (the same for the angular momentum, rotation, frame mirror).  The chains of FP64
 // operations are half as long and twice as many warps hide them; a warp never diverges on the
 // kind of motion.
-template <typename V4>
+template <typename V4, bool F32 = false>
 __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 	__shared__ float3 s_a1[32], s_bk[32];
 	const int lane = threadIdx.x & 31;
@@ -176,7 +212,59 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 	pdl_wait();
 	pdl_trigger();
 	if(!early) load_state();
-	if(live) {
+	if constexpr(F32) {
+		if(live) {
+		// backend_precision = float (CUDA_MD.cuh:11-60,556-578): the kicks, the drift and the
+		// rotation in FP32 arithmetic on the FP32-representable state (exact conversions); the
+		// thermostats act in FP64 on the completed momenta, rounded back to FP32
+		const long long s = step_of(a.th);
+		const float dt = (float) a.dt, hdt = 0.5f * dt;
+		const bool complete = *a.th.open_step == s - 1;
+		const long long sp = s - 1;
+		const bool brownian = complete && a.th.thermostat == 1 && sp % a.th.newtonian_steps == 0;
+		const bool bussi = complete && a.th.thermostat == 2 && *a.th.bussi_stamp == sp;
+		const V4 G = reinterpret_cast<const V4 *>(rot ? a.torques : a.forces)[i];
+		const float gx = (float) G.x, gy = (float) G.y, gz = (float) G.z;
+		float3 u = make_float3(narrow(x.x), narrow(x.y), narrow(x.z));
+		if(complete) {
+			u.x += gx * hdt;
+			u.y += gy * hdt;
+			u.z += gz * hdt;
+			if(brownian || bussi) {
+				x = widen4(u.x, u.y, u.z, 0.f);
+				if(brownian) x = brownian_redraw_part(a.th, sy, (a.th.id ? a.th.id[i] : i) - a.th.sys_off[sy], sp, rot ? 1 : 0, x);
+				else bussi_rescale_part(a.th, sy, rot ? 1 : 0, x);
+				u = make_float3(narrow(x.x), narrow(x.y), narrow(x.z));
+			}
+		}
+		u.x += gx * hdt;
+		u.y += gy * hdt;
+		u.z += gz * hdt;
+		x = widen4(u.x, u.y, u.z, 0.f);
+		if(!rot) {
+			float3 r = make_float3(narrow(y.x), narrow(y.y), narrow(y.z));
+			r.x += u.x * dt;
+			r.y += u.y * dt;
+			r.z += u.z * dt;
+			const double4_32a rd = widen4(r.x, r.y, r.z, 0.f);
+			a.vel[i] = x;
+			a.pos[i] = rd;
+			r32 = mirror_position(a, i, rd);
+		}
+		else {
+			float4 q = make_float4(narrow(y.x), narrow(y.y), narrow(y.z), narrow(y.w));
+			rotate_f32(q, u, dt);
+			const double4_32a qd = widen4(q.x, q.y, q.z, q.w);
+			a.angmom[i] = x;
+			a.quat[i] = qd;
+			float3 a1, bk;
+			mirror_frame(a, i, qd, a1, bk);
+			s_a1[lane] = a1;
+			s_bk[lane] = bk;
+		}
+		}
+	}
+	else if(live) {
 		const long long s = step_of(a.th);
 		const double hdt = 0.5 * a.dt;
 		// the previous step's second half kick and thermostat (kept as a separate half kick, so
@@ -295,12 +383,12 @@ __device__ __forceinline__ T warp_transpose_sum8(const T (&x)[8], Add add) {
 __device__ __forceinline__ void block_sum8(const double (&x)[8], double *red) {
 	__shared__ double part[8][8];
 	const double t = warp_transpose_sum8(x, [](double p, double q) { return p + q; });
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 	if((lane & 3) == 0) part[lane >> 2][w] = t;
 	__syncthreads();
 	if(threadIdx.x < 8) {
 		double r = 0;
-		for(int u = 0; u < 8; u++) r += part[threadIdx.x][u];
+		for(int u = 0; u < nw; u++) r += part[threadIdx.x][u];
 		red[threadIdx.x] = r;
 	}
 }
@@ -492,8 +580,8 @@ __global__ void k_step_flush(StepArgs a) {
 	const V4 T = reinterpret_cast<const V4 *>(a.torques)[i];
 	double4_32a v = a.vel[i], L = a.angmom[i];
 	complete_step(a.th, i, a.th.sys[i], sp, F, T, v, L);
-	a.vel[i] = v;
-	a.angmom[i] = L;
+	a.vel[i] = a.f32 ? round4(v) : v;
+	a.angmom[i] = a.f32 ? round4(L) : L;
 }
 
 // ... after which nothing is pending
@@ -522,10 +610,19 @@ __global__ void k_unpack_state(StepArgs a, const double *in, int *bad, int check
 		n = 1.0;
 	}
 	if(check_only) return;
-	a.pos[i] = make_double4_32a(p[0], p[1], p[2], 0.0);
-	a.quat[i] = make_double4_32a(__ddiv_rn(q[0], n), __ddiv_rn(q[1], n), __ddiv_rn(q[2], n), __ddiv_rn(q[3], n));
-	a.vel[i] = make_double4_32a(v[0], v[1], v[2], 0.0);
-	a.angmom[i] = make_double4_32a(l[0], l[1], l[2], 0.0);
+	double4_32a P = make_double4_32a(p[0], p[1], p[2], 0.0);
+	double4_32a Q = make_double4_32a(__ddiv_rn(q[0], n), __ddiv_rn(q[1], n), __ddiv_rn(q[2], n), __ddiv_rn(q[3], n));
+	double4_32a V = make_double4_32a(v[0], v[1], v[2], 0.0), M = make_double4_32a(l[0], l[1], l[2], 0.0);
+	if(a.f32) {  // backend_precision = float: the state FP32 from the start
+		P = round4(P);
+		Q = round4(Q);
+		V = round4(V);
+		M = round4(M);
+	}
+	a.pos[i] = P;
+	a.quat[i] = Q;
+	a.vel[i] = V;
+	a.angmom[i] = M;
 }
 
 // the FP64 state into the caller's layout and order (the reverse of k_unpack_state)
@@ -600,6 +697,7 @@ cudaError_t launch_first_step(const StepArgs &a, bool double_forces, cudaStream_
 	// two-warp blocks of 32 nucleotides: the FP64 work (1/64 of the FP32 rate) spreads evenly over
 	// the SMs
 	if(double_forces) return launch_after(k_first_step<double4_32a>, dim3(blocks_for(a.N, 32)), dim3(64), 0, s, a);
+	if(a.f32) return launch_after(k_first_step<float4, true>, dim3(blocks_for(a.N, 32)), dim3(64), 0, s, a);
 	return launch_after(k_first_step<float4>, dim3(blocks_for(a.N, 32)), dim3(64), 0, s, a);
 }
 

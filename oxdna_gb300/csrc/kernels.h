@@ -105,6 +105,7 @@ struct ForceArgs {
 	// split path (engine layout): backbone-site offsets (w = strand-end flag), term lists
 	// (column-major: element k of nucleotide i at [k * N + i]) and the per-bond buffers
 	const float4 *fback;
+	const float4 *fa1lo, *fbacklo;            // remainders of fa1 / fback (null: the FP32 sites unrefined)
 	const int *ev_nb, *ev_n, *base_nb, *base_n, *stk_nb, *stk_n;
 	int ev_cap, base_cap, stk_cap;            // capacities (an overflowed list is read up to them)
 	void *bond_f, *bond_tp, *bond_tq;         // per bond owner p (q = n3[p]): f on q with w = energy, torques
@@ -126,6 +127,9 @@ struct ForceArgs {
 	// owner of a base / stack pair as in an unsorted run, and the slot of each caller's index
 	// (external-force records name caller's indices)
 	const int *id, *slot;
+	// shape of the MD step's kernels (no energies; mixed / float engine): index into the
+	// autotuner's shape table, 0 the default
+	int shape;
 };
 
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
@@ -135,8 +139,12 @@ cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
 // energy = false: forces and torques only (w of F and T left 0), what an MD step needs
 cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool energy, cudaStream_t s,
 		cudaEvent_t wait = nullptr);
-// blocks of the split non-bonded kernel for N nucleotides
-int nonbonded_blocks(int N);
+// blocks of the split non-bonded kernel for N nucleotides at `lanes` lanes per nucleotide
+int nonbonded_blocks(int N, int lanes);
+// shapes of the MD step's force kernels (mixed / float engine, ForceArgs::shape): how many, and
+// shape k's nucleotides per pair-block warp queue, non-bonded lanes per nucleotide and register cap
+int force_shape_count();
+void force_shape_of(int k, int *npw, int *lanes, int *minb);
 // lets the split kernels use `bytes` of dynamic shared memory (per-block system tables);
 // nonzero if that is more than they may have
 int set_forces_smem(bool dbl, size_t bytes);
@@ -192,14 +200,15 @@ struct ListArgs {
 	int *id, *slot;         // [N] caller's index of each slot, and its inverse
 	int *perm, *inv;        // [N] scratch: old slot of new slot k, new slot of old slot
 	double4_32a *st[4];     // FP64 state: positions, velocities, angular momenta, quaternions
-	float4 *mir[5];         // mirrors: pos_hi, pos_lo, fa1, fa3, fback (any may be null)
+	float4 *mir[7];         // mirrors: pos_hi, pos_lo, fa1, fa3, fback, fa1lo, fbacklo (any may be null)
 	int2 *bonds_rw;         // the bonds the rows exclude (the array of `bonds`)
 	unsigned char *scratch; // [N * SORT_BYTES]
 };
 
-// bytes per nucleotide of the sort's staging buffer: 4 FP64 vectors, 5 FP32 vectors, bonds,
+// bytes per nucleotide of the sort's staging buffer: 4 FP64 vectors, 7 FP32 vectors, bonds,
 // id and cell
-#define SORT_BYTES (4 * 32 + 5 * 16 + 8 + 4 + 4)
+#define SORT_MIRRORS 7
+#define SORT_BYTES (4 * 32 + SORT_MIRRORS * 16 + 8 + 4 + 4)
 
 // full rebuild: cells (counting sort, deterministic order) then neighbour rows
 cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s);
@@ -210,10 +219,12 @@ struct StepArgs {
 	int N;
 	double dt;
 	double4_32a *pos, *vel, *angmom, *quat;   // FP64 state
+	int f32;                               // backend_precision = float: FP32 integration, the state kept FP32-representable
 	float4 *pos_hi, *pos_lo, *fa1, *fa3;  // FP32 mirrors written by the first step
 	const void *forces, *torques;         // float4 (mixed) or double4_32a (double)
 	const float4 *list_pos;
 	float4 *fback;                         // backbone offset (w: strand-end flag), written with the mirrors
+	float4 *fa1lo, *fbacklo;               // remainders of fa1 and fback (mixed / float engine; null: none)
 	const int2 *bonds;
 	const float4 *list_a1, *list_back;     // site data of the last list build (null: centres only)
 	float skin2;

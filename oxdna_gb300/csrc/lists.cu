@@ -216,12 +216,12 @@ __global__ void k_sort_gather(ListArgs a) {
 	const int from = a.perm[k];
 	double4_32a *sd = reinterpret_cast<double4_32a *>(a.scratch);
 	float4 *sf = reinterpret_cast<float4 *>(a.scratch + 4 * 32 * N);
-	int2 *sb = reinterpret_cast<int2 *>(a.scratch + (4 * 32 + 5 * 16) * N);
-	int *si = reinterpret_cast<int *>(a.scratch + (4 * 32 + 5 * 16 + 8) * N);
+	int2 *sb = reinterpret_cast<int2 *>(a.scratch + (4 * 32 + SORT_MIRRORS * 16) * N);
+	int *si = reinterpret_cast<int *>(a.scratch + (4 * 32 + SORT_MIRRORS * 16 + 8) * N);
 #pragma unroll
 	for(int t = 0; t < 4; t++) sd[t * N + k] = a.st[t][from];
 #pragma unroll
-	for(int t = 0; t < 5; t++)
+	for(int t = 0; t < SORT_MIRRORS; t++)
 		if(a.mir[t]) sf[t * N + k] = a.mir[t][from];
 	const int2 b = a.bonds_rw[from];
 	sb[k] = make_int2(b.x >= 0 ? a.inv[b.x] : -1, b.y >= 0 ? a.inv[b.y] : -1);
@@ -240,12 +240,12 @@ __global__ void k_sort_scatter(ListArgs a) {
 	const long long N = a.N;
 	const double4_32a *sd = reinterpret_cast<const double4_32a *>(a.scratch);
 	const float4 *sf = reinterpret_cast<const float4 *>(a.scratch + 4 * 32 * N);
-	const int2 *sb = reinterpret_cast<const int2 *>(a.scratch + (4 * 32 + 5 * 16) * N);
-	const int *si = reinterpret_cast<const int *>(a.scratch + (4 * 32 + 5 * 16 + 8) * N);
+	const int2 *sb = reinterpret_cast<const int2 *>(a.scratch + (4 * 32 + SORT_MIRRORS * 16) * N);
+	const int *si = reinterpret_cast<const int *>(a.scratch + (4 * 32 + SORT_MIRRORS * 16 + 8) * N);
 #pragma unroll
 	for(int t = 0; t < 4; t++) a.st[t][k] = sd[t * N + k];
 #pragma unroll
-	for(int t = 0; t < 5; t++)
+	for(int t = 0; t < SORT_MIRRORS; t++)
 		if(a.mir[t]) a.mir[t][k] = sf[t * N + k];
 	a.bonds_rw[k] = sb[k];
 	const int id = si[k];

@@ -12,8 +12,8 @@
 // set aside when the module is loaded.
 //
 // The host finds the scratch with cudaGetSymbolAddress, once per device (with that device
-// current); the first call on a device may load the module, so it should not be the first
-// CUDA work issued inside a stream capture.  Calls on one device share the scratch: two calls
+// current), and checks on every call that the module was not reloaded since; the first call
+// on a device may load the module, so it should come before any stream capture.  Calls on one device share the scratch: two calls
 // that overlap in time (different streams or threads) race and must be serialised by the
 // caller.  Each call clears what must start at zero (the status word; the cell counts are
 // zeroed by the build itself), so consecutive calls never see each other's leftovers.
@@ -50,13 +50,21 @@ static std::mutex g_scratch_mutex;
 static Scratch g_scratch[64];
 static bool g_scratch_ok[64];
 
-// device addresses of the scratch arrays on the current device (looked up once per device)
+// device addresses of the scratch arrays on the current device: looked up together once per
+// device; every later call looks up the status word's address alone (cheap once the module is
+// loaded) and redoes the whole lookup if it moved, which happens when a device reset or a new
+// primary context has loaded the module again
 static cudaError_t scratch_of_current_device(Scratch &out) {
 	int dev = 0;
 	cudaError_t e = cudaGetDevice(&dev);
 	if(e != cudaSuccess) return e;
 	if(dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
 	std::lock_guard<std::mutex> lock(g_scratch_mutex);
+	if(g_scratch_ok[dev]) {
+		void *p = nullptr;
+		if((e = cudaGetSymbolAddress(&p, g_status)) != cudaSuccess) return e;
+		if((int *) p != g_scratch[dev].status) g_scratch_ok[dev] = false;
+	}
 	if(!g_scratch_ok[dev]) {
 		Scratch s{};
 		void *p = nullptr;

@@ -75,6 +75,8 @@ OXGB_HD float m_log(float x) { return logf(x); }
 OXGB_HD double m_log(double x) { return log(x); }
 OXGB_HD float m_acos(float x) { return acosf(x); }
 OXGB_HD double m_acos(double x) { return acos(x); }
+OXGB_HD float m_atan2(float y, float x) { return atan2f(y, x); }
+OXGB_HD double m_atan2(double y, double x) { return atan2(y, x); }
 OXGB_HD float m_fabs(float x) { return fabsf(x); }
 OXGB_HD double m_fabs(double x) { return fabs(x); }
 OXGB_HD float m_fma(float a, float b, float c) { return fmaf(a, b, c); }

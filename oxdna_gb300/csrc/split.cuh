@@ -194,33 +194,74 @@ OXGB_HD F2 twice_sum2(F2 a, F2 b, float sign) {
 
 OXGB_HD float round2(F2 a) { return OXGB_FADD(a.s, a.e); }
 
-// b1 x + b2 y of two pairs with float constants, rounded
-OXGB_HD float lin2(float b1, F2 x, float b2, F2 y) {
+// b1 x + b2 y of two pairs with float constants, as a pair (round2 rounds it)
+OXGB_HD F2 lin2_pair(float b1, F2 x, float b2, F2 y) {
 	const float u = OXGB_FMUL(b1, x.s), eu = OXGB_FMAF(b1, x.s, -u);
 	const float v = OXGB_FMUL(b2, y.s), ev = OXGB_FMAF(b2, y.s, -v);
 	const F2 w = two_sum(u, v);
 	const float e = OXGB_FADD(OXGB_FADD(w.e, OXGB_FADD(eu, ev)), OXGB_FMAF(b1, x.e, OXGB_FMUL(b2, y.e)));
-	return OXGB_FADD(w.s, e);
+	return F2{w.s, e};
 }
 
-// The body axes a1, a3 and the backbone offset b1 a1 + b2 a2 of the unit quaternion
-// (x, y, z, w) = (qh + ql) given as FP32 pairs (split_rn), each rounded to FP32 from a pair
-// accurate to ~2^-46: the same values (to within an ulp, nearly always equal) as the FP64
-// frame rounded once, computed on the FP32 pipe.  The frame is that of quat_frame.
-OXGB_HD void frame_mirror(const float qh[4], const float ql[4], float b1, float b2, float a1[3], float a3[3], float back[3]) {
+// the remainder of a pair's FP32 rounding r = round2(a): a - r (a.s - r is exact, the two being
+// a few ulps apart)
+OXGB_HD float rem2(F2 a, float r) { return OXGB_FADD(OXGB_FSUB(a.s, r), a.e); }
+
+// The body axes a1, a2, a3 of the unit quaternion (x, y, z, w) = (qh + ql) given as FP32 pairs
+// (split_rn), as pairs accurate to ~2^-46.  The frame is that of quat_frame.
+OXGB_HD void frame_pairs(const float qh[4], const float ql[4], F2 a1[3], F2 a2[3], F2 a3[3]) {
 	const F2 xx = prod2(qh[0], ql[0], qh[0], ql[0]), yy = prod2(qh[1], ql[1], qh[1], ql[1]),
 			 zz = prod2(qh[2], ql[2], qh[2], ql[2]), ww = prod2(qh[3], ql[3], qh[3], ql[3]);
 	const F2 xy = prod2(qh[0], ql[0], qh[1], ql[1]), xz = prod2(qh[0], ql[0], qh[2], ql[2]),
 			 xw = prod2(qh[0], ql[0], qh[3], ql[3]), yz = prod2(qh[1], ql[1], qh[2], ql[2]),
 			 yw = prod2(qh[1], ql[1], qh[3], ql[3]), zw = prod2(qh[2], ql[2], qh[3], ql[3]);
-	const F2 a1x = diff_of_sums2(xx, ww, yy, zz), a1y = twice_sum2(xy, zw, 1.f), a1z = twice_sum2(xz, yw, -1.f);
-	const F2 a2x = twice_sum2(xy, zw, -1.f), a2y = diff_of_sums2(yy, ww, xx, zz), a2z = twice_sum2(yz, xw, 1.f);
-	const F2 a3x = twice_sum2(xz, yw, 1.f), a3y = twice_sum2(yz, xw, -1.f), a3z = diff_of_sums2(zz, ww, xx, yy);
-	a1[0] = round2(a1x), a1[1] = round2(a1y), a1[2] = round2(a1z);
-	a3[0] = round2(a3x), a3[1] = round2(a3y), a3[2] = round2(a3z);
-	back[0] = lin2(b1, a1x, b2, a2x);
-	back[1] = lin2(b1, a1y, b2, a2y);
-	back[2] = lin2(b1, a1z, b2, a2z);
+	a1[0] = diff_of_sums2(xx, ww, yy, zz), a1[1] = twice_sum2(xy, zw, 1.f), a1[2] = twice_sum2(xz, yw, -1.f);
+	a2[0] = twice_sum2(xy, zw, -1.f), a2[1] = diff_of_sums2(yy, ww, xx, zz), a2[2] = twice_sum2(yz, xw, 1.f);
+	a3[0] = twice_sum2(xz, yw, 1.f), a3[1] = twice_sum2(yz, xw, -1.f), a3[2] = diff_of_sums2(zz, ww, xx, yy);
+}
+
+// The body axes a1, a3 and the backbone offset b1 a1 + b2 a2 of the unit quaternion
+// (x, y, z, w) = (qh + ql) given as FP32 pairs (split_rn), each rounded to FP32 from a pair
+// accurate to ~2^-46: the same values (to within an ulp, nearly always equal) as the FP64
+// frame rounded once, computed on the FP32 pipe.
+OXGB_HD void frame_mirror(const float qh[4], const float ql[4], float b1, float b2, float a1[3], float a3[3], float back[3]) {
+	F2 p1[3], p2[3], p3[3];
+	frame_pairs(qh, ql, p1, p2, p3);
+#pragma unroll
+	for(int k = 0; k < 3; k++) {
+		a1[k] = round2(p1[k]);
+		a3[k] = round2(p3[k]);
+		back[k] = round2(lin2_pair(b1, p1[k], b2, p2[k]));
+	}
+}
+
+// The remainders of frame_mirror's a1 and backbone offset: a1 = a1_mirror + a1lo and back =
+// back_mirror + backlo to ~2^-46 (the mirrors are recomputed here, bit-identical)
+OXGB_HD void frame_remainders(const float qh[4], const float ql[4], float b1, float b2, float a1lo[3], float backlo[3]) {
+	F2 p1[3], p2[3], p3[3];
+	frame_pairs(qh, ql, p1, p2, p3);
+#pragma unroll
+	for(int k = 0; k < 3; k++) {
+		a1lo[k] = rem2(p1[k], round2(p1[k]));
+		const F2 bk = lin2_pair(b1, p1[k], b2, p2[k]);
+		backlo[k] = rem2(bk, round2(bk));
+	}
+}
+
+// frame_mirror and frame_remainders from one evaluation of the pairs
+OXGB_HD void frame_mirror_rem(const float qh[4], const float ql[4], float b1, float b2, float a1[3], float a3[3], float back[3],
+		float a1lo[3], float backlo[3]) {
+	F2 p1[3], p2[3], p3[3];
+	frame_pairs(qh, ql, p1, p2, p3);
+#pragma unroll
+	for(int k = 0; k < 3; k++) {
+		a1[k] = round2(p1[k]);
+		a3[k] = round2(p3[k]);
+		const F2 bk = lin2_pair(b1, p1[k], b2, p2[k]);
+		back[k] = round2(bk);
+		a1lo[k] = rem2(p1[k], a1[k]);
+		backlo[k] = rem2(bk, back[k]);
+	}
 }
 
 // ---------------------------------------------------------------- pairs as ~48-bit numbers

@@ -46,7 +46,8 @@ def dna2_settings(T: float, salt: float = 0.5, average: bool = True, seq: Option
 def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = "no", newtonian_steps: int = 103,
                 pt: float = 0.0, diff_coeff: float = 2.5, bussi_tau: float = 1000.0, seed: int = 1,
                 precision: str = "mixed", cells_auto_optimisation: bool = True, max_neigh: int = 0,
-                steps_per_graph: int = 16, list_rebuild_node: str = "conditional", sort_every: int = 0) -> _abi.MDSettings:
+                steps_per_graph: int = 16, list_rebuild_node: str = "conditional", sort_every: int = 0,
+                autotune: bool = False) -> _abi.MDSettings:
     m = _abi.MDSettings()
     _abi.lib().oxgb_md_default_settings(C.byref(m))
     m.dt = dt
@@ -57,12 +58,13 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
     m.diff_coeff = diff_coeff
     m.bussi_tau = bussi_tau
     m.seed = seed
-    m.precision = {"mixed": 0, "float": 0, "double": 1}[precision]
+    m.precision = {"mixed": 0, "double": 1, "float": 2}[precision]
     m.cells_auto_optimisation = 1 if cells_auto_optimisation else 0
     m.max_neigh = max_neigh
     m.steps_per_graph = steps_per_graph
     m.list_rebuild_node = {"conditional": 0, "kernel": 1}[list_rebuild_node]
     m.sort_every = sort_every
+    m.autotune = 1 if autotune else 0
     return m
 
 
@@ -151,12 +153,13 @@ class MDSystem:
         _abi.check(_abi.lib().oxgb_md_get_forces(self._h, _abi.ptr(F), _abi.ptr(T), _abi.ptr(E)))
         return F, T, E
 
-    def energies(self):
+    def energies(self, potential: bool = True):
         """potential, translational and rotational kinetic energy (FP64 sums; arrays per system
-        for a batch)"""
+        for a batch).  potential=False skips the force evaluation the potential energy needs and
+        returns 0 for it."""
         n = self.n_systems
         U, Kt, Kr = np.zeros(n), np.zeros(n), np.zeros(n)
-        _abi.check(_abi.lib().oxgb_md_energies(self._h, _abi.ptr(U), _abi.ptr(Kt), _abi.ptr(Kr)))
+        _abi.check(_abi.lib().oxgb_md_energies(self._h, _abi.ptr(U) if potential else None, _abi.ptr(Kt), _abi.ptr(Kr)))
         if n == 1:
             return float(U[0]), float(Kt[0]), float(Kr[0])
         return U, Kt, Kr
@@ -197,28 +200,19 @@ class MDSystem:
 
     def replica_exchange(self, temps, rng, parity: int = 0):
         """One round of parallel-tempering swaps between neighbouring rungs of a temperature
-        ladder.  temps[k] is the current temperature of system k; rungs (r, r + 1) with r of the
-        given parity are tried with the Metropolis rule on the FP64 potential energies,
-        min(1, exp((1/T_r - 1/T_r+1) (U_r - U_r+1))); an accepted pair exchanges temperatures
-        (tables, thermostat) and rescales its momenta by sqrt(T_new / T_old).  Returns the new
+        ladder (oxdna_gb300.pt.swap_round).  temps[k] is the current temperature of system k;
+        rungs (r, r + 1) with r of the given parity are tried with the Metropolis rule on the
+        FP64 potential energies, min(1, exp((1/T_r - 1/T_r+1) (U_r - U_r+1))), one uniform
+        draw from rng per tried pair; an accepted pair exchanges temperatures (tables,
+        thermostat) and rescales its momenta by sqrt(T_new / T_old).  Returns the new
         temperatures and the number of accepted swaps."""
-        temps = np.asarray(temps, np.float64).copy()
+        from . import pt
+        temps = np.asarray(temps, np.float64)
         U, _, _ = self.energies()
-        U = np.atleast_1d(U)
-        order = np.argsort(temps)  # order[r] = system at rung r
-        accepted = 0
-        for r in range(parity, len(order) - 1, 2):
-            i, j = order[r], order[r + 1]
-            d = (1.0 / temps[i] - 1.0 / temps[j]) * (U[i] - U[j])
-            if d >= 0 or rng.uniform() < np.exp(d):
-                Ti, Tj = temps[i], temps[j]
-                self.set_temperature(Tj, i)
-                self.set_temperature(Ti, j)
-                self.scale_momenta(np.sqrt(Tj / Ti), i)
-                self.scale_momenta(np.sqrt(Ti / Tj), j)
-                temps[i], temps[j] = Tj, Ti
-                accepted += 1
-        return temps, accepted
+        draws = rng.uniform(size=pt.pairs_in_round(len(temps), parity))
+        new, swaps = pt.swap_round(temps, np.atleast_1d(U), parity, draws)
+        pt.apply_swaps(self, temps, swaps)
+        return new, len(swaps)
 
     def neighbours(self):
         N = self.N
@@ -231,6 +225,17 @@ class MDSystem:
         _abi.check(_abi.lib().oxgb_md_neighbours(self._h, _abi.ptr(nnb), _abi.ptr(nb), mx.value, _abi.ptr(cell),
                                                  C.byref(ns)))
         return nnb, nb.reshape(N, mx.value), cell, ns.value
+
+    def force_shape(self):
+        """the shape of the MD step's force kernels (autotuned with md_settings(autotune=True)):
+        pair_npw, nb_lanes, nb_min_blocks and the measured launch time in microseconds"""
+        a, b, c, t = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        _abi.check(_abi.lib().oxgb_md_force_shape(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(t)))
+        return dict(pair_npw=a.value, nb_lanes=b.value, nb_min_blocks=c.value, launch_us=t.value)
+
+    def set_force_shape(self, k: int):
+        """pins shape k of the MD step's force kernels (0 the default)"""
+        _abi.check(_abi.lib().oxgb_md_set_force_shape(self._h, int(k)))
 
     def info(self):
         r, s, m = C.c_longlong(0), C.c_longlong(0), C.c_int(0)

@@ -7,8 +7,8 @@ topology and configuration, and the harness prints its internal state, full-prec
 torques and energy split (interaction_type = DNA2_nomesh, the exact-f4 oxDNA2 force field).
 Cases that ask for steps also record the state after a short reference MD run.
 
-    make -C oracle/ref -j8 REF=/root/reference      # once
-    python tests/golden/make_golden.py --ref /root/reference
+    make -C oracle/ref -j8 REF=$OXDNA_REFERENCE      # once
+    python tests/golden/make_golden.py --ref $OXDNA_REFERENCE
 
 The .npz files are small (tens of KB) and committed; tests never need the reference itself.
 """
@@ -55,6 +55,9 @@ def parse_dump(path):
             i += n + 1
         elif k == "energy":
             d["energy"] = float(ln[1])
+            i += 1
+        elif k == "step":
+            d["step"] = int(ln[1])
             i += 1
         elif k == "split":
             n = int(ln[1])
@@ -128,6 +131,82 @@ def run_case(name, top_path, conf_path, settings, extra="", steps=0, dt=0.003):
     print(f"{name}: N={top.shape[0]} E={d['energy']:.6f} max|F|={np.abs(rec['F']).max():.3f}")
 
 
+# the external forces of the ext_forces fixture, as the dicts MDSystem.set_external_forces and
+# oracle.external_forces take, and as the reference's external_forces_file records
+# (src/Forces/{ConstantRateForce,MutualTrap,MovingTrap,LowdimMovingTrap,RepulsionPlane,
+# AttractionPlane}.cpp): six types, rates and a periodic mutual trap
+def ext_force_set(N, box):
+    return [
+        dict(type="string", particle=0, F0=0.3, rate=1e-3, dir=(0.0, 0.6, 0.8)),
+        dict(type="string", particle=5, F0=0.2, rate=0.0, dir=(1.0, 2.0, 3.0), dir_as_centre=True),
+        dict(type="mutual_trap", particle=2, ref_particle=N - 3, stiff=0.9, r0=1.2, rate=2e-3, stiff_rate=1e-3),
+        dict(type="mutual_trap", particle=N - 3, ref_particle=2, stiff=0.9, r0=1.2, PBC=True),
+        dict(type="trap", particle=7, stiff=1.5, pos0=(1.0, -2.0, 0.5), rate=1e-2, dir=(0.0, 0.0, 1.0)),
+        dict(type="lowdim_trap", particle=7, stiff=0.7, pos0=(0.5, 0.0, -0.5), rate=3e-3, dir=(1.0, 0.0, 0.0),
+             visibility=(True, False, True)),
+        dict(type="repulsion_plane", particle=9, stiff=2.0, dir=(0.0, 0.0, 1.0), position=box, r0=0.0, rate=-0.05),
+        dict(type="attraction_plane", particle=11, stiff=0.4, dir=(1.0, 0.0, 0.0), position=-1.0),
+    ]
+
+
+def ext_force_file(forces):
+    vec = lambda v: ", ".join(repr(float(x)) for x in v)
+    out = []
+    for d in forces:
+        kv = {"type": d["type"], "particle": d["particle"]}
+        t = d["type"]
+        if t == "string":
+            kv.update(F0=d["F0"], rate=d["rate"], dir=vec(d["dir"]))
+            if d.get("dir_as_centre"):
+                kv["dir_as_centre"] = "true"
+        elif t == "mutual_trap":
+            kv.update(ref_particle=d["ref_particle"], stiff=d["stiff"], r0=d["r0"], rate=d.get("rate", 0.0),
+                      stiff_rate=d.get("stiff_rate", 0.0))
+            if d.get("PBC"):
+                kv["PBC"] = "true"
+        elif t == "trap":
+            kv.update(stiff=d["stiff"], rate=d["rate"], pos0=vec(d["pos0"]), dir=vec(d["dir"]))
+        elif t == "lowdim_trap":
+            kv.update(stiff=d["stiff"], rate=d["rate"], pos0=vec(d["pos0"]), dir=vec(d["dir"]),
+                      visibility=", ".join(str(int(bool(v))) for v in d["visibility"]))
+        elif t == "repulsion_plane":
+            kv.update(stiff=d["stiff"], position=d["position"], end_position=d["r0"], v=d["rate"], dir=vec(d["dir"]))
+        elif t == "attraction_plane":
+            kv.update(stiff=d["stiff"], position=d["position"], dir=vec(d["dir"]))
+        out.append("{\n" + "".join(f"{k} = {v}\n" for k, v in kv.items()) + "}\n")
+    return "".join(out)
+
+
+def run_ext_case(name, s, settings, step):
+    """the external forces the reference adds at MD step `step` (the configuration's time, kept
+    by restart_step_counter = 0): the reference's forces with and without them"""
+    import json
+    forces = ext_force_set(s.N, float(s.box))
+    dumps = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        s.write(os.path.join(tmp, "init.top"), os.path.join(tmp, "init.dat"))
+        conf = open(os.path.join(tmp, "init.dat")).read().split("\n", 1)[1]
+        open(os.path.join(tmp, "init.dat"), "w").write(f"t = {step}\n" + conf)
+        open(os.path.join(tmp, "forces.txt"), "w").write(ext_force_file(forces))
+        for tag, ext in (("no", "external_forces = 0\n"),
+                         ("ext", "external_forces = 1\nexternal_forces_file = forces.txt\n")):
+            text = BASE_INPUT.format(steps=0, dt=0.003, T=settings["T_str"], salt=settings["salt"])
+            text = text.replace("restart_step_counter = 1\n", "restart_step_counter = 0\n")
+            text = text.replace("external_forces = 0\n", ext)
+            open(os.path.join(tmp, "input"), "w").write(text)
+            out = os.path.join(tmp, f"dump_{tag}.txt")
+            subprocess.run([DUMP, "input", out], cwd=tmp, check=True, stdout=subprocess.DEVNULL,
+                           stderr=subprocess.DEVNULL)
+            dumps[tag] = parse_dump(out)
+    d0, d1 = dumps["no"], dumps["ext"]
+    assert d1.get("step") == step, d1.get("step")
+    st = d1["state"]
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), box=d1["box"][0], step=step, pos=st[:, 0:3],
+                        F_ext=d1["forces"][:, 0:3] - d0["forces"][:, 0:3], T_ext=d1["forces"][:, 3:6] - d0["forces"][:, 3:6],
+                        forces=json.dumps(forces))
+    print(f"{name}: step {step}, max |F_ext| {np.abs(d1['forces'][:, 0:3] - d0['forces'][:, 0:3]).max():.3f}")
+
+
 def write_system(tmp, s):
     tp, cp = os.path.join(tmp, "s.top"), os.path.join(tmp, "s.dat")
     s.write(tp, cp)
@@ -136,8 +215,17 @@ def write_system(tmp, s):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("OXDNA_REFERENCE"),
+                    help="oxDNA reference checkout (default: $OXDNA_REFERENCE)")
+    ap.add_argument("--only", default=None, help="regenerate this fixture only (ext_forces)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("name the oxDNA reference checkout with --ref or OXDNA_REFERENCE")
+    if args.only == "ext_forces":
+        if not os.path.exists(DUMP):
+            subprocess.run(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8", f"REF={args.ref}"], check=True)
+        run_ext_case("ext_forces", G.system_for_config(0, seed=1), dict(T_str="300K", salt="0.5"), 1000)
+        return
     if not os.path.exists(DUMP):
         subprocess.run(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8", f"REF={args.ref}"], check=True)
     ff = os.path.join(args.ref, "test", "DNA", "FORCE_FIELD")
@@ -202,6 +290,9 @@ def main():
         # 8: integrator pin, 200 NVE steps of a thermal 12-bp duplex
         s = G.system_for_config(0, seed=3)
         run_case("md_nve", *write_system(tmp, s), T300, steps=200, dt=0.003)
+
+    # 9: the external forces of six types at MD step 1000 on the workload-0 duplex
+    run_ext_case("ext_forces", G.system_for_config(0, seed=1), dict(T_str="300K", salt="0.5"), 1000)
 
 
 if __name__ == "__main__":

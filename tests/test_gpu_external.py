@@ -1,6 +1,12 @@
-"""External forces through the C ABI against the oracle's restatement of the reference CUDA
-backend's set_external_forces (every force type, constant rates, a periodic mutual trap), and a
-mutual trap that pulls two nucleotides together over an MD run."""
+"""External forces through the C ABI against the oracle's restatement (every force type the
+engine implements, with rates, dir_as_centre and a periodic mutual trap), and a mutual trap that
+pulls two nucleotides together over an MD run.
+
+The record set is the one of fixture ext_forces, for which test_oracle_pin.py holds the oracle
+to the reference's own CPU force classes (1e-12), so the chain GPU -> oracle -> reference is
+closed on the same records."""
+import json
+
 import numpy as np
 import pytest
 
@@ -12,16 +18,9 @@ pytestmark = pytest.mark.gpu
 
 
 def _forces(N, box):
-    return [
-        dict(type="string", particle=0, F0=0.3, rate=1e-3, dir=(0.0, 0.6, 0.8)),
-        dict(type="constant", particle=5, F0=0.2, dir=(1.0, 2.0, 3.0), dir_as_centre=True),
-        dict(type="mutual_trap", particle=2, ref_particle=N - 3, stiff=0.9, r0=1.2, rate=2e-3, stiff_rate=1e-3),
-        dict(type="mutual_trap", particle=N - 3, ref_particle=2, stiff=0.9, r0=1.2, PBC=True),
-        dict(type="trap", particle=7, stiff=1.5, pos0=(1.0, -2.0, 0.5), rate=1e-2, dir=(0.0, 0.0, 1.0)),
-        dict(type="lowdim_trap", particle=7, stiff=0.7, pos0=(0.0, 0.0, 0.0), visibility=(True, False, True)),
-        dict(type="repulsion_plane", particle=9, stiff=2.0, dir=(0.0, 0.0, 1.0), position=box, r0=0.0, rate=-0.05),
-        dict(type="attraction_plane", particle=11, stiff=0.4, dir=(1.0, 0.0, 0.0), position=-1.0),
-    ]
+    recs = json.loads(str(load_golden("ext_forces")["forces"]))
+    assert max(max(d["particle"], d.get("ref_particle", 0)) for d in recs) < N
+    return recs
 
 
 @pytest.mark.parametrize("run_before", [0, 12])

@@ -39,6 +39,27 @@ def test_nve_matches_reference_md(precision, tol):
     sysm.close()
 
 
+def test_float_precision_integrates_in_fp32():
+    """backend_precision = float: the state stays FP32-representable, and the 200-step NVE run
+    of the reference follows it to FP32 accuracy"""
+    g = load_golden("md_nve")
+    sysm, _ = system_from_golden(g, precision="float", dt=float(g["dt"]))
+    st0 = sysm.get_state()
+    for key in ("pos", "quat", "vel", "Lmom"):
+        assert np.array_equal(st0[key], st0[key].astype(np.float32).astype(np.float64)), key
+    sysm.run(int(g["steps"]))
+    st = sysm.get_state()
+    for key in ("pos", "quat", "vel", "Lmom"):
+        assert np.array_equal(st[key], st[key].astype(np.float32).astype(np.float64)), key
+    L = float(g["box"])
+    err = np.abs(wrapped_diff(st["pos"], g["final_pos"], L)).max()
+    assert 1e-7 < err < 1e-3
+    a1, a2, a3 = oxio.quat_to_frame(st["quat"])
+    assert np.abs(a1 - g["final_a1"]).max() < 1e-3
+    assert np.abs(np.linalg.norm(st["quat"], axis=1) - 1).max() < 1e-6
+    sysm.close()
+
+
 def oracle_run(g, thermostat, nsteps, n, seed, pt=0.0, tau=10.0, dt=0.003):
     p = oracle.make_params(oracle.make_settings(float(g["T"]), float(g["salt"])))
     md = oracle.MD()

@@ -70,3 +70,18 @@ def test_oracle_integrator_matches_reference_md():
     assert np.abs(a3 - g["final_a3"]).max() < 1e-9
     assert np.abs(st["vel"] - g["final_vel"]).max() < 1e-9
     assert np.abs(st["Lmom"] - g["final_Lmom"]).max() < 1e-9
+
+
+def test_oracle_external_forces_match_reference():
+    """The six external-force types the engine implements (constant / string with a rate and
+    with dir_as_centre, mutual traps with rates and periodic images, moving trap, low-dimensional
+    moving trap, moving repulsion plane with an end position, attraction plane), as the
+    reference's CPU force classes compute them at MD step 1000 (fixture ext_forces: the
+    reference's forces with the records minus its forces without); the records add no torques."""
+    import json
+    g = load_golden("ext_forces")
+    forces = json.loads(str(g["forces"]))
+    F = oracle.external_forces(g["pos"], int(g["step"]), forces, float(g["box"]))
+    assert np.abs(g["F_ext"]).max() > 1.0
+    assert np.abs(F - g["F_ext"]).max() <= 1e-12 * np.abs(g["F_ext"]).max()
+    assert np.abs(g["T_ext"]).max() == 0.0

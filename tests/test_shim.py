@@ -1,8 +1,9 @@
 """The reference-side plugin (oxdna_gb300/shim) compiles against the reference's own headers and
 exports the entry points the reference's plugin manager looks up.
 
-Needs the oxDNA sources (the OXDNA_SRC directory, by default the reference checkout) and nvcc;
-skipped where either is missing.  No GPU is used: the object is
+Needs the oxDNA sources (the src/ folder of the checkout OXDNA_REFERENCE names, or of the copy
+oracle/ref/Makefile's `stage` target leaves in baseline/_ref/oxDNA) and nvcc; skipped where either
+is missing.  No GPU is used: the object is
 compiled, not run.
 """
 import os
@@ -13,7 +14,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SHIM = os.path.join(ROOT, "oxdna_gb300", "shim", "CUDAGB300DNA2Interaction.cu")
-OXDNA_SRC = os.environ.get("OXDNA_SRC", "/root/reference/src")
+_REF = os.environ.get("OXDNA_REFERENCE") or os.path.join(ROOT, "baseline", "_ref", "oxDNA")
+OXDNA_SRC = os.path.join(_REF, "src")
 
 
 @pytest.fixture(scope="module")

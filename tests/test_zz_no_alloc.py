@@ -116,3 +116,25 @@ def test_noalloc_refuses_requests_beyond_its_limits():
     rc = L.oxgb_verlet_build_noalloc(8, 400.0, RCUT, SKIN, 0, *args)
     assert rc == 1 and b"cells" in L.oxgb_last_error()
     torch.cuda.synchronize()
+
+
+def test_noalloc_reports_overflow_and_the_next_call_starts_clean():
+    """A max_neigh below the longest row returns OXGB_E_NEIGH_OVERFLOW; the status word lives in
+    the shared scratch, so the next call with enough room must return OXGB_OK again, with the
+    rows of the handle path."""
+    L = _abi.lib()
+    a, _ = _systems()
+    pos, n3, n5, bt, box = a
+    d_pos, d_bonds = _inputs(pos, n3, n5, bt)
+    ref = _with_handle(d_pos, d_bonds, box)
+    assert int(ref[1].max()) > 2
+    N = d_pos.shape[0]
+    small = 2
+    d_nb = torch.zeros((small, N), dtype=torch.int32, device="cuda")
+    d_nnb = torch.zeros((N,), dtype=torch.int32, device="cuda")
+    d_lp = torch.zeros_like(d_pos)
+    rc = L.oxgb_verlet_build_noalloc(N, box, RCUT, SKIN, 1, d_pos.data_ptr(), d_lp.data_ptr(), d_bonds.data_ptr(),
+                                     d_nb.data_ptr(), d_nnb.data_ptr(), small, None)
+    assert rc == 4  # OXGB_E_NEIGH_OVERFLOW
+    got = _without_alloc(d_pos, d_bonds, box, ref[3])
+    _same(ref, got)
