@@ -431,7 +431,7 @@ def run_reference_cuda_arm(args, wl):
         try:
             line["energy_per_nucleotide"] = reference_cuda_energy_check(refrun, exe, s, wl)
         except Exception as e:  # noqa: BLE001
-            line["energy_per_nucleotide"] = {"error": str(e).splitlines()[0]}
+            line["energy_per_nucleotide"] = {"error": str(e)[-1500:]}
     print(json.dumps(line), flush=True)
 
 

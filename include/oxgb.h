@@ -232,11 +232,14 @@ int oxgb_md_energies(oxgb_md *h, double *U, double *K_t, double *K_r);
  * left to the caller (a swap usually rescales them by sqrt(T_new / T_old)). */
 int oxgb_md_set_temperature(oxgb_md *h, int k, double T);
 /*
- * External forces, the CUDA backend's set_external_forces (src/CUDA/Backends/CUDA_MD.cuh:97-200)
- * for the force types of src/Forces/{ConstantRateForce,MutualTrap,MovingTrap,LowdimMovingTrap,
- * RepulsionPlane,AttractionPlane}.cpp.  Each record acts on one nucleotide (global index) and
- * is evaluated at every force evaluation from the FP64 positions, with `step` the MD step being
- * computed (0 for a state just uploaded); no torques, no energies (as in the reference).
+ * External forces, the CUDA backend's set_external_forces (src/CUDA/Backends/CUDA_MD.cuh:97-555,
+ * records of src/CUDA/Forces/forces_defs.cuh) for the force types of src/Forces/
+ * {ConstantRateForce,MutualTrap,MovingTrap,LowdimMovingTrap,RepulsionPlane,AttractionPlane,
+ * RepulsiveSphere,RepulsiveSphereSmooth,LJWall,GenericCentralForce,RepulsionPlaneMoving,LJCone}.cpp.
+ * Each record acts on one nucleotide (global index) and is evaluated at every force evaluation
+ * from the FP64 positions, with `step` the MD step being computed (0 for a state just uploaded);
+ * no torques, no energies (as in the reference).  dir is taken as given (the reference
+ * normalises it when it reads the file).  With r the nucleotide's position:
  *   CONSTANT:          F += (F0 + rate step) dir, dir -> unit(dir - r) if flags & 1
  *   MUTUAL_TRAP:       d = r(ref) - r (minimum image if flags & 1), F += d (|d| - (r0 + rate step))
  *                      (stiff + stiff_rate step) / |d|
@@ -245,6 +248,22 @@ int oxgb_md_set_temperature(oxgb_md *h, int k, double T);
  *   REPULSION_PLANE:   p = position + rate step, stopped at r0 (the end position) when rate != 0;
  *                      d = dir . r + p; F += -d stiff dir where d < 0
  *   ATTRACTION_PLANE:  d = dir . r + position; F += -d stiff dir where d < 0, else -stiff dir
+ *   SPHERE:            d = minimum image of r - pos0 (the centre), R = r0 + rate step;
+ *                      F += -stiff (1 - R / |d|) d where R < |d| < cutoff (r_ext)
+ *   SPHERE_SMOOTH:     d = minimum image of r - pos0; where r0 <= |d| <= cutoff (r_ext):
+ *                      F += -(stiff / 2) exp((|d| - p1) / sigma) d / |d| if |d| >= p1 (alpha),
+ *                      else -(stiff |d| - (stiff / 2) exp(-(|d| - p1) / sigma)) d / |d|
+ *                      (sigma: the smoothing length)
+ *   LJ_WALL:           x = dir . r + position, y = x / sigma; where y <= cutoff:
+ *                      F += 4 n stiff (2 y^-2n - y^-n) / x dir
+ *   CENTRAL:           (generic_central_force, force_type = gravity) d = pos0 - r; unless |d| <
+ *                      p1 (inner cut-off) or, p2 > 0, |d| > p2 (outer): F += F0 d / |d|
+ *   REPULSION_PLANE_MOVING: x = (r - r(ref)) . dir; F += -stiff min(x, 0) dir (one record per
+ *                      reference particle; the records of a nucleotide add up)
+ *   LJ_CONE:           apex pos0, axis dir, half-angle p1 (alpha): with v = r - pos0, a = v . dir,
+ *                      b = |a dir - v|, x = a sin(alpha) - b cos(alpha), y = x / sigma; where
+ *                      y <= cutoff: F += 4 n stiff (2 y^-2n - y^-n) / x nrm, nrm = unit((a + b
+ *                      tan(alpha)) dir - v)
  */
 enum {
 	OXGB_FORCE_CONSTANT = 0,
@@ -252,12 +271,20 @@ enum {
 	OXGB_FORCE_MOVING_TRAP = 2,
 	OXGB_FORCE_LOWDIM_TRAP = 3,
 	OXGB_FORCE_REPULSION_PLANE = 4,
-	OXGB_FORCE_ATTRACTION_PLANE = 5
+	OXGB_FORCE_ATTRACTION_PLANE = 5,
+	OXGB_FORCE_SPHERE = 6,
+	OXGB_FORCE_SPHERE_SMOOTH = 7,
+	OXGB_FORCE_LJ_WALL = 8,
+	OXGB_FORCE_CENTRAL = 9,
+	OXGB_FORCE_REPULSION_PLANE_MOVING = 10,
+	OXGB_FORCE_LJ_CONE = 11
 };
 typedef struct oxgb_ext_force {
 	int type, particle, ref_particle, flags;
 	double F0, rate, stiff, stiff_rate, r0, position;
 	double dir[3], pos0[3];
+	double sigma, cutoff, p1, p2; /* parameters of the sphere, wall, cone and central types */
+	int n, pad;                   /* the Lennard-Jones exponent of LJ_WALL / LJ_CONE */
 } oxgb_ext_force;
 /* replaces the engine's external forces by f[0 .. n-1] (n = 0 removes them) */
 int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_force *f);

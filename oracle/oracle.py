@@ -194,11 +194,10 @@ def md_run(params: Params, md: MD, state: dict, n3, n5, typ, btype, L: float, st
 
 
 def external_forces(pos, step, forces, box):
-    """Forces of the external-force records on every nucleotide, as the reference CUDA backend's
-    set_external_forces computes them (src/CUDA/Backends/CUDA_MD.cuh:97-200: CUDA_TRAP_CONSTANT
-    :114-130, CUDA_TRAP_MUTUAL :131-143, CUDA_TRAP_MOVING :144-153, CUDA_TRAP_MOVING_LOWDIM
-    :154-163, CUDA_REPULSION_PLANE :164-177, CUDA_ATTRACTION_PLANE :178-190), in FP64.  `forces`
-    are the dicts MDSystem.set_external_forces takes."""
+    """Forces of the external-force records on every nucleotide, as the reference computes them
+    (src/CUDA/Backends/CUDA_MD.cuh:97-555 and the CPU force classes src/Forces/*.cpp cited per
+    type), in FP64.  `forces` are the dicts MDSystem.set_external_forces takes (the reference's
+    external_forces_file keys)."""
     pos = np.asarray(pos, np.float64)
     F = np.zeros_like(pos)
     st = float(step)
@@ -240,4 +239,51 @@ def external_forces(pos, step, forces, box):
         elif t == "attraction_plane":
             dist = direction @ r + d.get("position", 0.0)
             F[i] += (-dist if dist < 0 else -1.0) * d.get("stiff", 0.0) * direction
+        elif t in ("sphere", "sphere_smooth"):
+            # RepulsiveSphere::force, RepulsiveSphereSmooth::force (src/Forces/RepulsiveSphere*.cpp)
+            c0 = np.asarray(d.get("center", (0.0, 0.0, 0.0)), np.float64)
+            dv = r - c0
+            dv = dv - np.rint(dv / box) * box
+            m = np.linalg.norm(dv)
+            r_ext = d.get("r_ext", 1e10)
+            if t == "sphere":
+                R = d.get("r0", -1.0) + d.get("rate", 0.0) * st
+                if R < m < r_ext:
+                    F[i] += dv * (-d.get("stiff", 0.0) * (1.0 - R / m))
+            elif not (m < d.get("r0", -1.0) or m > r_ext):
+                k, alpha, smooth = d.get("stiff", 0.0), d.get("alpha", -1.0), d.get("smooth", -1.0)
+                if m >= alpha:
+                    F[i] += dv * (-(k * 0.5 * np.exp((m - alpha) / smooth)) / m)
+                else:
+                    F[i] += dv * (-(k * m - k * 0.5 * np.exp(-(m - alpha) / smooth)) / m)
+        elif t in ("LJ_wall", "LJ_cone"):
+            # LJWall::force, LJCone::force (src/Forces/LJWall.cpp, src/Forces/LJCone.cpp)
+            n = int(d.get("n", 6))
+            k, sigma = d.get("stiff", 1.0), d.get("sigma", 1.0)
+            cutoff = 2.0 ** (1.0 / n) if d.get("only_repulsive") else 1e6
+            if t == "LJ_wall":
+                x = direction @ r + d.get("position", -1.0)
+                nrm = direction
+            else:
+                alpha = d.get("alpha", 0.0)
+                v = r - np.asarray(d.get("pos0", (0.0, 0.0, 0.0)), np.float64)
+                along = v @ direction
+                from_axis = np.linalg.norm(direction * along - v)
+                x = along * np.sin(alpha) - from_axis * np.cos(alpha)
+                nrm = (along + from_axis * np.tan(alpha)) * direction - v
+                nrm = nrm / np.linalg.norm(nrm)
+            if x / sigma <= cutoff:
+                lj = (x / sigma) ** (-n)
+                F[i] += nrm * (4 * n * k * (2 * lj * lj - lj) / x)
+        elif t == "generic_central_force":
+            # GenericCentralForce::force, force_type = gravity (src/Forces/GenericCentralForce.cpp)
+            dv = np.asarray(d.get("center", (0.0, 0.0, 0.0)), np.float64) - r
+            d2 = dv @ dv
+            inner, outer = d.get("inner_cut_off", 0.0), d.get("outer_cut_off", 0.0)
+            if not (d2 < inner * inner) and not (outer > 0 and d2 > outer * outer):
+                F[i] += d.get("F0", 0.0) * dv / np.sqrt(d2)
+        elif t == "repulsion_plane_moving":
+            # RepulsionPlaneMoving::force (src/Forces/RepulsionPlaneMoving.cpp), one reference particle
+            x = (r - pos[int(d["ref_particle"])]) @ direction
+            F[i] += -d.get("stiff", 0.0) * direction * min(x, 0.0)
     return F

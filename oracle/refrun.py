@@ -33,7 +33,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_ref")
-PROGRAMS = {"cpu": os.path.join(OUT, "oxDNA_cpu"), "cuda": os.path.join(OUT, "oxDNA_cuda")}
+PROGRAMS = {"cpu": os.path.join(OUT, "oxDNA_cpu"), "cuda": os.path.join(OUT, "oxDNA_cuda"),
+            "cuda-gb300": os.path.join(OUT, "oxDNA_cuda_gb300"), "plugin": os.path.join(OUT, "plugins", "CUDAGB300DNA2.so")}
 
 
 def reference_checkout() -> Optional[str]:
@@ -45,7 +46,9 @@ def reference_checkout() -> Optional[str]:
 
 
 def build(kind: str, jobs: Optional[int] = None, log: Optional[str] = None) -> str:
-    """builds oxDNA_<kind> (kind: cpu or cuda) if it is missing; returns its path"""
+    """builds a reference program (kind: cpu, cuda, or cuda-gb300 -- the CUDA program with our
+    interaction and Verlet list linked in under the reference's class names) or the plugin
+    (plugin) if it is missing; returns its path"""
     exe = PROGRAMS[kind]
     if os.path.exists(exe):
         return exe
@@ -143,16 +146,18 @@ def time_steps(exe: str, s, steps_a: int, steps_b: int, folder: Optional[str] = 
 _CUDA_E = re.compile(r"CUDA_energy:\s*([-0-9.eE+]+)")
 
 
-def cuda_energy_per_nucleotide(exe: str, s, folder: Optional[str] = None, salt: float = 0.5) -> float:
+def cuda_energy_per_nucleotide(exe: str, s, folder: Optional[str] = None, salt: float = 0.5, interaction: str = "DNA2",
+                               extra: str = "") -> float:
     """the potential energy per nucleotide that the reference CUDA backend computes on the
     device (CUDA_print_energy) for the configuration of s: three steps with a vanishing time step
     and no thermostat, so the state does not move; the value printed after the first step"""
     tmp = folder or tempfile.mkdtemp(prefix="oxref_e_")
     write_system(tmp, s)
     # the backend_info observable prints the string CUDA_print_energy fills in each step
-    extra = ("CUDA_print_energy = true\n"
-             "data_output_1 = {\n  name = backend_info.dat\n  print_every = 1\n  col_1 = {\n    type = backend_info\n  }\n}\n")
-    text = deck(s, backend="CUDA", steps=3, dt=1e-12, salt=salt, print_every=1, extra=extra)
+    extra = extra + ("CUDA_print_energy = true\n"
+                     "data_output_1 = {\n  name = backend_info.dat\n  print_every = 1\n  col_1 = {\n"
+                     "    type = backend_info\n  }\n}\n")
+    text = deck(s, backend="CUDA", steps=3, dt=1e-12, salt=salt, print_every=1, interaction=interaction, extra=extra)
     r = run(exe, tmp, text, tag="input_e")
     info = open(os.path.join(tmp, "backend_info.dat")).read() if os.path.exists(os.path.join(tmp, "backend_info.dat")) else ""
     vals = [float(v) for v in _CUDA_E.findall(info + r["log"])]

@@ -44,11 +44,14 @@ class ExtForce(C.Structure):
         ("type", C.c_int), ("particle", C.c_int), ("ref_particle", C.c_int), ("flags", C.c_int),
         ("F0", C.c_double), ("rate", C.c_double), ("stiff", C.c_double), ("stiff_rate", C.c_double),
         ("r0", C.c_double), ("position", C.c_double), ("dir", C.c_double * 3), ("pos0", C.c_double * 3),
+        ("sigma", C.c_double), ("cutoff", C.c_double), ("p1", C.c_double), ("p2", C.c_double),
+        ("n", C.c_int), ("pad", C.c_int),
     ]
 
 
 FORCE_TYPES = {"constant": 0, "string": 0, "mutual_trap": 1, "trap": 2, "moving_trap": 2, "lowdim_trap": 3,
-               "repulsion_plane": 4, "attraction_plane": 5}
+               "repulsion_plane": 4, "attraction_plane": 5, "sphere": 6, "sphere_smooth": 7, "LJ_wall": 8,
+               "generic_central_force": 9, "repulsion_plane_moving": 10, "LJ_cone": 11}
 
 
 class MDSettings(C.Structure):

@@ -1498,15 +1498,17 @@ extern "C" int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_for
 	if(!h || n < 0 || (n > 0 && !f)) return fail(OXGB_E_INVALID, "invalid argument");
 	for(int m = 0; m < n; m++) {
 		const oxgb_ext_force &e = f[m];
-		if(e.type < OXGB_FORCE_CONSTANT || e.type > OXGB_FORCE_ATTRACTION_PLANE)
+		if(e.type < OXGB_FORCE_CONSTANT || e.type > OXGB_FORCE_LJ_CONE)
 			return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": unknown type");
 		if(e.particle < 0 || e.particle >= h->N) return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": particle out of range");
-		if(e.type == OXGB_FORCE_MUTUAL_TRAP) {
+		if((e.type == OXGB_FORCE_LJ_WALL || e.type == OXGB_FORCE_LJ_CONE) && (e.n <= 0 || e.n % 2 != 0 || !(e.sigma > 0)))
+			return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": n must be a positive even integer and sigma positive");
+		if(e.type == OXGB_FORCE_MUTUAL_TRAP || e.type == OXGB_FORCE_REPULSION_PLANE_MOVING) {
 			if(e.ref_particle < 0 || e.ref_particle >= h->N || e.ref_particle == e.particle)
 				return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": invalid ref_particle");
 			const auto sys_of = [&](int i) { return (int) (std::upper_bound(h->offsets.begin(), h->offsets.end(), i) - h->offsets.begin()) - 1; };
 			if(sys_of(e.ref_particle) != sys_of(e.particle))
-				return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": a mutual trap crosses two systems");
+				return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": the reference particle is in another system");
 		}
 	}
 	CK(cudaStreamSynchronize(h->stream));

@@ -804,6 +804,13 @@ OXGB_HD bool bonded_both(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q
 			e = R(0);
 			force = v3<R>{R(0), R(0), R(0)};
 		}
+		else if(sizeof(R) == 4) {
+			// FP32: Delta^2 - x^2 as (Delta - x)(Delta + x), exact to an ulp where a stretched
+			// bond makes the difference of squares cancel (Delta - x is exact there)
+			const R dd = (R(OXM_FENE_DELTA) - x) * (R(OXM_FENE_DELTA) + x);
+			e = -(R(OXM_FENE_EPS) / R(2)) * m_log(dd / R(OXM_FENE_DELTA2));
+			force = rback * (-(R(OXM_FENE_EPS) * x / dd) / rmod);
+		}
 		else {
 			e = -(R(OXM_FENE_EPS) / R(2)) * m_log(R(1) - x * x / R(OXM_FENE_DELTA2));
 			force = rback * (-(R(OXM_FENE_EPS) * x / (R(OXM_FENE_DELTA2) - x * x)) / rmod);

@@ -998,7 +998,7 @@ void force_shape_of(int k, int *npw, int *lanes, int *minb) {
 	if(minb) *minb = d.minb;
 }
 
-// External forces (CUDA_MD.cuh:97-200): one thread per nucleotide that has some, its records
+// External forces (CUDA_MD.cuh:97-555): one thread per nucleotide that has some, its records
 // in order (deterministic), added to the force the pair kernels left; FP64 positions.
 template <typename V4>
 __global__ void k_external(ForceArgs a) {
@@ -1061,6 +1061,74 @@ __global__ void k_external(ForceArgs a) {
 			const double d = e.dir[0] * r.x + e.dir[1] * r.y + e.dir[2] * r.z + e.position;
 			if(d < 0.0) fx += -d * e.stiff * e.dir[0], fy += -d * e.stiff * e.dir[1], fz += -d * e.stiff * e.dir[2];
 			else fx += -e.stiff * e.dir[0], fy += -e.stiff * e.dir[1], fz += -e.stiff * e.dir[2];
+			break;
+		}
+		case OXGB_FORCE_SPHERE:
+		case OXGB_FORCE_SPHERE_SMOOTH: {
+			// RepulsiveSphere / RepulsiveSphereSmooth::force (src/Forces/RepulsiveSphere*.cpp):
+			// minimum image of r - centre
+			const double L = a.sys_box ? (double) a.sys_box[a.sys ? a.sys[i] : 0] : (double) a.box;
+			double dx = r.x - e.pos0[0], dy = r.y - e.pos0[1], dz = r.z - e.pos0[2];
+			dx -= rint(dx / L) * L, dy -= rint(dy / L) * L, dz -= rint(dz / L) * L;
+			const double m = sqrt(dx * dx + dy * dy + dz * dz);
+			double c = 0.0;
+			if(e.type == OXGB_FORCE_SPHERE) {
+				const double R = e.r0 + e.rate * st;
+				if(m > R && m < e.cutoff) c = -e.stiff * (1.0 - R / m);
+			}
+			else if(!(m < e.r0 || m > e.cutoff)) {
+				if(m >= e.p1) c = -(e.stiff * 0.5 * exp((m - e.p1) / e.sigma)) / m;
+				else c = -(e.stiff * m - e.stiff * 0.5 * exp(-(m - e.p1) / e.sigma)) / m;
+			}
+			fx += dx * c, fy += dy * c, fz += dz * c;
+			break;
+		}
+		case OXGB_FORCE_LJ_WALL: {
+			// LJWall::force (src/Forces/LJWall.cpp)
+			const double x = e.dir[0] * r.x + e.dir[1] * r.y + e.dir[2] * r.z + e.position;
+			const double y = x / e.sigma;
+			if(y <= e.cutoff) {
+				const double lj = pow(y, (double) -e.n);
+				const double c = 4.0 * e.n * e.stiff * (2.0 * lj * lj - lj) / x;
+				fx += e.dir[0] * c, fy += e.dir[1] * c, fz += e.dir[2] * c;
+			}
+			break;
+		}
+		case OXGB_FORCE_CENTRAL: {
+			// GenericCentralForce::force, force_type = gravity (src/Forces/GenericCentralForce.cpp)
+			const double dx = e.pos0[0] - r.x, dy = e.pos0[1] - r.y, dz = e.pos0[2] - r.z;
+			const double d2 = dx * dx + dy * dy + dz * dz;
+			if(!(d2 < e.p1 * e.p1) && !(e.p2 > 0.0 && d2 > e.p2 * e.p2)) {
+				const double c = e.F0 / sqrt(d2);
+				fx += dx * c, fy += dy * c, fz += dz * c;
+			}
+			break;
+		}
+		case OXGB_FORCE_REPULSION_PLANE_MOVING: {
+			// RepulsionPlaneMoving::force (src/Forces/RepulsionPlaneMoving.cpp), one reference particle
+			const double4_32a q = a.posd[a.slot ? a.slot[e.ref_particle] : e.ref_particle];
+			const double x = (r.x - q.x) * e.dir[0] + (r.y - q.y) * e.dir[1] + (r.z - q.z) * e.dir[2];
+			const double c = -e.stiff * fmin(x, 0.0);
+			fx += e.dir[0] * c, fy += e.dir[1] * c, fz += e.dir[2] * c;
+			break;
+		}
+		case OXGB_FORCE_LJ_CONE: {
+			// LJCone::force (src/Forces/LJCone.cpp): apex pos0, axis dir, half-angle p1
+			const double vx = r.x - e.pos0[0], vy = r.y - e.pos0[1], vz = r.z - e.pos0[2];
+			const double along = vx * e.dir[0] + vy * e.dir[1] + vz * e.dir[2];
+			const double wx = e.dir[0] * along - vx, wy = e.dir[1] * along - vy, wz = e.dir[2] * along - vz;
+			const double from_axis = sqrt(wx * wx + wy * wy + wz * wz);
+			const double x = along * sin(e.p1) - from_axis * cos(e.p1);
+			const double y = x / e.sigma;
+			if(y <= e.cutoff) {
+				const double C = from_axis * tan(e.p1);
+				double nx = (along + C) * e.dir[0] - vx, ny = (along + C) * e.dir[1] - vy, nz = (along + C) * e.dir[2] - vz;
+				const double nn = sqrt(nx * nx + ny * ny + nz * nz);
+				nx /= nn, ny /= nn, nz /= nn;
+				const double lj = pow(y, (double) -e.n);
+				const double c = 4.0 * e.n * e.stiff * (2.0 * lj * lj - lj) / x;
+				fx += nx * c, fy += ny * c, fz += nz * c;
+			}
 			break;
 		}
 		default:

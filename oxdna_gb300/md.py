@@ -169,14 +169,19 @@ class MDSystem:
 
     def set_external_forces(self, forces):
         """External forces (oxgb_md_set_external_forces): a list of dicts with 'type' (constant /
-        string, mutual_trap, trap / moving_trap, lowdim_trap, repulsion_plane, attraction_plane),
-        'particle' and the parameters of oxgb_ext_force ('ref_particle', 'F0', 'rate', 'stiff',
-        'stiff_rate', 'r0', 'position', 'dir', 'pos0', and 'dir_as_centre' / 'PBC' / 'visibility'
-        for the flags).  Particle indices are global (offsets[k] + index within system k)."""
+        string, mutual_trap, trap / moving_trap, lowdim_trap, repulsion_plane, attraction_plane,
+        sphere, sphere_smooth, LJ_wall, generic_central_force, repulsion_plane_moving, LJ_cone),
+        'particle' and the parameters under the reference's external_forces_file keys
+        ('ref_particle', 'F0', 'rate', 'stiff', 'stiff_rate', 'r0', 'position', 'dir', 'pos0',
+        'center', 'r_ext', 'smooth', 'alpha', 'sigma', 'n', 'only_repulsive', 'inner_cut_off',
+        'outer_cut_off', and 'dir_as_centre' / 'PBC' / 'visibility' for the flags; the reference's
+        defaults where a key is left out).  Particle indices are global (offsets[k] + index
+        within system k); repulsion_plane_moving takes one reference particle per record."""
         arr = (_abi.ExtForce * max(1, len(forces)))()
         for m, d in enumerate(forces):
             e = arr[m]
-            e.type = _abi.FORCE_TYPES[d["type"]]
+            t = d["type"]
+            e.type = _abi.FORCE_TYPES[t]
             e.particle = int(d["particle"])
             e.ref_particle = int(d.get("ref_particle", -1))
             flags = 0
@@ -187,12 +192,32 @@ class MDSystem:
                 if on:
                     flags |= bit
             e.flags = flags
-            for key in ("F0", "rate", "stiff", "stiff_rate", "r0", "position"):
+            stiff_default = 1.0 if t in ("LJ_wall", "LJ_cone") else 0.0
+            for key in ("F0", "rate", "stiff_rate", "r0", "position"):
                 setattr(e, key, float(d.get(key, 0.0)))
-            for key in ("dir", "pos0"):
-                v = d.get(key, (0.0, 0.0, 0.0))
-                for c in range(3):
-                    getattr(e, key)[c] = float(v[c])
+            e.stiff = float(d.get("stiff", stiff_default))
+            pos0 = d.get("center", d.get("pos0", (0.0, 0.0, 0.0)))
+            for c in range(3):
+                e.dir[c] = float(d.get("dir", (0.0, 0.0, 0.0))[c])
+                e.pos0[c] = float(pos0[c])
+            e.n = int(d.get("n", 6))
+            if t in ("sphere", "sphere_smooth"):
+                e.cutoff = float(d.get("r_ext", 1e10))
+                e.sigma = float(d.get("smooth", -1.0))
+                e.p1 = float(d.get("alpha", -1.0))
+                if t == "sphere_smooth":
+                    e.r0 = float(d.get("r0", -1.0))
+                if t == "sphere":
+                    e.r0 = float(d.get("r0", -1.0))
+            elif t in ("LJ_wall", "LJ_cone"):
+                e.sigma = float(d.get("sigma", 1.0))
+                e.cutoff = 2.0 ** (1.0 / e.n) if d.get("only_repulsive") else 1e6
+                e.p1 = float(d.get("alpha", 0.0))
+                if t == "LJ_wall":
+                    e.position = float(d.get("position", -1.0))
+            elif t == "generic_central_force":
+                e.p1 = float(d.get("inner_cut_off", 0.0))
+                e.p2 = float(d.get("outer_cut_off", 0.0))
         _abi.check(_abi.lib().oxgb_md_set_external_forces(self._h, len(forces), arr))
 
     def scale_momenta(self, f: float, k: int = 0):

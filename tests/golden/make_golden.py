@@ -134,18 +134,36 @@ def run_case(name, top_path, conf_path, settings, extra="", steps=0, dt=0.003):
 # the external forces of the ext_forces fixture, as the dicts MDSystem.set_external_forces and
 # oracle.external_forces take, and as the reference's external_forces_file records
 # (src/Forces/{ConstantRateForce,MutualTrap,MovingTrap,LowdimMovingTrap,RepulsionPlane,
-# AttractionPlane}.cpp): six types, rates and a periodic mutual trap
-def ext_force_set(N, box):
+# AttractionPlane,RepulsiveSphere,RepulsiveSphereSmooth,LJWall,GenericCentralForce,
+# RepulsionPlaneMoving,LJCone}.cpp): twelve types, rates, a periodic mutual trap; the geometric
+# parameters are placed relative to the configuration pos so that every record acts
+def ext_force_set(N, box, pos):
+    com = pos.mean(axis=0)
+    zmin = float(pos[:, 2].min())
+    u = np.array([0.48, -0.6, 0.64])
     return [
         dict(type="string", particle=0, F0=0.3, rate=1e-3, dir=(0.0, 0.6, 0.8)),
         dict(type="string", particle=5, F0=0.2, rate=0.0, dir=(1.0, 2.0, 3.0), dir_as_centre=True),
         dict(type="mutual_trap", particle=2, ref_particle=N - 3, stiff=0.9, r0=1.2, rate=2e-3, stiff_rate=1e-3),
-        dict(type="mutual_trap", particle=N - 3, ref_particle=2, stiff=0.9, r0=1.2, PBC=True),
+        dict(type="mutual_trap", particle=N - 3, ref_particle=2, stiff=0.9, r0=0.5, PBC=True),
         dict(type="trap", particle=7, stiff=1.5, pos0=(1.0, -2.0, 0.5), rate=1e-2, dir=(0.0, 0.0, 1.0)),
         dict(type="lowdim_trap", particle=7, stiff=0.7, pos0=(0.5, 0.0, -0.5), rate=3e-3, dir=(1.0, 0.0, 0.0),
              visibility=(True, False, True)),
-        dict(type="repulsion_plane", particle=9, stiff=2.0, dir=(0.0, 0.0, 1.0), position=box, r0=0.0, rate=-0.05),
+        dict(type="repulsion_plane", particle=9, stiff=2.0, dir=(0.0, 0.0, 1.0), position=box,
+             r0=-(float(pos[:, 2].max()) + 1.0), rate=-0.05),
         dict(type="attraction_plane", particle=11, stiff=0.4, dir=(1.0, 0.0, 0.0), position=-1.0),
+        dict(type="sphere", particle=13, stiff=0.8, r0=0.2, rate=1e-4, center=tuple(com)),
+        dict(type="sphere", particle=1, stiff=0.8, r0=0.2, rate=1e-4, r_ext=30.0, center=tuple(com + box)),
+        dict(type="sphere_smooth", particle=14, stiff=0.3, r0=0.1, r_ext=30.0, smooth=30.0, alpha=30.0,
+             center=tuple(com)),
+        dict(type="LJ_wall", particle=15, stiff=1.0, sigma=1.0, n=6, dir=(0.0, 0.0, 1.0), position=1.0 - zmin),
+        dict(type="LJ_wall", particle=16, stiff=0.5, sigma=1.2, n=8, dir=(0.0, 0.0, 1.0), position=1.0 - float(pos[16, 2]),
+             only_repulsive=True),
+        dict(type="generic_central_force", particle=17, F0=0.7, inner_cut_off=0.5, center=tuple(com + [3.0, 0.0, 0.0])),
+        dict(type="repulsion_plane_moving", particle=18, ref_particle=3, stiff=1.7, dir=tuple(u)),
+        dict(type="repulsion_plane_moving", particle=18, ref_particle=4, stiff=1.7, dir=tuple(u)),
+        dict(type="LJ_cone", particle=19, stiff=1.0, sigma=1.0, n=6, alpha=1.0, dir=(0.0, 0.0, 1.0),
+             pos0=tuple(pos[19] - [0.2, 0.1, 1.8])),
     ]
 
 
@@ -173,6 +191,27 @@ def ext_force_file(forces):
             kv.update(stiff=d["stiff"], position=d["position"], end_position=d["r0"], v=d["rate"], dir=vec(d["dir"]))
         elif t == "attraction_plane":
             kv.update(stiff=d["stiff"], position=d["position"], dir=vec(d["dir"]))
+        elif t == "sphere":
+            kv.update(stiff=d["stiff"], r0=d["r0"], rate=d.get("rate", 0.0), center=vec(d["center"]))
+            if "r_ext" in d:
+                kv["r_ext"] = d["r_ext"]
+        elif t == "sphere_smooth":
+            # the reference reads the smoothing length and alpha from the key r_ext as well
+            # (src/Forces/RepulsiveSphereSmooth.cpp:27-29): the fixture keeps the three equal
+            assert d["smooth"] == d["alpha"] == d["r_ext"]
+            kv.update(stiff=d["stiff"], r0=d["r0"], r_ext=d["r_ext"], center=vec(d["center"]))
+        elif t == "LJ_wall":
+            kv.update(stiff=d["stiff"], sigma=d["sigma"], n=d["n"], position=d["position"], dir=vec(d["dir"]))
+            if d.get("only_repulsive"):
+                kv["only_repulsive"] = "true"
+        elif t == "generic_central_force":
+            kv.update(force_type="gravity", F0=d["F0"], inner_cut_off=d.get("inner_cut_off", 0.0),
+                      outer_cut_off=d.get("outer_cut_off", 0.0), center=vec(d["center"]))
+        elif t == "repulsion_plane_moving":
+            kv.update(ref_particle=d["ref_particle"], stiff=d["stiff"], dir=vec(d["dir"]))
+        elif t == "LJ_cone":
+            kv.update(stiff=d["stiff"], sigma=d["sigma"], n=d["n"], alpha=d["alpha"], dir=vec(d["dir"]),
+                      pos0=vec(d["pos0"]))
         out.append("{\n" + "".join(f"{k} = {v}\n" for k, v in kv.items()) + "}\n")
     return "".join(out)
 
@@ -181,7 +220,7 @@ def run_ext_case(name, s, settings, step):
     """the external forces the reference adds at MD step `step` (the configuration's time, kept
     by restart_step_counter = 0): the reference's forces with and without them"""
     import json
-    forces = ext_force_set(s.N, float(s.box))
+    forces = ext_force_set(s.N, float(s.box), s.pos)
     dumps = {}
     with tempfile.TemporaryDirectory() as tmp:
         s.write(os.path.join(tmp, "init.top"), os.path.join(tmp, "init.dat"))

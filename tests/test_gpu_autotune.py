@@ -34,8 +34,12 @@ def test_every_shape_gives_the_default_forces():
         F, T, _ = m.get_forces()
         assert np.abs(F - F0).max() <= 1e-6 * scale, k
         assert np.abs(T - T0).max() <= 1e-6 * max(1.0, np.abs(T0).max()), k
-        m.run(50)  # a graph with this shape runs
     assert len(shapes) == 6
+    # every shape also runs inside the step graph (captured again after each change)
+    for k in range(6):
+        m.set_force_shape(k)
+        m.run(50)
+        assert np.all(np.isfinite(m.get_state()["pos"])), k
     m.close()
 
 

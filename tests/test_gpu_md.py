@@ -177,3 +177,29 @@ def test_state_round_trip_and_rejected_state():
     sysm.run(10)
     assert np.all(np.isfinite(sysm.get_state()["pos"]))
     sysm.close()
+
+
+def test_output_files_follow_the_engine(tmp_path):
+    """Energy file and trajectory written from the engine (oxdna_gb300.output) agree with the
+    engine's own state and FP64 energies at the printing steps."""
+    from oxdna_gb300 import output
+    g = load_golden("duplex24")
+    sysm, _ = system_from_golden(g, precision="mixed", dt=0.003)
+    from gpu_util import topology_from_golden
+    top = topology_from_golden(g)
+    e, t = str(tmp_path / "energy.dat"), str(tmp_path / "traj.dat")
+    out = output.Output(sysm, top, float(g["box"]), 0.003, energy_file=e, trajectory_file=t, back_in_box=False)
+    output.run_with_output(sysm, 300, out, print_energy_every=100, print_conf_interval=300)
+    rows = np.loadtxt(e)
+    assert rows.shape == (4, 4)
+    U, Kt, Kr = sysm.energies()
+    N = g["pos"].shape[0]
+    assert abs(rows[-1, 1] - U / N) < 1e-6 and abs(rows[-1, 2] - (Kt + Kr) / N) < 1e-6
+    frames = open(t).read().split("t = ")[1:]
+    assert len(frames) == 2
+    last = tmp_path / "last.dat"
+    last.write_text("t = " + frames[-1])
+    conf = oxio.read_conf(str(last))
+    st = sysm.get_state()
+    assert conf.t == 300 and np.abs(conf.pos - st["pos"]).max() < 1e-12
+    sysm.close()
