@@ -697,7 +697,7 @@ def plain_run(args, name, rank, world, torch, ox, _abi, peak):
     md = ox.md_settings(dt=wl["dt"], thermostat=wl["thermostat"], newtonian_steps=wl["newtonian_steps"],
                         bussi_tau=wl.get("bussi_tau", 1000.0), diff_coeff=wl.get("diff_coeff", 2.5), seed=1 + rank,
                         precision="mixed", steps_per_graph=25, list_rebuild_node=args.list_node,
-                        sort_every=sort_every, autotune=not args.no_autotune)
+                        sort_every=sort_every, autotune=not args.no_autotune, use_edge=args.use_edge)
     sysm = ox.MDSystem(s.box, s.top, ox.dna2_settings(s.T, 0.5), md)
     sysm.set_state(s.pos, quat, s.vel, s.L)
     shape = sysm.force_shape()
@@ -740,7 +740,8 @@ def plain_run(args, name, rank, world, torch, ox, _abi, peak):
     rebuilds = info1["rebuilds"] - info0["rebuilds"]
     out = {"value": world * s.N * steps_total / t_dev, "unit": "particle-steps/s", "ms_per_step": t_dev / args.steps * 1e3,
            "n_nucleotides": s.N, "md_steps_per_step": M, "md_steps_per_s": steps_total / t_dev,
-           "list_rebuilds": rebuilds, "clocks": clk, "description": wl["desc"], "force_shape": shape}
+           "list_rebuilds": rebuilds, "clocks": clk, "description": wl["desc"], "force_shape": shape,
+           "use_edge": bool(args.use_edge)}
     out["roofline"] = roofline_of(ox, L, _abi, sysm, stream, torch, [s], peak, FORCE_TRAFFIC.get(name))
     st = sysm.get_state()
     if rank == 0 and not args.no_cpu_baseline:
@@ -824,6 +825,8 @@ def main():
     ap.add_argument("--port-baseline", action="store_true", help="time the FP64 oracle port as the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default force-kernel shape instead of the autotuned one")
+    ap.add_argument("--use-edge", action="store_true",
+                    help="use_edge: Debye-Hueckel and excluded volume once per pair with atomic adds (A/B variant)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-system batched workload")
     ap.add_argument("--list-node", default="conditional", choices=["conditional", "kernel"],
                     help="list rebuild as a conditional graph node, or as always-launched kernels that "

@@ -26,6 +26,9 @@
 #define OXGB_H
 
 #include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -97,6 +100,24 @@ int oxgb_dna2_set_temperature(oxgb_dna2 *h, double T);
 int oxgb_dna2_compute_forces(oxgb_dna2 *h, int N, double box, const void *d_poss, const void *d_orientations,
 		void *d_forces, void *d_torques, const void *d_bonds, const int *d_matrix_neighs, const int *d_number_neighs,
 		int max_neigh, long long stride_i, long long stride_k, void *stream);
+/*
+ * The FFS order-parameter kernels of CUDADNAInteraction (_hb_op_precalc, _near_hb_op_precalc,
+ * _dist_op_precalc: src/CUDA/Interactions/CUDADNAInteraction.cu:205-218, kernels in
+ * src/CUDA/Interactions/CUDA_DNA.cuh:910-1067) on the same device layout as compute_forces, for
+ * the n_pairs pairs (d_op_pairs1[k], d_op_pairs2[k]):
+ *   hb_op_precalc       d_hb_energies[k] = the pair's hydrogen-bonding energy (f1 times the six
+ *                       f4 factors; no hb_multiplier, as the reference kernel);
+ *   near_hb_op_precalc  d_nearly_bonded[k] (one byte, C bool) = at least six of those seven
+ *                       factors are on (f1 < 0, each f4 > 0);
+ *   dist_op_precalc     d_op_dists[k] = the distance between the two base sites.
+ * Centre separations at the minimum image of the cubic box of side box.  Asynchronous on stream.
+ */
+int oxgb_dna2_hb_op_precalc(oxgb_dna2 *h, double box, const void *d_poss, const void *d_orientations,
+		const int *d_op_pairs1, const int *d_op_pairs2, int n_pairs, float *d_hb_energies, void *stream);
+int oxgb_dna2_near_hb_op_precalc(oxgb_dna2 *h, double box, const void *d_poss, const void *d_orientations,
+		const int *d_op_pairs1, const int *d_op_pairs2, int n_pairs, bool *d_nearly_bonded, void *stream);
+int oxgb_dna2_dist_op_precalc(oxgb_dna2 *h, double box, const void *d_poss, const void *d_orientations,
+		const int *d_op_pairs1, const int *d_op_pairs2, int n_pairs, float *d_op_dists, void *stream);
 int oxgb_dna2_destroy(oxgb_dna2 *h);
 
 /* ------------------------------------------------------------------ Verlet list layer */
@@ -182,6 +203,12 @@ typedef struct oxgb_md_settings {
 	                               work distribution, not the arithmetic of a pair.  The reference has
 	                               no counterpart (a fixed 64 threads per block,
 	                               src/CUDA/Backends/CUDABaseBackend.cu:244-261). */
+	int use_edge;               /* use_edge (CUDABaseInteraction / CUDASimpleVerletList get_settings;
+	                               kernels CUDA_DNA.cuh:727-830): 1 evaluates Debye-Hueckel and the
+	                               excluded volume once per unordered pair, adding both nucleotides'
+	                               shares with atomic adds (the summation order, and so the last bits of
+	                               the forces, then vary from run to run; the shape is the default one);
+	                               0 (default): each pair from both ends, a fixed order */
 } oxgb_md_settings;
 
 void oxgb_md_default_settings(oxgb_md_settings *s);

@@ -773,6 +773,52 @@ long oxo_pairs_within(int N, const double *pos, double L, double rc, int *pairs,
 	return count;
 }
 
+/* ---------------------------------------------------------------- FFS order parameters */
+
+/* The per-pair order-parameter quantities of the reference's FFS backend, as its CUDA kernels
+ * define them (src/CUDA/Interactions/CUDA_DNA.cuh:910-1067): for the pair (op1[k], op2[k]), with
+ * the centre separation taken at its minimum image and the base sites at POS_BASE a1,
+ *   mode 0 (hb_op_precalc):      the hydrogen-bonding energy f1 f4(t1) f4(t2) f4(t3) f4(t4)
+ *                                f4(t7) f4(t8) of the pair (0 unless the bases are complementary
+ *                                and the base-base distance is inside (RCLOW, RCHIGH)); unlike
+ *                                the force field's own term it carries no hb_multiplier;
+ *   mode 1 (near_hb_op_precalc): 1 if at least six of the seven factors are "on" (f1 < 0, each
+ *                                f4 > 0), else 0;
+ *   mode 2 (dist_op_precalc):    the base-base distance |r + b1 POS_BASE - a1 POS_BASE|.
+ * FP64; out[k] receives the value. */
+void oxo_order_params(const oxo_params *P, const double *pos, const double *a1v, const double *a3v, const int *type,
+		const int *btype, double L, const int *op1, const int *op2, int n, int mode, double *out) {
+	for(int k = 0; k < n; k++) {
+		const int i = op1[k], j = op2[k];
+		vec r = sub(load(pos, j), load(pos, i));
+		r = V(min_image1(r.x, L), min_image1(r.y, L), min_image1(r.z, L));
+		const vec a1 = load(a1v, i), a3 = load(a3v, i), b1 = load(a1v, j), b3 = load(a3v, j);
+		const vec rb = add(r, sub(mul(b1, (double) OXM_POS_BASE), mul(a1, (double) OXM_POS_BASE)));
+		const double r2 = dot(rb, rb);
+		if(mode == 2) {
+			out[k] = sqrt(r2);
+			continue;
+		}
+		double e = 0., near = 0.;
+		if(btype[i] + btype[j] == 3 && SQR(OXM_HYDR_RCLOW) < r2 && r2 < SQR(OXM_HYDR_RCHIGH)) {
+			const double rmod = sqrt(r2);
+			const vec rd = mul(rb, 1. / rmod);
+			const double F1 = f1(P, rmod, OXM_F1_HB, type[i], type[j]);
+			const double g[6] = {cf4(P, -dot(a1, b1), OXM_F4_HB_T1), cf4(P, -dot(b1, rd), OXM_F4_HB_T2),
+					cf4(P, dot(a1, rd), OXM_F4_HB_T2), cf4(P, dot(a3, b3), OXM_F4_HB_T4), cf4(P, -dot(rd, b3), OXM_F4_HB_T7),
+					cf4(P, dot(rd, a3), OXM_F4_HB_T7)};
+			e = F1;
+			int on = F1 < 0;
+			for(int m = 0; m < 6; m++) {
+				e *= g[m];
+				on += g[m] > 0;
+			}
+			near = on >= 6;
+		}
+		out[k] = mode == 0 ? e : near;
+	}
+}
+
 /* ---------------------------------------------------------------- full force evaluation */
 
 int oxo_forces(const oxo_params *P, int N, const double *pos, const double *a1, const double *a2, const double *a3,

@@ -79,6 +79,11 @@ int oxo_forces(const oxo_params *p, int N, const double *pos, const double *a1, 
  */
 long oxo_pairs_within(int N, const double *pos, double L, double rc, int *pairs, long max_pairs);
 
+/* FFS order-parameter quantities of pairs (op1[k], op2[k]): mode 0 hydrogen-bonding energy, 1
+ * nearly-bonded flag, 2 base-base distance (CUDA_DNA.cuh:910-1067) */
+void oxo_order_params(const oxo_params *P, const double *pos, const double *a1, const double *a3, const int *type,
+		const int *btype, double L, const int *op1, const int *op2, int n, int mode, double *out);
+
 /*
  * FP32 restatement of the GPU Verlet-list build: cell of every particle and the full
  * neighbour set, with the cell count rules of CUDASimpleVerletList::_compute_N_cells_side

@@ -83,6 +83,8 @@ def lib():
         L.oxo_forces.restype = C.c_int
         L.oxo_pairs_within.argtypes = [C.c_int, dp, C.c_double, C.c_double, ip, C.c_long]
         L.oxo_pairs_within.restype = C.c_long
+        L.oxo_order_params.argtypes = [C.POINTER(Params), dp, dp, dp, ip, ip, C.c_double, ip, ip, C.c_int, C.c_int, dp]
+        L.oxo_order_params.restype = None
         L.oxo_verlet_f32.argtypes = [C.c_int, fp, C.c_float, C.c_float, ip, ip, C.c_int, C.POINTER(C.c_int), ip, ip,
                                      ip, C.c_int]
         L.oxo_verlet_f32.restype = C.c_int
@@ -149,6 +151,17 @@ def forces(params: Params, pos, a1, a2, a3, n3, n5, typ, btype, L: float, pairs=
                           _c(n5, np.int32), _c(typ, np.int32), _c(btype, np.int32), float(L), pp, npairs, F, T, Es,
                           Ep, nthreads)
     return rc, F.reshape(N, 3), T.reshape(N, 3), Es, Ep[:N]
+
+
+def order_params(params: Params, pos, a1, a3, typ, btype, L: float, op1, op2, mode: int) -> np.ndarray:
+    """FFS order-parameter quantities of the pairs (op1[k], op2[k]) (oxo_order_params): mode 0
+    hydrogen-bonding energy, 1 nearly-bonded flag (0/1), 2 base-base distance."""
+    op1, op2 = _c(op1, np.int32), _c(op2, np.int32)
+    out = np.zeros(op1.size)
+    lib().oxo_order_params(C.byref(params), _c(pos, np.float64).reshape(-1), _c(a1, np.float64).reshape(-1),
+                           _c(a3, np.float64).reshape(-1), _c(typ, np.int32), _c(btype, np.int32), float(L), op1, op2,
+                           int(op1.size), int(mode), out)
+    return out
 
 
 def pairs_within(pos, L: float, rc: float) -> np.ndarray:

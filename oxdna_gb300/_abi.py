@@ -61,6 +61,7 @@ class MDSettings(C.Structure):
         ("precision", C.c_int), ("cells_auto_optimisation", C.c_int), ("max_neigh", C.c_int),
         ("steps_per_graph", C.c_int), ("list_rebuild_node", C.c_int), ("sort_every", C.c_int),
         ("autotune", C.c_int),
+        ("use_edge", C.c_int),
     ]
 
 
@@ -80,6 +81,9 @@ SIGNATURES = {
     "oxgb_dna2_set_temperature": (C.c_int, [_VP, C.c_double]),
     "oxgb_dna2_compute_forces": (C.c_int, [_VP, C.c_int, C.c_double, _VP, _VP, _VP, _VP, _VP, _VP, _VP, C.c_int,
                                            C.c_longlong, C.c_longlong, _VP]),
+    "oxgb_dna2_hb_op_precalc": (C.c_int, [_VP, C.c_double, _VP, _VP, _VP, _VP, C.c_int, _VP, _VP]),
+    "oxgb_dna2_near_hb_op_precalc": (C.c_int, [_VP, C.c_double, _VP, _VP, _VP, _VP, C.c_int, _VP, _VP]),
+    "oxgb_dna2_dist_op_precalc": (C.c_int, [_VP, C.c_double, _VP, _VP, _VP, _VP, C.c_int, _VP, _VP]),
     "oxgb_dna2_destroy": (C.c_int, [_VP]),
     "oxgb_verlet_create": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.POINTER(_VP)]),
     "oxgb_verlet_update": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),

@@ -163,6 +163,37 @@ extern "C" int oxgb_dna2_compute_forces(oxgb_dna2 *h, int N, double box, const v
 	return OXGB_OK;
 }
 
+// the FFS order-parameter kernels (CUDA_DNA.cuh:910-1067) behind the three entry points below
+static int dna2_order_params(oxgb_dna2 *h, int mode, double box, const void *d_poss, const void *d_orientations,
+		const int *op1, const int *op2, int n, float *val, bool *flag, void *stream) {
+	if(!h || n < 0 || !(box > 0)) return fail(OXGB_E_INVALID, "invalid argument");
+	if(n == 0) return OXGB_OK;
+	if(!d_poss || !d_orientations || !op1 || !op2 || (mode == 1 ? !flag : !val)) return fail(OXGB_E_INVALID, "null device buffer");
+	if(box != h->box_uploaded) {
+		int rc = dna2_upload(h, box);
+		if(rc) return rc;
+	}
+	CK(launch_order_params(mode, (const float4 *) d_poss, (const float4 *) d_orientations, op1, op2, n, h->d_tab, val, flag,
+			(cudaStream_t) stream));
+	return OXGB_OK;
+}
+
+extern "C" int oxgb_dna2_hb_op_precalc(oxgb_dna2 *h, double box, const void *d_poss, const void *d_orientations,
+		const int *d_op_pairs1, const int *d_op_pairs2, int n_pairs, float *d_hb_energies, void *stream) {
+	return dna2_order_params(h, 0, box, d_poss, d_orientations, d_op_pairs1, d_op_pairs2, n_pairs, d_hb_energies, nullptr, stream);
+}
+
+extern "C" int oxgb_dna2_near_hb_op_precalc(oxgb_dna2 *h, double box, const void *d_poss, const void *d_orientations,
+		const int *d_op_pairs1, const int *d_op_pairs2, int n_pairs, bool *d_nearly_bonded, void *stream) {
+	return dna2_order_params(h, 1, box, d_poss, d_orientations, d_op_pairs1, d_op_pairs2, n_pairs, nullptr, d_nearly_bonded,
+			stream);
+}
+
+extern "C" int oxgb_dna2_dist_op_precalc(oxgb_dna2 *h, double box, const void *d_poss, const void *d_orientations,
+		const int *d_op_pairs1, const int *d_op_pairs2, int n_pairs, float *d_op_dists, void *stream) {
+	return dna2_order_params(h, 2, box, d_poss, d_orientations, d_op_pairs1, d_op_pairs2, n_pairs, d_op_dists, nullptr, stream);
+}
+
 extern "C" int oxgb_dna2_destroy(oxgb_dna2 *h) {
 	if(!h) return OXGB_OK;
 	cudaFree(h->d_tab);
@@ -364,6 +395,7 @@ struct oxgb_md {
 	float4 *list_a1 = nullptr, *list_back = nullptr;
 	int2 *bonds = nullptr;
 	void *F = nullptr, *T = nullptr, *bond_f = nullptr, *bond_tp = nullptr, *bond_tq = nullptr;
+	void *edge_acc = nullptr;  // use_edge: per-nucleotide sums of the edge blocks (2 V4 each)
 	void *Fe = nullptr, *Te = nullptr;    // forces with energies (w), evaluated on request
 	void *d_tab = nullptr;                // one table per system
 	int *d_sys = nullptr, *d_sys_off = nullptr, *d_sys_nside = nullptr, *d_sys_cell0 = nullptr, *d_cell_sys = nullptr;
@@ -421,7 +453,7 @@ struct oxgb_md {
 		free_layout();
 		for(void *p : {(void *) posd, (void *) veld, (void *) Ld, (void *) quatd, (void *) pos_hi, (void *) pos_lo, (void *) fa1, (void *) fa3,
 					(void *) fback, (void *) fa1lo, (void *) fbacklo, (void *) list_pos, (void *) list_a1, (void *) list_back, (void *) bonds, F, T, Fe, Te, bond_f,
-					bond_tp, bond_tq, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
+					bond_tp, bond_tq, edge_acc, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
 					(void *) bussi_stamp, (void *) open_step, (void *) bussi_done, (void *) bussi_prep_done, (void *) bussi_tot, (void *) bussi_fpart, (void *) term_max, ext_rec, (void *) ext_nuc, (void *) ext_off, (void *) d_rebuilds})
@@ -532,6 +564,8 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.status = h->status;
 	a.esplit = h->esplit;
 	a.shape = h->shape;
+	a.edge = h->md.use_edge ? 1 : 0;
+	a.edge_acc = h->edge_acc;
 	a.fback = h->fback;
 	a.fa1lo = h->fa1lo;
 	a.fbacklo = h->fbacklo;
@@ -742,6 +776,10 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	ok &= cudaMalloc(&h->bond_f, v4 * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->bond_tp, v4 * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->bond_tq, v4 * N) == cudaSuccess;
+	if(h->md.use_edge) {
+		ok &= cudaMalloc(&h->edge_acc, 2 * v4 * N) == cudaSuccess;
+		ok = ok && cudaMemset(h->edge_acc, 0, 2 * v4 * N) == cudaSuccess;
+	}
 	ok &= cudaMalloc(&h->bonds, sizeof(int2) * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->F, v4 * N) == cudaSuccess;
 	ok &= cudaMalloc(&h->T, v4 * N) == cudaSuccess;
@@ -1129,7 +1167,8 @@ extern "C" int oxgb_md_set_state(oxgb_md *h, const double *pos, const double *qu
 	if(rc) return rc;
 	rc = compute_forces_now(h);
 	if(rc) return rc;
-	if(h->md.autotune) {
+	// use_edge runs the default shape: nothing to tune
+	if(h->md.autotune && !h->md.use_edge) {
 		rc = autotune_shape(h);
 		if(rc) return rc;
 	}

@@ -105,32 +105,38 @@ struct LoadMixed {
 	// (|q - p| < r_verlet, far below box / 2) has d / box at least 0.4 from a half-integer, so
 	// the product with an approximate inverse rounds to the same integer as the quotient;
 	// rounding by the 1.5 * 2^23 addition (|d / box| < 2^22) keeps it on the FMA pipe.
-	// In one image (m = 0) the hi difference of two nearby coordinates is within half an ulp
-	// of |d| < r_verlet.  Across images (unwrapped coordinates a box side or more apart) it
-	// rounds at the ulp of the box side, 7.6e-6 for a box of 158, which the stiff excluded
-	// volume (force slope ~10^4) turns into force errors of 1e-2: there the exact remainder of
-	// the hi difference (two_sum) joins the low part.  The shift by m box sides is then exact
-	// (the result is a small multiple of the ulp of d and of box_hi); the box remainder goes
-	// to lo.  Pairs across images are few and sit in the cells at the box faces, so the branch
-	// is taken by few warps.  sep_soft leaves the remainder out, for Debye-Hueckel alone: its
-	// force slope is below 0.1, so the 7.6e-6 moves its force by less than 1e-6.
+	// The FP32 difference of the hi parts is exact only for coordinates of one sign within a
+	// factor of two of each other.  Otherwise -- coordinates on both sides of zero (a few per
+	// cent of the nucleotides of a large box, in each dimension), or unwrapped coordinates a box
+	// side or more apart -- it rounds at half an ulp of the result (2e-8 for a bonded
+	// separation of 0.66, 3.8e-6 across the images of a box of 158), which the stiff excluded
+	// volume (force slope up to 1.6e4) turns into force errors of 1e-4 and more.  The exact
+	// remainder of the hi difference (two_sum) therefore always joins the low part.  The shift
+	// by m box sides is then exact (the result is a small multiple of the ulp of d and of
+	// box_hi); the box remainder goes to lo.  sep_soft leaves the remainder out, for
+	// Debye-Hueckel and for screening: Debye-Hueckel's force slope is below 0.1, so the 3.8e-6
+	// moves its force by less than 1e-6.
 	template <bool EXACT = true>
 	__device__ __forceinline__ Sep<float> sep(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql,
 			const DNA2Table<float> &P) const {
-		float d[3] = {qh.x - ph.x, qh.y - ph.y, qh.z - ph.z};
-		float l[3] = {ql.x - pl.x, ql.y - pl.y, ql.z - pl.z};
-		float m[3];
+		const float qv[3] = {qh.x, qh.y, qh.z}, pv[3] = {ph.x, ph.y, ph.z};
+		float d[3], l[3] = {ql.x - pl.x, ql.y - pl.y, ql.z - pl.z};
 #pragma unroll
-		for(int k = 0; k < 3; k++) m[k] = __fsub_rn(__fmaf_rn(d[k], P.inv_box, 12582912.f), 12582912.f);
-		if(EXACT && (m[0] != 0.f || m[1] != 0.f || m[2] != 0.f)) {
-			const float qv[3] = {qh.x, qh.y, qh.z}, pv[3] = {ph.x, ph.y, ph.z};
-#pragma unroll
-			for(int k = 0; k < 3; k++) l[k] = __fadd_rn(l[k], two_sum(qv[k], -pv[k]).e);
+		for(int k = 0; k < 3; k++) {
+			if(EXACT) {
+				const F2 t = two_sum(qv[k], -pv[k]);
+				d[k] = t.s;
+				l[k] = __fadd_rn(l[k], t.e);
+			}
+			else {
+				d[k] = qv[k] - pv[k];
+			}
 		}
 #pragma unroll
 		for(int k = 0; k < 3; k++) {
-			d[k] = fmaf(-m[k], P.box_hi, d[k]);
-			l[k] = fmaf(-m[k], P.box_lo, l[k]);
+			const float m = __fsub_rn(__fmaf_rn(d[k], P.inv_box, 12582912.f), 12582912.f);
+			d[k] = fmaf(-m, P.box_hi, d[k]);
+			l[k] = fmaf(-m, P.box_lo, l[k]);
 		}
 		return Sep<float>{v3<float>{d[0], d[1], d[2]}, v3<float>{l[0], l[1], l[2]}};
 	}
@@ -138,9 +144,11 @@ struct LoadMixed {
 			const DNA2Table<float> &P) const {
 		return sep<false>(ph, pl, qh, ql, P);
 	}
-	// bonded neighbours: no periodic image
+	// bonded neighbours: no periodic image; the hi difference's remainder as in sep
 	__device__ __forceinline__ Sep<float> diff(const float4 &ph, const float4 &pl, const float4 &qh, const float4 &ql) const {
-		return Sep<float>{v3<float>{qh.x - ph.x, qh.y - ph.y, qh.z - ph.z}, v3<float>{ql.x - pl.x, ql.y - pl.y, ql.z - pl.z}};
+		const F2 x = two_sum(qh.x, -ph.x), y = two_sum(qh.y, -ph.y), z = two_sum(qh.z, -ph.z);
+		return Sep<float>{v3<float>{x.s, y.s, z.s}, v3<float>{__fadd_rn(ql.x - pl.x, x.e), __fadd_rn(ql.y - pl.y, y.e),
+				__fadd_rn(ql.z - pl.z, z.e)}};
 	}
 };
 
@@ -336,6 +344,69 @@ static int grid_for(int N, int warps_per_block) {
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s) {
 	LoadRef ld{a.pos_hi, a.quat};
 	k_forces<float, LoadRef, false, true><<<grid_for(a.N, 4), 128, 0, s>>>(a, ld);
+	return cudaGetLastError();
+}
+
+// FFS order parameters on the reference layout (hb_op_precalc, near_hb_op_precalc and
+// dist_op_precalc, src/CUDA/Interactions/CUDA_DNA.cuh:910-1067): one thread per listed pair
+// (op1[k], op2[k]), centre separation at its FP32 minimum image, base sites at POS_BASE a1.
+//   MODE 0: the pair's hydrogen-bonding energy f1 f4(t1) f4(t2) f4(t3) f4(t4) f4(t7) f4(t8)
+//           (no hb_multiplier, as the reference's kernel), 0 unless the bases are complementary
+//           and their distance is inside the hydrogen-bonding window;
+//   MODE 1: "nearly bonded": at least six of those seven factors on (f1 < 0, each f4 > 0);
+//   MODE 2: the base-base distance.
+template <int MODE>
+__global__ void k_order_params(const float4 *poss, const float4 *quat, const int *op1, const int *op2, int n,
+		const DNA2Table<float> *table, float *val, bool *flag) {
+	__shared__ DNA2Table<float> P;
+	load_table(table, &P);
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= n) return;
+	const LoadRef ld{poss, quat};
+	Nuc<float> p, q;
+	float4 ph, pl, qh, ql;
+	ld.load(op1[k], P, make_int2(0, 0), p, ph, pl);
+	ld.load(op2[k], P, make_int2(0, 0), q, qh, ql);
+	const v3<float> rb = site_vec(ld.sep(ph, pl, qh, ql, P), q.base, p.base);
+	const float r2 = dot(rb, rb);
+	if(MODE == 2) {
+		val[k] = m_sqrt(r2);
+		return;
+	}
+	float e = 0.f;
+	bool near = false;
+	if(p.btype + q.btype == 3 && float(OXM_HYDR_RCLOW) * float(OXM_HYDR_RCLOW) < r2 &&
+			r2 < float(OXM_HYDR_RCHIGH) * float(OXM_HYDR_RCHIGH)) {
+		const float rmod = m_sqrt(r2);
+		const v3<float> rd = rb * (1.f / rmod);
+		float f1, f1d, g[6], gd;
+		f1_both(P, rmod, OXM_F1_HB, p.type, q.type, f1, f1d);
+		f4_both(P, -dot(p.a1, q.a1), sin_between(p.a1, q.a1), OXM_F4_HB_T1, g[0], gd);
+		f4_both(P, -dot(q.a1, rd), sin_between(q.a1, rd), OXM_F4_HB_T2, g[1], gd);
+		f4_both(P, dot(p.a1, rd), sin_between(p.a1, rd), OXM_F4_HB_T2, g[2], gd);
+		f4_both(P, dot(p.a3, q.a3), sin_between(p.a3, q.a3), OXM_F4_HB_T4, g[3], gd);
+		f4_both(P, -dot(rd, q.a3), sin_between(q.a3, rd), OXM_F4_HB_T7, g[4], gd);
+		f4_both(P, dot(rd, p.a3), sin_between(p.a3, rd), OXM_F4_HB_T7, g[5], gd);
+		e = f1;
+		int on = f1 < 0.f;
+#pragma unroll
+		for(int m = 0; m < 6; m++) {
+			e *= g[m];
+			on += g[m] > 0.f;
+		}
+		near = on >= 6;
+	}
+	if(MODE == 0) val[k] = e;
+	else flag[k] = near;
+}
+
+cudaError_t launch_order_params(int mode, const float4 *poss, const float4 *quat, const int *op1, const int *op2, int n,
+		const void *table, float *val, bool *flag, cudaStream_t s) {
+	const int blocks = (n + 127) / 128;
+	const DNA2Table<float> *t = reinterpret_cast<const DNA2Table<float> *>(table);
+	if(mode == 0) k_order_params<0><<<blocks, 128, 0, s>>>(poss, quat, op1, op2, n, t, val, flag);
+	else if(mode == 1) k_order_params<1><<<blocks, 128, 0, s>>>(poss, quat, op1, op2, n, t, val, flag);
+	else k_order_params<2><<<blocks, 128, 0, s>>>(poss, quat, op1, op2, n, t, val, flag);
 	return cudaGetLastError();
 }
 
@@ -789,21 +860,11 @@ __device__ __forceinline__ void pair_block(const ForceArgs &a, const Loader &ld,
 	if(n1 > 0) eval_terms<R, Loader, SPLIT, ENERGY>(a, ld, Ps, s0, tq[w][1], n1, 1);
 }
 
-// The bonded and the base/stack pair work are independent (both read the mirrors, each writes
-// its own result buffers), so they share one launch: blocks 0 .. 2 pair_blocks - 1 are pair
-// blocks (the costliest, dispatched first), the rest bonded blocks, which fill the tail.
 // minimum resident blocks per SM asked of the register allocator for the bonded/pair kernel
 #ifndef OXGB_PAIR_MINB
 #define OXGB_PAIR_MINB 5
 #endif
 
-template <typename R, class Loader, bool SPLIT, bool ENERGY, int NPW = OXGB_PAIR_NPW>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_PAIR_MINB : 1) k_bonded_pairs(ForceArgs a, Loader ld, int pair_blocks) {
-	pdl_trigger();  // the non-bonded kernel may start (it waits before reading these results)
-	const int b = blockIdx.x;
-	if(b < 2 * pair_blocks) pair_block<R, Loader, SPLIT, ENERGY, NPW>(a, ld, b, pair_blocks);
-	else bonded_block<R, Loader, SPLIT, ENERGY>(a, ld, b - 2 * pair_blocks);
-}
 
 // compensated sum over the K lanes of a group (TwoSum at every level); every lane of the group
 // receives it
@@ -823,6 +884,110 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 	return s + err;
 }
 
+// Edge block b (use_edge): K lanes per nucleotide i take the entries of its full row and of its
+// excluded-volume list whose partner j lies above i (by slot), so every unordered pair is
+// evaluated once -- the pair-parallel scheme of the reference's use_edge kernels
+// (CUDA_DNA.cuh:727-775), with a nucleotide's pairs kept on one lane group.  The partner's
+// share goes to edge_acc[j] by atomic vector adds (force with energy, lab torque), the
+// nucleotide's own share to edge_acc[i] after a compensated group sum; the non-bonded kernel
+// gathers edge_acc.  The partner's Debye-Hueckel torque is its backbone offset times its force;
+// the excluded volume's follows from the rigid-rotation balance T_j = -T_i + d x F_i (error-free
+// products).  Atomic adds make the summation order, and so the last bits, vary from run to run.
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int K>
+__device__ __forceinline__ void edge_block(const ForceArgs &a, const Loader &ld, int b) {
+	using V4 = typename Vec4Of<R>::T;
+	const long long N = a.N;
+	const int sub = threadIdx.x % K;
+	const int per_block = blockDim.x / K;
+	const int first = b * per_block;
+	DNA2Table<R> *Ps = reinterpret_cast<DNA2Table<R> *>(g_tables_smem);
+	const int s0 = load_table_span<R>(a, first, min(first + per_block, a.N) - 1, Ps);
+	const int i_raw = first + (int) threadIdx.x / K;
+	const bool live = i_raw < a.N;
+	const int i = live ? i_raw : a.N - 1;
+	const int sy = a.sys ? a.sys[i] : 0;
+	const DNA2Table<R> &P = Ps[sy - s0];
+	Nuc<R> p;
+	V4 ph, pl;
+	load_full<Loader, R>(ld, i, P, p, ph, pl);
+	SplitAcc<R, SPLIT, ENERGY> acc{};
+	V4 *out = reinterpret_cast<V4 *>(a.edge_acc);
+	auto partner = [&](int j, const v3<R> &fj, const v3<R> &tj, R e) {
+		V4 f, t;
+		f.x = fj.x, f.y = fj.y, f.z = fj.z, f.w = ENERGY ? e : R(0);
+		t.x = tj.x, t.y = tj.y, t.z = tj.z, t.w = R(0);
+		atomic_add_v4(out + 2 * (long long) j, f);
+		atomic_add_v4(out + 2 * (long long) j + 1, t);
+	};
+	// Debye-Hueckel over the owned entries of the full row
+	const int ndh = live ? min(a.nnb[i], a.max_nb) : 0;
+	for(int k = sub; k < ndh; k += K) {
+		const int j = a.nb[(long long) k * N + i];
+		if(j < i) continue;
+		Nuc<R> q;
+		V4 qh, ql;
+		load_dh<Loader, R>(ld, j, P, q, qh, ql);
+		PairOut<R> o{};
+		pair_dh<R, SPLIT>(P, p, q, ld.sep_soft(ph, pl, qh, ql, P).plain(), o);
+		acc.add(o);
+		if(o.F.x != R(0) || o.F.y != R(0) || o.F.z != R(0)) partner(j, -o.F, cross(q.back, -o.F), o.E);
+	}
+	// excluded volume over the owned centre-close pairs
+	const int nev = live ? min(a.ev_n[i], a.ev_cap) : 0;
+	for(int k = sub; k < nev; k += K) {
+		const int j = a.ev_nb[(long long) k * N + i];
+		if(j < i) continue;
+		Nuc<R> q;
+		V4 qh, ql;
+		load_full<Loader, R>(ld, j, P, q, qh, ql);
+		PairOut<R> o{};
+		const Sep<R> sp = ld.sep(ph, pl, qh, ql, P);
+		if constexpr(decltype(ld.refine(0, 0))::on) {
+			if(!ev_contact(p, q, sp.plain())) continue;
+			float3 t;
+			const float4 fe = ev_pair_refined_call(ld.a1lo, ld.backlo, i, j, make_float4(sp.hi.x, sp.hi.y, sp.hi.z, 0.f),
+					make_float4(sp.lo.x, sp.lo.y, sp.lo.z, 0.f), make_float4(p.back.x, p.back.y, p.back.z, 0.f),
+					make_float4(p.base.x, p.base.y, p.base.z, 0.f), make_float4(p.a1.x, p.a1.y, p.a1.z, 0.f),
+					make_float4(q.back.x, q.back.y, q.back.z, 0.f), make_float4(q.base.x, q.base.y, q.base.z, 0.f),
+					make_float4(q.a1.x, q.a1.y, q.a1.z, 0.f), &t);
+			o.F = v3<R>{fe.x, fe.y, fe.z};
+			o.T = v3<R>{t.x, t.y, t.z};
+			add_e<R, SPLIT>(o, T_NEXC, fe.w);
+		}
+		else {
+			pair_ev<R, SPLIT>(p, q, sp, o);
+		}
+		if(o.F.x == R(0) && o.F.y == R(0) && o.F.z == R(0) && o.E == R(0)) continue;
+		acc.add(o);
+		partner(j, -o.F, cross_accurate(sp, o.F) - o.T, o.E);
+	}
+	if(SPLIT && live) {
+#pragma unroll
+		for(int k = 0; k < N_TERMS; k++)
+			if(acc.split[k] != R(0)) atomicAdd(a.esplit + 8 * sy + k, (double) acc.split[k]);
+	}
+	const R fx = group_sum_comp<R, K>(acc.F.s.x, acc.F.c.x), fy = group_sum_comp<R, K>(acc.F.s.y, acc.F.c.y),
+			fz = group_sum_comp<R, K>(acc.F.s.z, acc.F.c.z);
+	const R tx = group_sum_comp<R, K>(acc.T.s.x, acc.T.c.x), ty = group_sum_comp<R, K>(acc.T.s.y, acc.T.c.y),
+			tz = group_sum_comp<R, K>(acc.T.s.z, acc.T.c.z);
+	const R e = ENERGY ? group_sum_comp<R, K>(acc.E, acc.Ec) : R(0);
+	if(sub == 0 && live) partner(i, v3<R>{fx, fy, fz}, v3<R>{tx, ty, tz}, e);
+}
+
+// The bonded and the base/stack pair work are independent (both read the mirrors, each writes
+// its own result buffers), so they share one launch: blocks 0 .. 2 pair_blocks - 1 are pair
+// blocks (the costliest, dispatched first), then the bonded blocks, which fill the tail, and
+// with use_edge the edge blocks.
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int NPW = OXGB_PAIR_NPW, bool EDGE = false, int K = 4>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? OXGB_PAIR_MINB : 1) k_bonded_pairs(ForceArgs a, Loader ld, int pair_blocks) {
+	pdl_trigger();  // the non-bonded kernel may start (it waits before reading these results)
+	const int b = blockIdx.x;
+	const int bonded_blocks = (a.N + (int) blockDim.x - 1) / (int) blockDim.x;
+	if(b < 2 * pair_blocks) pair_block<R, Loader, SPLIT, ENERGY, NPW>(a, ld, b, pair_blocks);
+	else if(!EDGE || b < 2 * pair_blocks + bonded_blocks) bonded_block<R, Loader, SPLIT, ENERGY>(a, ld, b - 2 * pair_blocks);
+	else if constexpr(EDGE) edge_block<R, Loader, SPLIT, ENERGY, K>(a, ld, b - 2 * pair_blocks - bonded_blocks);
+}
+
 // K lanes per nucleotide: lane l of a group takes entries l, l + K, ... of every term list, so a
 // warp holds 32 / K nucleotides and all its lanes run the same term loop
 // minimum resident blocks per SM asked of the register allocator for the non-bonded kernel
@@ -830,7 +995,7 @@ __device__ __forceinline__ R group_sum_comp(R s, R c) {
 #define OXGB_NB_MINB 8
 #endif
 
-template <typename R, class Loader, bool SPLIT, bool ENERGY, int K, int MINB = OXGB_NB_MINB>
+template <typename R, class Loader, bool SPLIT, bool ENERGY, int K, int MINB = OXGB_NB_MINB, bool EDGE = false>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_split(ForceArgs a, Loader ld) {
 	using V4 = typename Vec4Of<R>::T;
 	const long long N = a.N;
@@ -851,8 +1016,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_sp
 		load_full<Loader, R>(ld, i, P, p, ph, pl);
 		SplitAcc<R, SPLIT, ENERGY> acc{};
 
-		// Debye-Hueckel over the full Verlet row
-		const int ndh = live ? min(a.nnb[i], a.max_nb) : 0;
+		// Debye-Hueckel over the full Verlet row (use_edge: the edge blocks did it)
+		const int ndh = (live && !EDGE) ? min(a.nnb[i], a.max_nb) : 0;
 		for(int k = sub; k < ndh; k += K) {
 			const int j = a.nb[(long long) k * N + i];
 			Nuc<R> q;
@@ -862,8 +1027,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_sp
 			pair_dh<R, SPLIT>(P, p, q, ld.sep_soft(ph, pl, qh, ql, P).plain(), o);
 			acc.add_short(o);
 		}
-		// excluded volume over centre-close pairs
-		const int nev = live ? min(a.ev_n[i], a.ev_cap) : 0;
+		// excluded volume over centre-close pairs (use_edge: the edge blocks did it)
+		const int nev = (live && !EDGE) ? min(a.ev_n[i], a.ev_cap) : 0;
 		if constexpr(decltype(ld.refine(0, 0))::on) {
 			// FP32: each window of 64 of the lane's entries is screened (a site pair inside its
 			// cutoff: a few in a thousand entries); the pairs found are evaluated refined after the
@@ -877,7 +1042,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_sp
 					Nuc<R> q;
 					V4 qh, ql;
 					load_full<Loader, R>(ld, j, P, q, qh, ql);
-					if(ev_contact(p, q, ld.sep(ph, pl, qh, ql, P).plain())) stiff |= 1ull << m;
+					if(ev_contact(p, q, ld.sep_soft(ph, pl, qh, ql, P).plain())) stiff |= 1ull << m;
 				}
 				while(stiff) {
 					const int mm = __ffsll((long long) stiff) - 1;
@@ -928,8 +1093,20 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_sp
 		}
 
 		// bonded pairs of this nucleotide, evaluated by the bonded blocks of k_bonded_pairs (first
-		// lane of the group)
+		// lane of the group); with use_edge also its Debye-Hueckel and excluded-volume sums, which
+		// are cleared for the next evaluation
 		if(sub == 0 && live) {
+			if constexpr(EDGE) {
+				V4 *ea = reinterpret_cast<V4 *>(a.edge_acc) + 2 * (long long) i;
+				const V4 f = ea[0], t = ea[1];
+				acc.F.add(v3<R>{f.x, f.y, f.z});
+				acc.T.add(v3<R>{t.x, t.y, t.z});
+				if(ENERGY) KahanV<R>::kadd(acc.E, acc.Ec, f.w);
+				V4 z;
+				z.x = z.y = z.z = z.w = R(0);
+				ea[0] = z;
+				ea[1] = z;
+			}
 			const int2 bi = a.bonds[i];
 			const V4 *bf = reinterpret_cast<const V4 *>(a.bond_f);
 			if(bi.x >= 0) {
@@ -1144,31 +1321,33 @@ __global__ void k_external(ForceArgs a) {
 }
 
 template <typename R, class Loader, bool SPLIT, bool ENERGY, int NPW = OXGB_PAIR_NPW, int K = OXGB_NB_LANES,
-		int NBMINB = OXGB_NB_MINB>
+		int NBMINB = OXGB_NB_MINB, bool EDGE = false>
 static void launch_split_t(const ForceArgs &a, Loader ld, cudaStream_t s, cudaEvent_t wait) {
 	const int tpb = 128;
 	const int blocks = a.N > 0 ? (a.N + tpb - 1) / tpb : 1;
 	const size_t smem = sizeof(DNA2Table<R>) * (size_t) (a.tab_span > 0 ? a.tab_span : 1);
 	// pair blocks of 4 warps x NPW nucleotides per term, then one bonded block per 128
-	// nucleotides
+	// nucleotides, then (use_edge) one edge block per 128 / K nucleotides
 	const int pair_blocks = (a.N + 4 * NPW - 1) / (4 * NPW);
-	k_bonded_pairs<R, Loader, SPLIT, ENERGY, NPW><<<2 * pair_blocks + blocks, tpb, smem, s>>>(a, ld, pair_blocks);
+	const int edge_blocks = EDGE ? nonbonded_blocks(a.N, K) : 0;
+	k_bonded_pairs<R, Loader, SPLIT, ENERGY, NPW, EDGE, K><<<2 * pair_blocks + blocks + edge_blocks, tpb, smem, s>>>(a, ld, pair_blocks);
 	// the non-bonded kernel starts its Debye-Hueckel and excluded-volume work while the tail of
 	// the bonded and pair blocks runs; the external forces follow it the same way
 	if(wait) cudaStreamWaitEvent(s, wait, 0);
-	if(wait) k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB><<<nonbonded_blocks(a.N, K), tpb, smem, s>>>(a, ld);
-	else launch_after(k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB>, dim3(nonbonded_blocks(a.N, K)), dim3(tpb), smem, s, a,
-			ld);
+	if(wait) k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB, EDGE><<<nonbonded_blocks(a.N, K), tpb, smem, s>>>(a, ld);
+	else launch_after(k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB, EDGE>, dim3(nonbonded_blocks(a.N, K)), dim3(tpb), smem,
+			s, a, ld);
 	if(a.ext_n > 0) launch_after(k_external<typename Vec4Of<R>::T>, dim3((a.ext_n + tpb - 1) / tpb), dim3(tpb), 0, s, a);
 }
 
 template <typename R, class Loader, bool SPLIT, bool ENERGY, int NPW = OXGB_PAIR_NPW, int K = OXGB_NB_LANES,
-		int NBMINB = OXGB_NB_MINB>
+		int NBMINB = OXGB_NB_MINB, bool EDGE = false>
 static cudaError_t allow_smem_t(int bytes) {
-	cudaError_t e = cudaFuncSetAttribute(k_bonded_pairs<R, Loader, SPLIT, ENERGY, NPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	cudaError_t e = cudaFuncSetAttribute(k_bonded_pairs<R, Loader, SPLIT, ENERGY, NPW, EDGE, K>,
+			cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	if(e == cudaSuccess)
-		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-				bytes);
+		e = cudaFuncSetAttribute(k_nonbonded_split<R, Loader, SPLIT, ENERGY, K, NBMINB, EDGE>,
+				cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	return e;
 }
 
@@ -1190,6 +1369,9 @@ static cudaError_t allow_smem(int bytes) {
 	cudaError_t e = allow_smem_t<R, Loader, true, true>(bytes);
 	if(e == cudaSuccess) e = allow_smem_t<R, Loader, false, true>(bytes);
 	if(e == cudaSuccess) e = allow_smem_t<R, Loader, false, false>(bytes);
+	if(e == cudaSuccess) e = allow_smem_t<R, Loader, true, true, OXGB_PAIR_NPW, OXGB_NB_LANES, OXGB_NB_MINB, true>(bytes);
+	if(e == cudaSuccess) e = allow_smem_t<R, Loader, false, true, OXGB_PAIR_NPW, OXGB_NB_LANES, OXGB_NB_MINB, true>(bytes);
+	if(e == cudaSuccess) e = allow_smem_t<R, Loader, false, false, OXGB_PAIR_NPW, OXGB_NB_LANES, OXGB_NB_MINB, true>(bytes);
 	if constexpr(sizeof(R) == 4) {
 		if(e == cudaSuccess) e = allow_smem_shape<1>(bytes);
 		if(e == cudaSuccess) e = allow_smem_shape<2>(bytes);
@@ -1206,7 +1388,22 @@ int set_forces_smem(bool dbl, size_t bytes) {
 	return (dbl ? allow_smem<double, SplitDouble>((int) bytes) : allow_smem<float, SplitMixed>((int) bytes)) != cudaSuccess;
 }
 
+// use_edge: the default shape with the edge blocks
+template <typename R, class Loader>
+static void launch_edge(const ForceArgs &a, Loader ld, bool split, bool energy, cudaStream_t s, cudaEvent_t wait) {
+	constexpr int NPW = OXGB_PAIR_NPW, K = OXGB_NB_LANES, MB = OXGB_NB_MINB;
+	if(split) launch_split_t<R, Loader, true, true, NPW, K, MB, true>(a, ld, s, wait);
+	else if(energy) launch_split_t<R, Loader, false, true, NPW, K, MB, true>(a, ld, s, wait);
+	else launch_split_t<R, Loader, false, false, NPW, K, MB, true>(a, ld, s, wait);
+}
+
 cudaError_t launch_forces_split(const ForceArgs &a, bool dbl, bool split, bool energy, cudaStream_t s, cudaEvent_t wait) {
+	if(a.edge) {
+		if(dbl) launch_edge<double, SplitDouble>(a, SplitDouble{a.posd, a.quatd, a.pos_hi, a.pos_lo, a.bonds}, split, energy, s, wait);
+		else launch_edge<float, SplitMixed>(a, SplitMixed{a.pos_hi, a.pos_lo, a.fa1, a.fa3, a.fback, a.fa1lo, a.fbacklo}, split, energy,
+				s, wait);
+		return cudaGetLastError();
+	}
 	if(dbl) {
 		SplitDouble ld{a.posd, a.quatd, a.pos_hi, a.pos_lo, a.bonds};
 		if(split) launch_split_t<double, SplitDouble, true, true>(a, ld, s, wait);

@@ -130,9 +130,19 @@ struct ForceArgs {
 	// shape of the MD step's kernels (no energies; mixed / float engine): index into the
 	// autotuner's shape table, 0 the default
 	int shape;
+	// use_edge: Debye-Hueckel and excluded volume evaluated once per unordered pair by the edge
+	// blocks of the bonded/pair kernel, both nucleotides' shares added atomically into edge_acc
+	// ([2 N] V4: force with w = energy, lab torque with w = hydrogen-bonding energy), which the
+	// non-bonded kernel gathers and clears; 0 (default): both from each end of the full rows
+	int edge;
+	void *edge_acc;
 };
 
 cudaError_t launch_forces_reference_layout(const ForceArgs &a, cudaStream_t s);
+// FFS order parameters of listed pairs on the reference layout (mode 0 hydrogen-bonding energy,
+// 1 nearly-bonded flag, 2 base-base distance)
+cudaError_t launch_order_params(int mode, const float4 *poss, const float4 *quat, const int *op1, const int *op2, int n,
+		const void *table, float *val, bool *flag, cudaStream_t s);
 // split path: bonded pairs (one thread per bond, both sides), then non-bonded terms (one
 // thread per nucleotide, one loop per term list) with the bonded results gathered in its epilogue
 // wait: an event the non-bonded kernel waits for, or null

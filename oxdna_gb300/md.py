@@ -47,7 +47,7 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
                 pt: float = 0.0, diff_coeff: float = 2.5, bussi_tau: float = 1000.0, seed: int = 1,
                 precision: str = "mixed", cells_auto_optimisation: bool = True, max_neigh: int = 0,
                 steps_per_graph: int = 16, list_rebuild_node: str = "conditional", sort_every: int = 0,
-                autotune: bool = False) -> _abi.MDSettings:
+                autotune: bool = False, use_edge: bool = False) -> _abi.MDSettings:
     m = _abi.MDSettings()
     _abi.lib().oxgb_md_default_settings(C.byref(m))
     m.dt = dt
@@ -65,6 +65,7 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
     m.list_rebuild_node = {"conditional": 0, "kernel": 1}[list_rebuild_node]
     m.sort_every = sort_every
     m.autotune = 1 if autotune else 0
+    m.use_edge = 1 if use_edge else 0
     return m
 
 

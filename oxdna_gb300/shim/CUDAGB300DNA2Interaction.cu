@@ -145,6 +145,28 @@ public:
 				"oxgb_dna2_compute_forces");
 	}
 
+	// the FFS backend's order parameters (CUDABaseInteraction.h:61-63, CUDADNAInteraction.cu:205-218)
+	void _hb_op_precalc(c_number4 *poss, GPU_quat *orientations, int *op_pairs1, int *op_pairs2, float *hb_energies, int n_threads,
+			bool *, CUDA_kernel_cfg, CUDABox *) override {
+		oxgb_check(oxgb_dna2_hb_op_precalc(_h, cubic_side(), poss, orientations, op_pairs1, op_pairs2, n_threads, hb_energies, nullptr),
+				"oxgb_dna2_hb_op_precalc");
+	}
+
+	void _near_hb_op_precalc(c_number4 *poss, GPU_quat *orientations, int *op_pairs1, int *op_pairs2, bool *nearly_bonded_array,
+			int n_threads, bool *, CUDA_kernel_cfg, CUDABox *) override {
+		oxgb_check(oxgb_dna2_near_hb_op_precalc(_h, cubic_side(), poss, orientations, op_pairs1, op_pairs2, n_threads,
+						   nearly_bonded_array, nullptr),
+				"oxgb_dna2_near_hb_op_precalc");
+	}
+
+	void _dist_op_precalc(c_number4 *poss, GPU_quat *orientations, int *op_pairs1, int *op_pairs2, c_number *op_dists, int n_threads,
+			CUDA_kernel_cfg, CUDABox *) override {
+		static_assert(sizeof(c_number) == sizeof(float), "the order-parameter distances are FP32 (mixed or float backend)");
+		oxgb_check(oxgb_dna2_dist_op_precalc(_h, cubic_side(), poss, orientations, op_pairs1, op_pairs2, n_threads,
+						   reinterpret_cast<float *>(op_dists), nullptr),
+				"oxgb_dna2_dist_op_precalc");
+	}
+
 	~CUDAGB300DNA2Interaction() override {
 		if(_h) oxgb_dna2_destroy(_h);
 	}

@@ -12,7 +12,7 @@
 // stacking and hydrogen-bonding well depths, FENE r0, Debye-Hueckel).  The reference's own CUDA
 // class keeps the oxDNA1 average-sequence well depths there (CUDADNAInteraction.cu:61-64); the
 // input key gb300_reference_cuda_eps = true reproduces that choice.  The order-parameter
-// helpers of the reference's FFS backend are not provided (they throw).
+// helpers of the reference's FFS backend run liboxgb's kernels.
 //
 // Built by oracle/ref/Makefile (target cuda-gb300) against the reference headers; not part of
 // liboxgb itself.
@@ -133,14 +133,26 @@ void CUDADNAInteraction::_on_T_update() {
 
 void CUDADNAInteraction::_init_strand_ends(LR_bonds *) {}
 
-void CUDADNAInteraction::_hb_op_precalc(c_number4 *, GPU_quat *, int *, int *, float *, int, bool *, CUDA_kernel_cfg, CUDABox *) {
-	throw oxDNAException("FFS order parameters are not provided by the GB300 substitute");
+// the FFS backend's order parameters (CUDADNAInteraction.cu:205-218): the same kernels in liboxgb
+// (the launch configuration is the library's own)
+void CUDADNAInteraction::_hb_op_precalc(c_number4 *poss, GPU_quat *orientations, int *op_pairs1, int *op_pairs2, float *hb_energies,
+		int n_threads, bool *, CUDA_kernel_cfg, CUDABox *) {
+	oxgb_check(oxgb_dna2_hb_op_precalc(g_state[this].h, cubic_side(), poss, orientations, op_pairs1, op_pairs2, n_threads, hb_energies,
+					   nullptr),
+			"oxgb_dna2_hb_op_precalc");
 }
 
-void CUDADNAInteraction::_near_hb_op_precalc(c_number4 *, GPU_quat *, int *, int *, bool *, int, bool *, CUDA_kernel_cfg, CUDABox *) {
-	throw oxDNAException("FFS order parameters are not provided by the GB300 substitute");
+void CUDADNAInteraction::_near_hb_op_precalc(c_number4 *poss, GPU_quat *orientations, int *op_pairs1, int *op_pairs2,
+		bool *nearly_bonded_array, int n_threads, bool *, CUDA_kernel_cfg, CUDABox *) {
+	oxgb_check(oxgb_dna2_near_hb_op_precalc(g_state[this].h, cubic_side(), poss, orientations, op_pairs1, op_pairs2, n_threads,
+					   nearly_bonded_array, nullptr),
+			"oxgb_dna2_near_hb_op_precalc");
 }
 
-void CUDADNAInteraction::_dist_op_precalc(c_number4 *, GPU_quat *, int *, int *, c_number *, int, CUDA_kernel_cfg, CUDABox *) {
-	throw oxDNAException("FFS order parameters are not provided by the GB300 substitute");
+void CUDADNAInteraction::_dist_op_precalc(c_number4 *poss, GPU_quat *orientations, int *op_pairs1, int *op_pairs2, c_number *op_dists,
+		int n_threads, CUDA_kernel_cfg, CUDABox *) {
+	static_assert(sizeof(c_number) == sizeof(float), "the order-parameter distances are FP32 (mixed or float backend)");
+	oxgb_check(oxgb_dna2_dist_op_precalc(g_state[this].h, cubic_side(), poss, orientations, op_pairs1, op_pairs2, n_threads,
+					   reinterpret_cast<float *>(op_dists), nullptr),
+			"oxgb_dna2_dist_op_precalc");
 }

@@ -85,3 +85,27 @@ def test_oracle_external_forces_match_reference():
     assert np.abs(g["F_ext"]).max() > 1.0
     assert np.abs(F - g["F_ext"]).max() <= 1e-12 * np.abs(g["F_ext"]).max()
     assert np.abs(g["T_ext"]).max() == 0.0
+
+
+@pytest.mark.parametrize("case", ["contact", "mixed", "duplex24", "ff16_seqdep"])
+def test_order_parameter_hb_energies_sum_to_the_reference_hb_term(case):
+    """The oracle's FFS order-parameter energies (CUDA_DNA.cuh:910-961: f1 times the six f4
+    factors of a pair) summed over every pair equal the hydrogen-bonding term the reference
+    printed for the fixture; the nearly-bonded flag is set on every pair with a non-zero energy."""
+    g = load_golden(case)
+    p = oracle.make_params(oracle_settings(g))
+    N = g["pos"].shape[0]
+    i, j = np.triu_indices(N, 1)
+    bonded = (g["n3"][i] == j) | (g["n5"][i] == j)
+    i, j = i[~bonded], j[~bonded]
+    args = (p, g["pos"], g["a1"], g["a3"], g["type"], g["btype"], float(g["box"]), i, j)
+    e = oracle.order_params(*args, 0)
+    near = oracle.order_params(*args, 1)
+    dist = oracle.order_params(*args, 2)
+    hb = float(g["split"][4])
+    assert abs(e.sum() - hb) <= 1e-12 * max(1.0, abs(hb)), (e.sum(), hb)
+    assert np.all(near[e != 0] == 1)
+    r = g["pos"][j] - g["pos"][i]
+    r -= np.rint(r / float(g["box"])) * float(g["box"])
+    rb = r + float(np.float32(0.4)) * g["a1"][j] - float(np.float32(0.4)) * g["a1"][i]
+    assert np.allclose(dist, np.linalg.norm(rb, axis=1), rtol=1e-12, atol=1e-12)
