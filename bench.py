@@ -697,9 +697,12 @@ def plain_run(args, name, rank, world, torch, ox, _abi, peak):
     md = ox.md_settings(dt=wl["dt"], thermostat=wl["thermostat"], newtonian_steps=wl["newtonian_steps"],
                         bussi_tau=wl.get("bussi_tau", 1000.0), diff_coeff=wl.get("diff_coeff", 2.5), seed=1 + rank,
                         precision="mixed", steps_per_graph=25, list_rebuild_node=args.list_node,
-                        sort_every=sort_every, autotune=not args.no_autotune, use_edge=args.use_edge)
+                        sort_every=sort_every, autotune=not args.no_autotune and args.force_shape is None,
+                        use_edge=args.use_edge)
     sysm = ox.MDSystem(s.box, s.top, ox.dna2_settings(s.T, 0.5), md)
     sysm.set_state(s.pos, quat, s.vel, s.L)
+    if args.force_shape is not None:
+        sysm.set_force_shape(args.force_shape)
     shape = sysm.force_shape()
     L = _abi.lib()
     stream = torch.cuda.ExternalStream(sysm.stream)
@@ -825,6 +828,8 @@ def main():
     ap.add_argument("--port-baseline", action="store_true", help="time the FP64 oracle port as the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default force-kernel shape instead of the autotuned one")
+    ap.add_argument("--force-shape", type=int, default=None,
+                    help="pin force-kernel shape k of the autotuner's table instead of tuning (profiling)")
     ap.add_argument("--use-edge", action="store_true",
                     help="use_edge: Debye-Hueckel and excluded volume once per pair with atomic adds (A/B variant)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-system batched workload")
@@ -906,7 +911,8 @@ def main():
                    "md_steps_per_step": args.md_steps,
                    "l2": "flushed before every timed iteration (256 MiB write)", "precision": "FP32 forces, FP64 state",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "sort_every": wl.get("sort_every", 0) if args.sort_every is None else args.sort_every},
+                   "sort_every": wl.get("sort_every", 0) if args.sort_every is None else args.sort_every,
+                   "force_shape": head["force_shape"], "use_edge": bool(args.use_edge)},
         "md_steps_per_s": head["md_steps_per_s"],
         "list_rebuilds": head["list_rebuilds"],
         "roofline": head["roofline"],

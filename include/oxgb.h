@@ -262,7 +262,8 @@ int oxgb_md_set_temperature(oxgb_md *h, int k, double T);
  * External forces, the CUDA backend's set_external_forces (src/CUDA/Backends/CUDA_MD.cuh:97-555,
  * records of src/CUDA/Forces/forces_defs.cuh) for the force types of src/Forces/
  * {ConstantRateForce,MutualTrap,MovingTrap,LowdimMovingTrap,RepulsionPlane,AttractionPlane,
- * RepulsiveSphere,RepulsiveSphereSmooth,LJWall,GenericCentralForce,RepulsionPlaneMoving,LJCone}.cpp.
+ * RepulsiveSphere,RepulsiveSphereSmooth,LJWall,GenericCentralForce,RepulsionPlaneMoving,LJCone,
+ * ConstantRateTorque,RepulsiveEllipsoid,COMForce,YukawaSphere,RepulsiveSphereMoving}.cpp.
  * Each record acts on one nucleotide (global index) and is evaluated at every force evaluation
  * from the FP64 positions, with `step` the MD step being computed (0 for a state just uploaded);
  * no torques, no energies (as in the reference).  dir is taken as given (the reference
@@ -291,6 +292,23 @@ int oxgb_md_set_temperature(oxgb_md *h, int k, double T);
  *                      b = |a dir - v|, x = a sin(alpha) - b cos(alpha), y = x / sigma; where
  *                      y <= cutoff: F += 4 n stiff (2 y^-2n - y^-n) / x nrm, nrm = unit((a + b
  *                      tan(alpha)) dir - v)
+ *   TWIST:             (twist) the trap pos0 rotated by F0 + rate step radians about the unit axis
+ *                      dir through v1 (the centre): F += -stiff (r - trap) * v2 (the mask,
+ *                      component-wise)
+ *   ELLIPSOID:         d = minimum image of r - pos0 (the centre); unless sum (d_k / v2_k)^2 < 1
+ *                      (inside r_2) and sum (d_k / v1_k)^2 > 1 (outside r_1): F += -stiff d / |d|
+ *   COM:               (com) with c = centre of mass of group n (com_list, oxgb_md_set_force_groups)
+ *                      and c' = that of group ref_particle (ref_list), d = c' - c: F += d (|d| -
+ *                      (r0 + rate step)) stiff / (|d| n_com), one record per member of group n
+ *   YUKAWA_SPHERE:     d = minimum image of r - pos0 (the centre), s = r0 (the radius) - |d|;
+ *                      where s < cutoff: F += -d / |d| (F0 exp(-s / p2) (1 / (s p2) + 1 / s^2)),
+ *                      F0 = debye_A, p2 = debye_length; where also s < p1 (the WCA cut-off):
+ *                      F += -d / |d| 4 stiff n (2 w^2 - w) / s, w = (sigma / s)^6, n = WCA_n
+ *   SPHERE_MOVING:     (repulsive_sphere_moving) centre v1 + (v2 - v1) clamp(step / p1, 0, 1)
+ *                      (origin v1, target v2, p1 steps; the origin if p1 <= 0); d = minimum image
+ *                      of r - centre, g = |d| - (r0 + rate step); where g < cutoff (r_ext) and
+ *                      g < sqrt 2: A = 1 / max(g, 1e-9)^2, F += 8 stiff (2 A - 1) A / max(g,
+ *                      1e-9) d / |d|
  */
 enum {
 	OXGB_FORCE_CONSTANT = 0,
@@ -304,17 +322,29 @@ enum {
 	OXGB_FORCE_LJ_WALL = 8,
 	OXGB_FORCE_CENTRAL = 9,
 	OXGB_FORCE_REPULSION_PLANE_MOVING = 10,
-	OXGB_FORCE_LJ_CONE = 11
+	OXGB_FORCE_LJ_CONE = 11,
+	OXGB_FORCE_TWIST = 12,
+	OXGB_FORCE_ELLIPSOID = 13,
+	OXGB_FORCE_COM = 14,
+	OXGB_FORCE_YUKAWA_SPHERE = 15,
+	OXGB_FORCE_SPHERE_MOVING = 16
 };
 typedef struct oxgb_ext_force {
 	int type, particle, ref_particle, flags;
 	double F0, rate, stiff, stiff_rate, r0, position;
 	double dir[3], pos0[3];
 	double sigma, cutoff, p1, p2; /* parameters of the sphere, wall, cone and central types */
-	int n, pad;                   /* the Lennard-Jones exponent of LJ_WALL / LJ_CONE */
+	int n, pad;                   /* the Lennard-Jones exponent of LJ_WALL / LJ_CONE, the WCA
+	                                 exponent of YUKAWA_SPHERE, the centre-of-mass group of COM */
+	double v1[3], v2[3];          /* further vectors: TWIST centre and mask, ELLIPSOID r_1 and r_2,
+	                                 SPHERE_MOVING origin and target */
 } oxgb_ext_force;
 /* replaces the engine's external forces by f[0 .. n-1] (n = 0 removes them) */
 int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_force *f);
+/* the particle groups of COM records (COMForce's com_list / ref_list): group g holds the caller's
+ * indices members[offsets[g] .. offsets[g + 1] - 1]; replaces the previous groups.  Call before
+ * oxgb_md_set_external_forces; no counterpart in the reference, whose records hold the lists. */
+int oxgb_md_set_force_groups(oxgb_md *h, int n_groups, const int *offsets, const int *members);
 /* velocities and angular momenta of system k times f (after a temperature swap: f =
  * sqrt(T_new / T_old)); no counterpart in the reference's CUDA backend, which has no batches */
 int oxgb_md_scale_momenta(oxgb_md *h, int k, double f);
@@ -336,6 +366,9 @@ int oxgb_md_force_shape(oxgb_md *h, int *pair_npw, int *nb_lanes, int *nb_min_bl
  * on another engine; the forces of the current state are recomputed with it.  No counterpart in
  * the reference. */
 int oxgb_md_set_force_shape(oxgb_md *h, int k);
+/* the shape table itself: shape k's nucleotides per pair-block warp queue, non-bonded lanes per
+ * nucleotide and register cap (OXGB_E_INVALID past the last shape) */
+int oxgb_force_shape_table(int k, int *pair_npw, int *nb_lanes, int *nb_min_blocks);
 /* device pointers (for zero-copy callers): FP64 positions, velocities, angular momenta and
  * quaternions (double4 each), FP32 forces and torques (float4; double4 in double precision) */
 int oxgb_md_device_buffers(oxgb_md *h, void **pos, void **vel, void **L, void **quat, void **F, void **T);

@@ -215,9 +215,19 @@ def external_forces(pos, step, forces, box):
     F = np.zeros_like(pos)
     st = float(step)
     for d in forces:
+        t = d["type"]
+        if t == "com":
+            # COMForce::force (src/Forces/COMForce.cpp): on every particle of com_list
+            com = pos[np.asarray(d["com_list"], np.int64)].mean(axis=0)
+            ref = pos[np.asarray(d["ref_list"], np.int64)].mean(axis=0)
+            dv = ref - com
+            dm = np.linalg.norm(dv)
+            f = dv * ((dm - (d.get("r0", 0.0) + d.get("rate", 0.0) * st)) * d.get("stiff", 0.0) / len(d["com_list"]) / dm)
+            for i in d["com_list"]:
+                F[int(i)] += f
+            continue
         i = int(d["particle"])
         r = pos[i]
-        t = d["type"]
         direction = np.asarray(d.get("dir", (0.0, 0.0, 0.0)), np.float64)
         if t in ("constant", "string"):
             inten = d.get("F0", 0.0) + st * d.get("rate", 0.0)
@@ -299,4 +309,52 @@ def external_forces(pos, step, forces, box):
             # RepulsionPlaneMoving::force (src/Forces/RepulsionPlaneMoving.cpp), one reference particle
             x = (r - pos[int(d["ref_particle"])]) @ direction
             F[i] += -d.get("stiff", 0.0) * direction * min(x, 0.0)
+        elif t == "twist":
+            # ConstantRateTorque::force (src/Forces/ConstantRateTorque.cpp): the trap pos0 rotated by
+            # base + rate step radians about the (normalised) axis through the centre, masked
+            ax = np.asarray(d["axis"], np.float64)
+            ax = ax / np.linalg.norm(ax)
+            th = d.get("base", 0.0) + d.get("rate", 0.0) * st
+            K = np.array([[0.0, -ax[2], ax[1]], [ax[2], 0.0, -ax[0]], [-ax[1], ax[0], 0.0]])
+            R = np.cos(th) * np.eye(3) + np.sin(th) * K + (1.0 - np.cos(th)) * np.outer(ax, ax)
+            centre = np.asarray(d.get("center", (0.0, 0.0, 0.0)), np.float64)
+            trap = R @ (np.asarray(d["pos0"], np.float64) - centre) + centre
+            F[i] += -d.get("stiff", 0.0) * (r - trap) * np.asarray(d.get("mask", (0.0, 0.0, 0.0)), np.float64)
+        elif t == "ellipsoid":
+            # RepulsiveEllipsoid::force (src/Forces/RepulsiveEllipsoid.cpp)
+            dv = r - np.asarray(d.get("center", (0.0, 0.0, 0.0)), np.float64)
+            dv = dv - np.rint(dv / box) * box
+            inner = np.sum(dv ** 2 / np.asarray(d["r_2"], np.float64) ** 2)
+            outer = np.sum(dv ** 2 / np.asarray(d.get("r_1", (1e-6, 1e-6, 1e-6)), np.float64) ** 2)
+            if not (inner < 1.0 and outer > 1.0):
+                F[i] += -d.get("stiff", 0.0) * dv / np.linalg.norm(dv)
+        elif t == "yukawa_sphere":
+            # YukawaSphere::force (src/Forces/YukawaSphere.cpp)
+            dv = r - np.asarray(d.get("center", (0.0, 0.0, 0.0)), np.float64)
+            dv = dv - np.rint(dv / box) * box
+            m = np.linalg.norm(dv)
+            lam, A = d["debye_length"], d["debye_A"]
+            eps, sig, n = d.get("WCA_epsilon", 1.0), d.get("WCA_sigma", 1.0), int(d.get("WCA_n", 6))
+            s_ = d["radius"] - m
+            if s_ < d.get("cutoff", 4.0 * lam):
+                c = A * np.exp(-s_ / lam) * (1.0 / (s_ * lam) + 1.0 / s_ ** 2)
+                if s_ < sig * 2.0 ** (1.0 / n):
+                    w = (sig / s_) ** 6
+                    c += 4 * eps * n * (2 * w * w - w) / s_
+                F[i] += -dv / m * c
+        elif t == "repulsive_sphere_moving":
+            # RepulsiveSphereMoving::force (src/Forces/RepulsiveSphereMoving.cpp)
+            centre = np.asarray(d.get("center", (0.0, 0.0, 0.0)), np.float64)
+            origin = np.asarray(d.get("origin", centre), np.float64)
+            target = np.asarray(d.get("target", (0.0, 0.0, 0.0)), np.float64)
+            nsteps = int(d.get("steps", d.get("move_steps", 0)))
+            f = min(max(st / nsteps, 0.0), 1.0) if nsteps > 0 else 0.0
+            dv = r - (origin + (target - origin) * f)
+            dv = dv - np.rint(dv / box) * box
+            m = np.linalg.norm(dv)
+            g = m - (d["r0"] + d.get("rate", 0.0) * st)
+            if g < d.get("r_ext", 1e10) and m > 0 and g < np.sqrt(2.0):
+                gs = max(g, 1e-9)
+                A = 1.0 / gs ** 2
+                F[i] += dv * (8.0 * d.get("stiff", 0.0) * (2 * A - 1) * A / gs / m)
     return F

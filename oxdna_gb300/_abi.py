@@ -45,13 +45,14 @@ class ExtForce(C.Structure):
         ("F0", C.c_double), ("rate", C.c_double), ("stiff", C.c_double), ("stiff_rate", C.c_double),
         ("r0", C.c_double), ("position", C.c_double), ("dir", C.c_double * 3), ("pos0", C.c_double * 3),
         ("sigma", C.c_double), ("cutoff", C.c_double), ("p1", C.c_double), ("p2", C.c_double),
-        ("n", C.c_int), ("pad", C.c_int),
+        ("n", C.c_int), ("pad", C.c_int), ("v1", C.c_double * 3), ("v2", C.c_double * 3),
     ]
 
 
 FORCE_TYPES = {"constant": 0, "string": 0, "mutual_trap": 1, "trap": 2, "moving_trap": 2, "lowdim_trap": 3,
                "repulsion_plane": 4, "attraction_plane": 5, "sphere": 6, "sphere_smooth": 7, "LJ_wall": 8,
-               "generic_central_force": 9, "repulsion_plane_moving": 10, "LJ_cone": 11}
+               "generic_central_force": 9, "repulsion_plane_moving": 10, "LJ_cone": 11, "twist": 12, "ellipsoid": 13,
+               "com": 14, "yukawa_sphere": 15, "repulsive_sphere_moving": 16}
 
 
 class MDSettings(C.Structure):
@@ -101,10 +102,12 @@ SIGNATURES = {
     "oxgb_md_get_forces": (C.c_int, [_VP, _VP, _VP, _VP]),
     "oxgb_md_scale_momenta": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_set_external_forces": (C.c_int, [_VP, C.c_int, C.POINTER(ExtForce)]),
+    "oxgb_md_set_force_groups": (C.c_int, [_VP, C.c_int, _VP, _VP]),
     "oxgb_md_energies": (C.c_int, [_VP, _VP, _VP, _VP]),
     "oxgb_md_force_shape": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                       C.POINTER(C.c_double)]),
     "oxgb_md_set_force_shape": (C.c_int, [_VP, C.c_int]),
+    "oxgb_force_shape_table": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "oxgb_md_set_temperature": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_neighbours": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
     "oxgb_md_info": (C.c_int, [_VP, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),

@@ -416,6 +416,9 @@ struct oxgb_md {
 	int *term_max = nullptr;
 	void *ext_rec = nullptr;              // external forces grouped by nucleotide
 	int *ext_nuc = nullptr, *ext_off = nullptr;
+	int *grp_off = nullptr, *grp_mem = nullptr;  // particle groups of COM records (caller's indices)
+	int n_groups = 0;
+	std::vector<int> h_grp_off;
 	int ext_n = 0;
 	bool energies_fresh = false;  // Fe / Te hold the forces and energies of the current state
 
@@ -456,7 +459,7 @@ struct oxgb_md {
 					bond_tp, bond_tq, edge_acc, d_tab, (void *) d_sys, (void *) d_sys_off, (void *) d_sys_stale, (void *) d_chunk_sys,
 					(void *) d_chunk_first, (void *) d_sys_chunk0, (void *) d_sys_par, (void *) d_sys_seed, (void *) status,
 					(void *) flag, (void *) step, (void *) esplit, (void *) sums, (void *) bussi_partials, (void *) bussi_state,
-					(void *) bussi_stamp, (void *) open_step, (void *) bussi_done, (void *) bussi_prep_done, (void *) bussi_tot, (void *) bussi_fpart, (void *) term_max, ext_rec, (void *) ext_nuc, (void *) ext_off, (void *) d_rebuilds})
+					(void *) bussi_stamp, (void *) open_step, (void *) bussi_done, (void *) bussi_prep_done, (void *) bussi_tot, (void *) bussi_fpart, (void *) term_max, ext_rec, (void *) ext_nuc, (void *) ext_off, (void *) grp_off, (void *) grp_mem, (void *) d_rebuilds})
 			if(p) cudaFree(p);
 		lb.free_all();
 		tl.free_all();
@@ -589,6 +592,8 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.ext_rec = h->ext_rec;
 	a.ext_nuc = h->ext_nuc;
 	a.ext_off = h->ext_off;
+	a.grp_off = h->grp_off;
+	a.grp_mem = h->grp_mem;
 	a.ext_n = h->ext_n;
 	a.box = (float) h->box[0];
 	a.sys_box = h->n_systems > 1 ? h->d_sys_box : nullptr;
@@ -1190,6 +1195,12 @@ extern "C" int oxgb_md_set_force_shape(oxgb_md *h, int k) {
 	return h->have_state ? compute_forces_now(h) : OXGB_OK;
 }
 
+extern "C" int oxgb_force_shape_table(int k, int *pair_npw, int *nb_lanes, int *nb_min_blocks) {
+	if(k < 0 || k >= force_shape_count()) return fail(OXGB_E_INVALID, "no such force-kernel shape");
+	force_shape_of(k, pair_npw, nb_lanes, nb_min_blocks);
+	return OXGB_OK;
+}
+
 extern "C" int oxgb_md_force_shape(oxgb_md *h, int *pair_npw, int *nb_lanes, int *nb_min_blocks, double *launch_us) {
 	if(!h) return fail(OXGB_E_INVALID, "null handle");
 	force_shape_of(h->dbl ? 0 : h->shape, pair_npw, nb_lanes, nb_min_blocks);
@@ -1537,8 +1548,21 @@ extern "C" int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_for
 	if(!h || n < 0 || (n > 0 && !f)) return fail(OXGB_E_INVALID, "invalid argument");
 	for(int m = 0; m < n; m++) {
 		const oxgb_ext_force &e = f[m];
-		if(e.type < OXGB_FORCE_CONSTANT || e.type > OXGB_FORCE_LJ_CONE)
+		if(e.type < OXGB_FORCE_CONSTANT || e.type > OXGB_FORCE_SPHERE_MOVING)
 			return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": unknown type");
+		if(e.type == OXGB_FORCE_COM) {
+			if(e.n < 0 || e.n >= h->n_groups || e.ref_particle < 0 || e.ref_particle >= h->n_groups)
+				return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": no such particle group (oxgb_md_set_force_groups)");
+			if(h->h_grp_off[e.n + 1] == h->h_grp_off[e.n] || h->h_grp_off[e.ref_particle + 1] == h->h_grp_off[e.ref_particle])
+				return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": empty particle group");
+		}
+		if(e.type == OXGB_FORCE_YUKAWA_SPHERE && (e.n <= 0 || !(e.p2 > 0) || !(e.sigma > 0)))
+			return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": WCA_n, debye_length and sigma must be positive");
+		if(e.type == OXGB_FORCE_ELLIPSOID) {
+			for(int k = 0; k < 3; k++)
+				if(e.v1[k] == 0.0 || e.v2[k] == 0.0)
+					return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": ellipsoid semi-axes must be non-zero");
+		}
 		if(e.particle < 0 || e.particle >= h->N) return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": particle out of range");
 		if((e.type == OXGB_FORCE_LJ_WALL || e.type == OXGB_FORCE_LJ_CONE) && (e.n <= 0 || e.n % 2 != 0 || !(e.sigma > 0)))
 			return fail(OXGB_E_INVALID, "external force " + std::to_string(m) + ": n must be a positive even integer and sigma positive");
@@ -1574,6 +1598,31 @@ extern "C" int oxgb_md_set_external_forces(oxgb_md *h, int n, const oxgb_ext_for
 	return OXGB_OK;
 }
 
+
+extern "C" int oxgb_md_set_force_groups(oxgb_md *h, int n_groups, const int *offsets, const int *members) {
+	if(!h || n_groups < 0 || (n_groups > 0 && (!offsets || !members))) return fail(OXGB_E_INVALID, "invalid argument");
+	if(h->ext_n > 0) return fail(OXGB_E_INVALID, "external forces are set: remove them before replacing the groups they use");
+	if(n_groups > 0 && offsets[0] != 0) return fail(OXGB_E_INVALID, "offsets[0] must be 0");
+	for(int g = 0; g < n_groups; g++)
+		if(offsets[g + 1] < offsets[g]) return fail(OXGB_E_INVALID, "offsets must not decrease");
+	const int total = n_groups > 0 ? offsets[n_groups] : 0;
+	for(int k = 0; k < total; k++)
+		if(members[k] < 0 || members[k] >= h->N) return fail(OXGB_E_INVALID, "group member out of range");
+	CK(cudaStreamSynchronize(h->stream));
+	for(void *p : {(void *) h->grp_off, (void *) h->grp_mem})
+		if(p) cudaFree(p);
+	h->grp_off = h->grp_mem = nullptr;
+	h->n_groups = 0;
+	h->h_grp_off.assign(offsets, offsets + (n_groups > 0 ? n_groups + 1 : 0));
+	if(n_groups > 0) {
+		CK(cudaMalloc(&h->grp_off, sizeof(int) * (n_groups + 1)));
+		CK(cudaMalloc(&h->grp_mem, sizeof(int) * (total > 0 ? total : 1)));
+		CK(cudaMemcpy(h->grp_off, offsets, sizeof(int) * (n_groups + 1), cudaMemcpyHostToDevice));
+		if(total > 0) CK(cudaMemcpy(h->grp_mem, members, sizeof(int) * total, cudaMemcpyHostToDevice));
+	}
+	h->n_groups = n_groups;
+	return OXGB_OK;
+}
 
 extern "C" int oxgb_md_scale_momenta(oxgb_md *h, int k, double f) {
 	if(!h || k < 0 || k >= h->n_systems || !(f > 0)) return fail(OXGB_E_INVALID, "invalid argument");

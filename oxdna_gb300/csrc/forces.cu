@@ -1308,6 +1308,96 @@ __global__ void k_external(ForceArgs a) {
 			}
 			break;
 		}
+		case OXGB_FORCE_TWIST: {
+			// ConstantRateTorque::force (src/Forces/ConstantRateTorque.cpp): the trap pos0 rotated
+			// about the axis dir through the centre v1 by F0 + rate step radians (Rodrigues'
+			// matrix), the pull masked component-wise by v2
+			const double t = e.F0 + e.rate * st;
+			const double sn = sin(t), cs = cos(t), oc = 1.0 - cs;
+			const double ax = e.dir[0], ay = e.dir[1], az = e.dir[2];
+			const double ux = e.pos0[0] - e.v1[0], uy = e.pos0[1] - e.v1[1], uz = e.pos0[2] - e.v1[2];
+			const double tx = (ax * ax * oc + cs) * ux + (ax * ay * oc - az * sn) * uy + (ax * az * oc + ay * sn) * uz + e.v1[0];
+			const double ty = (ax * ay * oc + az * sn) * ux + (ay * ay * oc + cs) * uy + (ay * az * oc - ax * sn) * uz + e.v1[1];
+			const double tz = (ax * az * oc - ay * sn) * ux + (ay * az * oc + ax * sn) * uy + (az * az * oc + cs) * uz + e.v1[2];
+			fx += -e.stiff * (r.x - tx) * e.v2[0];
+			fy += -e.stiff * (r.y - ty) * e.v2[1];
+			fz += -e.stiff * (r.z - tz) * e.v2[2];
+			break;
+		}
+		case OXGB_FORCE_ELLIPSOID: {
+			// RepulsiveEllipsoid::force (src/Forces/RepulsiveEllipsoid.cpp): pushed towards the
+			// centre unless inside r_2 and outside r_1
+			const double L = a.sys_box ? (double) a.sys_box[a.sys ? a.sys[i] : 0] : (double) a.box;
+			double dx = r.x - e.pos0[0], dy = r.y - e.pos0[1], dz = r.z - e.pos0[2];
+			dx -= rint(dx / L) * L, dy -= rint(dy / L) * L, dz -= rint(dz / L) * L;
+			const double in = dx * dx / (e.v2[0] * e.v2[0]) + dy * dy / (e.v2[1] * e.v2[1]) + dz * dz / (e.v2[2] * e.v2[2]);
+			const double out = dx * dx / (e.v1[0] * e.v1[0]) + dy * dy / (e.v1[1] * e.v1[1]) + dz * dz / (e.v1[2] * e.v1[2]);
+			if(!(in < 1.0 && out > 1.0)) {
+				const double m = sqrt(dx * dx + dy * dy + dz * dz);
+				fx += -e.stiff * dx / m, fy += -e.stiff * dy / m, fz += -e.stiff * dz / m;
+			}
+			break;
+		}
+		case OXGB_FORCE_COM: {
+			// COMForce::force (src/Forces/COMForce.cpp): centres of mass of group n (com_list) and
+			// of group ref_particle (ref_list) from the unwrapped FP64 positions
+			double c[2][3] = {{0, 0, 0}, {0, 0, 0}};
+			int cnt[2];
+			const int gs[2] = {e.n, e.ref_particle};
+			for(int w = 0; w < 2; w++) {
+				const int g0 = a.grp_off[gs[w]], g1 = a.grp_off[gs[w] + 1];
+				cnt[w] = g1 - g0;
+				for(int u = g0; u < g1; u++) {
+					const double4_32a q = a.posd[a.slot ? a.slot[a.grp_mem[u]] : a.grp_mem[u]];
+					c[w][0] += q.x, c[w][1] += q.y, c[w][2] += q.z;
+				}
+				for(int d = 0; d < 3; d++) c[w][d] /= (double) cnt[w];
+			}
+			const double dx = c[1][0] - c[0][0], dy = c[1][1] - c[0][1], dz = c[1][2] - c[0][2];
+			const double m = sqrt(dx * dx + dy * dy + dz * dz);
+			const double f = (m - (e.r0 + e.rate * st)) * e.stiff / (double) cnt[0] / m;
+			fx += dx * f, fy += dy * f, fz += dz * f;
+			break;
+		}
+		case OXGB_FORCE_YUKAWA_SPHERE: {
+			// YukawaSphere::force (src/Forces/YukawaSphere.cpp): screened repulsion from the inside
+			// of a sphere of radius r0, with a WCA core near its surface
+			const double L = a.sys_box ? (double) a.sys_box[a.sys ? a.sys[i] : 0] : (double) a.box;
+			double dx = r.x - e.pos0[0], dy = r.y - e.pos0[1], dz = r.z - e.pos0[2];
+			dx -= rint(dx / L) * L, dy -= rint(dy / L) * L, dz -= rint(dz / L) * L;
+			const double m = sqrt(dx * dx + dy * dy + dz * dz);
+			const double sd = e.r0 - m;
+			if(sd < e.cutoff) {
+				double c = e.F0 * exp(-sd / e.p2) * (1.0 / (sd * e.p2) + 1.0 / (sd * sd));
+				if(sd < e.p1) {
+					const double w = pow(e.sigma / sd, 6.0);
+					c += 4.0 * e.stiff * e.n * (2.0 * w * w - w) / sd;
+				}
+				fx += -dx / m * c, fy += -dy / m * c, fz += -dz / m * c;
+			}
+			break;
+		}
+		case OXGB_FORCE_SPHERE_MOVING: {
+			// RepulsiveSphereMoving::force (src/Forces/RepulsiveSphereMoving.cpp): WCA (the
+			// 2x-x form with x = 2, sigma = 1, eps = stiff) of the gap to a growing sphere whose
+			// centre moves from v1 to v2 over p1 steps
+			double t = 0.0;
+			if(e.p1 > 0.0) t = fmin(fmax(st / floor(e.p1), 0.0), 1.0);
+			const double cx = e.v1[0] + (e.v2[0] - e.v1[0]) * t, cy = e.v1[1] + (e.v2[1] - e.v1[1]) * t,
+						 cz = e.v1[2] + (e.v2[2] - e.v1[2]) * t;
+			const double L = a.sys_box ? (double) a.sys_box[a.sys ? a.sys[i] : 0] : (double) a.box;
+			double dx = r.x - cx, dy = r.y - cy, dz = r.z - cz;
+			dx -= rint(dx / L) * L, dy -= rint(dy / L) * L, dz -= rint(dz / L) * L;
+			const double m = sqrt(dx * dx + dy * dy + dz * dz);
+			const double g = m - (e.r0 + e.rate * st);
+			if(!(g >= e.cutoff) && m > 0.0 && g < 1.4142135623730951) {
+				const double gs = g > 1e-9 ? g : 1e-9;
+				const double A = 1.0 / (gs * gs);
+				const double c = 8.0 * e.stiff * (2.0 * A - 1.0) * A / gs / m;
+				fx += dx * c, fy += dy * c, fz += dz * c;
+			}
+			break;
+		}
 		default:
 			break;
 		}

@@ -121,6 +121,7 @@ struct ForceArgs {
 	const void *ext_rec;
 	const int *ext_nuc, *ext_off;
 	int ext_n;
+	const int *grp_off, *grp_mem;             // particle groups of COM records (caller's indices)
 	float box;                                // cubic box of the (single-system) engine
 	const float *sys_box;                     // per system (batches), or null
 	// cell-order storage (null: never sorted): caller's index of each slot, which decides the

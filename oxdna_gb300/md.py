@@ -69,6 +69,16 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
     return m
 
 
+def force_shapes():
+    """the autotuner's shape table: (pair_npw, nb_lanes, nb_min_blocks) of shape 0, 1, ..."""
+    out, k = [], 0
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    while _abi.lib().oxgb_force_shape_table(k, C.byref(a), C.byref(b), C.byref(c)) == 0:
+        out.append((a.value, b.value, c.value))
+        k += 1
+    return out
+
+
 class MDSystem:
     """One system -- or a batch of independent systems -- on the GPU: topology, FP64 state,
     Verlet lists, integrator and thermostat.
@@ -171,15 +181,35 @@ class MDSystem:
     def set_external_forces(self, forces):
         """External forces (oxgb_md_set_external_forces): a list of dicts with 'type' (constant /
         string, mutual_trap, trap / moving_trap, lowdim_trap, repulsion_plane, attraction_plane,
-        sphere, sphere_smooth, LJ_wall, generic_central_force, repulsion_plane_moving, LJ_cone),
-        'particle' and the parameters under the reference's external_forces_file keys
-        ('ref_particle', 'F0', 'rate', 'stiff', 'stiff_rate', 'r0', 'position', 'dir', 'pos0',
-        'center', 'r_ext', 'smooth', 'alpha', 'sigma', 'n', 'only_repulsive', 'inner_cut_off',
-        'outer_cut_off', and 'dir_as_centre' / 'PBC' / 'visibility' for the flags; the reference's
-        defaults where a key is left out).  Particle indices are global (offsets[k] + index
-        within system k); repulsion_plane_moving takes one reference particle per record."""
-        arr = (_abi.ExtForce * max(1, len(forces)))()
-        for m, d in enumerate(forces):
+        sphere, sphere_smooth, LJ_wall, generic_central_force, repulsion_plane_moving, LJ_cone,
+        twist, ellipsoid, com, yukawa_sphere, repulsive_sphere_moving), 'particle' and the
+        parameters under the reference's external_forces_file keys ('ref_particle', 'F0',
+        'rate', 'stiff', 'stiff_rate', 'r0', 'position', 'dir', 'pos0', 'center', 'r_ext',
+        'smooth', 'alpha', 'sigma', 'n', 'only_repulsive', 'inner_cut_off', 'outer_cut_off',
+        'base', 'axis', 'mask', 'r_1', 'r_2', 'com_list', 'ref_list', 'radius', 'WCA_epsilon',
+        'WCA_sigma', 'WCA_n', 'debye_length', 'debye_A', 'cutoff', 'origin', 'target', 'steps',
+        and 'dir_as_centre' / 'PBC' / 'visibility' for the flags; the reference's defaults where
+        a key is left out).  Particle indices are global (offsets[k] + index within system k);
+        repulsion_plane_moving takes one reference particle per record; a com record (lists of
+        indices in com_list and ref_list) acts on every particle of its com_list, as the
+        reference's COMForce does."""
+        recs, groups = [], {}
+
+        def group(members):
+            key = tuple(int(x) for x in members)
+            if key not in groups:
+                groups[key] = len(groups)
+            return groups[key]
+
+        for d in forces:
+            if d["type"] == "com":
+                g_com, g_ref = group(d["com_list"]), group(d["ref_list"])
+                for i in d["com_list"]:
+                    recs.append((dict(d, particle=int(i)), g_com, g_ref))
+            else:
+                recs.append((d, -1, -1))
+        arr = (_abi.ExtForce * max(1, len(recs)))()
+        for m, (d, g_com, g_ref) in enumerate(recs):
             e = arr[m]
             t = d["type"]
             e.type = _abi.FORCE_TYPES[t]
@@ -219,7 +249,49 @@ class MDSystem:
             elif t == "generic_central_force":
                 e.p1 = float(d.get("inner_cut_off", 0.0))
                 e.p2 = float(d.get("outer_cut_off", 0.0))
-        _abi.check(_abi.lib().oxgb_md_set_external_forces(self._h, len(forces), arr))
+            elif t == "twist":
+                # ConstantRateTorque reads the start angle as 'base' and normalises the axis
+                e.F0 = float(d.get("base", 0.0))
+                axis = np.asarray(d["axis"], np.float64)
+                axis = axis / np.linalg.norm(axis)
+                centre, mask = d.get("center", (0.0, 0.0, 0.0)), d.get("mask", (0.0, 0.0, 0.0))
+                for c in range(3):
+                    e.dir[c], e.pos0[c] = float(axis[c]), float(d["pos0"][c])
+                    e.v1[c], e.v2[c] = float(centre[c]), float(mask[c])
+            elif t == "ellipsoid":
+                r1, r2 = d.get("r_1", (1e-6, 1e-6, 1e-6)), d["r_2"]
+                for c in range(3):
+                    e.v1[c], e.v2[c] = float(r1[c]), float(r2[c])
+            elif t == "com":
+                e.n, e.ref_particle = g_com, g_ref
+            elif t == "yukawa_sphere":
+                e.r0 = float(d["radius"])
+                e.stiff = float(d.get("WCA_epsilon", 1.0))
+                e.sigma = float(d.get("WCA_sigma", 1.0))
+                e.n = int(d.get("WCA_n", 6))
+                e.p1 = e.sigma * 2.0 ** (1.0 / e.n)
+                e.p2 = float(d["debye_length"])
+                e.F0 = float(d["debye_A"])
+                e.cutoff = float(d.get("cutoff", 4.0 * e.p2))
+            elif t == "repulsive_sphere_moving":
+                e.r0 = float(d["r0"])
+                e.cutoff = float(d.get("r_ext", 1e10))
+                centre = d.get("center", (0.0, 0.0, 0.0))
+                origin, target = d.get("origin", centre), d.get("target", (0.0, 0.0, 0.0))
+                e.p1 = float(int(d.get("steps", d.get("move_steps", 0))))
+                for c in range(3):
+                    e.v1[c], e.v2[c] = float(origin[c]), float(target[c])
+        lib = _abi.lib()
+        if groups:
+            # the groups are replaced with no records pointing at them
+            _abi.check(lib.oxgb_md_set_external_forces(self._h, 0, arr))
+            members = [list(k) for k in sorted(groups, key=groups.get)]
+            off = np.zeros(len(members) + 1, np.int32)
+            off[1:] = np.cumsum([len(x) for x in members])
+            flat = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int32) for x in members]), np.int32)
+            _abi.check(lib.oxgb_md_set_force_groups(self._h, len(members), off.ctypes.data_as(C.c_void_p),
+                                                    flat.ctypes.data_as(C.c_void_p)))
+        _abi.check(lib.oxgb_md_set_external_forces(self._h, len(recs), arr))
 
     def scale_momenta(self, f: float, k: int = 0):
         _abi.check(_abi.lib().oxgb_md_scale_momenta(self._h, int(k), float(f)))
@@ -257,7 +329,9 @@ class MDSystem:
         pair_npw, nb_lanes, nb_min_blocks and the measured launch time in microseconds"""
         a, b, c, t = C.c_int(), C.c_int(), C.c_int(), C.c_double()
         _abi.check(_abi.lib().oxgb_md_force_shape(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(t)))
-        return dict(pair_npw=a.value, nb_lanes=b.value, nb_min_blocks=c.value, launch_us=t.value)
+        out = dict(pair_npw=a.value, nb_lanes=b.value, nb_min_blocks=c.value, launch_us=t.value)
+        out["index"] = next((k for k, sh in enumerate(force_shapes()) if sh == (a.value, b.value, c.value)), None)
+        return out
 
     def set_force_shape(self, k: int):
         """pins shape k of the MD step's force kernels (0 the default)"""

@@ -164,6 +164,16 @@ def ext_force_set(N, box, pos):
         dict(type="repulsion_plane_moving", particle=18, ref_particle=4, stiff=1.7, dir=tuple(u)),
         dict(type="LJ_cone", particle=19, stiff=1.0, sigma=1.0, n=6, alpha=1.0, dir=(0.0, 0.0, 1.0),
              pos0=tuple(pos[19] - [0.2, 0.1, 1.8])),
+        dict(type="twist", particle=6, stiff=1.3, rate=1e-3, base=0.5, axis=(0.0, 0.6, 0.8),
+             pos0=tuple(pos[6] + [1.0, 0.5, -0.3]), center=tuple(com), mask=(1.0, 1.0, 0.5)),
+        dict(type="ellipsoid", particle=8, stiff=0.6, r_2=(0.4, 0.5, 0.3), center=tuple(com)),
+        dict(type="ellipsoid", particle=10, stiff=0.6, r_2=(30.0, 30.0, 30.0), center=tuple(com)),
+        dict(type="com", com_list=[20, 22], ref_list=[0, 1, 2, 3], stiff=0.8, r0=1.0, rate=1e-3),
+        dict(type="yukawa_sphere", particle=12, radius=float(np.linalg.norm(pos[12] - com)) + 0.8, WCA_epsilon=0.3,
+             WCA_sigma=1.0, debye_length=0.5, debye_A=2.0, center=tuple(com)),
+        dict(type="repulsive_sphere_moving", particle=23, stiff=0.5, rate=1e-4, origin=tuple(com + [3.0, 0.0, 0.0]),
+             target=tuple(com), steps=4000,
+             r0=float(np.linalg.norm(pos[23] - (com + [2.25, 0.0, 0.0]))) - 0.6 - 0.1),
     ]
 
 
@@ -171,7 +181,7 @@ def ext_force_file(forces):
     vec = lambda v: ", ".join(repr(float(x)) for x in v)
     out = []
     for d in forces:
-        kv = {"type": d["type"], "particle": d["particle"]}
+        kv = {"type": d["type"], "particle": d.get("particle")}
         t = d["type"]
         if t == "string":
             kv.update(F0=d["F0"], rate=d["rate"], dir=vec(d["dir"]))
@@ -212,6 +222,25 @@ def ext_force_file(forces):
         elif t == "LJ_cone":
             kv.update(stiff=d["stiff"], sigma=d["sigma"], n=d["n"], alpha=d["alpha"], dir=vec(d["dir"]),
                       pos0=vec(d["pos0"]))
+        elif t == "twist":
+            kv.update(stiff=d["stiff"], rate=d["rate"], base=d["base"], axis=vec(d["axis"]), pos0=vec(d["pos0"]),
+                      center=vec(d["center"]), mask=vec(d["mask"]))
+        elif t == "ellipsoid":
+            kv.update(stiff=d["stiff"], r_2=vec(d["r_2"]), center=vec(d["center"]))
+            if "r_1" in d:
+                kv["r_1"] = vec(d["r_1"])
+        elif t == "com":
+            del kv["particle"]
+            kv.update(com_list=",".join(str(i) for i in d["com_list"]), ref_list=",".join(str(i) for i in d["ref_list"]),
+                      stiff=d["stiff"], r0=d["r0"], rate=d["rate"])
+        elif t == "yukawa_sphere":
+            # (the reference reads the key WCA_n into the WCA sigma, YukawaSphere.cpp init: left out)
+            kv.update(radius=d["radius"], WCA_epsilon=d["WCA_epsilon"], WCA_sigma=d["WCA_sigma"],
+                      debye_length=d["debye_length"], debye_A=d["debye_A"],
+                      center=",".join(repr(float(x)) for x in d["center"]))  # its parser takes no spaces
+        elif t == "repulsive_sphere_moving":
+            kv.update(stiff=d["stiff"], r0=d["r0"], rate=d["rate"], origin=vec(d["origin"]), target=vec(d["target"]),
+                      steps=d["steps"])
         out.append("{\n" + "".join(f"{k} = {v}\n" for k, v in kv.items()) + "}\n")
     return "".join(out)
 

@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 
 def _forces(N, box):
     recs = json.loads(str(load_golden("ext_forces")["forces"]))
-    assert max(max(d["particle"], d.get("ref_particle", 0)) for d in recs) < N
+    assert max(max(d.get("particle", 0), d.get("ref_particle", 0), *d.get("com_list", []), *d.get("ref_list", []))
+               for d in recs) < N
     return recs
 
 
