@@ -60,8 +60,10 @@ WORKLOADS = {
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of k_bonded_pairs + k_nonbonded_split per force
-# launch, from the ncu --set full capture summarised in profiles/ (cold caches)
-FORCE_TRAFFIC = {"plain40k": 7.293e6 + 8.4e3 + 26.257e6, "large250k": 26.941e6 + 25.1e3 + 62.383e6 + 0.946e6}
+# launch (the MD step's variant, autotuned shape 4), from the one-kernel ncu --set full captures
+# summarised in profiles/k_*_{plain40k,large250k}.md (cold caches)
+FORCE_TRAFFIC = {"plain40k": 8.596992e6 + 22.528e3 + 26.290432e6 + 1.28e3,
+                 "large250k": 34.994688e6 + 162.56e3 + 62.455296e6 + 1.440768e6}
 
 
 def env_rank():
@@ -206,6 +208,29 @@ def batched_workload(seed):
     return systems
 
 
+def batched_reference_cpu(systems, steps):
+    """the reference's Release CPU program on the 256 systems, one process per host core at a
+    time (the reference's own way to run many small systems), each system `steps` MD steps with
+    its own temperature and the workload's Bussi thermostat; None where the reference sources are
+    absent"""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import refrun
+    if refrun.reference_checkout() is None and not os.path.exists(refrun.PROGRAMS["cpu"]):
+        return None
+    try:
+        exe = refrun.build("cpu")
+        n = cpu_cores()
+        r = refrun.cpu_batch_rate(exe, systems, n, steps, backend="CPU", dt=0.003, thermostat="bussi",
+                                  newtonian_steps=1, bussi_tau=1000.0)
+    except Exception as e:  # noqa: BLE001
+        print(f"reference CPU batch baseline unavailable: {e}", file=sys.stderr)
+        return None
+    return {"value": r["value"], "unit": "particle-steps/s", "cores": n, "kind": "reference",
+            "sample": f"the reference Release CPU program on each of the {len(systems)} systems, {n} processes at a "
+                      f"time, {steps} MD steps each timed by its own step-loop timer; throughput = sum N_i / "
+                      f"(sum of seconds per step / {n}) ({r['wall_s']:.0f} s wall)"}
+
+
 def bench_batched(args, torch, ox, _abi):
     """256 independent systems (16-4000 nt, duplexes and hairpins, each in its own cube at
     0.005 nt/unit^3, temperatures on a geometric 280-360 K ladder, 0.5 M, dt 0.003, Bussi tau
@@ -261,9 +286,13 @@ def bench_batched(args, torch, ox, _abi):
         t_plain += time.perf_counter() - t1
         m.close()
     v_plain = n_tot * M / t_plain
+    out_cpu = None
+    if not args.no_cpu_baseline:
+        out_cpu = batched_reference_cpu(systems, args.cpu_steps)
     return {"value": v_batch, "unit": "particle-steps/s", "n_systems": len(systems), "n_nucleotides": n_tot,
             "md_steps": M * args.steps, "pt_swaps_tried": tried, "pt_swaps_accepted": accepted,
             "plain_one_at_a_time": v_plain, "speedup_vs_plain": v_batch / v_plain, "force_shape": shape,
+            "cpu_baseline": out_cpu,
             "description": "256 systems, 16-4000 nt log-uniform, duplexes/hairpins, 0.005 nt/unit^3, "
                            "280-360 K geometric ladder, Bussi tau 1000, PT swaps every 1000 steps; "
                            "wall clock including the swaps"}

@@ -166,6 +166,51 @@ def cuda_energy_per_nucleotide(exe: str, s, folder: Optional[str] = None, salt: 
     return vals[0]
 
 
+def cpu_batch_rate(exe: str, systems, n_proc: int, steps: int, **deck_kw) -> dict:
+    """The reference CPU program on every system of a batch (each with its own temperature),
+    n_proc processes at a time, one per core, `steps` MD steps each timed by the program's own
+    step-loop timer.  The batch's throughput on n_proc cores with perfect packing: sum N_i /
+    (sum t_i / n_proc), t_i the seconds per step of system i."""
+    import concurrent.futures as cf
+    tmp = tempfile.mkdtemp(prefix="oxref_batch_")
+
+    def one(k):
+        s = systems[k]
+        d = os.path.join(tmp, f"s{k}")
+        os.makedirs(d, exist_ok=True)
+        write_system(d, s)
+        r = run(exe, d, deck(s, steps=steps, seed=1 + k, **deck_kw), tag="input")
+        if r["own_ms_per_step"] is None:
+            raise RuntimeError(f"no step timer in the output of system {k}")
+        return r["own_ms_per_step"] * 1e-3
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=n_proc) as ex:
+        per = list(ex.map(one, range(len(systems))))
+    wall = time.perf_counter() - t0
+    n_tot = sum(s.N for s in systems)
+    return {"value": n_tot / (sum(per) / n_proc), "s_per_step_sum": sum(per), "wall_s": wall}
+
+
+def reference_verlet_list(exe: str, plugin_dir: str, s, salt: float = 0.5) -> dict:
+    """the first Verlet list the reference CUDA backend builds for system s with its own
+    CUDASimpleVerletList (CUDA_list = verlet), as handed to the GB300DNA2 plugin, which writes it
+    (key gb300_dump_list) with the FP32 positions it was built from: counts[N], the column-major
+    rows and pos[N, 4]"""
+    tmp = tempfile.mkdtemp(prefix="oxref_list_")
+    write_system(tmp, s)
+    dump = os.path.join(tmp, "list.bin")
+    extra = f"plugin_search_path = {plugin_dir}\ngb300_dump_list = {dump}\n"
+    run(exe, tmp, deck(s, backend="CUDA", steps=1, dt=1e-12, salt=salt, interaction="GB300DNA2", extra=extra),
+        tag="input_list")
+    raw = np.fromfile(dump, dtype=np.int32)
+    N, maxc = int(raw[0]), int(raw[1])
+    counts = raw[2:2 + N].copy()
+    rows = raw[2 + N:2 + N + maxc * N].reshape(maxc, N).T.copy()
+    pos = raw[2 + N + maxc * N:2 + N + maxc * N + 4 * N].view(np.float32).reshape(N, 4).copy()
+    return {"counts": counts, "rows": rows, "pos": pos}
+
+
 def cpu_rates(exe: str, s, n_proc: int, steps: int, **deck_kw) -> dict:
     """n_proc independent copies of the single-threaded CPU program on system s, run at the same
     time, one per core; each copy's seconds per step come from its own timer of the step loop

@@ -63,6 +63,8 @@ class MDSettings(C.Structure):
         ("steps_per_graph", C.c_int), ("list_rebuild_node", C.c_int), ("sort_every", C.c_int),
         ("autotune", C.c_int),
         ("use_edge", C.c_int),
+        ("sort_order", C.c_int),
+        ("list_kernel", C.c_int),
     ]
 
 
@@ -108,6 +110,7 @@ SIGNATURES = {
                                       C.POINTER(C.c_double)]),
     "oxgb_md_set_force_shape": (C.c_int, [_VP, C.c_int]),
     "oxgb_force_shape_table": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "oxgb_md_list_kernel": (C.c_int, [_VP, C.POINTER(C.c_int)]),
     "oxgb_md_set_temperature": (C.c_int, [_VP, C.c_int, C.c_double]),
     "oxgb_md_neighbours": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
     "oxgb_md_info": (C.c_int, [_VP, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),

@@ -441,11 +441,13 @@ struct oxgb_md {
 	int *d_id = nullptr, *d_slot = nullptr, *d_perm = nullptr, *d_inv = nullptr;
 	int2 *bonds0 = nullptr;
 	unsigned char *sort_scratch = nullptr;
+	int *d_cell_hil = nullptr, *d_hcount = nullptr, *d_hstart = nullptr, *d_hcursor = nullptr;  // Hilbert order
+	int list_thread = 0;  // neighbour-row kernel (OXGB_LIST_*: chosen at creation or by the autotuner)
 	bool sorting() const { return md.sort_every > 0; }
 
 	void free_layout() {
 		for(void **p : {(void **) &d_sys_nside, (void **) &d_sys_cell0, (void **) &d_cell_sys, (void **) &d_sys_box,
-					(void **) &d_sys_rv2}) {
+					(void **) &d_sys_rv2, (void **) &d_cell_hil, (void **) &d_hcount, (void **) &d_hstart, (void **) &d_hcursor}) {
 			if(*p) cudaFree(*p);
 			*p = nullptr;
 		}
@@ -650,6 +652,46 @@ static int upload_systems(oxgb_md *h, int k0, int k1) {
 	return OXGB_OK;
 }
 
+// The position of cell (x, y, z) of an n^3 grid along a 3D Hilbert curve of 2^b cells per side
+// (2^b >= n): Skilling's transform of the coordinates to the curve's transposed index
+// ("Programming the Hilbert curve", AIP Conf. Proc. 707, 381 (2004)), its bits interleaved
+// most significant first.  The cells of the grid are then ranked by that key.
+static unsigned long long hilbert_key(unsigned x, unsigned y, unsigned z, int b) {
+	unsigned X[3] = {x, y, z};
+	const unsigned M = 1u << (b - 1);
+	for(unsigned Q = M; Q > 1; Q >>= 1) {
+		const unsigned P = Q - 1;
+		for(int i = 0; i < 3; i++) {
+			if(X[i] & Q) X[0] ^= P;
+			else {
+				const unsigned t = (X[0] ^ X[i]) & P;
+				X[0] ^= t;
+				X[i] ^= t;
+			}
+		}
+	}
+	for(int i = 1; i < 3; i++) X[i] ^= X[i - 1];
+	unsigned t = 0;
+	for(unsigned Q = M; Q > 1; Q >>= 1)
+		if(X[2] & Q) t ^= Q - 1;
+	for(int i = 0; i < 3; i++) X[i] ^= t;
+	unsigned long long key = 0;
+	for(int k = b - 1; k >= 0; k--)
+		for(int i = 0; i < 3; i++) key = (key << 1) | ((X[i] >> k) & 1u);
+	return key;
+}
+
+// cell_hil[c0 + c] = c0 + the rank of cell c of an n^3 grid along the Hilbert curve
+static void hilbert_ranks(int n, int c0, std::vector<int> &cell_hil) {
+	int b = 1;
+	while((1 << b) < n) b++;
+	const int nc = n * n * n;
+	std::vector<std::pair<unsigned long long, int>> key(nc);
+	for(int c = 0; c < nc; c++) key[c] = {hilbert_key(c % n, (c / n) % n, c / (n * n), b), c};
+	std::sort(key.begin(), key.end());
+	for(int r = 0; r < nc; r++) cell_hil[c0 + key[r].second] = c0 + r;
+}
+
 // cell grids of all systems (cells per side from each system's own box and cutoff) and the
 // device copies of the geometry the list kernels read; reallocates the cell buffers
 static int layout_cells(oxgb_md *h) {
@@ -682,6 +724,15 @@ static int layout_cells(oxgb_md *h) {
 	CK(cudaMemcpy(h->d_cell_sys, cell_sys.data(), sizeof(int) * n_cells, cudaMemcpyHostToDevice));
 	CK(cudaMemcpy(h->d_sys_box, bx.data(), sizeof(float) * S, cudaMemcpyHostToDevice));
 	CK(cudaMemcpy(h->d_sys_rv2, rv2.data(), sizeof(float) * S, cudaMemcpyHostToDevice));
+	if(h->sorting() && h->md.sort_order == OXGB_SORT_HILBERT) {
+		std::vector<int> cell_hil(n_cells);
+		for(int k = 0; k < S; k++) hilbert_ranks(h->nside[k], h->cell0[k], cell_hil);
+		CK(cudaMalloc(&h->d_cell_hil, sizeof(int) * n_cells));
+		CK(cudaMalloc(&h->d_hcount, sizeof(int) * (n_cells + 1)));
+		CK(cudaMalloc(&h->d_hstart, sizeof(int) * (n_cells + 1)));
+		CK(cudaMalloc(&h->d_hcursor, sizeof(int) * (n_cells + 1)));
+		CK(cudaMemcpy(h->d_cell_hil, cell_hil.data(), sizeof(int) * n_cells, cudaMemcpyHostToDevice));
+	}
 	return OXGB_OK;
 }
 
@@ -725,6 +776,15 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	h->md = *md;
 	if(h->md.steps_per_graph <= 0) h->md.steps_per_graph = 16;
 	if(h->md.sort_every < 0) h->md.sort_every = 0;
+	if(h->md.sort_order != OXGB_SORT_HILBERT && h->md.sort_order != OXGB_SORT_CELLS) {
+		delete h;
+		return fail(OXGB_E_INVALID, "sort_order must be OXGB_SORT_HILBERT or OXGB_SORT_CELLS");
+	}
+	if(h->md.list_kernel < OXGB_LIST_AUTO || h->md.list_kernel > OXGB_LIST_THREAD) {
+		delete h;
+		return fail(OXGB_E_INVALID, "list_kernel must be OXGB_LIST_AUTO, _WARP or _THREAD");
+	}
+	h->list_thread = h->md.list_kernel == OXGB_LIST_THREAD ? 1 : 0;
 	h->conditional_ok = h->md.list_rebuild_node == 0;
 	h->dbl = md->precision == OXGB_PRECISION_DOUBLE;
 	h->rcut.assign(n_systems, 0.0);
@@ -962,6 +1022,7 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	a.term_max = h->term_max;
 	a.base_pos = h->tl.base_pos;
 	a.stk_pos = h->tl.stk_pos;
+	a.list_thread = h->list_thread;
 	if(h->sorting()) {
 		a.sort_every = h->md.sort_every;
 		a.id = h->d_id;
@@ -973,6 +1034,10 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 		a.mir[5] = h->fa1lo, a.mir[6] = h->fbacklo;
 		a.bonds_rw = h->bonds;
 		a.scratch = h->sort_scratch;
+		a.cell_hil = h->d_cell_hil;
+		a.hcount = h->d_hcount;
+		a.hstart = h->d_hstart;
+		a.hcursor = h->d_hcursor;
 	}
 	return a;
 }
@@ -1006,7 +1071,12 @@ static int compute_forces_now(oxgb_md *h) {
 // size), so engines of the same class reuse it without timing.
 
 static std::mutex g_tune_mutex;
-static std::map<std::tuple<int, int, int>, std::pair<int, double>> g_tune_cache;
+struct TuneResult {
+	int shape;
+	double shape_us;
+	int list_thread;  // -1: not timed (the engine keeps its own choice)
+};
+static std::map<std::tuple<int, int, int>, TuneResult> g_tune_cache;
 
 static int ilog2(long long v) {
 	int k = 0;
@@ -1024,8 +1094,9 @@ static int autotune_shape(oxgb_md *h) {
 		std::lock_guard<std::mutex> lock(g_tune_mutex);
 		auto it = g_tune_cache.find(key);
 		if(it != g_tune_cache.end()) {
-			h->shape = it->second.first;
-			h->shape_us = it->second.second;
+			h->shape = it->second.shape;
+			h->shape_us = it->second.shape_us;
+			if(it->second.list_thread >= 0 && h->md.list_kernel == OXGB_LIST_AUTO) h->list_thread = it->second.list_thread;
 			h->tuned = true;
 			return OXGB_OK;
 		}
@@ -1055,6 +1126,36 @@ static int autotune_shape(oxgb_md *h) {
 			best = k;
 		}
 	}
+	// the neighbour-row kernel: both build the same rows from the current positions (a rebuild
+	// is idempotent); not timed when sorting, where extra builds would move the sort schedule
+	int list_thread = -1;
+	if(h->md.list_kernel == OXGB_LIST_AUTO && !h->sorting()) {
+		double best_list = 1e30;
+		for(int v = 0; v < 2; v++) {
+			h->list_thread = v;
+			int rc = build_list_now(h);
+			if(rc) return rc;
+			std::vector<double> t;
+			for(int rep = 0; rep < 3; rep++) {
+				CK(cudaEventRecord(e0, h->stream));
+				for(int r = 0; r < 3; r++) {
+					rc = build_list_now(h);
+					if(rc) return rc;
+				}
+				CK(cudaEventRecord(e1, h->stream));
+				CK(cudaEventSynchronize(e1));
+				float ms = 0.f;
+				CK(cudaEventElapsedTime(&ms, e0, e1));
+				t.push_back(ms);
+			}
+			std::sort(t.begin(), t.end());
+			if(t[1] < best_list) {
+				best_list = t[1];
+				list_thread = v;
+			}
+		}
+		h->list_thread = list_thread;
+	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
 	h->shape = best;
@@ -1062,7 +1163,7 @@ static int autotune_shape(oxgb_md *h) {
 	h->tuned = true;
 	{
 		std::lock_guard<std::mutex> lock(g_tune_mutex);
-		g_tune_cache[key] = std::make_pair(best, best_us);
+		g_tune_cache[key] = TuneResult{best, best_us, list_thread};
 	}
 	// the forces of the state, from the chosen shape (the same values: shapes differ in work
 	// distribution and summation order only)
@@ -1193,6 +1294,12 @@ extern "C" int oxgb_md_set_force_shape(oxgb_md *h, int k) {
 		h->gexec = nullptr;
 	}
 	return h->have_state ? compute_forces_now(h) : OXGB_OK;
+}
+
+extern "C" int oxgb_md_list_kernel(oxgb_md *h, int *kernel) {
+	if(!h || !kernel) return fail(OXGB_E_INVALID, "null argument");
+	*kernel = h->list_thread ? OXGB_LIST_THREAD : OXGB_LIST_WARP;
+	return OXGB_OK;
 }
 
 extern "C" int oxgb_force_shape_table(int k, int *pair_npw, int *nb_lanes, int *nb_min_blocks) {

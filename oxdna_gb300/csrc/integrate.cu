@@ -182,12 +182,12 @@ __device__ __forceinline__ double4_32a round4(const double4_32a &v) {
 // kind of motion.
 template <typename V4, bool F32 = false>
 __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
-	__shared__ float3 s_a1[32], s_bk[32];
+	__shared__ float3 s_r32[32];
 	const int lane = threadIdx.x & 31;
 	const bool rot = threadIdx.x >= 32;
 	const int i = blockIdx.x * 32 + lane;
 	const bool live = i < a.N;
-	float3 r32 = make_float3(0.f, 0.f, 0.f);
+	float3 r32 = make_float3(0.f, 0.f, 0.f), fa1 = r32, fbk = r32;
 	int sy = 0;
 	double4_32a x, y;  // (v, r) on the translation warp, (L, q) on the rotation warp
 	float4 lp, la1, lbk;
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 			sy = a.th.sys[i];
 			x = rot ? a.angmom[i] : a.vel[i];
 			y = rot ? a.quat[i] : a.pos[i];
-			if(!rot) {
+			if(rot) {
 				lp = a.list_pos[i];
 				if(a.list_a1) la1 = a.list_a1[i], lbk = a.list_back[i];
 			}
@@ -257,10 +257,7 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 			const double4_32a qd = widen4(q.x, q.y, q.z, q.w);
 			a.angmom[i] = x;
 			a.quat[i] = qd;
-			float3 a1, bk;
-			mirror_frame(a, i, qd, a1, bk);
-			s_a1[lane] = a1;
-			s_bk[lane] = bk;
+			mirror_frame(a, i, qd, fa1, fbk);
 		}
 		}
 	}
@@ -301,16 +298,19 @@ __global__ void __launch_bounds__(64) k_first_step(StepArgs a) {
 			if(!(sizeof(V4) == sizeof(float4) && rotate_small(q.x, q.y, q.z, q.w, x.x, x.y, x.z, 0.5 * a.dt))) rotate(q, x, a.dt);
 			a.angmom[i] = x;
 			a.quat[i] = q;
-			float3 a1, bk;
-			mirror_frame(a, i, q, a1, bk);
-			s_a1[lane] = a1;
-			s_bk[lane] = bk;
+			mirror_frame(a, i, q, fa1, fbk);
 		}
 	}
-	__syncthreads();
 	// Verlet list staleness (CUDA_mixed.cuh:68, extended to the interaction sites for the term
-	// lists), per system, on the translation warp with the rotation warp's a1 and backbone offset
-	if(live && !rot && list_stale(a, lp, la1, lbk, r32, s_a1[lane], s_bk[lane])) {
+	// lists), per system, on the rotation warp (the slower one) with the translation warp's FP32
+	// position: the translation warp posts it and leaves (named barrier 1: arrive, no wait)
+	if(!rot) {
+		s_r32[lane] = r32;
+		asm volatile("bar.arrive 1, 64;" ::: "memory");
+		return;
+	}
+	asm volatile("bar.sync 1, 64;" ::: "memory");
+	if(live && list_stale(a, lp, la1, lbk, s_r32[lane], fa1, fbk)) {
 		a.sys_stale[sy] = 1;
 		atomicOr(a.flag, 1);
 	}

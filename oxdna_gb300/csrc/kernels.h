@@ -214,6 +214,14 @@ struct ListArgs {
 	float4 *mir[7];         // mirrors: pos_hi, pos_lo, fa1, fa3, fback, fa1lo, fbacklo (any may be null)
 	int2 *bonds_rw;         // the bonds the rows exclude (the array of `bonds`)
 	unsigned char *scratch; // [N * SORT_BYTES]
+	// Hilbert order of the cells (null: row-major cell order): cell c of the global numbering is
+	// the cell_hil[c]-th of its system's cells along a Hilbert curve (plus the system's first
+	// cell); hcount / hstart / hcursor [n_cells + 1] are the counts and the exclusive scan in that
+	// order.  hilbert_pass marks the argument copy that runs the scan kernels on them.
+	const int *cell_hil;
+	int *hcount, *hstart, *hcursor;
+	int hilbert_pass;
+	int list_thread;        // neighbour rows by k_neighbours_thread (1) or k_neighbours (0)
 };
 
 // bytes per nucleotide of the sort's staging buffer: 4 FP64 vectors, 7 FP32 vectors, bonds,

@@ -31,6 +31,11 @@ __device__ __forceinline__ float sqr_min_image(float4 a, float4 b, float L) {
 #define SKIP_IF_FRESH(a) \
 	if((a).check_flag && *(a).flag == 0) return
 
+// the scan kernels' copy for the Hilbert order runs only in the builds that sort
+#define SKIP_IF_NO_SORT(a) \
+	if((a).hilbert_pass && !((a).sort_every > 0 && (a).id && ((a).rebuilds ? *(a).rebuilds : 0ull) % (unsigned long long) (a).sort_every == 0ull)) \
+		return
+
 // geometry of system s: box side, r_verlet^2, cells per side, first cell
 struct CellGeo {
 	float box, rv2;
@@ -109,6 +114,7 @@ __device__ __forceinline__ int block_incl_scan(int v, int *warp_tot) {
 
 __global__ void __launch_bounds__(SCAN_TPB) k_scan_tiles(ListArgs a, int n_cells) {
 	SKIP_IF_FRESH(a);
+	SKIP_IF_NO_SORT(a);
 	__shared__ int wt[32];
 	const int base = blockIdx.x * SCAN_TILE + threadIdx.x * 4;
 	int v = 0;
@@ -122,6 +128,7 @@ __global__ void __launch_bounds__(SCAN_TPB) k_scan_tiles(ListArgs a, int n_cells
 // exclusive scan of the tile sums in place (one block, any number of tiles)
 __global__ void __launch_bounds__(SCAN_TPB) k_scan_top(ListArgs a, int n_tiles) {
 	SKIP_IF_FRESH(a);
+	SKIP_IF_NO_SORT(a);
 	__shared__ int wt[32];
 	__shared__ int carry;
 	if(threadIdx.x == 0) carry = 0;
@@ -141,6 +148,7 @@ __global__ void __launch_bounds__(SCAN_TPB) k_scan_top(ListArgs a, int n_tiles) 
 
 __global__ void __launch_bounds__(SCAN_TPB) k_scan_apply(ListArgs a, int n_cells, int n_tiles) {
 	SKIP_IF_FRESH(a);
+	SKIP_IF_NO_SORT(a);
 	__shared__ int wt[32];
 	const int base = blockIdx.x * SCAN_TILE + threadIdx.x * 4;
 	int c[4], v = 0;
@@ -204,6 +212,34 @@ __global__ void k_sort_perm(ListArgs a) {
 	const int from = rebuilt(a, sys_of(a, k)) ? a.cell_list[k] : k;
 	a.perm[k] = from;
 	a.inv[from] = k;
+}
+
+// Hilbert order: every cell's count at its Hilbert position (counts of systems not rebuilt are
+// those of their last build, so every system's cells still hold exactly its nucleotides)
+__global__ void k_sort_hcount(ListArgs a, int n_cells) {
+	SKIP_IF_FRESH(a);
+	if(!sort_now(a)) return;
+	const int c = blockIdx.x * blockDim.x + threadIdx.x;
+	if(c < n_cells) a.hcount[a.cell_hil[c]] = a.cell_count[c];
+}
+
+// Hilbert order: the nucleotide at position p of the cell-ordered list moves to the position of
+// its cell along the curve plus its rank within the cell (rebuilt systems; the others stay)
+__global__ void k_sort_perm_hilbert(ListArgs a) {
+	SKIP_IF_FRESH(a);
+	if(!sort_now(a)) return;
+	const int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= a.N) return;
+	if(!rebuilt(a, sys_of(a, p))) {
+		a.perm[p] = p;
+		a.inv[p] = p;
+		return;
+	}
+	const int i = a.cell_list[p];
+	const int c = a.cell_of[i];
+	const int q = a.hstart[a.cell_hil[c]] + (p - a.cell_start[c]);
+	a.perm[q] = i;
+	a.inv[i] = q;
 }
 
 // everything of old slot perm[k] into the staging buffer at k; bonds renumbered
@@ -388,6 +424,85 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	}
 }
 
+// One thread per nucleotide, the 27 cells in the same serial order (dz, dy, dx from -1 to 1, each
+// cell's segment by index) and the same FP32 tests, so the rows are those of k_neighbours entry for
+// entry.  Consecutive threads are consecutive nucleotides, so the stores of entry k into the
+// column-major rows ([k N + i]) of a warp fall into one or two sectors, where k_neighbours' lanes
+// store the entries of one row N apart.  Fewer instructions and coalesced stores win where a
+// nucleotide's 27 cells hold few candidates (measured: the 250,000-nucleotide melt, 0.8 per cell);
+// the warp kernel wins where they hold many (clustered duplexes): the engine's autotuner times both.
+__global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
+	SKIP_IF_FRESH(a);
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= a.N) return;
+	const int sy = sys_of(a, i);
+	if(!rebuilt(a, sy)) return;
+	const CellGeo g = cell_geo(a, sy);
+	const float4 r = a.pos[i];
+	const int2 b = a.bonds[i];
+	const int n = g.n;
+	const int c = a.cell_of[i] - g.cell0;
+	const int cx = c % n, cy = (c / n) % n, cz = c / (n * n);
+	const bool terms = a.ev_nb != nullptr;
+	const long long N = a.N;
+	float4 a1i = make_float4(0.f, 0.f, 0.f, 0.f), bki = a1i;
+	if(terms) {
+		a1i = a.fa1[i];
+		bki = a.fback[i];
+	}
+	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
+	for(int l = 0; l < 27; l++) {
+		const int z = (cz + l / 9 - 1 + n) % n, y = (cy + (l / 3) % 3 - 1 + n) % n, x = (cx + l % 3 - 1 + n) % n;
+		const int cc = g.cell0 + (z * n + y) * n + x;
+		const int s1 = a.cell_start[cc + 1];
+		for(int u = a.cell_start[cc]; u < s1; u++) {
+			const int j = a.cell_list[u];
+			if(j == i || j == b.x || j == b.y) continue;
+			const float4 rj = a.pos[j];
+			const float d2 = sqr_min_image(r, rj, g.box);
+			if(!(d2 < g.rv2)) continue;
+			if(cnt < a.max_nb) put(a.nb, a.col_major != 0, N, a.max_nb, i, cnt, j);
+			cnt++;
+			if(terms && d2 < a.ev_r2) {
+				if(nev < a.ev_cap) a.ev_nb[(long long) nev * N + i] = j;
+				nev++;
+				const float3 d = min_image_vec(r, rj, g.box);
+				const float4 a1j = a.fa1[j];
+				// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
+				const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
+						bz = d.z + 0.4f * (a1j.z - a1i.z);
+				if(bx * bx + by * by + bz * bz < a.base_r2) {
+					if(nbase < a.base_cap) a.base_nb[(long long) nbase * N + i] = j;
+					nbase++;
+				}
+				const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy2 = d.y + 0.34f * (a1j.y - a1i.y),
+						sz = d.z + 0.34f * (a1j.z - a1i.z);
+				if(sx * sx + sy2 * sy2 + sz * sz < a.stk_r2) {
+					if(nstk < a.stk_cap) a.stk_nb[(long long) nstk * N + i] = j;
+					nstk++;
+				}
+			}
+		}
+	}
+	if(cnt > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
+	if(a.term_max && cnt > a.term_max[3]) atomicMax(a.term_max + 3, cnt);
+	a.nnb[i] = cnt;
+	a.list_pos[i] = r;
+	if(terms) {
+		if(nev > a.ev_cap || nbase > a.base_cap || nstk > a.stk_cap) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
+		if(a.term_max) {
+			if(nev > a.term_max[0]) atomicMax(a.term_max, nev);
+			if(nbase > a.term_max[1]) atomicMax(a.term_max + 1, nbase);
+			if(nstk > a.term_max[2]) atomicMax(a.term_max + 2, nstk);
+		}
+		a.ev_n[i] = nev;
+		a.base_n[i] = nbase;
+		a.stk_n[i] = nstk;
+		a.list_a1[i] = a1i;
+		a.list_back[i] = bki;
+	}
+}
+
 // For every base / stack list entry (k, i) with partner j above i by caller's index (i owns the
 // pair, as in an unsorted run): where i sits in
 // j's list (the lists are symmetric: the pair criteria are exactly symmetric in FP32).  One
@@ -443,13 +558,32 @@ cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s) {
 	k_scan_apply<<<tiles, SCAN_TPB, 0, s>>>(a, n_cells, tiles);
 	k_cell_scatter<<<gp, tpb, 0, s>>>(a);
 	k_cell_rank<<<gp, tpb, 0, s>>>(a);
-	if(a.sort_every > 0 && a.id) {
+	if(a.sort_every > 0 && a.id && a.cell_hil) {
+		// the counts in Hilbert order, scanned by the same three kernels on a copy of the
+		// arguments, then the permutation
+		k_sort_hcount<<<(n_cells + tpb - 1) / tpb, tpb, 0, s>>>(a, n_cells);
+		ListArgs h = a;
+		h.cell_count = a.hcount;
+		h.cell_start = a.hstart;
+		h.cell_cursor = a.hcursor;
+		h.hilbert_pass = 1;
+		k_scan_tiles<<<tiles, SCAN_TPB, 0, s>>>(h, n_cells);
+		k_scan_top<<<1, SCAN_TPB, 0, s>>>(h, tiles);
+		k_scan_apply<<<tiles, SCAN_TPB, 0, s>>>(h, n_cells, tiles);
+		k_sort_perm_hilbert<<<gp, tpb, 0, s>>>(a);
+		k_sort_gather<<<gp, tpb, 0, s>>>(a);
+		k_sort_scatter<<<gp, tpb, 0, s>>>(a);
+	}
+	else if(a.sort_every > 0 && a.id) {
 		k_sort_perm<<<gp, tpb, 0, s>>>(a);
 		k_sort_gather<<<gp, tpb, 0, s>>>(a);
 		k_sort_scatter<<<gp, tpb, 0, s>>>(a);
 	}
-	const long long warps = (long long) a.N * 32;
-	k_neighbours<<<(int) ((warps + tpb - 1) / tpb), tpb, 0, s>>>(a);
+	if(a.list_thread) k_neighbours_thread<<<(a.N + 127) / 128, 128, 0, s>>>(a);
+	else {
+		const long long warps = (long long) a.N * 32;
+		k_neighbours<<<(int) ((warps + tpb - 1) / tpb), tpb, 0, s>>>(a);
+	}
 	if(a.base_pos && a.stk_pos) k_term_pos<<<2 * gp, tpb, 0, s>>>(a, gp);
 	k_list_done<<<1, 256, 0, s>>>(a);
 	return cudaGetLastError();

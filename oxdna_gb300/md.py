@@ -47,7 +47,8 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
                 pt: float = 0.0, diff_coeff: float = 2.5, bussi_tau: float = 1000.0, seed: int = 1,
                 precision: str = "mixed", cells_auto_optimisation: bool = True, max_neigh: int = 0,
                 steps_per_graph: int = 16, list_rebuild_node: str = "conditional", sort_every: int = 0,
-                autotune: bool = False, use_edge: bool = False) -> _abi.MDSettings:
+                autotune: bool = False, use_edge: bool = False, sort_order: str = "hilbert",
+                list_kernel: str = "auto") -> _abi.MDSettings:
     m = _abi.MDSettings()
     _abi.lib().oxgb_md_default_settings(C.byref(m))
     m.dt = dt
@@ -66,6 +67,8 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
     m.sort_every = sort_every
     m.autotune = 1 if autotune else 0
     m.use_edge = 1 if use_edge else 0
+    m.sort_order = {"hilbert": 0, "cells": 1}[sort_order]
+    m.list_kernel = {"auto": 0, "warp": 1, "thread": 2}[list_kernel]
     return m
 
 
@@ -331,6 +334,9 @@ class MDSystem:
         _abi.check(_abi.lib().oxgb_md_force_shape(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(t)))
         out = dict(pair_npw=a.value, nb_lanes=b.value, nb_min_blocks=c.value, launch_us=t.value)
         out["index"] = next((k for k, sh in enumerate(force_shapes()) if sh == (a.value, b.value, c.value)), None)
+        lk = C.c_int()
+        _abi.check(_abi.lib().oxgb_md_list_kernel(self._h, C.byref(lk)))
+        out["list_kernel"] = {1: "warp", 2: "thread"}[lk.value]
         return out
 
     def set_force_shape(self, k: int):

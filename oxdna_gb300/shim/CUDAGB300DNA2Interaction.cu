@@ -27,7 +27,10 @@
 
 #include "oxgb.h"
 
+#include <algorithm>
+#include <cstdio>
 #include <string>
+#include <vector>
 
 namespace {
 
@@ -85,6 +88,32 @@ public:
 class CUDAGB300DNA2Interaction: public CUDABaseInteraction, public DNA2Interaction {
 	oxgb_dna2 *_h = nullptr;
 	oxgb_dna2_settings _s{};
+	// gb300_dump_list: a file that receives the first neighbour list the backend hands over
+	// (whatever CUDABaseList built it) with the positions it was built from, so that a test can
+	// compare the reference's own list with the library's
+	std::string _dump_list;
+	bool _dumped = false;
+
+	void _dump(CUDABaseList *lists, const c_number4 *d_poss) {
+		if(cudaDeviceSynchronize() != cudaSuccess) throw oxDNAException("gb300_dump_list: CUDA error");
+		const int N = _N;
+		std::vector<int> cnt(N);
+		cudaMemcpy(cnt.data(), lists->d_number_neighs, sizeof(int) * N, cudaMemcpyDeviceToHost);
+		const int maxc = N > 0 ? *std::max_element(cnt.begin(), cnt.end()) : 0;
+		std::vector<int> rows((size_t) maxc * N);  // column-major: entry k of i at [k N + i]
+		if(maxc > 0) cudaMemcpy(rows.data(), lists->d_matrix_neighs, sizeof(int) * rows.size(), cudaMemcpyDeviceToHost);
+		std::vector<float> pos((size_t) 4 * N);
+		cudaMemcpy(pos.data(), d_poss, sizeof(float) * pos.size(), cudaMemcpyDeviceToHost);
+		if(cudaGetLastError() != cudaSuccess) throw oxDNAException("gb300_dump_list: CUDA error");
+		FILE *f = std::fopen(_dump_list.c_str(), "wb");
+		if(!f) throw oxDNAException("gb300_dump_list: cannot open %s", _dump_list.c_str());
+		const int head[2] = {N, maxc};
+		std::fwrite(head, sizeof(int), 2, f);
+		std::fwrite(cnt.data(), sizeof(int), cnt.size(), f);
+		std::fwrite(rows.data(), sizeof(int), rows.size(), f);
+		std::fwrite(pos.data(), sizeof(float), pos.size(), f);
+		std::fclose(f);
+	}
 
 	// the oxgb settings from what the CPU class read and derived
 	void _fill_settings() {
@@ -120,7 +149,10 @@ class CUDAGB300DNA2Interaction: public CUDABaseInteraction, public DNA2Interacti
 	}
 
 public:
-	void get_settings(input_file &inp) override { DNA2Interaction::get_settings(inp); }
+	void get_settings(input_file &inp) override {
+		DNA2Interaction::get_settings(inp);
+		getInputString(&inp, "gb300_dump_list", _dump_list, 0);
+	}
 
 	void cuda_init(int N) override {
 		CUDABaseInteraction::cuda_init(N);
@@ -139,6 +171,10 @@ public:
 	// arrive initialised (zeros or external forces) and are accumulated into
 	void compute_forces(CUDABaseList *lists, c_number4 *d_poss, GPU_quat *d_orientations, c_number4 *d_forces, c_number4 *d_torques,
 			LR_bonds *d_bonds, CUDABox *d_box) override {
+		if(!_dump_list.empty() && !_dumped) {
+			_dump(lists, d_poss);
+			_dumped = true;
+		}
 		// the rows are read up to d_number_neighs, which the list keeps within its capacity
 		oxgb_check(oxgb_dna2_compute_forces(_h, _N, cubic_side(), d_poss, d_orientations, d_forces, d_torques, d_bonds,
 						   lists->d_matrix_neighs, lists->d_number_neighs, _N, 1, _N, nullptr),

@@ -44,14 +44,57 @@ def test_list_matches_oracle_on_fixtures(case):
     sysm.close()
 
 
+@pytest.mark.parametrize("kernel", ["warp", "thread"])
 @pytest.mark.parametrize("cfg,scale", [(1, 0.1), (2, 0.02)])
-def test_list_matches_oracle_on_generated(cfg, scale):
+def test_list_matches_oracle_on_generated(cfg, scale, kernel):
     s = G.system_for_config(cfg, seed=11, scale=scale)
     a1, a2, a3 = s.frames()
     q = oxio.frame_to_quat(a1, a2, a3)
     from oxdna_gb300 import dna2_settings
-    sysm = MDSystem(s.box, s.top, dna2_settings(s.T, 0.5), md_settings())
+    sysm = MDSystem(s.box, s.top, dna2_settings(s.T, 0.5), md_settings(list_kernel=kernel))
     sysm.set_state(s.pos, q, s.vel, s.L)
     p = oracle.make_params(oracle.make_settings(s.T, 0.5))
     check_list(sysm, s.pos, s.box, s.top.n3, s.top.n5, p.rcut)
     sysm.close()
+
+
+@pytest.mark.parametrize("cfg,scale", [(1, 0.1), (2, 0.02)])
+def test_list_kernels_give_identical_rows_and_trajectories(cfg, scale):
+    """the warp and the thread neighbour kernels write the same rows, entry for entry (the order
+    of every row, not only its set), so Brownian trajectories are bit-identical"""
+    from oxdna_gb300 import dna2_settings
+    s = G.system_for_config(cfg, seed=12, scale=scale)
+    a1, a2, a3 = s.frames()
+    q = oxio.frame_to_quat(a1, a2, a3)
+    out = []
+    for kernel in ("warp", "thread"):
+        m = MDSystem(s.box, s.top, dna2_settings(s.T, 0.5),
+                     md_settings(dt=0.003, thermostat="john", newtonian_steps=3, pt=0.2, seed=9, list_kernel=kernel))
+        m.set_state(s.pos, q, s.vel, s.L)
+        assert m.force_shape()["list_kernel"] == kernel
+        rows0 = m.neighbours()
+        m.run(300)
+        rows1 = m.neighbours()
+        st = m.get_state()
+        out.append((rows0, rows1, st, m.info()["rebuilds"]))
+        m.close()
+    (w0, w1, ws, wr), (t0, t1, ts, tr) = out
+    assert wr == tr and wr >= 3
+    for a_, b_ in ((w0, t0), (w1, t1)):
+        assert np.array_equal(a_[0], b_[0])
+        for i in range(s.N):
+            assert np.array_equal(a_[1][i, :a_[0][i]], b_[1][i, :b_[0][i]]), i
+    for key in ("pos", "quat", "vel", "Lmom"):
+        assert np.array_equal(ws[key], ts[key]), key
+
+
+def test_autotuner_picks_a_list_kernel():
+    from oxdna_gb300 import dna2_settings
+    s = G.system_for_config(2, seed=13, scale=0.02)
+    a1, a2, a3 = s.frames()
+    m = MDSystem(s.box, s.top, dna2_settings(s.T, 0.5), md_settings(autotune=True))
+    m.set_state(s.pos, oxio.frame_to_quat(a1, a2, a3), s.vel, s.L)
+    sh = m.force_shape()
+    print(f"autotuned: {sh}")
+    assert sh["list_kernel"] in ("warp", "thread")
+    m.close()

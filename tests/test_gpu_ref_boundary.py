@@ -1,4 +1,5 @@
-"""The drop-in boundary run inside the reference's own program, on the GPU.
+"""The drop-in boundary run inside the reference's own program, on the GPU, and the reference's
+own Verlet list against ours.
 
 Both routes are built from the reference's sources by oracle/ref/Makefile (no CMake) and run:
 
@@ -91,3 +92,47 @@ def test_substituted_program_runs_md(programs, system):
         assert np.all(np.isfinite(conf.pos)) and conf.pos.shape == system.pos.shape
         assert r["own_ms_per_step"] is not None
         print(f"substituted program: {r['own_ms_per_step']:.4f} ms per step (its own timer), 2000 steps")
+
+
+def test_reference_verlet_list_has_our_pair_sets(programs, system):
+    """The reference's own CUDASimpleVerletList (CUDA_list = verlet) on the GPU, dumped by the
+    plugin with the FP32 positions it was built from, against the library's list built from the
+    same positions (oxgb_verlet_*): the same partners for every nucleotide.  The reference fills
+    its cells with atomic increments, so only the sets are compared, not the order in a row."""
+    import ctypes as C
+    import torch
+    from oxdna_gb300 import _abi
+    d = os.path.dirname(programs["plugin"])
+    ref = refrun.reference_verlet_list(programs["cuda"], d, system)
+    N = system.N
+    L = _abi.lib()
+    h = C.c_void_p()
+    st = dna2_settings(system.T, 0.5)
+    _abi.check(L.oxgb_dna2_create(C.byref(st), C.byref(h)))
+    rcut = C.c_double()
+    _abi.check(L.oxgb_dna2_get_rcut(h, C.byref(rcut)))
+    _abi.check(L.oxgb_dna2_destroy(h))
+    v = C.c_void_p()
+    _abi.check(L.oxgb_verlet_create(N, float(system.box), rcut.value, 0.05, 1, 0, C.byref(v)))
+    d_pos = torch.from_numpy(ref["pos"]).cuda()
+    d_list_pos = torch.zeros_like(d_pos)
+    bonds = np.stack([system.top.n3, system.top.n5], axis=1).astype(np.int32)
+    d_bonds = torch.from_numpy(bonds).cuda()
+    _abi.check(L.oxgb_verlet_update(v, d_pos.data_ptr(), d_list_pos.data_ptr(), d_bonds.data_ptr(), None))
+    torch.cuda.synchronize()
+    _abi.check(L.oxgb_verlet_status(v))
+    nb_ptr, nnb_ptr = C.c_void_p(), C.c_void_p()
+    max_nb, ns = C.c_int(), C.c_int()
+    _abi.check(L.oxgb_verlet_buffers(v, C.byref(nb_ptr), C.byref(nnb_ptr), C.byref(max_nb), C.byref(ns)))
+    from test_gpu_plugin_layers import view
+    nnb = view(nnb_ptr.value, (N,), "<i4").cpu().numpy()
+    nb = view(nb_ptr.value, (max_nb.value, N), "<i4").cpu().numpy()
+    _abi.check(L.oxgb_verlet_destroy(v))
+    assert np.array_equal(nnb, ref["counts"])
+    total = 0
+    for i in range(N):
+        ours = np.sort(nb[:nnb[i], i])
+        theirs = np.sort(ref["rows"][i, :ref["counts"][i]])
+        assert np.array_equal(ours, theirs), i
+        total += nnb[i]
+    print(f"reference CUDASimpleVerletList vs ours on {N} nucleotides: {total} entries, identical sets")

@@ -1,5 +1,6 @@
-"""Cell-order storage (md_settings(sort_every=k), the reference's CUDA_sort_every): every k-th
-list rebuild moves the nucleotides on the device into the order of their cells.  Cells are
+"""Spatially ordered storage (md_settings(sort_every=k), the reference's CUDA_sort_every): every
+k-th list rebuild moves the nucleotides on the device into the order of their cells -- along a
+Hilbert curve (sort_order "hilbert", the default, the reference's key) or row-major ("cells").  Cells are
 ordered and base/stack pairs owned by the caller's index, so the neighbour rows list the same
 partners in the same order as without sorting, and the Philox draws are keyed by the caller's
 index: forces, Brownian and NVE trajectories are bit-identical to an unsorted run, and the state,
@@ -40,11 +41,12 @@ def _same(a, b):
     assert np.array_equal(Fa, Fb) and np.array_equal(Ta, Tb)
 
 
+@pytest.mark.parametrize("order", ["hilbert", "cells"])
 @pytest.mark.parametrize("thermostat,every", [("john", 1), ("no", 1), ("john", 3)])
-def test_sorted_run_is_bit_identical(duplexes, thermostat, every):
+def test_sorted_run_is_bit_identical(duplexes, thermostat, every, order):
     kw = dict(dt=0.003, thermostat=thermostat, newtonian_steps=3, pt=0.2, seed=5, steps_per_graph=10)
     a = _engine(duplexes, **kw)
-    b = _engine(duplexes, sort_every=every, **kw)
+    b = _engine(duplexes, sort_every=every, sort_order=order, **kw)
     N = duplexes.N
     for n in (100, 105, 95):  # graph launches and eager remainders
         a.run(n)
@@ -120,3 +122,15 @@ def test_state_and_topology_round_trip_while_sorted(duplexes):
     m.run(50)
     assert np.all(np.isfinite(m.get_state()["pos"]))
     m.close()
+
+
+def test_hilbert_and_cell_orders_differ(duplexes):
+    kw = dict(dt=0.003, thermostat="john", newtonian_steps=3, pt=0.2, seed=5, steps_per_graph=10, sort_every=1)
+    h = _engine(duplexes, sort_order="hilbert", **kw)
+    c = _engine(duplexes, sort_order="cells", **kw)
+    h.run(50)
+    c.run(50)
+    _same(h, c)
+    assert not np.array_equal(h.storage_order(), c.storage_order())
+    h.close()
+    c.close()
