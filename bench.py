@@ -727,7 +727,7 @@ def plain_run(args, name, rank, world, torch, ox, _abi, peak):
                         bussi_tau=wl.get("bussi_tau", 1000.0), diff_coeff=wl.get("diff_coeff", 2.5), seed=1 + rank,
                         precision="mixed", steps_per_graph=25, list_rebuild_node=args.list_node,
                         sort_every=sort_every, autotune=not args.no_autotune and args.force_shape is None,
-                        use_edge=args.use_edge)
+                        use_edge=args.use_edge, list_kernel=args.list_kernel)
     sysm = ox.MDSystem(s.box, s.top, ox.dna2_settings(s.T, 0.5), md)
     sysm.set_state(s.pos, quat, s.vel, s.L)
     if args.force_shape is not None:
@@ -782,18 +782,19 @@ def plain_run(args, name, rank, world, torch, ox, _abi, peak):
         host = dict(pos=np.ascontiguousarray(st["pos"]), quat=np.ascontiguousarray(st["quat"]),
                     vel=np.ascontiguousarray(st["vel"]), L=np.ascontiguousarray(st["Lmom"]))
         ne = max(1, min(args.steps, 5))
+        got = sysm.get_state()  # the host arrays the loop reads the state back into
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(ne):
             sysm.set_state(host["pos"], host["quat"], host["vel"], host["L"])
             sysm.run(M, sync=True)
-            got = sysm.get_state()
+            got = sysm.get_state(out=got)
         t_e2e = time.perf_counter() - t0
         h2d = s.N * (3 + 4 + 3 + 3) * 8
         out["e2e"] = {"value": world * s.N * M * ne / t_e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": h2d, "md_steps_per_step": M,
                       "what": "per step: oxgb_md_set_state from host arrays (upload, list build, forces), M MD "
-                              "steps, oxgb_md_get_state to host arrays; wall clock"}
+                              "steps, oxgb_md_get_state into the same host arrays every step; wall clock"}
         assert np.all(np.isfinite(got["pos"]))
     # our kernels in the timed region: per MD step the first step, the bonded + pair kernel and
     # the non-bonded kernel, the Bussi draws and sums (the last block of a system makes its
@@ -859,6 +860,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="default force-kernel shape instead of the autotuned one")
     ap.add_argument("--force-shape", type=int, default=None,
                     help="pin force-kernel shape k of the autotuner's table instead of tuning (profiling)")
+    ap.add_argument("--list-kernel", default="auto", choices=["auto", "warp", "thread"],
+                    help="neighbour-row kernel of the list build (auto: the autotuner's choice)")
     ap.add_argument("--use-edge", action="store_true",
                     help="use_edge: Debye-Hueckel and excluded volume once per pair with atomic adds (A/B variant)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-system batched workload")

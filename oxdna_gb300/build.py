@@ -69,7 +69,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(srcs)) as pool:
         objs = list(pool.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    r = subprocess.run([exe, *ARCH, "-shared", "-o", tmp, *objs], capture_output=True, text=True)
+    r = subprocess.run([exe, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)

@@ -28,6 +28,18 @@ __device__ __forceinline__ float sqr_min_image(float4 a, float4 b, float L) {
 	return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
+// The same separation with the image picked by a product with 1 / L rounded by the 1.5 * 2^23
+// addition instead of the IEEE quotient: the two images differ only where d / L sits within an
+// ulp of a half-integer, i.e. |d| ~ L / 2, where both images leave a separation of ~L / 2 > the
+// Verlet radius (L > 2 r_verlet).  So every pair that is listed, and its d^2, are exactly those of
+// sqr_min_image (listed pairs have |d| < r_verlet, image 0 either way).
+__device__ __forceinline__ float sqr_min_image_inv(float4 a, float4 b, float L, float inv) {
+	float d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
+#pragma unroll
+	for(int k = 0; k < 3; k++) d[k] = __fmaf_rn(-__fsub_rn(__fmaf_rn(d[k], inv, 12582912.f), 12582912.f), L, d[k]);
+	return __fmaf_rn(d[2], d[2], __fmaf_rn(d[1], d[1], __fmul_rn(d[0], d[0])));
+}
+
 #define SKIP_IF_FRESH(a) \
 	if((a).check_flag && *(a).flag == 0) return
 
@@ -451,15 +463,20 @@ __global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
 		bki = a.fback[i];
 	}
 	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
+	const float inv_box = __frcp_rn(g.box);
+	// the 27 cells in the serial order (dz, dy, dx from -1 to 1), wrapped without integer division
 	for(int l = 0; l < 27; l++) {
-		const int z = (cz + l / 9 - 1 + n) % n, y = (cy + (l / 3) % 3 - 1 + n) % n, x = (cx + l % 3 - 1 + n) % n;
+		int z = cz + l / 9 - 1, y = cy + (l / 3) % 3 - 1, x = cx + l % 3 - 1;
+		z += z < 0 ? n : (z >= n ? -n : 0);
+		y += y < 0 ? n : (y >= n ? -n : 0);
+		x += x < 0 ? n : (x >= n ? -n : 0);
 		const int cc = g.cell0 + (z * n + y) * n + x;
 		const int s1 = a.cell_start[cc + 1];
 		for(int u = a.cell_start[cc]; u < s1; u++) {
 			const int j = a.cell_list[u];
 			if(j == i || j == b.x || j == b.y) continue;
 			const float4 rj = a.pos[j];
-			const float d2 = sqr_min_image(r, rj, g.box);
+			const float d2 = sqr_min_image_inv(r, rj, g.box, inv_box);
 			if(!(d2 < g.rv2)) continue;
 			if(cnt < a.max_nb) put(a.nb, a.col_major != 0, N, a.max_nb, i, cnt, j);
 			cnt++;

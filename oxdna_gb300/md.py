@@ -136,11 +136,19 @@ class MDSystem:
         c = lambda a: np.ascontiguousarray(a, np.float64).reshape(-1)
         _abi.check(_abi.lib().oxgb_md_set_state(self._h, c(pos), c(quat), c(vel), c(Lmom)))
 
-    def get_state(self):
+    def get_state(self, out=None):
+        """the FP64 state in the caller's order; `out` (a dict from an earlier call) is filled in
+        place instead of allocating new arrays"""
         N = self.N
-        pos, quat, vel, Lm = np.zeros((N, 3)), np.zeros((N, 4)), np.zeros((N, 3)), np.zeros((N, 3))
-        _abi.check(_abi.lib().oxgb_md_get_state(self._h, _abi.ptr(pos), _abi.ptr(quat), _abi.ptr(vel), _abi.ptr(Lm)))
-        return dict(pos=pos, quat=quat, vel=vel, Lmom=Lm)
+        if out is None:
+            out = dict(pos=np.zeros((N, 3)), quat=np.zeros((N, 4)), vel=np.zeros((N, 3)), Lmom=np.zeros((N, 3)))
+        for key, w in (("pos", 3), ("quat", 4), ("vel", 3), ("Lmom", 3)):
+            a = out[key]
+            if a.dtype != np.float64 or a.shape != (N, w) or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"out[{key!r}] must be a C-contiguous float64 array of shape ({N}, {w})")
+        _abi.check(_abi.lib().oxgb_md_get_state(self._h, _abi.ptr(out["pos"]), _abi.ptr(out["quat"]),
+                                                _abi.ptr(out["vel"]), _abi.ptr(out["Lmom"])))
+        return out
 
     def run(self, nsteps: int, sync: bool = True):
         _abi.check(_abi.lib().oxgb_md_run(self._h, int(nsteps), 1 if sync else 0))
