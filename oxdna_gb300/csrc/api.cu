@@ -293,6 +293,11 @@ extern "C" int oxgb_verlet_create(int N, double box, double rcut, double skin, i
 	h->skin = skin;
 	h->auto_opt = cells_auto_optimisation != 0;
 	h->rverlet = (float) rcut + 2.f * (float) skin;
+	// the minimum image of a listed pair is unique only below half the box
+	if(!(box > 2.0 * h->rverlet)) {
+		delete h;
+		return fail(OXGB_E_INVALID, "box side must exceed twice the Verlet radius (rcut + 2 skin)");
+	}
 	int cap = max_neigh > 0 ? max_neigh : std::min(N, 256);
 	int n_side = cells_per_side(N, (float) box, h->rverlet, h->auto_opt);
 	int rc = h->lb.alloc(N, n_side, cap);
@@ -612,6 +617,8 @@ static int derive_system(oxgb_md *h, int k, DNA2Table<double> &t64) {
 	if(build_table(h->dna[k], h->box[k], t64, rc)) return fail(OXGB_E_INVALID, "invalid interaction settings of system " + std::to_string(k));
 	h->rcut[k] = rc;
 	h->rverlet[k] = (float) rc + 2.f * (float) h->md.verlet_skin;
+	// the minimum image of a listed pair is unique only below half the box
+	if(!(h->box[k] > 2.0 * h->rverlet[k])) return fail(OXGB_E_INVALID, "system " + std::to_string(k) + ": box side must exceed twice the Verlet radius (rcut + 2 skin)");
 	// Brownian probabilities (src/Backends/Thermostats/BrownianThermostat.cpp:43-54); dt and
 	// diff_coeff are read as floats there
 	const double T = h->dna[k].T;

@@ -20,19 +20,13 @@ __device__ __forceinline__ int cell_coord(float x, float L, int n) {
 	return (int) (((s - floorf(s)) * (1.f - FLT_EPSILON)) * (float) n);
 }
 
-__device__ __forceinline__ float sqr_min_image(float4 a, float4 b, float L) {
-	float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
-	dx = __fmaf_rn(-rintf(__fdiv_rn(dx, L)), L, dx);
-	dy = __fmaf_rn(-rintf(__fdiv_rn(dy, L)), L, dy);
-	dz = __fmaf_rn(-rintf(__fdiv_rn(dz, L)), L, dz);
-	return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-}
-
-// The same separation with the image picked by a product with 1 / L rounded by the 1.5 * 2^23
-// addition instead of the IEEE quotient: the two images differ only where d / L sits within an
-// ulp of a half-integer, i.e. |d| ~ L / 2, where both images leave a separation of ~L / 2 > the
-// Verlet radius (L > 2 r_verlet).  So every pair that is listed, and its d^2, are exactly those of
-// sqr_min_image (listed pairs have |d| < r_verlet, image 0 either way).
+// Squared minimum-image separation in the reference's FP32 geometry (CUDABox.h:42-60: d - rint(d /
+// L) L per axis, then the sum of squares as fused multiply-adds), with the image picked by a
+// product with 1 / L rounded by the 1.5 * 2^23 addition instead of the IEEE quotient: the two
+// images differ only where d / L sits within an ulp of a half-integer, i.e. |d| ~ L / 2, where both
+// images leave a separation of ~L / 2 > the Verlet radius (L > 2 r_verlet).  So every pair that is
+// listed, and its d^2, are exactly those of the quotient form (listed pairs have |d| < r_verlet,
+// image 0 either way).
 __device__ __forceinline__ float sqr_min_image_inv(float4 a, float4 b, float L, float inv) {
 	float d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
 #pragma unroll
@@ -335,6 +329,7 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	const int cx = c % n, cy = (c / n) % n, cz = c / (n * n);
 	const bool terms = a.ev_nb != nullptr;
 	const long long N = a.N;
+	const float inv_box = __frcp_rn(g.box);
 	// lane l < 27 owns the l-th cell of the scan
 	int cs = 0, cn = 0;
 	if(lane < 27) {
@@ -374,7 +369,7 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 			j = a.cell_list[cs_l + (t - ex_l)];
 			if(j != i && j != b.x && j != b.y) {
 				const float4 rj = a.pos[j];
-				const float d2 = sqr_min_image(r, rj, g.box);
+				const float d2 = sqr_min_image_inv(r, rj, g.box, inv_box);
 				hit = d2 < g.rv2;
 				if(terms && hit && d2 < a.ev_r2) {
 					hev = true;
