@@ -714,36 +714,44 @@ OXGB_HD void pair_stack(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q,
 	if(g.cxst) cxst_term<R, SPLIT>(P, p, q, g, o);
 }
 
-// Debye-Hueckel between backbone sites, halved charges at strand ends (DNA2Interaction.cpp:157-212).
-// Reads only p.back, q.back and the strand-end flags.
+// Debye-Hueckel between backbone sites rback = back site of q - back site of p, halved charges at
+// strand ends (DNA2Interaction.cpp:157-212): the force on p and the energy; false outside the
+// cutoff
+template <typename R>
+OXGB_HD bool dh_sites(const DNA2Table<R> &P, const v3<R> &rback, bool p_end, bool q_end, v3<R> &f, R &e) {
+	const R rb2 = dot(rback, rback);
+	if(!(rb2 < P.dh_rc * P.dh_rc)) return false;
+	const R rmod = m_sqrt(rb2);
+	if(!(rmod < P.dh_rc)) return false;
+	R cut = R(1);
+	if(P.dh_half_charged_ends && p_end) cut *= R(0.5);
+	if(P.dh_half_charged_ends && q_end) cut *= R(0.5);
+	const v3<R> rd = rback * (R(1) / rmod);
+	R en, fm;
+	if(rmod < P.dh_rhigh) {
+		const R ex = m_exp(P.dh_minus_kappa * rmod);
+		en = ex * (P.dh_prefactor / rmod);
+		fm = -(P.dh_prefactor * ex) * (P.dh_minus_kappa / rmod - R(1) / (rmod * rmod));
+	}
+	else {
+		en = P.dh_b * (rmod - P.dh_rc) * (rmod - P.dh_rc);
+		fm = -(R(2) * P.dh_b * (rmod - P.dh_rc));
+	}
+	f = rd * (-(fm * cut));
+	e = en * cut;
+	return true;
+}
+
+// Debye-Hueckel of a pair from its centre separation r.  Reads only p.back, q.back and the
+// strand-end flags.
 template <typename R, bool SPLIT>
 OXGB_HD void pair_dh(const DNA2Table<R> &P, const Nuc<R> &p, const Nuc<R> &q, const v3<R> r, PairOut<R> &o) {
-	{
-		const v3<R> rback = r + q.back - p.back;
-		const R rb2 = dot(rback, rback);
-		if(rb2 < P.dh_rc * P.dh_rc) {
-			const R rmod = m_sqrt(rb2);
-			if(rmod < P.dh_rc) {
-				R cut = R(1);
-				if(P.dh_half_charged_ends && p.is_end) cut *= R(0.5);
-				if(P.dh_half_charged_ends && q.is_end) cut *= R(0.5);
-				const v3<R> rd = rback * (R(1) / rmod);
-				R e, fm;
-				if(rmod < P.dh_rhigh) {
-					const R ex = m_exp(P.dh_minus_kappa * rmod);
-					e = ex * (P.dh_prefactor / rmod);
-					fm = -(P.dh_prefactor * ex) * (P.dh_minus_kappa / rmod - R(1) / (rmod * rmod));
-				}
-				else {
-					e = P.dh_b * (rmod - P.dh_rc) * (rmod - P.dh_rc);
-					fm = -(R(2) * P.dh_b * (rmod - P.dh_rc));
-				}
-				const v3<R> force = rd * (fm * cut);
-				add_e<R, SPLIT>(o, T_DH, e * cut);
-				o.F -= force;
-				o.T -= cross(p.back, force);
-			}
-		}
+	v3<R> f;
+	R e;
+	if(dh_sites(P, r + q.back - p.back, p.is_end, q.is_end, f, e)) {
+		add_e<R, SPLIT>(o, T_DH, e);
+		o.F += f;
+		o.T += cross(p.back, f);
 	}
 }
 

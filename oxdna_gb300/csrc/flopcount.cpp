@@ -102,6 +102,7 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 			BondOut<CF> b;
 			bonded_both(P, p, q, sp, b);
 		}
+		g_flops += 9;  // the nucleotide's Debye-Hueckel torque from its summed force
 		const int nn = nnb[i] < max_nb ? nnb[i] : max_nb;
 		for(int k = 0; k < nn; k++) {
 			const int j = nb[(long long) i * max_nb + k];
@@ -119,7 +120,11 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 			sp.lo = v3<CF>{CF(0.f), CF(0.f), CF(0.f)};
 			const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
 			PairOut<CF> o{};
-			pair_dh<CF, false>(P, p, q, sp.plain(), o);
+			// Debye-Hueckel: the force of the pair; each nucleotide's torque is one cross product
+			// of its backbone offset with its summed force (below)
+			v3<CF> fdh;
+			CF edh;
+			dh_sites(P, sp.plain() + q.back - p.back, p.is_end, q.is_end, fdh, edh);
 			if(r2 < tr.ev2) {
 				pair_ev<CF, false>(p, q, sp, o);
 				double bb = 0, ss = 0;
@@ -131,7 +136,7 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 				if(bb < tr.base2) pair_base<CF, false>(P, p, q, sp, o);
 				if(ss < tr.stk2) pair_stack<CF, false>(P, p, q, sp, o);
 			}
-			g_flops += 12;  // the partner's torque
+			if(r2 < tr.ev2) g_flops += 12;  // the partner's torque (rigid-rotation balance)
 			pairs += 1;
 			if(r2 < rcut * rcut) in_range += 1;
 		}

@@ -115,3 +115,30 @@ def test_mixed_precision_across_periodic_images():
         assert np.abs(Esm - Esd).max() <= 1e-5 * max(1.0, np.abs(Esd).max())
     # the same contacts, so the shifted errors stay at the level of the local ones
     assert errs[True][0] <= 4 * errs[False][0] + 1e-6
+
+
+@pytest.mark.parametrize("box", [7.5, 9.5])
+def test_mixed_precision_small_boxes(box):
+    """A 12-bp duplex in cubes of side 7.5 and 9.5, just above the list's limit of 2 r_verlet
+    (6.73 at salt 0.5, skin 0.05): three cells per side, the 27 cells of a scan are the whole
+    grid, and Debye-Hueckel acts across the faces; the mixed path against the FP64 path."""
+    from oxdna_gb300 import MDSystem, dna2_settings, md_settings
+    from oxdna_gb300 import generate as G
+    from oxdna_gb300 import io as oxio
+    s = G.system_for_config(0, seed=3)
+    a1, a2, a3 = s.frames()
+    quat = oxio.frame_to_quat(a1, a2, a3)
+    out = []
+    for precision in ("mixed", "double"):
+        m = MDSystem(box, s.top, dna2_settings(s.T, 0.5), md_settings(precision=precision))
+        m.set_state(s.pos, quat, s.vel, s.L)
+        out.append(m.compute_forces())
+        m.close()
+    (Fm, Tm, _, Esm), (Fd, Td, _, Esd) = out
+    fmax, fnorm = force_errors(Fm, Fd)
+    tmax, tnorm = force_errors(Tm, Td)
+    print(f"box {box}: force max-rel {fmax:.2e} norm {fnorm:.2e}; torque max-rel {tmax:.2e} norm {tnorm:.2e}; "
+          f"E_DH {Esd[:, 7].sum() if Esd.ndim == 2 else Esd[7]:.4g}")
+    assert fnorm <= 1e-5 and tnorm <= 1e-5
+    assert fmax <= 5e-5 and tmax <= 5e-5
+    assert np.abs(Esm - Esd).max() <= 1e-5 * max(1.0, np.abs(Esd).max())
