@@ -1051,8 +1051,13 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 }
 
 // rebuilds every system's lists now
-static int build_list_now(oxgb_md *h) {
-	CK(cudaMemsetAsync(h->d_sys_stale, 1, sizeof(int) * h->n_systems, h->stream));  // nonzero: rebuild
+// a list build of every system, or (only >= 0) of system `only` alone
+static int build_list_now(oxgb_md *h, int only = -1) {
+	if(only < 0) CK(cudaMemsetAsync(h->d_sys_stale, 1, sizeof(int) * h->n_systems, h->stream));  // nonzero: rebuild
+	else {
+		CK(cudaMemsetAsync(h->d_sys_stale, 0, sizeof(int) * h->n_systems, h->stream));
+		CK(cudaMemsetAsync(h->d_sys_stale + only, 1, sizeof(int), h->stream));
+	}
 	ListArgs a = md_list_args(h, 0);
 	CK(launch_list_build(a, h->stream));
 	return OXGB_OK;
@@ -1135,19 +1140,31 @@ static int autotune_shape(oxgb_md *h) {
 		}
 	}
 	// the neighbour-row kernel: both build the same rows from the current positions (a rebuild
-	// is idempotent); not timed when sorting, where extra builds would move the sort schedule
+	// is idempotent); not timed when sorting, where extra builds would move the sort schedule.
+	// A single system rebuilds whole, so that is what is timed; a batch rebuilds a few of its
+	// systems at a time (each its own staleness), nearly every step, so a rebuild of its largest
+	// system alone is timed: there a nucleotide's serial walk over its 27 cells (the thread
+	// kernel) is latency that no other work hides (measured on the 256-system batch: the warp
+	// kernel 291 us per MD step, the thread kernel 374 us, although the thread kernel rebuilds
+	// the whole batch faster)
 	int list_thread = -1;
 	if(h->md.list_kernel == OXGB_LIST_AUTO && !h->sorting()) {
+		int only = -1;
+		if(h->n_systems > 1) {
+			only = 0;
+			for(int k = 1; k < h->n_systems; k++)
+				if(h->offsets[k + 1] - h->offsets[k] > h->offsets[only + 1] - h->offsets[only]) only = k;
+		}
 		double best_list = 1e30;
 		for(int v = 0; v < 2; v++) {
 			h->list_thread = v;
-			int rc = build_list_now(h);
+			int rc = build_list_now(h, only);
 			if(rc) return rc;
 			std::vector<double> t;
 			for(int rep = 0; rep < 3; rep++) {
 				CK(cudaEventRecord(e0, h->stream));
 				for(int r = 0; r < 3; r++) {
-					rc = build_list_now(h);
+					rc = build_list_now(h, only);
 					if(rc) return rc;
 				}
 				CK(cudaEventRecord(e1, h->stream));
