@@ -231,7 +231,7 @@ def batched_reference_cpu(systems, steps):
                       f"(sum of seconds per step / {n}) ({r['wall_s']:.0f} s wall)"}
 
 
-def bench_batched(args, torch, ox, _abi):
+def bench_batched(args, torch, ox, _abi, compare=True):
     """256 independent systems (16-4000 nt, duplexes and hairpins, each in its own cube at
     0.005 nt/unit^3, temperatures on a geometric 280-360 K ladder, 0.5 M, dt 0.003, Bussi tau
     1000) in one engine, with parallel-tempering swaps every 1000 steps on FP64 energies, against
@@ -241,7 +241,7 @@ def bench_batched(args, torch, ox, _abi):
     systems = batched_workload(args.seed)
     n_tot = sum(s.N for s in systems)
     md = dict(dt=0.003, thermostat="bussi", newtonian_steps=1, bussi_tau=1000.0, seed=7, precision="mixed",
-              steps_per_graph=25, autotune=not args.no_autotune)
+              steps_per_graph=25, autotune=not args.no_autotune, list_rebuild_node=args.list_node)
 
     def state(s):
         a1, a2, a3 = s.frames()
@@ -272,6 +272,9 @@ def bench_batched(args, torch, ox, _abi):
     _abi.check(_abi.lib().oxgb_md_status(b.handle))
     b.close()
     v_batch = n_tot * M * args.steps / t_batch
+    if not compare:
+        return {"value": v_batch, "unit": "particle-steps/s", "n_systems": len(systems), "n_nucleotides": n_tot,
+                "md_steps": M * args.steps, "force_shape": shape}
 
     # the same systems through the plain path, one engine each, one after the other
     t_plain = 0.0
@@ -865,6 +868,8 @@ def main():
     ap.add_argument("--use-edge", action="store_true",
                     help="use_edge: Debye-Hueckel and excluded volume once per pair with atomic adds (A/B variant)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-system batched workload")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="only the batched engine (no plain workloads, no one-at-a-time comparison): profiling")
     ap.add_argument("--list-node", default="conditional", choices=["conditional", "kernel"],
                     help="list rebuild as a conditional graph node, or as always-launched kernels that "
                          "return at once on a fresh list (what a kernel-level profiler can see)")
@@ -915,6 +920,9 @@ def main():
     peak = C.c_double(0)
     _abi.check(L.oxgb_probe_fp32_peak(C.byref(peak)))
 
+    if args.batched_only:
+        print(json.dumps(bench_batched(args, torch, ox, _abi, compare=False)))
+        return
     head = plain_run(args, args.workload, rank, world, torch, ox, _abi, peak.value)
     s = head.pop("_system")
     subs = {}
