@@ -213,14 +213,17 @@ typedef struct oxgb_md_settings {
 	                               reference's key, CUDA_sort.cu:106-200): the cells of each system
 	                               along a 3D Hilbert curve, nucleotides by caller's index within a
 	                               cell; OXGB_SORT_CELLS: row-major cell order */
-	int list_kernel;            /* OXGB_LIST_AUTO (default), _WARP or _THREAD (below) */
+	int list_kernel;            /* OXGB_LIST_AUTO (default), _WARP, _THREAD or _GROUP4/8/16 (below) */
 } oxgb_md_settings;
 enum { OXGB_SORT_HILBERT = 0, OXGB_SORT_CELLS = 1 };
-/* oxgb_md_settings.list_kernel: the neighbour-row kernel of the list build.  Both give the same
- * rows entry for entry; which is faster depends on how many candidates a nucleotide's 27 cells hold.
- * AUTO: timed by the autotuner (md.autotune), else WARP; WARP: a warp per nucleotide, lanes over
- * the candidates; THREAD: a thread per nucleotide, coalesced stores into the column-major rows */
-enum { OXGB_LIST_AUTO = 0, OXGB_LIST_WARP = 1, OXGB_LIST_THREAD = 2 };
+/* oxgb_md_settings.list_kernel: the neighbour-row kernel of the list build.  All give the same
+ * rows entry for entry; which is faster depends on how many candidates a nucleotide's 27 cells hold
+ * and on how many nucleotides a build covers.  AUTO: timed by the autotuner (md.autotune), else
+ * WARP; WARP: a warp per nucleotide, lanes over the candidates; THREAD: a thread per nucleotide,
+ * coalesced stores into the column-major rows; GROUP4 / GROUP8 / GROUP16: 4, 8 or 16 lanes per
+ * nucleotide over its candidates */
+enum { OXGB_LIST_AUTO = 0, OXGB_LIST_WARP = 1, OXGB_LIST_THREAD = 2, OXGB_LIST_GROUP4 = 3, OXGB_LIST_GROUP8 = 4,
+	OXGB_LIST_GROUP16 = 5 };
 
 void oxgb_md_default_settings(oxgb_md_settings *s);
 
@@ -380,7 +383,7 @@ int oxgb_md_set_force_shape(oxgb_md *h, int k);
 /* the shape table itself: shape k's nucleotides per pair-block warp queue, non-bonded lanes per
  * nucleotide and register cap (OXGB_E_INVALID past the last shape) */
 int oxgb_force_shape_table(int k, int *pair_npw, int *nb_lanes, int *nb_min_blocks);
-/* the neighbour-row kernel the engine's list builds use: OXGB_LIST_WARP or OXGB_LIST_THREAD */
+/* the neighbour-row kernel the engine's list builds use: OXGB_LIST_WARP, _THREAD or _GROUP4/8/16 */
 int oxgb_md_list_kernel(oxgb_md *h, int *kernel);
 /* device pointers (for zero-copy callers): FP64 positions, velocities, angular momenta and
  * quaternions (double4 each), FP32 forces and torques (float4; double4 in double precision) */

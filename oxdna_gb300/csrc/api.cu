@@ -448,7 +448,7 @@ struct oxgb_md {
 	int2 *bonds0 = nullptr;
 	unsigned char *sort_scratch = nullptr;
 	int *d_cell_hil = nullptr, *d_hcount = nullptr, *d_hstart = nullptr, *d_hcursor = nullptr;  // Hilbert order
-	int list_thread = 0;  // neighbour-row kernel (OXGB_LIST_*: chosen at creation or by the autotuner)
+	int list_kind = OXGB_LIST_WARP;  // neighbour-row kernel (OXGB_LIST_*: chosen at creation or by the autotuner)
 	bool sorting() const { return md.sort_every > 0; }
 
 	void free_layout() {
@@ -788,11 +788,11 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 		delete h;
 		return fail(OXGB_E_INVALID, "sort_order must be OXGB_SORT_HILBERT or OXGB_SORT_CELLS");
 	}
-	if(h->md.list_kernel < OXGB_LIST_AUTO || h->md.list_kernel > OXGB_LIST_THREAD) {
+	if(h->md.list_kernel < OXGB_LIST_AUTO || h->md.list_kernel > OXGB_LIST_GROUP16) {
 		delete h;
-		return fail(OXGB_E_INVALID, "list_kernel must be OXGB_LIST_AUTO, _WARP or _THREAD");
+		return fail(OXGB_E_INVALID, "list_kernel must be OXGB_LIST_AUTO, _WARP, _THREAD or _GROUP4/8/16");
 	}
-	h->list_thread = h->md.list_kernel == OXGB_LIST_THREAD ? 1 : 0;
+	h->list_kind = h->md.list_kernel == OXGB_LIST_AUTO ? OXGB_LIST_WARP : h->md.list_kernel;
 	h->conditional_ok = h->md.list_rebuild_node == 0;
 	h->dbl = md->precision == OXGB_PRECISION_DOUBLE;
 	h->rcut.assign(n_systems, 0.0);
@@ -1030,7 +1030,7 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	a.term_max = h->term_max;
 	a.base_pos = h->tl.base_pos;
 	a.stk_pos = h->tl.stk_pos;
-	a.list_thread = h->list_thread;
+	a.list_kind = h->list_kind;
 	if(h->sorting()) {
 		a.sort_every = h->md.sort_every;
 		a.id = h->d_id;
@@ -1087,7 +1087,7 @@ static std::mutex g_tune_mutex;
 struct TuneResult {
 	int shape;
 	double shape_us;
-	int list_thread;  // -1: not timed (the engine keeps its own choice)
+	int list_kind;  // -1: not timed (the engine keeps its own choice)
 };
 static std::map<std::tuple<int, int, int>, TuneResult> g_tune_cache;
 
@@ -1109,7 +1109,7 @@ static int autotune_shape(oxgb_md *h) {
 		if(it != g_tune_cache.end()) {
 			h->shape = it->second.shape;
 			h->shape_us = it->second.shape_us;
-			if(it->second.list_thread >= 0 && h->md.list_kernel == OXGB_LIST_AUTO) h->list_thread = it->second.list_thread;
+			if(it->second.list_kind >= 0 && h->md.list_kernel == OXGB_LIST_AUTO) h->list_kind = it->second.list_kind;
 			h->tuned = true;
 			return OXGB_OK;
 		}
@@ -1147,7 +1147,7 @@ static int autotune_shape(oxgb_md *h) {
 	// kernel) is latency that no other work hides (measured on the 256-system batch: the warp
 	// kernel 291 us per MD step, the thread kernel 374 us, although the thread kernel rebuilds
 	// the whole batch faster)
-	int list_thread = -1;
+	int list_kind = -1;
 	if(h->md.list_kernel == OXGB_LIST_AUTO && !h->sorting()) {
 		int only = -1;
 		if(h->n_systems > 1) {
@@ -1156,8 +1156,8 @@ static int autotune_shape(oxgb_md *h) {
 				if(h->offsets[k + 1] - h->offsets[k] > h->offsets[only + 1] - h->offsets[only]) only = k;
 		}
 		double best_list = 1e30;
-		for(int v = 0; v < 2; v++) {
-			h->list_thread = v;
+		for(int v = OXGB_LIST_WARP; v <= OXGB_LIST_GROUP16; v++) {
+			h->list_kind = v;
 			int rc = build_list_now(h, only);
 			if(rc) return rc;
 			std::vector<double> t;
@@ -1176,10 +1176,10 @@ static int autotune_shape(oxgb_md *h) {
 			std::sort(t.begin(), t.end());
 			if(t[1] < best_list) {
 				best_list = t[1];
-				list_thread = v;
+				list_kind = v;
 			}
 		}
-		h->list_thread = list_thread;
+		h->list_kind = list_kind;
 	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
@@ -1188,7 +1188,7 @@ static int autotune_shape(oxgb_md *h) {
 	h->tuned = true;
 	{
 		std::lock_guard<std::mutex> lock(g_tune_mutex);
-		g_tune_cache[key] = TuneResult{best, best_us, list_thread};
+		g_tune_cache[key] = TuneResult{best, best_us, list_kind};
 	}
 	// the forces of the state, from the chosen shape (the same values: shapes differ in work
 	// distribution and summation order only)
@@ -1356,7 +1356,7 @@ extern "C" int oxgb_md_set_force_shape(oxgb_md *h, int k) {
 
 extern "C" int oxgb_md_list_kernel(oxgb_md *h, int *kernel) {
 	if(!h || !kernel) return fail(OXGB_E_INVALID, "null argument");
-	*kernel = h->list_thread ? OXGB_LIST_THREAD : OXGB_LIST_WARP;
+	*kernel = h->list_kind;
 	return OXGB_OK;
 }
 

@@ -221,7 +221,7 @@ struct ListArgs {
 	const int *cell_hil;
 	int *hcount, *hstart, *hcursor;
 	int hilbert_pass;
-	int list_thread;        // neighbour rows by k_neighbours_thread (1) or k_neighbours (0)
+	int list_kind;          // neighbour-row kernel: OXGB_LIST_WARP, _THREAD or _GROUP4/8/16
 };
 
 // bytes per nucleotide of the sort's staging buffer: 4 FP64 vectors, 7 FP32 vectors, bonds,

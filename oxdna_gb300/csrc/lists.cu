@@ -12,6 +12,7 @@
 #include "kernels.h"
 
 #include <cfloat>
+#include <climits>
 
 namespace oxgb {
 
@@ -515,6 +516,157 @@ __global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
 	}
 }
 
+// K lanes per nucleotide (K = 4, 8 or 16; 128 / K nucleotides per block): the rows of
+// k_neighbours, entry for entry, with shorter serial chains than the thread kernel and fewer idle
+// lanes than the warp kernel where a nucleotide has a few dozen candidates.  Lane s of a group
+// owns the C = ceil(27 / K) consecutive cells s C .. s C + C - 1 of the serial scan order and
+// counts them; a group scan gives every cell's first candidate number, kept with its segment
+// start in shared memory; then the group takes candidates t0 + s, t0 + K + s, ..., each lane
+// finding its candidate's cell by a binary search of those numbers, and the hits of every round
+// are compacted in order with a ballot over the group's lanes.  All lanes of a group see the same
+// candidate count, so a group never diverges; the groups of a warp may.
+template <int K>
+__global__ void __launch_bounds__(128) k_neighbours_group(ListArgs a) {
+	constexpr int C = (27 + K - 1) / K;
+	constexpr int G = 128 / K;
+	__shared__ int s_first[G][32], s_start[G][32];  // per group: cell l's first candidate, its segment start
+	SKIP_IF_FRESH(a);
+	const int lane = threadIdx.x & 31, sub = lane % K, grp = (int) threadIdx.x / K;
+	const unsigned gmask = (K == 32 ? 0xffffffffu : ((1u << K) - 1u)) << (lane - sub);
+	const int i = (int) (((long long) blockIdx.x * blockDim.x + threadIdx.x) / K);
+	if(i >= a.N) return;  // group-uniform
+	const int sy = sys_of(a, i);
+	if(!rebuilt(a, sy)) return;  // group-uniform
+	const CellGeo g = cell_geo(a, sy);
+	const float4 r = a.pos[i];
+	const int2 b = a.bonds[i];
+	const int n = g.n;
+	const int c = a.cell_of[i] - g.cell0;
+	const int cx = c % n, cy = (c / n) % n, cz = c / (n * n);
+	const bool terms = a.ev_nb != nullptr;
+	const long long N = a.N;
+	const float inv_box = __frcp_rn(g.box);
+	// this lane's cells: segment starts and counts, and their running total
+	int st[C], ct[C], run = 0;
+#pragma unroll
+	for(int q = 0; q < C; q++) {
+		const int l = sub * C + q;
+		st[q] = 0;
+		ct[q] = 0;
+		if(l < 27) {
+			int z = cz + l / 9 - 1, y = cy + (l / 3) % 3 - 1, x = cx + l % 3 - 1;
+			z += z < 0 ? n : (z >= n ? -n : 0);
+			y += y < 0 ? n : (y >= n ? -n : 0);
+			x += x < 0 ? n : (x >= n ? -n : 0);
+			const int cc = g.cell0 + (z * n + y) * n + x;
+			st[q] = a.cell_start[cc];
+			ct[q] = a.cell_start[cc + 1] - st[q];
+		}
+		run += ct[q];
+	}
+	// exclusive scan of the lanes' totals over the group
+	int incl = run;
+#pragma unroll
+	for(int off = 1; off < K; off <<= 1) {
+		const int u = __shfl_up_sync(gmask, incl, off, K);
+		if(sub >= off) incl += u;
+	}
+	const int total = __shfl_sync(gmask, incl, K - 1, K);
+	int first = incl - run;
+#pragma unroll
+	for(int q = 0; q < C; q++) {
+		const int l = sub * C + q;
+		if(l < 32) {
+			s_first[grp][l] = l < 27 ? first : INT_MAX;
+			s_start[grp][l] = st[q];
+		}
+		first += ct[q];
+	}
+	// the padding entries 27..31 (cells of no lane when K C < 32)
+	for(int l = K * C + sub; l < 32; l += K) s_first[grp][l] = INT_MAX;
+	__syncwarp(gmask);
+	float4 a1i = make_float4(0.f, 0.f, 0.f, 0.f), bki = a1i;
+	if(terms) {
+		a1i = a.fa1[i];
+		bki = a.fback[i];
+	}
+	const unsigned below = ((1u << lane) - 1u) & gmask;
+	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
+	for(int t0 = 0; t0 < total; t0 += K) {
+		const int t = t0 + sub;
+		bool hit = false, hev = false, hbase = false, hstk = false;
+		int j = -1;
+		if(t < total) {
+			// the cell holding candidate t: the last one whose first candidate is at most t
+			int l = 0;
+#pragma unroll
+			for(int step = 16; step > 0; step >>= 1)
+				if(s_first[grp][l + step] <= t) l += step;
+			j = a.cell_list[s_start[grp][l] + (t - s_first[grp][l])];
+			if(j != i && j != b.x && j != b.y) {
+				const float4 rj = a.pos[j];
+				const float d2 = sqr_min_image_inv(r, rj, g.box, inv_box);
+				hit = d2 < g.rv2;
+				if(terms && hit && d2 < a.ev_r2) {
+					hev = true;
+					const float3 d = min_image_vec(r, rj, g.box);
+					const float4 a1j = a.fa1[j];
+					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
+					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
+							bz = d.z + 0.4f * (a1j.z - a1i.z);
+					hbase = bx * bx + by * by + bz * bz < a.base_r2;
+					const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy2 = d.y + 0.34f * (a1j.y - a1i.y),
+							sz = d.z + 0.34f * (a1j.z - a1i.z);
+					hstk = sx * sx + sy2 * sy2 + sz * sz < a.stk_r2;
+				}
+			}
+		}
+		const unsigned m = __ballot_sync(gmask, hit) & gmask;
+		if(hit) {
+			const int k = cnt + __popc(m & below);
+			if(k < a.max_nb) put(a.nb, a.col_major != 0, N, a.max_nb, i, k, j);
+		}
+		cnt += __popc(m);
+		if(terms) {
+			const unsigned me = __ballot_sync(gmask, hev) & gmask, mb = __ballot_sync(gmask, hbase) & gmask,
+					ms = __ballot_sync(gmask, hstk) & gmask;
+			if(hev) {
+				const int k = nev + __popc(me & below);
+				if(k < a.ev_cap) a.ev_nb[(long long) k * N + i] = j;
+			}
+			if(hbase) {
+				const int k = nbase + __popc(mb & below);
+				if(k < a.base_cap) a.base_nb[(long long) k * N + i] = j;
+			}
+			if(hstk) {
+				const int k = nstk + __popc(ms & below);
+				if(k < a.stk_cap) a.stk_nb[(long long) k * N + i] = j;
+			}
+			nev += __popc(me);
+			nbase += __popc(mb);
+			nstk += __popc(ms);
+		}
+	}
+	if(sub != 0) return;
+	if(cnt > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
+	if(a.term_max && cnt > a.term_max[3]) atomicMax(a.term_max + 3, cnt);
+	a.nnb[i] = cnt;
+	a.list_pos[i] = r;
+	if(terms) {
+		if(nev > a.ev_cap || nbase > a.base_cap || nstk > a.stk_cap) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
+		if(a.term_max) {
+			if(nev > a.term_max[0]) atomicMax(a.term_max, nev);
+			if(nbase > a.term_max[1]) atomicMax(a.term_max + 1, nbase);
+			if(nstk > a.term_max[2]) atomicMax(a.term_max + 2, nstk);
+		}
+		a.ev_n[i] = nev;
+		a.base_n[i] = nbase;
+		a.stk_n[i] = nstk;
+		a.list_a1[i] = a1i;
+		a.list_back[i] = bki;
+	}
+}
+
 // For every base / stack list entry (k, i) with partner j above i by caller's index (i owns the
 // pair, as in an unsorted run): where i sits in
 // j's list (the lists are symmetric: the pair criteria are exactly symmetric in FP32).  One
@@ -591,10 +743,15 @@ cudaError_t launch_list_build(const ListArgs &a, cudaStream_t s) {
 		k_sort_gather<<<gp, tpb, 0, s>>>(a);
 		k_sort_scatter<<<gp, tpb, 0, s>>>(a);
 	}
-	if(a.list_thread) k_neighbours_thread<<<(a.N + 127) / 128, 128, 0, s>>>(a);
-	else {
+	switch(a.list_kind) {
+	case OXGB_LIST_THREAD: k_neighbours_thread<<<(a.N + 127) / 128, 128, 0, s>>>(a); break;
+	case OXGB_LIST_GROUP4: k_neighbours_group<4><<<(int) (((long long) a.N * 4 + 127) / 128), 128, 0, s>>>(a); break;
+	case OXGB_LIST_GROUP8: k_neighbours_group<8><<<(int) (((long long) a.N * 8 + 127) / 128), 128, 0, s>>>(a); break;
+	case OXGB_LIST_GROUP16: k_neighbours_group<16><<<(int) (((long long) a.N * 16 + 127) / 128), 128, 0, s>>>(a); break;
+	default: {
 		const long long warps = (long long) a.N * 32;
 		k_neighbours<<<(int) ((warps + tpb - 1) / tpb), tpb, 0, s>>>(a);
+	}
 	}
 	if(a.base_pos && a.stk_pos) k_term_pos<<<2 * gp, tpb, 0, s>>>(a, gp);
 	k_list_done<<<1, 256, 0, s>>>(a);

@@ -43,6 +43,10 @@ def dna2_settings(T: float, salt: float = 0.5, average: bool = True, seq: Option
     return s
 
 
+# the neighbour-row kernels of the list build (OXGB_LIST_*): identical rows, different speeds
+LIST_KERNELS = {"auto": 0, "warp": 1, "thread": 2, "group4": 3, "group8": 4, "group16": 5}
+
+
 def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = "no", newtonian_steps: int = 103,
                 pt: float = 0.0, diff_coeff: float = 2.5, bussi_tau: float = 1000.0, seed: int = 1,
                 precision: str = "mixed", cells_auto_optimisation: bool = True, max_neigh: int = 0,
@@ -68,7 +72,7 @@ def md_settings(dt: float = 0.003, verlet_skin: float = 0.05, thermostat: str = 
     m.autotune = 1 if autotune else 0
     m.use_edge = 1 if use_edge else 0
     m.sort_order = {"hilbert": 0, "cells": 1}[sort_order]
-    m.list_kernel = {"auto": 0, "warp": 1, "thread": 2}[list_kernel]
+    m.list_kernel = LIST_KERNELS[list_kernel]
     return m
 
 
@@ -344,7 +348,7 @@ class MDSystem:
         out["index"] = next((k for k, sh in enumerate(force_shapes()) if sh == (a.value, b.value, c.value)), None)
         lk = C.c_int()
         _abi.check(_abi.lib().oxgb_md_list_kernel(self._h, C.byref(lk)))
-        out["list_kernel"] = {1: "warp", 2: "thread"}[lk.value]
+        out["list_kernel"] = {v: k for k, v in LIST_KERNELS.items()}[lk.value]
         return out
 
     def set_force_shape(self, k: int):
