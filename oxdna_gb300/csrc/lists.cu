@@ -460,15 +460,24 @@ __global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
 	}
 	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
 	const float inv_box = __frcp_rn(g.box);
-	// the 27 cells in the serial order (dz, dy, dx from -1 to 1), wrapped without integer division
-	for(int l = 0; l < 27; l++) {
-		int z = cz + l / 9 - 1, y = cy + (l / 3) % 3 - 1, x = cx + l % 3 - 1;
+	// the 27 cells in the serial order (dz, dy, dx from -1 to 1), wrapped without integer division.
+	// The cells x = cx - 1, cx, cx + 1 of a (z, y) row are consecutive cells, so their segments
+	// are one run of cell_list: cells [x0, e0) of the row, and where the row wraps at the box face
+	// a second run [x1, e1) -- nine rows of at most two runs instead of 27 cells
+	int x0, e0, x1 = 0, e1 = 0;
+	if(cx > 0 && cx < n - 1) x0 = cx - 1, e0 = cx + 2;
+	else if(cx == 0) x0 = n - 1, e0 = n, e1 = 2;  // cells n - 1 | 0, 1
+	else x0 = n - 2, e0 = n, e1 = 1;              // cells n - 2, n - 1 | 0
+	for(int zy = 0; zy < 9; zy++)
+	for(int run = 0; run < 2; run++) {
+		const int xa = run ? x1 : x0, xb = run ? e1 : e0;
+		if(xa >= xb) continue;
+		int z = cz + zy / 3 - 1, y = cy + zy % 3 - 1;
 		z += z < 0 ? n : (z >= n ? -n : 0);
 		y += y < 0 ? n : (y >= n ? -n : 0);
-		x += x < 0 ? n : (x >= n ? -n : 0);
-		const int cc = g.cell0 + (z * n + y) * n + x;
-		const int s1 = a.cell_start[cc + 1];
-		for(int u = a.cell_start[cc]; u < s1; u++) {
+		const int row = g.cell0 + (z * n + y) * n;
+		const int s1 = a.cell_start[row + xb];
+		for(int u = a.cell_start[row + xa]; u < s1; u++) {
 			const int j = a.cell_list[u];
 			if(j == i || j == b.x || j == b.y) continue;
 			const float4 rj = a.pos[j];
