@@ -297,13 +297,14 @@ __global__ void k_sort_scatter(ListArgs a) {
 	a.cell_of[k] = si[N + k];
 }
 
-// minimum-image separation vector (the reference's fp32 geometry, explicit fused multiply-adds)
-__device__ __forceinline__ float3 min_image_vec(float4 a, float4 b, float L) {
-	float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
-	dx = __fmaf_rn(-rintf(__fdiv_rn(dx, L)), L, dx);
-	dy = __fmaf_rn(-rintf(__fdiv_rn(dy, L)), L, dy);
-	dz = __fmaf_rn(-rintf(__fdiv_rn(dz, L)), L, dz);
-	return make_float3(dx, dy, dz);
+// the minimum-image separation vector of a listed pair (the reference's FP32 geometry, explicit
+// fused multiply-adds), the image picked as in sqr_min_image_inv: the same integer as the IEEE
+// quotient's rint for any pair closer than the Verlet radius, so the same vector
+__device__ __forceinline__ float3 min_image_vec_inv(float4 a, float4 b, float L, float inv) {
+	float d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
+#pragma unroll
+	for(int k = 0; k < 3; k++) d[k] = __fmaf_rn(-__fsub_rn(__fmaf_rn(d[k], inv, 12582912.f), 12582912.f), L, d[k]);
+	return make_float3(d[0], d[1], d[2]);
 }
 
 __device__ __forceinline__ void put(int *rows, bool col_major, long long N, int stride, int i, int k, int j) {
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 				hit = d2 < g.rv2;
 				if(terms && hit && d2 < a.ev_r2) {
 					hev = true;
-					const float3 d = min_image_vec(r, rj, g.box);
+					const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
 					const float4 a1j = a.fa1[j];
 					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
 					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
@@ -488,7 +489,7 @@ __global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
 			if(terms && d2 < a.ev_r2) {
 				if(nev < a.ev_cap) a.ev_nb[(long long) nev * N + i] = j;
 				nev++;
-				const float3 d = min_image_vec(r, rj, g.box);
+				const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
 				const float4 a1j = a.fa1[j];
 				// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
 				const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
@@ -618,7 +619,7 @@ __global__ void __launch_bounds__(128) k_neighbours_group(ListArgs a) {
 				hit = d2 < g.rv2;
 				if(terms && hit && d2 < a.ev_r2) {
 					hev = true;
-					const float3 d = min_image_vec(r, rj, g.box);
+					const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
 					const float4 a1j = a.fa1[j];
 					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
 					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
