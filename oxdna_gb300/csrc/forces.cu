@@ -1103,10 +1103,36 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_sp
 		// mirrors and lists, complete before k_bonded_pairs started)
 		pdl_wait();
 		pdl_trigger();
+		// the base slots then the stack slots as one sequence, the next slot loaded before the
+		// current one is added
 		const int nb_ = live ? min(a.base_n[i], a.base_cap) : 0;
-		for(int k = sub; k < nb_; k += K) acc.add_slot(reinterpret_cast<const V4 *>(a.base_res), N, i, k);
 		const int ns = live ? min(a.stk_n[i], a.stk_cap) : 0;
-		for(int k = sub; k < ns; k += K) acc.add_slot(reinterpret_cast<const V4 *>(a.stk_res), N, i, k);
+		{
+			const int nt = nb_ + ns;
+			const V4 *rb = reinterpret_cast<const V4 *>(a.base_res), *rs = reinterpret_cast<const V4 *>(a.stk_res);
+			auto slot = [&](int k) { return k < nb_ ? rb + 2 * ((long long) k * N + i) : rs + 2 * ((long long) (k - nb_) * N + i); };
+			V4 f, t;
+			int k = sub;
+			if(k < nt) {
+				const V4 *q = slot(k);
+				f = q[0];
+				t = q[1];
+			}
+			for(; k < nt; k += K) {
+				const V4 cf = f, ct = t;
+				if(k + K < nt) {
+					const V4 *q = slot(k + K);
+					f = q[0];
+					t = q[1];
+				}
+				acc.F.add(v3<R>{cf.x, cf.y, cf.z});
+				acc.T.add(v3<R>{ct.x, ct.y, ct.z});
+				if(ENERGY) {
+					KahanV<R>::kadd(acc.E, acc.Ec, cf.w);
+					KahanV<R>::kadd(acc.Eh, acc.Ehc, ct.w);
+				}
+			}
+		}
 		if(SPLIT && live) {
 #pragma unroll
 			for(int k = 0; k < N_TERMS; k++)

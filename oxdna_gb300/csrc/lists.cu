@@ -335,7 +335,11 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	// lane l < 27 owns the l-th cell of the scan
 	int cs = 0, cn = 0;
 	if(lane < 27) {
-		const int z = (cz + lane / 9 - 1 + n) % n, y = (cy + (lane / 3) % 3 - 1 + n) % n, x = (cx + lane % 3 - 1 + n) % n;
+		// wrapped with compares (an integer modulo by the grid size costs a division)
+		int z = cz + lane / 9 - 1, y = cy + (lane / 3) % 3 - 1, x = cx + lane % 3 - 1;
+		z += z < 0 ? n : (z >= n ? -n : 0);
+		y += y < 0 ? n : (y >= n ? -n : 0);
+		x += x < 0 ? n : (x >= n ? -n : 0);
 		const int cc = g.cell0 + (z * n + y) * n + x;
 		cs = a.cell_start[cc];
 		cn = a.cell_start[cc + 1] - cs;
