@@ -1023,6 +1023,7 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	a.base_cap = h->tl.base_cap;
 	a.stk_cap = h->tl.stk_cap;
 	a.ev_r2 = h->radii.ev2;
+	for(int k = 0; k < 3; k++) a.evs_r2[k] = h->radii.evs2[k];
 	a.base_r2 = h->radii.base2;
 	a.stk_r2 = h->radii.stk2;
 	a.list_a1 = h->list_a1;

@@ -191,6 +191,9 @@ struct ListArgs {
 	int *base_pos, *stk_pos;
 	int ev_cap, base_cap, stk_cap;
 	float ev_r2, base_r2, stk_r2;
+	// the excluded-volume list keeps only pairs with a site pair within its cutoff plus twice the
+	// skin (squared: backbone-backbone, base-base, backbone-base)
+	float evs_r2[3];
 	float4 *list_a1, *list_back;   // body axis a1 and backbone offset at this build
 	int *term_max;          // [4] longest EV / base / stack list and full row of any build so far (may be null)
 	int col_major;          // full rows column-major ([k * N + i]) instead of row-major

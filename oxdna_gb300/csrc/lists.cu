@@ -307,6 +307,20 @@ __device__ __forceinline__ float3 min_image_vec_inv(float4 a, float4 b, float L,
 	return make_float3(d[0], d[1], d[2]);
 }
 
+// A pair's excluded volume can act before the next rebuild only if one of its four site pairs
+// (backbone-backbone, base-base, backbone-base both ways) is within that pair's cutoff plus twice
+// the skin: the staleness test rebuilds before any site moves farther than the skin.  d is the
+// centres' separation, a1 and bk the axes and backbone offsets (base site at 0.4 a1).
+__device__ __forceinline__ bool ev_sites_near(const ListArgs &a, float3 d, float4 a1i, float4 bki, float4 a1j, float4 bkj) {
+	const float ix = 0.4f * a1i.x, iy = 0.4f * a1i.y, iz = 0.4f * a1i.z;
+	const float jx = 0.4f * a1j.x, jy = 0.4f * a1j.y, jz = 0.4f * a1j.z;
+	auto sq = [](float x, float y, float z) { return x * x + y * y + z * z; };
+	return sq(d.x + bkj.x - bki.x, d.y + bkj.y - bki.y, d.z + bkj.z - bki.z) < a.evs_r2[0] ||
+			sq(d.x + jx - ix, d.y + jy - iy, d.z + jz - iz) < a.evs_r2[1] ||
+			sq(d.x + jx - bki.x, d.y + jy - bki.y, d.z + jz - bki.z) < a.evs_r2[2] ||
+			sq(d.x + bkj.x - ix, d.y + bkj.y - iy, d.z + bkj.z - iz) < a.evs_r2[2];
+}
+
 __device__ __forceinline__ void put(int *rows, bool col_major, long long N, int stride, int i, int k, int j) {
 	if(col_major) rows[(long long) k * N + i] = j;
 	else rows[(long long) i * stride + k] = j;
@@ -378,9 +392,9 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 				const float d2 = sqr_min_image_inv(r, rj, g.box, inv_box);
 				hit = d2 < g.rv2;
 				if(terms && hit && d2 < a.ev_r2) {
-					hev = true;
 					const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
 					const float4 a1j = a.fa1[j];
+					hev = ev_sites_near(a, d, a1i, bki, a1j, a.fback[j]);
 					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
 					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
 							bz = d.z + 0.4f * (a1j.z - a1i.z);
@@ -491,10 +505,12 @@ __global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
 			if(cnt < a.max_nb) put(a.nb, a.col_major != 0, N, a.max_nb, i, cnt, j);
 			cnt++;
 			if(terms && d2 < a.ev_r2) {
-				if(nev < a.ev_cap) a.ev_nb[(long long) nev * N + i] = j;
-				nev++;
 				const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
 				const float4 a1j = a.fa1[j];
+				if(ev_sites_near(a, d, a1i, bki, a1j, a.fback[j])) {
+					if(nev < a.ev_cap) a.ev_nb[(long long) nev * N + i] = j;
+					nev++;
+				}
 				// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
 				const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
 						bz = d.z + 0.4f * (a1j.z - a1i.z);
@@ -622,9 +638,9 @@ __global__ void __launch_bounds__(128) k_neighbours_group(ListArgs a) {
 				const float d2 = sqr_min_image_inv(r, rj, g.box, inv_box);
 				hit = d2 < g.rv2;
 				if(terms && hit && d2 < a.ev_r2) {
-					hev = true;
 					const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
 					const float4 a1j = a.fa1[j];
+					hev = ev_sites_near(a, d, a1i, bki, a1j, a.fback[j]);
 					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
 					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
 							bz = d.z + 0.4f * (a1j.z - a1i.z);

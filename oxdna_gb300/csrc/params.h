@@ -180,9 +180,12 @@ inline void to_float(const DNA2Table<double> &d, double box, DNA2Table<float> &f
 // pair-distance bounds of the force kernel's term lists: a term can only act within these
 // distances (model constants), widened by twice the skin so that a list built now stays complete
 // until the next rebuild.  ev: centre-centre (excluded volume), base: base-base (hydrogen bonding,
-// cross stacking), stk: stack-stack (coaxial stacking).  Squared, FP32.
+// cross stacking), stk: stack-stack (coaxial stacking); evs: the excluded volume's four site
+// pairs, of which one must be within its bound for a pair to enter the excluded-volume list.
+// Squared, FP32.
 struct TermRadii {
 	float ev2, base2, stk2;
+	float evs2[3];  // site pairs of the excluded volume: backbone-backbone, base-base, backbone-base
 };
 
 inline TermRadii term_radii(double skin) {
@@ -197,6 +200,8 @@ inline TermRadii term_radii(double skin) {
 	t.ev2 = (float) ((ev + 2 * skin + margin) * (ev + 2 * skin + margin));
 	t.base2 = (float) ((hb + 2 * skin + margin) * (hb + 2 * skin + margin));
 	t.stk2 = (float) (((double) OXM_CXST_RCHIGH + 2 * skin + margin) * ((double) OXM_CXST_RCHIGH + 2 * skin + margin));
+	const double rc[3] = {OXM_EXCL_RC1, OXM_EXCL_RC2, std::fmax((double) OXM_EXCL_RC3, (double) OXM_EXCL_RC4)};
+	for(int k = 0; k < 3; k++) t.evs2[k] = (float) ((rc[k] + 2 * skin + margin) * (rc[k] + 2 * skin + margin));
 	return t;
 }
 
