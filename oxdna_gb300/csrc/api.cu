@@ -210,6 +210,10 @@ struct ListBuffers {
 	int *cell_of = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_cursor = nullptr, *cell_list = nullptr;
 	int *cell_tmp = nullptr, *scan_part = nullptr;
 	int *nb = nullptr, *nnb = nullptr;
+	// engine only (dh set before alloc): the Debye-Hueckel rows, the pairs of the full rows whose
+	// backbone sites are within the Debye-Hueckel cutoff plus twice the skin, same capacity
+	bool dh = false;
+	int *dh_nb = nullptr, *dh_n = nullptr;
 
 	// n_cells_: cells of all systems of a batch (0: one grid of n_side^3)
 	int alloc(int N_, int n_side_, int max_nb_, int n_cells_ = 0) {
@@ -227,10 +231,14 @@ struct ListBuffers {
 		CK(cudaMalloc(&scan_part, sizeof(int) * (scan_tiles(n_cells) + 1)));
 		CK(cudaMalloc(&nb, sizeof(int) * (size_t) std::max(N, 1) * max_nb));
 		CK(cudaMalloc(&nnb, sizeof(int) * std::max(N, 1)));
+		if(dh) {
+			CK(cudaMalloc(&dh_nb, sizeof(int) * (size_t) std::max(N, 1) * max_nb));
+			CK(cudaMalloc(&dh_n, sizeof(int) * std::max(N, 1)));
+		}
 		return OXGB_OK;
 	}
 	void free_all() {
-		for(int **p : {&cell_of, &cell_count, &cell_start, &cell_cursor, &cell_list, &cell_tmp, &scan_part, &nb, &nnb}) {
+		for(int **p : {&cell_of, &cell_count, &cell_start, &cell_cursor, &cell_list, &cell_tmp, &scan_part, &nb, &nnb, &dh_nb, &dh_n}) {
 			if(*p) cudaFree(*p);
 			*p = nullptr;
 		}
@@ -388,6 +396,7 @@ struct oxgb_md {
 	// per-system derived parameters (host copies of the device arrays below)
 	std::vector<double> rcut, par;        // interaction cutoff; SP_STRIDE thermostat values each
 	std::vector<float> rverlet;
+	std::vector<float> dh2;               // bound of the Debye-Hueckel rows: (dh_rc + 2 skin + 1e-3)^2 on backbone sites
 	std::vector<int> nside, cell0;        // cells per side, first cell (cell0[n_systems] = all cells)
 	std::vector<int> chunk_sys, chunk_first, sys_chunk0;  // Bussi / energy chunks of <= 256 nucleotides
 	int n_chunks = 0, tab_span = 1;
@@ -406,7 +415,7 @@ struct oxgb_md {
 	void *d_tab = nullptr;                // one table per system
 	int *d_sys = nullptr, *d_sys_off = nullptr, *d_sys_nside = nullptr, *d_sys_cell0 = nullptr, *d_cell_sys = nullptr;
 	int *d_sys_stale = nullptr, *d_chunk_sys = nullptr, *d_chunk_first = nullptr, *d_sys_chunk0 = nullptr;
-	float *d_sys_box = nullptr, *d_sys_rv2 = nullptr;
+	float *d_sys_box = nullptr, *d_sys_rv2 = nullptr, *d_sys_dh2 = nullptr;
 	double *d_sys_par = nullptr;
 	unsigned long long *d_sys_seed = nullptr;
 	ListBuffers lb;
@@ -453,7 +462,7 @@ struct oxgb_md {
 
 	void free_layout() {
 		for(void **p : {(void **) &d_sys_nside, (void **) &d_sys_cell0, (void **) &d_cell_sys, (void **) &d_sys_box,
-					(void **) &d_sys_rv2, (void **) &d_cell_hil, (void **) &d_hcount, (void **) &d_hstart, (void **) &d_hcursor}) {
+					(void **) &d_sys_rv2, (void **) &d_sys_dh2, (void **) &d_cell_hil, (void **) &d_hcount, (void **) &d_hstart, (void **) &d_hcursor}) {
 			if(*p) cudaFree(*p);
 			*p = nullptr;
 		}
@@ -564,6 +573,8 @@ static ForceArgs force_args(oxgb_md *h, int step_offset = 0, bool engine_step = 
 	a.bonds = h->bonds;
 	a.nb = h->lb.nb;
 	a.nnb = h->lb.nnb;
+	a.dh_nb = h->lb.dh_nb;
+	a.dh_n = h->lb.dh_n;
 	a.max_nb = h->lb.max_nb;
 	a.nb_stride_i = 1;  // the engine's rows are column-major
 	a.nb_stride_k = h->N;
@@ -617,6 +628,8 @@ static int derive_system(oxgb_md *h, int k, DNA2Table<double> &t64) {
 	if(build_table(h->dna[k], h->box[k], t64, rc)) return fail(OXGB_E_INVALID, "invalid interaction settings of system " + std::to_string(k));
 	h->rcut[k] = rc;
 	h->rverlet[k] = (float) rc + 2.f * (float) h->md.verlet_skin;
+	const double dhr = t64.dh_rc + 2.0 * h->md.verlet_skin + 1e-3;
+	h->dh2[k] = (float) (dhr * dhr);
 	// the minimum image of a listed pair is unique only below half the box
 	if(!(h->box[k] > 2.0 * h->rverlet[k])) return fail(OXGB_E_INVALID, "system " + std::to_string(k) + ": box side must exceed twice the Verlet radius (rcut + 2 skin)");
 	// Brownian probabilities (src/Backends/Thermostats/BrownianThermostat.cpp:43-54); dt and
@@ -727,11 +740,13 @@ static int layout_cells(oxgb_md *h) {
 	CK(cudaMalloc(&h->d_cell_sys, sizeof(int) * n_cells));
 	CK(cudaMalloc(&h->d_sys_box, sizeof(float) * S));
 	CK(cudaMalloc(&h->d_sys_rv2, sizeof(float) * S));
+	CK(cudaMalloc(&h->d_sys_dh2, sizeof(float) * S));
 	CK(cudaMemcpy(h->d_sys_nside, h->nside.data(), sizeof(int) * S, cudaMemcpyHostToDevice));
 	CK(cudaMemcpy(h->d_sys_cell0, h->cell0.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice));
 	CK(cudaMemcpy(h->d_cell_sys, cell_sys.data(), sizeof(int) * n_cells, cudaMemcpyHostToDevice));
 	CK(cudaMemcpy(h->d_sys_box, bx.data(), sizeof(float) * S, cudaMemcpyHostToDevice));
 	CK(cudaMemcpy(h->d_sys_rv2, rv2.data(), sizeof(float) * S, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(h->d_sys_dh2, h->dh2.data(), sizeof(float) * S, cudaMemcpyHostToDevice));
 	if(h->sorting() && h->md.sort_order == OXGB_SORT_HILBERT) {
 		std::vector<int> cell_hil(n_cells);
 		for(int k = 0; k < S; k++) hilbert_ranks(h->nside[k], h->cell0[k], cell_hil);
@@ -797,6 +812,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	h->dbl = md->precision == OXGB_PRECISION_DOUBLE;
 	h->rcut.assign(n_systems, 0.0);
 	h->rverlet.assign(n_systems, 0.f);
+	h->dh2.assign(n_systems, 0.f);
 	h->par.assign((size_t) n_systems * SP_STRIDE, 0.0);
 	const size_t v4 = h->dbl ? sizeof(double4_32a) : sizeof(float4);
 	const size_t tab = h->dbl ? sizeof(DNA2Table<double>) : sizeof(DNA2Table<float>);
@@ -920,6 +936,7 @@ extern "C" int oxgb_md_create(int n_systems, const int *offsets, const double *b
 	rc = layout_cells(h);
 	if(rc) return bail(rc);
 	const int cap = md->max_neigh > 0 ? md->max_neigh : std::min(std::max(N - 1, 1), 512);
+	h->lb.dh = true;
 	rc = h->lb.alloc(N, h->nside[0], cap, h->cell0[n_systems]);
 	if(rc) return bail(rc);
 	h->radii = term_radii(h->md.verlet_skin);
@@ -1008,6 +1025,10 @@ static ListArgs md_list_args(oxgb_md *h, int check_flag) {
 	a.cell_sys = h->d_cell_sys;
 	a.sys_box = h->d_sys_box;
 	a.sys_rv2 = h->d_sys_rv2;
+	a.dh_nb = h->lb.dh_nb;
+	a.dh_n = h->lb.dh_n;
+	a.dh_r2 = h->dh2[0];
+	a.sys_dh2 = h->n_systems > 1 ? h->d_sys_dh2 : nullptr;
 	a.sys_stale = h->d_sys_stale;
 	a.n_systems = h->n_systems;
 	a.n_cells_total = h->cell0[h->n_systems];
@@ -1667,6 +1688,7 @@ extern "C" int oxgb_md_set_temperature(oxgb_md *h, int k, double T) {
 	else {
 		const float rv2 = h->rverlet[k] * h->rverlet[k];
 		CK(cudaMemcpy(h->d_sys_rv2 + k, &rv2, sizeof(float), cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(h->d_sys_dh2 + k, &h->dh2[k], sizeof(float), cudaMemcpyHostToDevice));
 	}
 	// system k's lists are rebuilt now (a larger cutoff needs it); a new cell layout rebuilds
 	// every system

@@ -81,7 +81,14 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 	// the kernels repeat (Debye-Hueckel and excluded volume are evaluated from both ends of the
 	// full rows) is not counted, so it shows as lost efficiency.
 	const TermRadii tr = term_radii(skin);
+	const double dh_bound = P64.dh_rc + 2.0 * skin + 1e-3;
 	g_flops = g_sfu = 0;
+	// squared distance of sites a (of p) and b (of q) of a pair with centre separation d, in
+	// double and uncounted (the list build's test, not the pair's arithmetic)
+	auto site_sq = [](const double *d, const v3<CF> &a, const v3<CF> &b) {
+		const double x = d[0] + b.x.v - a.x.v, y = d[1] + b.y.v - a.y.v, z = d[2] + b.z.v - a.z.v;
+		return x * x + y * y + z * z;
+	};
 	double pairs = 0, in_range = 0;
 	auto load = [&](int j, Nuc<CF> &q) {
 		frame_of(a1, a3, j, q, P);
@@ -122,11 +129,18 @@ extern "C" int oxgb_count_flops(int N, const double *pos, const double *a1, cons
 			PairOut<CF> o{};
 			// Debye-Hueckel: the force of the pair; each nucleotide's torque is one cross product
 			// of its backbone offset with its summed force (below)
-			v3<CF> fdh;
-			CF edh;
-			dh_sites(P, sp.plain() + q.back - p.back, p.is_end, q.is_end, fdh, edh);
+			// each term over the pairs its list admits: Debye-Hueckel over the pairs whose backbone
+			// sites are within its cutoff plus twice the skin, the excluded volume over those with a
+			// site pair within that pair's cutoff plus twice the skin
+			if(site_sq(d, p.back, q.back) < dh_bound * dh_bound) {
+				v3<CF> fdh;
+				CF edh;
+				dh_sites(P, sp.plain() + q.back - p.back, p.is_end, q.is_end, fdh, edh);
+			}
 			if(r2 < tr.ev2) {
-				pair_ev<CF, false>(p, q, sp, o);
+				const bool ev_near = site_sq(d, p.back, q.back) < tr.evs2[0] || site_sq(d, p.base, q.base) < tr.evs2[1] ||
+						site_sq(d, p.back, q.base) < tr.evs2[2] || site_sq(d, p.base, q.back) < tr.evs2[2];
+				if(ev_near) pair_ev<CF, false>(p, q, sp, o);
 				double bb = 0, ss = 0;
 				for(int c = 0; c < 3; c++) {
 					const double da = a1[3 * j + c] - a1[3 * i + c];

@@ -1019,7 +1019,10 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_sp
 		// Debye-Hueckel over the full Verlet row (use_edge: the edge blocks did it).  The lever
 		// arm of every pair's torque on i is i's backbone offset, so the forces are summed
 		// (compensated) and the torque is taken once from the sum.
-		const int ndh = (live && !EDGE) ? min(a.nnb[i], a.max_nb) : 0;
+		// (the engine's Debye-Hueckel rows where built: the full rows' entries whose backbone sites
+		// are within the cutoff plus twice the skin)
+		const int *dhr = a.dh_nb ? a.dh_nb : a.nb;
+		const int ndh = (live && !EDGE) ? min(a.dh_nb ? a.dh_n[i] : a.nnb[i], a.max_nb) : 0;
 		{
 			KahanV<R> fdh{};
 			// the next partner's data is loaded before this partner's arithmetic, and the index
@@ -1028,14 +1031,14 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? MINB : 1) k_nonbonded_sp
 			Nuc<R> qn;
 			V4 qhn, qln;
 			int k = sub;
-			if(k < ndh) load_dh<Loader, R>(ld, a.nb[(long long) k * N + i], P, qn, qhn, qln);
-			int jnn = (k + K < ndh) ? a.nb[(long long) (k + K) * N + i] : 0;
+			if(k < ndh) load_dh<Loader, R>(ld, dhr[(long long) k * N + i], P, qn, qhn, qln);
+			int jnn = (k + K < ndh) ? dhr[(long long) (k + K) * N + i] : 0;
 			for(; k < ndh; k += K) {
 				const v3<R> qback = qn.back;
 				const bool qend = qn.is_end;
 				const V4 qh = qhn, ql = qln;
 				if(k + K < ndh) load_dh<Loader, R>(ld, jnn, P, qn, qhn, qln);
-				if(k + 2 * K < ndh) jnn = a.nb[(long long) (k + 2 * K) * N + i];
+				if(k + 2 * K < ndh) jnn = dhr[(long long) (k + 2 * K) * N + i];
 				v3<R> f;
 				R e;
 				if(dh_sites(P, ld.sep_soft(ph, pl, qh, ql, P).plain() + qback - p.back, p.is_end, qend, f, e)) {

@@ -94,6 +94,7 @@ struct ForceArgs {
 	const double4_32a *posd, *quatd;          // FP64 state
 	const int2 *bonds;                    // (n3, n5), -1 if none
 	const int *nb, *nnb;                  // neighbour rows and counts
+	const int *dh_nb, *dh_n;              // Debye-Hueckel rows (engine; null: the full rows)
 	int max_nb;
 	long long nb_stride_i, nb_stride_k;   // element (i, k) at nb[i * stride_i + k * stride_k]
 	void *forces, *torques;               // float4 or double4_32a per particle
@@ -194,6 +195,12 @@ struct ListArgs {
 	// the excluded-volume list keeps only pairs with a site pair within its cutoff plus twice the
 	// skin (squared: backbone-backbone, base-base, backbone-base)
 	float evs_r2[3];
+	// Debye-Hueckel rows (null: none): the entries of the full rows whose backbone sites are
+	// closer than sqrt(dh_r2) (the Debye-Hueckel cutoff plus twice the skin; per system in
+	// sys_dh2 for a batch), column-major with the full rows' capacity
+	int *dh_nb, *dh_n;
+	float dh_r2;
+	const float *sys_dh2;
 	float4 *list_a1, *list_back;   // body axis a1 and backbone offset at this build
 	int *term_max;          // [4] longest EV / base / stack list and full row of any build so far (may be null)
 	int col_major;          // full rows column-major ([k * N + i]) instead of row-major

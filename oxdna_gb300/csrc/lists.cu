@@ -43,17 +43,19 @@ __device__ __forceinline__ float sqr_min_image_inv(float4 a, float4 b, float L, 
 	if((a).hilbert_pass && !((a).sort_every > 0 && (a).id && ((a).rebuilds ? *(a).rebuilds : 0ull) % (unsigned long long) (a).sort_every == 0ull)) \
 		return
 
-// geometry of system s: box side, r_verlet^2, cells per side, first cell
+// geometry of system s: box side, r_verlet^2, cells per side, first cell, bound of the
+// Debye-Hueckel rows (squared, on backbone sites)
 struct CellGeo {
 	float box, rv2;
 	int n, cell0;
+	float dh2;
 };
 
 __device__ __forceinline__ int sys_of(const ListArgs &a, int i) { return a.sys ? a.sys[i] : 0; }
 
 __device__ __forceinline__ CellGeo cell_geo(const ListArgs &a, int s) {
-	if(!a.sys) return CellGeo{a.box, a.rverlet2, a.n_side, 0};
-	return CellGeo{a.sys_box[s], a.sys_rv2[s], a.sys_nside[s], a.sys_cell0[s]};
+	if(!a.sys) return CellGeo{a.box, a.rverlet2, a.n_side, 0, a.dh_r2};
+	return CellGeo{a.sys_box[s], a.sys_rv2[s], a.sys_nside[s], a.sys_cell0[s], a.sys_dh2 ? a.sys_dh2[s] : a.dh_r2};
 }
 
 // system s is rebuilt in this pass (always, unless per-system requests are given)
@@ -307,6 +309,13 @@ __device__ __forceinline__ float3 min_image_vec_inv(float4 a, float4 b, float L,
 	return make_float3(d[0], d[1], d[2]);
 }
 
+// squared distance of the backbone sites of a listed pair (d: the centres' separation, bk: the
+// backbone offsets)
+__device__ __forceinline__ float back_sq(float3 d, float4 bki, float4 bkj) {
+	const float x = d.x + bkj.x - bki.x, y = d.y + bkj.y - bki.y, z = d.z + bkj.z - bki.z;
+	return x * x + y * y + z * z;
+}
+
 // A pair's excluded volume can act before the next rebuild only if one of its four site pairs
 // (backbone-backbone, base-base, backbone-base both ways) is within that pair's cutoff plus twice
 // the skin: the staleness test rebuilds before any site moves farther than the skin.  d is the
@@ -366,13 +375,14 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	}
 	const int total = __shfl_sync(0xffffffffu, incl, 31);
 	const int excl = incl - cn;
+	const bool dhl = a.dh_nb != nullptr;
 	float4 a1i = make_float4(0.f, 0.f, 0.f, 0.f), bki = a1i;
-	if(terms) {
+	if(terms || dhl) {
 		a1i = a.fa1[i];
 		bki = a.fback[i];
 	}
 	const unsigned below = (1u << lane) - 1u;
-	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
+	int cnt = 0, nev = 0, nbase = 0, nstk = 0, ndh = 0;
 	for(int t0 = 0; t0 < total; t0 += 32) {
 		const int t = t0 + lane;
 		// the cell holding candidate t: the first lane whose inclusive count exceeds t
@@ -383,7 +393,7 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 			if(v <= t) l += step;
 		}
 		const int cs_l = __shfl_sync(0xffffffffu, cs, l & 31), ex_l = __shfl_sync(0xffffffffu, excl, l & 31);
-		bool hit = false, hev = false, hbase = false, hstk = false;
+		bool hit = false, hev = false, hbase = false, hstk = false, hdh = false;
 		int j = -1;
 		if(t < total) {
 			j = a.cell_list[cs_l + (t - ex_l)];
@@ -391,17 +401,21 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 				const float4 rj = a.pos[j];
 				const float d2 = sqr_min_image_inv(r, rj, g.box, inv_box);
 				hit = d2 < g.rv2;
-				if(terms && hit && d2 < a.ev_r2) {
+				if(hit && (terms || dhl)) {
 					const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
-					const float4 a1j = a.fa1[j];
-					hev = ev_sites_near(a, d, a1i, bki, a1j, a.fback[j]);
-					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
-					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
-							bz = d.z + 0.4f * (a1j.z - a1i.z);
-					hbase = bx * bx + by * by + bz * bz < a.base_r2;
-					const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy = d.y + 0.34f * (a1j.y - a1i.y),
-							sz = d.z + 0.34f * (a1j.z - a1i.z);
-					hstk = sx * sx + sy * sy + sz * sz < a.stk_r2;
+					const float4 bkj = a.fback[j];
+					hdh = dhl && back_sq(d, bki, bkj) < g.dh2;
+					if(terms && d2 < a.ev_r2) {
+						const float4 a1j = a.fa1[j];
+						hev = ev_sites_near(a, d, a1i, bki, a1j, bkj);
+						// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
+						const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
+								bz = d.z + 0.4f * (a1j.z - a1i.z);
+						hbase = bx * bx + by * by + bz * bz < a.base_r2;
+						const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy = d.y + 0.34f * (a1j.y - a1i.y),
+								sz = d.z + 0.34f * (a1j.z - a1i.z);
+						hstk = sx * sx + sy * sy + sz * sz < a.stk_r2;
+					}
 				}
 			}
 		}
@@ -411,6 +425,14 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 			if(k < a.max_nb) put(a.nb, a.col_major != 0, N, a.max_nb, i, k, j);
 		}
 		cnt += __popc(m);
+		if(dhl) {
+			const unsigned md = __ballot_sync(0xffffffffu, hdh);
+			if(hdh) {
+				const int k = ndh + __popc(md & below);
+				if(k < a.max_nb) a.dh_nb[(long long) k * N + i] = j;
+			}
+			ndh += __popc(md);
+		}
 		if(terms) {
 			const unsigned me = __ballot_sync(0xffffffffu, hev), mb = __ballot_sync(0xffffffffu, hbase),
 					ms = __ballot_sync(0xffffffffu, hstk);
@@ -435,6 +457,7 @@ __global__ void __launch_bounds__(256) k_neighbours(ListArgs a) {
 	if(cnt > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
 	if(a.term_max && cnt > a.term_max[3]) atomicMax(a.term_max + 3, cnt);
 	a.nnb[i] = cnt;
+	if(dhl) a.dh_n[i] = ndh;
 	a.list_pos[i] = r;
 	if(terms) {
 		if(nev > a.ev_cap || nbase > a.base_cap || nstk > a.stk_cap) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
@@ -472,12 +495,13 @@ __global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
 	const int cx = c % n, cy = (c / n) % n, cz = c / (n * n);
 	const bool terms = a.ev_nb != nullptr;
 	const long long N = a.N;
+	const bool dhl = a.dh_nb != nullptr;
 	float4 a1i = make_float4(0.f, 0.f, 0.f, 0.f), bki = a1i;
-	if(terms) {
+	if(terms || dhl) {
 		a1i = a.fa1[i];
 		bki = a.fback[i];
 	}
-	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
+	int cnt = 0, nev = 0, nbase = 0, nstk = 0, ndh = 0;
 	const float inv_box = __frcp_rn(g.box);
 	// the 27 cells in the serial order (dz, dy, dx from -1 to 1), wrapped without integer division.
 	// The cells x = cx - 1, cx, cx + 1 of a (z, y) row are consecutive cells, so their segments
@@ -504,10 +528,16 @@ __global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
 			if(!(d2 < g.rv2)) continue;
 			if(cnt < a.max_nb) put(a.nb, a.col_major != 0, N, a.max_nb, i, cnt, j);
 			cnt++;
+			if(!(terms || dhl)) continue;
+			const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
+			const float4 bkj = a.fback[j];
+			if(dhl && back_sq(d, bki, bkj) < g.dh2) {
+				if(ndh < a.max_nb) a.dh_nb[(long long) ndh * N + i] = j;
+				ndh++;
+			}
 			if(terms && d2 < a.ev_r2) {
-				const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
 				const float4 a1j = a.fa1[j];
-				if(ev_sites_near(a, d, a1i, bki, a1j, a.fback[j])) {
+				if(ev_sites_near(a, d, a1i, bki, a1j, bkj)) {
 					if(nev < a.ev_cap) a.ev_nb[(long long) nev * N + i] = j;
 					nev++;
 				}
@@ -530,6 +560,7 @@ __global__ void __launch_bounds__(128) k_neighbours_thread(ListArgs a) {
 	if(cnt > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
 	if(a.term_max && cnt > a.term_max[3]) atomicMax(a.term_max + 3, cnt);
 	a.nnb[i] = cnt;
+	if(dhl) a.dh_n[i] = ndh;
 	a.list_pos[i] = r;
 	if(terms) {
 		if(nev > a.ev_cap || nbase > a.base_cap || nstk > a.stk_cap) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
@@ -615,16 +646,17 @@ __global__ void __launch_bounds__(128) k_neighbours_group(ListArgs a) {
 	// the padding entries 27..31 (cells of no lane when K C < 32)
 	for(int l = K * C + sub; l < 32; l += K) s_first[grp][l] = INT_MAX;
 	__syncwarp(gmask);
+	const bool dhl = a.dh_nb != nullptr;
 	float4 a1i = make_float4(0.f, 0.f, 0.f, 0.f), bki = a1i;
-	if(terms) {
+	if(terms || dhl) {
 		a1i = a.fa1[i];
 		bki = a.fback[i];
 	}
 	const unsigned below = ((1u << lane) - 1u) & gmask;
-	int cnt = 0, nev = 0, nbase = 0, nstk = 0;
+	int cnt = 0, nev = 0, nbase = 0, nstk = 0, ndh = 0;
 	for(int t0 = 0; t0 < total; t0 += K) {
 		const int t = t0 + sub;
-		bool hit = false, hev = false, hbase = false, hstk = false;
+		bool hit = false, hev = false, hbase = false, hstk = false, hdh = false;
 		int j = -1;
 		if(t < total) {
 			// the cell holding candidate t: the last one whose first candidate is at most t
@@ -637,17 +669,21 @@ __global__ void __launch_bounds__(128) k_neighbours_group(ListArgs a) {
 				const float4 rj = a.pos[j];
 				const float d2 = sqr_min_image_inv(r, rj, g.box, inv_box);
 				hit = d2 < g.rv2;
-				if(terms && hit && d2 < a.ev_r2) {
+				if(hit && (terms || dhl)) {
 					const float3 d = min_image_vec_inv(r, rj, g.box, inv_box);
-					const float4 a1j = a.fa1[j];
-					hev = ev_sites_near(a, d, a1i, bki, a1j, a.fback[j]);
-					// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
-					const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
-							bz = d.z + 0.4f * (a1j.z - a1i.z);
-					hbase = bx * bx + by * by + bz * bz < a.base_r2;
-					const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy2 = d.y + 0.34f * (a1j.y - a1i.y),
-							sz = d.z + 0.34f * (a1j.z - a1i.z);
-					hstk = sx * sx + sy2 * sy2 + sz * sz < a.stk_r2;
+					const float4 bkj = a.fback[j];
+					hdh = dhl && back_sq(d, bki, bkj) < g.dh2;
+					if(terms && d2 < a.ev_r2) {
+						const float4 a1j = a.fa1[j];
+						hev = ev_sites_near(a, d, a1i, bki, a1j, bkj);
+						// base sites at 0.4 a1, stacking sites at 0.34 a1 from the centres
+						const float bx = d.x + 0.4f * (a1j.x - a1i.x), by = d.y + 0.4f * (a1j.y - a1i.y),
+								bz = d.z + 0.4f * (a1j.z - a1i.z);
+						hbase = bx * bx + by * by + bz * bz < a.base_r2;
+						const float sx = d.x + 0.34f * (a1j.x - a1i.x), sy2 = d.y + 0.34f * (a1j.y - a1i.y),
+								sz = d.z + 0.34f * (a1j.z - a1i.z);
+						hstk = sx * sx + sy2 * sy2 + sz * sz < a.stk_r2;
+					}
 				}
 			}
 		}
@@ -657,6 +693,14 @@ __global__ void __launch_bounds__(128) k_neighbours_group(ListArgs a) {
 			if(k < a.max_nb) put(a.nb, a.col_major != 0, N, a.max_nb, i, k, j);
 		}
 		cnt += __popc(m);
+		if(dhl) {
+			const unsigned md = __ballot_sync(gmask, hdh) & gmask;
+			if(hdh) {
+				const int k = ndh + __popc(md & below);
+				if(k < a.max_nb) a.dh_nb[(long long) k * N + i] = j;
+			}
+			ndh += __popc(md);
+		}
 		if(terms) {
 			const unsigned me = __ballot_sync(gmask, hev) & gmask, mb = __ballot_sync(gmask, hbase) & gmask,
 					ms = __ballot_sync(gmask, hstk) & gmask;
@@ -681,6 +725,7 @@ __global__ void __launch_bounds__(128) k_neighbours_group(ListArgs a) {
 	if(cnt > a.max_nb) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
 	if(a.term_max && cnt > a.term_max[3]) atomicMax(a.term_max + 3, cnt);
 	a.nnb[i] = cnt;
+	if(dhl) a.dh_n[i] = ndh;
 	a.list_pos[i] = r;
 	if(terms) {
 		if(nev > a.ev_cap || nbase > a.base_cap || nstk > a.stk_cap) atomicOr(a.status, OXGB_ERR_NEIGH_OVERFLOW);
