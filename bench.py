@@ -62,8 +62,8 @@ WORKLOADS = {
 # dram__bytes_read.sum + dram__bytes_write.sum of k_bonded_pairs + k_nonbonded_split per force
 # launch (the MD step's variant, autotuned shape 4), from the one-kernel ncu --set full captures
 # summarised in profiles/k_*_{plain40k,large250k}.md (cold caches)
-FORCE_TRAFFIC = {"plain40k": 8.596992e6 + 22.528e3 + 26.285824e6 + 0.0,
-                 "large250k": 34.994688e6 + 162.56e3 + 62.454272e6 + 1.349376e6}
+FORCE_TRAFFIC = {"plain40k": 8.596992e6 + 22.528e3 + 21.910528e6 + 0.0,
+                 "large250k": 34.994688e6 + 162.56e3 + 50.4192e6 + 416.512e3}
 
 
 def env_rank():
